@@ -1,0 +1,200 @@
+// gbv_math.cuh -- host/device vector math, RNG and half conversion for the
+// structured-volume path.
+//
+// Arithmetic follows the reference renderer's FP32 expressions operation by
+// operation; translation units that include this header are compiled with
+// -fmad=false (device) and -ffp-contract=off (host) so no multiply-add is
+// fused and every result rounds exactly as the reference's CPU backend does.
+// owl::common semantics (a third-party dependency of the reference, absent
+// from its checkout) are written out here: min/max are std::min/std::max,
+// clamp(v,lo,hi)=min(hi,max(lo,v)), rcp(x)=1/x, normalize(v)=v*(1/sqrt(v.v)).
+#pragma once
+#include <cstdint>
+#include <cmath>
+
+#if defined(__CUDACC__)
+#define GBV_HD __host__ __device__ __forceinline__
+#else
+#define GBV_HD inline
+#endif
+
+namespace gbv {
+
+template <typename T> GBV_HD T mn(T a, T b) { return (b < a) ? b : a; }
+template <typename T> GBV_HD T mx(T a, T b) { return (a < b) ? b : a; }
+template <typename T> GBV_HD T clampv(T v, T lo, T hi) { return mn(hi, mx(lo, v)); }
+
+struct vec3 {
+  float x, y, z;
+  GBV_HD vec3() : x(0.f), y(0.f), z(0.f) {}
+  GBV_HD vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+  GBV_HD explicit vec3(float a) : x(a), y(a), z(a) {}
+};
+GBV_HD vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+GBV_HD vec3 operator-(vec3 a, vec3 b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+GBV_HD vec3 operator*(vec3 a, vec3 b) { return vec3(a.x * b.x, a.y * b.y, a.z * b.z); }
+GBV_HD vec3 operator*(float s, vec3 a) { return vec3(s * a.x, s * a.y, s * a.z); }
+GBV_HD vec3 operator*(vec3 a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
+GBV_HD vec3 operator/(vec3 a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
+GBV_HD vec3 operator-(vec3 a) { return vec3(-a.x, -a.y, -a.z); }
+GBV_HD bool is_zero(vec3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
+GBV_HD vec3 vmin(vec3 a, vec3 b) { return vec3(mn(a.x, b.x), mn(a.y, b.y), mn(a.z, b.z)); }
+GBV_HD vec3 vmax(vec3 a, vec3 b) { return vec3(mx(a.x, b.x), mx(a.y, b.y), mx(a.z, b.z)); }
+GBV_HD vec3 vabs(vec3 a) { return vec3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+GBV_HD vec3 rcp(vec3 a) { return vec3(1.f / a.x, 1.f / a.y, 1.f / a.z); }
+GBV_HD vec3 vfloor(vec3 a) { return vec3(floorf(a.x), floorf(a.y), floorf(a.z)); }
+GBV_HD float reduce_min(vec3 a) { return mn(mn(a.x, a.y), a.z); }
+GBV_HD float reduce_max(vec3 a) { return mx(mx(a.x, a.y), a.z); }
+GBV_HD float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+GBV_HD vec3 cross(vec3 a, vec3 b) {
+  return vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+GBV_HD vec3 normalize(vec3 v) { return v * (1.f / sqrtf(dot(v, v))); }
+GBV_HD float comp(vec3 v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+struct vec4 { float x, y, z, w; };
+
+#define GBV_INF (__int_as_float_hd(0x7f800000))
+GBV_HD float __int_as_float_hd(int i) {
+  union { int i; float f; } u;
+  u.i = i;
+  return u.f;
+}
+GBV_HD uint32_t float_bits(float f) {
+  union { float f; uint32_t u; } u;
+  u.f = f;
+  return u.u;
+}
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kTwoPi = 2.f * 3.14159265358979323846f;
+constexpr float kFourPi = 4.f * 3.14159265358979323846f;
+constexpr float kOneOverPi = 1.f / 3.14159265358979323846f;
+constexpr float kOneOverTwoPi = 1.f / (2.f * 3.14159265358979323846f);
+constexpr float kOneOverFourPi = 1.f / (4.f * 3.14159265358979323846f);
+
+// ---------------------------------------------------------------------------
+// Half precision, rounded as the reference's CPU backend rounds
+// (rtcore/embree/Float16.cpp float32ToFloat16: to nearest, ties away from
+// zero).  Path throughput lives in half precision (render/Ray.h:19), so the
+// rounding rule is part of the path's arithmetic.
+// ---------------------------------------------------------------------------
+GBV_HD uint16_t f2h(float value) {
+  int i = (int)float_bits(value);
+  int s = (i >> 16) & 0x00008000;
+  int e = ((i >> 23) & 0x000000ff) - (127 - 15);
+  int m = i & 0x007fffff;
+  if (e <= 0) {
+    if (e < -10) return uint16_t(s);
+    m = (m | 0x00800000) >> (1 - e);
+    if (m & 0x00001000) m += 0x00002000;
+    return uint16_t(s | (m >> 13));
+  } else if (e == 0xff - (127 - 15)) {
+    if (m == 0) return uint16_t(s | 0x7c00);
+    m >>= 13;
+    return uint16_t(s | 0x7c00 | m | (m == 0));
+  }
+  if (m & 0x00001000) {
+    m += 0x00002000;
+    if (m & 0x00800000) { m = 0; e += 1; }
+  }
+  if (e > 30) return uint16_t(s | 0x7c00);
+  return uint16_t(s | (e << 10) | (m >> 13));
+}
+// exact widening
+GBV_HD float h2f(uint16_t h) {
+  uint32_t s = (h >> 15) & 1u, e = (h >> 10) & 0x1fu, m = h & 0x3ffu, out;
+  if (e == 0) {
+    if (m == 0) out = s << 31;
+    else {
+      while (!(m & 0x400u)) { m <<= 1; e -= 1; }
+      e += 1;
+      m &= ~0x400u;
+      out = (s << 31) | ((e + 112u) << 23) | (m << 13);
+    }
+  } else if (e == 31) {
+    out = (s << 31) | 0x7f800000u | (m << 13);
+  } else {
+    out = (s << 31) | ((e + 112u) << 23) | (m << 13);
+  }
+  union { uint32_t u; float f; } u;
+  u.u = out;
+  return u.f;
+}
+struct vec3h { uint16_t x, y, z; };
+GBV_HD vec3h to_half(vec3 v) { return vec3h{f2h(v.x), f2h(v.y), f2h(v.z)}; }
+GBV_HD vec3 from_half(vec3h v) { return vec3(h2f(v.x), h2f(v.y), h2f(v.z)); }
+
+// ---------------------------------------------------------------------------
+// RNG streams (barney/common/barney-common.h:65-152): a 64-bit multiplicative
+// LCG with an xorshift output, 24-bit floats, FNV-style stream hashes.
+// ---------------------------------------------------------------------------
+struct RNGSeed {
+  uint64_t state;
+  GBV_HD uint32_t next() {
+    uint64_t x = state;
+    unsigned count = (unsigned)(x >> 61);
+    state = x * 6364136223846793005ull;
+    x ^= x >> 22;
+    return (uint32_t)(x >> (22 + count));
+  }
+  GBV_HD uint32_t next_h(uint64_t hash) {
+    state ^= (hash << 1);
+    return next();
+  }
+};
+GBV_HD RNGSeed seeded(uint32_t a, uint32_t b) {
+  RNGSeed r;
+  r.state = 0xcafef00dd15ea5e5ull;
+  r.state ^= (uint64_t)(uint32_t)(2u * a + 1u);
+  r.next();
+  r.state ^= (uint64_t)(uint32_t)(2u * b);
+  r.next();
+  return r;
+}
+struct Random {
+  RNGSeed s;
+  // Random2(RNGSeed &seed, b): copy, advance the source, then mix in b.
+  GBV_HD static Random derive(RNGSeed &seed, uint64_t b) {
+    Random r;
+    r.s.state = seed.state;
+    seed.next();
+    r.s.next_h(b ? b : 290374ull);
+    return r;
+  }
+  GBV_HD static Random from_pair(uint32_t a, uint32_t b) {
+    Random r;
+    r.s = seeded(a, b);
+    return r;
+  }
+  GBV_HD float operator()() { return (s.next() & 0x00FFFFFF) * (1.f / (float)0x01000000); }
+};
+// hash(0,0,0): the stream id of the only instance/geometry of the world
+constexpr uint64_t kFnvOffset = 0xcbf29ce484222325ull;
+constexpr uint64_t kFnvPrime = 0x100000001b3ull;
+constexpr uint64_t kVolumeStreamHash = ((kFnvOffset ^ (kFnvPrime * 0ull)) * kFnvPrime ^ 0ull) * kFnvPrime ^ 0ull;
+
+// Volume.h:174-184: three-term atanh series for log
+GBV_HD float fastLog(float f) {
+  f = (f - 1.f) / (f + 1.f);
+  float f2 = f * f;
+  float s = f;
+  f *= f2;
+  s += (1.f / 3.f) * f;
+  f *= f2;
+  s += (1.f / 5.f) * f;
+  return s + s;
+}
+
+GBV_HD float lerp_l(float f, float a, float b) { return (1.f - f) * a + f * b; }
+
+// rtcore/embree/Texture.cpp:324-336
+GBV_HD void lerp_coords(int N, float tc, int &i0, int &i1, float &f) {
+  if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; return; }
+  if (tc - .5f >= (float)(N - 1)) { i0 = i1 = N - 1; f = 0.f; return; }
+  f = (tc - .5f) - (float)(int)(tc - .5f);
+  i0 = (int)(tc - .5f);
+  i1 = i0 + 1;
+}
+
+}  // namespace gbv

@@ -1,0 +1,327 @@
+// gbv_volume.cuh -- device-side field sampling, transfer function and
+// macrocell traversal for the structured-volume path.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include "gbv_math.cuh"
+#include "../../include/gbvol.h"
+
+namespace gbv {
+
+constexpr int kBrick = 8;          // cells per brick edge
+constexpr int kBrickCells = 512;   // 8^3
+
+// Field geometry shared by every voxel store (StructuredData: numScalars,
+// numCells = dims-1, gridOrigin, rcp(gridSpacing); StructuredData.cu:127-180).
+struct FieldGeom {
+  int N[3];
+  int C[3];
+  vec3 origin;
+  vec3 rcpSpacing;
+  vec3 boundsLo, boundsHi;
+};
+
+// -------------------------------------------------------------------------
+// Voxel stores.  corners() returns the 8 voxels of the trilinear stencil in
+// the order (x0y0z0, x1y0z0, x0y1z0, x1y1z0, x0y0z1, x1y0z1, x0y1z1, x1y1z1).
+// -------------------------------------------------------------------------
+
+// The reference's own layout: x-fastest FP32 texels
+// (rtcore/embree/Texture.cpp:148-152).
+struct StoreLinearF32 {
+  const float *v;
+  int nx, ny;
+  __device__ __forceinline__ void corners(int x0, int x1, int y0, int y1, int z0, int z1, float c[8]) const {
+    const size_t sx = 1, sy = (size_t)nx, sz = (size_t)nx * ny;
+    const float *p00 = v + (size_t)z0 * sz + (size_t)y0 * sy;
+    const float *p01 = v + (size_t)z0 * sz + (size_t)y1 * sy;
+    const float *p10 = v + (size_t)z1 * sz + (size_t)y0 * sy;
+    const float *p11 = v + (size_t)z1 * sz + (size_t)y1 * sy;
+    c[0] = __ldg(p00 + x0 * sx); c[1] = __ldg(p00 + x1 * sx);
+    c[2] = __ldg(p01 + x0 * sx); c[3] = __ldg(p01 + x1 * sx);
+    c[4] = __ldg(p10 + x0 * sx); c[5] = __ldg(p10 + x1 * sx);
+    c[6] = __ldg(p11 + x0 * sx); c[7] = __ldg(p11 + x1 * sx);
+  }
+  static constexpr bool kCellStore = false;
+};
+
+// 8^3-cell bricks, each cell holding its 8 corner voxels contiguously: one
+// stencil is one aligned vector load (32 B FP32, 16 B FP16/BF16, 8 B U8).
+template <int FMT> struct StoreBrickCorners {
+  const void *v;
+  const float2 *so;  // U8: (scale, offset) per brick
+  int nbx, nby;
+  static constexpr bool kCellStore = true;
+  __device__ __forceinline__ size_t cell_index(int cx, int cy, int cz, size_t &brick) const {
+    brick = (size_t)(cx >> 3) + (size_t)nbx * ((size_t)(cy >> 3) + (size_t)nby * (size_t)(cz >> 3));
+    int local = (cx & 7) + 8 * ((cy & 7) + 8 * (cz & 7));
+    return brick * kBrickCells + (size_t)local;
+  }
+  __device__ __forceinline__ void cell(int cx, int cy, int cz, float c[8]) const {
+    size_t brick;
+    size_t idx = cell_index(cx, cy, cz, brick);
+    if (FMT == GBV_VOXEL_F32) {
+      const float4 *p = reinterpret_cast<const float4 *>(v) + 2 * idx;
+      float4 a = __ldg(p), b = __ldg(p + 1);
+      c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+      c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+    } else if (FMT == GBV_VOXEL_F16) {
+      uint4 q = __ldg(reinterpret_cast<const uint4 *>(v) + idx);
+      uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        c[2 * k] = __half2float(__ushort_as_half((unsigned short)(w[k] & 0xffffu)));
+        c[2 * k + 1] = __half2float(__ushort_as_half((unsigned short)(w[k] >> 16)));
+      }
+    } else if (FMT == GBV_VOXEL_BF16) {
+      uint4 q = __ldg(reinterpret_cast<const uint4 *>(v) + idx);
+      uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        c[2 * k] = __uint_as_float(w[k] << 16);
+        c[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+      }
+    } else {  // U8_SCALED
+      uint2 q = __ldg(reinterpret_cast<const uint2 *>(v) + idx);
+      float2 s = __ldg(so + brick);
+      uint32_t w[2] = {q.x, q.y};
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        float u = (float)((w[k >> 2] >> (8 * (k & 3))) & 0xffu);
+        c[k] = s.y + s.x * u;
+      }
+    }
+  }
+};
+
+// StructuredDataSampler::DD::sample (StructuredData.h:104-115) with the CPU
+// backend's trilinear filter (rtcore/embree/Texture.cpp:339-411).  NaN
+// outside [0, numCells).
+template <class Store>
+__device__ __forceinline__ float sample_field(const FieldGeom &F, const Store &S, vec3 P) {
+  vec3 rel = (P - F.origin) * F.rcpSpacing;
+  if (rel.x < 0.f || rel.y < 0.f || rel.z < 0.f) return __int_as_float(0x7fffffff);
+  if (rel.x >= (float)F.C[0] || rel.y >= (float)F.C[1] || rel.z >= (float)F.C[2])
+    return __int_as_float(0x7fffffff);
+  const vec3 tc = rel + vec3(.5f);
+  int x0, x1, y0, y1, z0, z1;
+  float fx, fy, fz;
+  lerp_coords(F.N[0], tc.x, x0, x1, fx);
+  lerp_coords(F.N[1], tc.y, y0, y1, fy);
+  lerp_coords(F.N[2], tc.z, z0, z1, fz);
+  float c[8];
+  if constexpr (Store::kCellStore) {
+    // A clamped axis (x0 == x1) reads the same voxel twice with weight 0 on
+    // the second; on a cell store that is cell 0 with f=0 or cell N-2 with
+    // f=1, which gives the identical value for finite data.
+    if (x0 == x1) { if (x0 > 0) { x0 -= 1; fx = 1.f; } }
+    if (y0 == y1) { if (y0 > 0) { y0 -= 1; fy = 1.f; } }
+    if (z0 == z1) { if (z0 > 0) { z0 -= 1; fz = 1.f; } }
+    S.cell(x0, y0, z0, c);
+  } else {
+    S.corners(x0, x1, y0, y1, z0, z1, c);
+  }
+  const float v00 = lerp_l(fx, c[0], c[1]), v01 = lerp_l(fx, c[2], c[3]);
+  const float v10 = lerp_l(fx, c[4], c[5]), v11 = lerp_l(fx, c[6], c[7]);
+  const float v0 = lerp_l(fy, v00, v01), v1 = lerp_l(fy, v10, v11);
+  return lerp_l(fz, v0, v1);
+}
+
+// -------------------------------------------------------------------------
+// Transfer function (TransferFunction.h:66-116)
+// -------------------------------------------------------------------------
+struct XF {
+  const float4 *v;
+  int n;
+  float lo, span, baseDensity;
+};
+
+__device__ __forceinline__ vec4 xf_map(const XF &xf, float s) {
+  float f = (s - xf.lo) / xf.span;
+  f = clampv(f, 0.f, 1.f);
+  f *= (float)(xf.n - 1);
+  int idx = clampv((int)f, 0, xf.n - 2);
+  f -= (float)idx;
+  const float4 v0 = __ldg(xf.v + idx), v1 = __ldg(xf.v + idx + 1);
+  vec4 r;
+  r.x = (1.f - f) * v0.x + f * v1.x;
+  r.y = (1.f - f) * v0.y + f * v1.y;
+  r.z = (1.f - f) * v0.z + f * v1.z;
+  r.w = (1.f - f) * v0.w + f * v1.w;
+  r.w *= xf.baseDensity;
+  return r;
+}
+
+__host__ __device__ __forceinline__ float xf_majorant(const float4 *v, int n, float lo, float span, float bd,
+                                                      float lower, float upper) {
+  if (lower > upper) return 0.f;
+  float f_lo = (lower - lo) / span;
+  float f_hi = (upper - lo) / span;
+  f_lo = clampv(f_lo, 0.f, 1.f);
+  f_hi = clampv(f_hi, 0.f, 1.f);
+  f_lo *= (float)(n - 1);
+  f_hi *= (float)(n - 1);
+  int idx0_lo = clampv((int)f_lo, 0, n - 2);
+  int idx0_hi = clampv((int)f_hi, 0, n - 2);
+  f_lo -= (float)idx0_lo;
+  f_hi -= (float)idx0_hi;
+  float lerp_lo = (1.f - f_lo) * v[idx0_lo].w + f_lo * v[idx0_lo + 1].w;
+  float lerp_hi = (1.f - f_hi) * v[idx0_hi].w + f_hi * v[idx0_hi + 1].w;
+  float m = 0.f;
+  m = mx(m, lerp_lo);
+  m = mx(m, lerp_hi);
+  for (int i = idx0_lo + 1; i <= idx0_hi; i++) m = mx(m, v[i].w);
+  return m * bd;
+}
+
+// Volume::DD::sampleAndMap (Volume.h:66-80): NaN -> 0, else TF map
+template <class Store>
+__device__ __forceinline__ vec4 sample_and_map(const FieldGeom &F, const Store &S, const XF &xf, vec3 P) {
+  float f = sample_field(F, S, P);
+  if (isnan(f)) return vec4{0.f, 0.f, 0.f, 0.f};
+  return xf_map(xf, f);
+}
+
+// Ray.h:175-187
+__device__ __forceinline__ bool box_test(vec3 org, vec3 dir, float &t0, float &t1, vec3 lo, vec3 hi) {
+  vec3 t_lo = (lo - org) * rcp(dir);
+  vec3 t_hi = (hi - org) * rcp(dir);
+  vec3 t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  t0 = mx(t0, reduce_max(t_nr));
+  t1 = mn(t1, reduce_min(t_fr));
+  return t0 <= t1;
+}
+
+// -------------------------------------------------------------------------
+// Macrocell grid (MCGrid / MajorantsGrid) as seen by the traversal
+// -------------------------------------------------------------------------
+struct MCGridDev {
+  const float *maj;
+  int M[3];
+  vec3 origin;      // = field world bounds lower
+  vec3 spacing;     // = cells_per_mc * gridSpacing
+};
+
+struct TraceCounters {
+  unsigned long long samples, mcs, rays, caps;
+};
+
+// Result of one ray-volume query
+struct Hit {
+  bool hit;
+  float t;
+  vec3 rgb;
+  vec3 P;
+};
+
+// MCVolumeAccel::isProg (MCAccelerator.h:569-708) with dda::dda3
+// (DDA.h:65-206) and Woodcock::sampleRange (Volume.h:188-223), dispatched as
+// the CPU backend does: tmin 0, tmax = ray.tMax, identity instance transform,
+// zero direction components replaced by 1e-6 (traceRays.dev.cu:41-44).
+// Advances `seed` exactly as the reference advances ray.rngSeed.
+template <class Store>
+__device__ __forceinline__ Hit trace_volume(const FieldGeom &F, const Store &S, const XF &xf, const MCGridDev &G,
+                                            vec3 org, vec3 rayDir, float rayTMax, RNGSeed &seed,
+                                            TraceCounters &cnt) {
+  Hit h;
+  h.hit = false;
+  cnt.rays++;
+  vec3 dir = rayDir;
+  if (dir.x == 0.f) dir.x = 1e-6f;
+  if (dir.y == 0.f) dir.y = 1e-6f;
+  if (dir.z == 0.f) dir.z = 1e-6f;
+  if (G.M[0] <= 0 || G.M[1] <= 0 || G.M[2] <= 0) return h;
+  float tLo = 0.f, tHi = rayTMax;
+  if (!box_test(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return h;
+
+  const vec3 rcpMc = rcp(G.spacing);
+  const vec3 dda_org = (org - G.origin) * rcpMc;
+  const vec3 dda_dir = dir * rcpMc;
+  Random rng = Random::derive(seed, kVolumeStreamHash);
+  const float tMax = tHi;
+
+  const vec3 f_size((float)G.M[0], (float)G.M[1], (float)G.M[2]);
+  const vec3 rcp_dir = rcp(dda_dir);
+  vec3 t_lo = (vec3(0.f) - dda_org) * rcp(dda_dir);
+  vec3 t_hi = (f_size - dda_org) * rcp(dda_dir);
+  vec3 t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  const float INF = __int_as_float(0x7f800000);
+  if (dda_dir.x == 0.f) {
+    if (dda_org.x < 0.f || dda_org.x > f_size.x) return h;
+    t_nr.x = -INF; t_fr.x = INF;
+  }
+  if (dda_dir.y == 0.f) {
+    if (dda_org.y < 0.f || dda_org.y > f_size.y) return h;
+    t_nr.y = -INF; t_fr.y = INF;
+  }
+  if (dda_dir.z == 0.f) {
+    if (dda_org.z < 0.f || dda_org.z > f_size.z) return h;
+    t_nr.z = -INF; t_fr.z = INF;
+  }
+  const float ray_t0 = mx(0.f, reduce_max(t_nr));
+  const float ray_t1 = mn(tMax, reduce_min(t_fr));
+  if (ray_t0 > ray_t1) return h;
+  const vec3 org_in_volume = dda_org + ray_t0 * dda_dir;
+  const vec3 f_cell = vmax(vec3(0.f), vmin(f_size - vec3(1.f), vfloor(org_in_volume)));
+  const vec3 f_cell_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
+                        dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
+  const vec3 t_step = vabs(rcp_dir);
+  vec3 t_next((dda_dir.x == 0.f) ? INF : (fabsf(f_cell_end.x - org_in_volume.x) * t_step.x),
+              (dda_dir.y == 0.f) ? INF : (fabsf(f_cell_end.y - org_in_volume.y) * t_step.y),
+              (dda_dir.z == 0.f) ? INF : (fabsf(f_cell_end.z - org_in_volume.z) * t_step.z));
+  const int stop_x = dda_dir.x > 0.f ? G.M[0] : -1, stop_y = dda_dir.y > 0.f ? G.M[1] : -1,
+            stop_z = dda_dir.z > 0.f ? G.M[2] : -1;
+  const int dx = dda_dir.x > 0.f ? 1 : -1, dy = dda_dir.y > 0.f ? 1 : -1, dz = dda_dir.z > 0.f ? 1 : -1;
+  int cx = (int)f_cell.x, cy = (int)f_cell.y, cz = (int)f_cell.z;
+  float next_cell_begin = 0.f;
+  const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
+  for (int it = 0; it < maxCells; it++) {
+    const float t_closest = reduce_min(t_next);
+    const float cell_t0 = ray_t0 + next_cell_begin;
+    const float cell_t1 = ray_t0 + mn(t_closest, tMax);
+    const float majorant = __ldg(G.maj + (cx + G.M[0] * (cy + G.M[1] * cz)));
+    if (majorant != 0.f) {
+      cnt.mcs++;
+      const float segHi0 = mn(cell_t1, rayTMax);
+      float t = cell_t0;
+      // Woodcock::sampleRange
+      for (int k = 0; k < (1 << 20); k++) {
+        const float r = rng();
+        const float dt = -fastLog(1.f - r) / majorant;
+        t += dt;
+        if (t >= segHi0) break;
+        const vec3 P = org + t * dir;
+        const vec4 smp = sample_and_map(F, S, xf, P);
+        cnt.samples++;
+        if (smp.w >= rng() * majorant) {
+          h.hit = true;
+          h.t = t;
+          h.rgb = vec3(smp.x, smp.y, smp.z);
+          h.P = org + t * dir;
+          return h;
+        }
+        if (k == (1 << 20) - 1) cnt.caps++;
+      }
+    }
+    next_cell_begin = t_closest;
+    if (t_next.x == t_closest) {
+      t_next.x += t_step.x;
+      cx += dx;
+      if (cx == stop_x) return h;
+    }
+    if (t_next.y == t_closest) {
+      t_next.y += t_step.y;
+      cy += dy;
+      if (cy == stop_y) return h;
+    }
+    if (t_next.z == t_closest) {
+      t_next.z += t_step.z;
+      cz += dz;
+      if (cz == stop_z) return h;
+    }
+  }
+  cnt.caps++;
+  return h;
+}
+
+}  // namespace gbv

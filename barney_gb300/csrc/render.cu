@@ -1,0 +1,653 @@
+// render.cu -- the structured-volume frame render on sm_103a.
+//
+// One thread owns one pixel for all of a launch's accumulation passes, so
+// the frame buffer needs no atomics and every pixel accumulates its
+// fragments in the reference's order (pass-major, then generation; within a
+// generation the shadow ray before the bounce ray).  A pass follows
+// Context::renderTiles (barney/Context.cpp:142-185): _generateRays, then per
+// generation the trace (MCVolumeAccel::isProg) and _shadeRays/bounce
+// (barney/kernels/shadeRays.cu:477-1041) of the pixel's queued rays.
+#include <cuda_runtime.h>
+#include "gbv_volume.cuh"
+#include "gbv_internal.h"
+
+namespace gbv {
+
+struct DirLightDev { vec3 direction; float radiance; vec3 color; };
+struct M3 { vec3 vx, vy, vz; };
+__device__ __forceinline__ vec3 xfm_vector(const M3 &m, vec3 v) { return m.vx * v.x + m.vy * v.y + m.vz * v.z; }
+
+struct EnvDev {
+  const float4 *tex;
+  const float *cdf_y, *cdf_x;
+  int W, H;
+  int addr[2];
+  M3 toWorld, toLocal;
+  float scale;
+};
+
+struct RenderParams {
+  FieldGeom F;
+  XF xf;
+  MCGridDev G;
+  // camera (PerspectiveCamera::commit)
+  vec3 lens00, dir00, du, dv;
+  int W, H;
+  int numDir;
+  DirLightDev dir[4];
+  int hasEnv;
+  EnvDev env;
+  float4 bg;
+  float ambient;
+  int multi, volMS, maxVB;
+  float aniso, scatAlb;
+  float4 *accum;
+  int accumIdStart, spp;
+  unsigned long long *counters;
+};
+
+struct LightSample {
+  vec3 radiance, direction;
+  float distance, pdf;
+};
+
+// rtcore/embree/Texture.cpp:25-93 (normalized coordinates)
+__device__ __forceinline__ void compute_address(int mode, float tc, int N, int &i0, int &i1, float &f) {
+  i0 = 0; i1 = 0; f = 0.f;
+  if (mode == GBV_ADDR_WRAP) {
+    tc = tc * (float)N - .5f;
+    tc = fmodf(tc, (float)N);
+    if (tc < 0.f) tc += (float)N;
+    float fc = floorf(tc);
+    int ic = (int)fc;
+    f = tc - (float)ic;
+    i0 = ic;
+    i1 = (int)fmodf(tc + 1.f, (float)N);
+  } else if (mode == GBV_ADDR_MIRROR) {
+    tc = tc * (float)N + .5f;
+    float fc = floorf(tc);
+    int ic = (int)fc;
+    f = tc - (float)ic;
+    int a = ic - 1, b = ic;
+    if (a < 0) a = -a;
+    if (b < 0) b = -b;
+    a = a % (2 * N);
+    b = b % (2 * N);
+    if (a >= N) a = 2 * N - 1 - a;
+    if (b >= N) b = 2 * N - 1 - b;
+    i0 = a;
+    i1 = b;
+  } else if (mode == GBV_ADDR_CLAMP) {
+    tc = tc * (float)N;
+    if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; }
+    else if (tc - .5f >= (float)(N - 1)) { i0 = i1 = N - 1; f = 0.f; }
+    else {
+      f = (tc - .5f) - (float)(int)(tc - .5f);
+      i0 = (int)(tc - .5f);
+      i1 = i0 + 1;
+    }
+  }
+}
+__device__ __forceinline__ float4 lerp4(float f, float4 a, float4 b) {
+  return make_float4((1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
+                     (1.f - f) * a.w + f * b.w);
+}
+// rtcore/embree/Texture.cpp:295-321
+__device__ __forceinline__ float4 tex2D(const EnvDev &e, float u, float v) {
+  int x0, x1, y0, y1;
+  float fx, fy;
+  compute_address(e.addr[0], u, e.W, x0, x1, fx);
+  compute_address(e.addr[1], v, e.H, y0, y1, fy);
+  float4 v00 = __ldg(e.tex + (size_t)x0 + (size_t)y0 * e.W), v01 = __ldg(e.tex + (size_t)x1 + (size_t)y0 * e.W);
+  float4 v10 = __ldg(e.tex + (size_t)x0 + (size_t)y1 * e.W), v11 = __ldg(e.tex + (size_t)x1 + (size_t)y1 * e.W);
+  return lerp4(fy, lerp4(fx, v00, v01), lerp4(fx, v10, v11));
+}
+
+// DG.h:97-106
+__device__ __forceinline__ float spherical_theta(vec3 v) { return acosf(clampv(v.z, -1.f, 1.f)); }
+__device__ __forceinline__ float spherical_phi(vec3 v) {
+  float p = atan2f(v.y, v.x);
+  return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
+}
+// EnvMap.h:98-134
+__device__ __forceinline__ float cdf_get_pdf(int position, const float *cdf, int N) {
+  float at = __ldg(cdf + position);
+  float before = position ? __ldg(cdf + position - 1) : 0.f;
+  return (float)N * (at - before);
+}
+__device__ __forceinline__ int sample_cdf(const float *cdf, int N, float v, float &pdf) {
+  int begin = 0, end = N;
+  while ((end - begin) > 1) {
+    int mid = (begin + end) / 2;
+    float f_mid = __ldg(cdf + mid - 1);
+    if (v < f_mid) end = mid;
+    else begin = mid;
+  }
+  float at = __ldg(cdf + begin);
+  float before = begin ? __ldg(cdf + begin - 1) : 0.f;
+  pdf = (float)N * (at - before);
+  return begin;
+}
+// EnvMap.h:136-180
+__device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
+  if (!p.hasEnv) return kOneOverFourPi;
+  const EnvDev &e = p.env;
+  vec3 localDir = xfm_vector(e.toLocal, dir);
+  float theta = spherical_theta(localDir);
+  float phi = spherical_phi(localDir);
+  float u = phi * kOneOverTwoPi, v = theta * kOneOverPi;
+  int px = (int)clampv(u * (float)e.W, 0.f, (float)e.W - 1.f);
+  int py = (int)clampv(v * (float)e.H, 0.f, (float)e.H - 1.f);
+  float pdf_y = cdf_get_pdf(py, e.cdf_y, e.H);
+  float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
+  float rel_y = ((float)py + .5f) / (float)e.H;
+  const float theta2 = kPi * rel_y;
+  return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta2));
+}
+// EnvMap.h:198-250
+__device__ __forceinline__ LightSample env_sample(const RenderParams &p, Random &r) {
+  const EnvDev &e = p.env;
+  LightSample s;
+  float r_y = r();
+  float r_x = r();
+  float pdf_y, pdf_x;
+  int iy = sample_cdf(e.cdf_y, e.H, r_y, pdf_y);
+  int ix = sample_cdf(e.cdf_x + (size_t)e.W * iy, e.W, r_x, pdf_x);
+  float sx = ((float)ix + r()) / (float)e.W;
+  float sy = ((float)iy + r()) / (float)e.H;
+  float4 t = tex2D(e, sx, sy);
+  s.radiance = e.scale * vec3(t.x, t.y, t.z);
+  const float phi = kTwoPi * sx;
+  const float theta = kPi * sy;
+  vec3 d;
+  d.z = cosf(theta);
+  d.x = cosf(phi) * sinf(theta);
+  d.y = sinf(phi) * sinf(theta);
+  s.direction = xfm_vector(e.toWorld, d);
+  s.pdf = pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta));
+  s.distance = __int_as_float(0x7f800000);
+  return s;
+}
+
+// DG.h:183-193
+__device__ __forceinline__ vec3 random_direction(Random &rng) {
+  for (int k = 0; k < 64; k++) {
+    vec3 v;
+    v.x = 1.f - 2.f * rng();
+    v.y = 1.f - 2.f * rng();
+    v.z = 1.f - 2.f * rng();
+    if (dot(v, v) <= 1.f) return normalize(v);
+  }
+  return vec3(0.f, 0.f, 1.f);
+}
+
+// shadeRays.cu:141-191 (the world's only normal here is the volume's N=0)
+__device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random &random, LightSample &ls) {
+  if (p.numDir == 0) return false;
+  int lID[2];
+  float weights[2];
+  float sumWeights = 0.f;
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    lID[i] = mn((int)(random() * (float)p.numDir), p.numDir - 1);
+    weights[i] = 0.f;
+    const DirLightDev &light = p.dir[lID[i]];
+    vec3 lr = light.color * light.radiance;
+    float weight = 1.f;  // N == 0
+    weight *= reduce_max(lr);
+    if (weight <= 1e-3f) continue;
+    weights[i] = weight;
+    sumWeights += weight;
+  }
+  if (sumWeights == 0.f) return false;
+  float r = random() * sumWeights;
+  int i = 0;
+  while (i < 2 && r >= weights[i]) { r -= weights[i]; ++i; }
+  if (i == 2) return false;
+  const DirLightDev &light = p.dir[lID[i]];
+  ls.direction = -light.direction;
+  ls.distance = __int_as_float(0x7f800000);
+  ls.radiance = light.color * light.radiance * 1.f / (weights[i] / sumWeights * (2.f / (float)p.numDir));
+  ls.pdf = __int_as_float(0x7f800000);
+  return weights[i] != 0.f;
+}
+
+// shadeRays.cu:268-404 (no area or point lights in this world)
+__device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &random, LightSample &ls,
+                                              bool &needsMIS, bool &isDir) {
+  needsMIS = false;
+  LightSample els;
+  if (p.hasEnv) {
+    els = env_sample(p, random);
+  } else {
+    els.direction = random_direction(random);
+    els.distance = __int_as_float(0x7f800000);
+    els.radiance = vec3(kFourPi * p.ambient);
+    els.pdf = kOneOverFourPi;
+  }
+  float elsWeight = reduce_max(els.radiance);
+  LightSample dls;
+  dls.pdf = 0.f;
+  float dlsWeight = sample_dir_lights(p, random, dls) ? reduce_max(dls.radiance) : 0.f;
+  float alsWeight = 0.f, plsWeight = 0.f;
+  float sumWeights = alsWeight + dlsWeight + elsWeight + plsWeight;
+  if (sumWeights == 0.f) return false;
+  elsWeight *= 1.f / sumWeights;
+  alsWeight *= 1.f / sumWeights;
+  dlsWeight *= 1.f / sumWeights;
+  float r = random();
+  if (r <= alsWeight) {
+    return false;  // empty area-light sample (pdf 0)
+  } else if (r <= alsWeight + elsWeight) {
+    ls = els;
+    ls.radiance = ls.radiance * (1.f / elsWeight);
+    needsMIS = true;
+  } else if (r <= alsWeight + elsWeight + plsWeight) {
+    return false;
+  } else {
+    ls = dls;
+    ls.radiance = ls.radiance * (1.f / dlsWeight);
+    isDir = true;
+  }
+  if (isnan(ls.pdf) || (ls.pdf <= 0.f)) return false;
+  return true;
+}
+
+// shadeRays.cu:437-456
+__device__ __forceinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
+  if (p.hasEnv) {
+    vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
+    float theta = spherical_theta(d);
+    float phi = spherical_phi(d);
+    const float invPi = 1.f / (float)3.14159265358979323846;
+    const float inv2Pi = 1.f / (2.f * (float)3.14159265358979323846);
+    float4 c = tex2D(p.env, phi * inv2Pi, theta * invPi);
+    return p.env.scale * vec3(c.x, c.y, c.z);
+  }
+  return vec3(p.ambient);
+}
+
+// Phase.h:49-57
+__device__ __forceinline__ float hg_phase(float g, float cosTheta) {
+  if (fabsf(g) < 1e-3f) return kOneOverFourPi;
+  float g2 = g * g;
+  float denom = 1.f + g2 - 2.f * g * cosTheta;
+  return kOneOverFourPi * (1.f - g2) / (denom * sqrtf(denom));
+}
+__device__ __forceinline__ float phase_pdf(const RenderParams &p, float g, vec3 wo, vec3 wi) {
+  if (!p.multi) return kOneOverFourPi;
+  vec3 wi_in = normalize(-wo);
+  return hg_phase(g, dot(wi_in, normalize(wi)));
+}
+// Phase.h:74-99
+__device__ __forceinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
+  float u0 = random();
+  float u1 = random();
+  float cosTheta;
+  if (fabsf(g) < 1e-3f) cosTheta = 1.f - 2.f * u0;
+  else {
+    float sqrTerm = (1.f - g * g) / (1.f + g - 2.f * g * u0);
+    cosTheta = (1.f + g * g - sqrTerm * sqrTerm) / (2.f * g);
+  }
+  float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
+  float phi = kTwoPi * u1;
+  vec3 local(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
+  vec3 w = normalize(wi_in);
+  vec3 u, v;
+  if (fabsf(w.x) > 0.1f) u = normalize(cross(vec3(0.f, 1.f, 0.f), w));
+  else u = normalize(cross(vec3(1.f, 0.f, 0.f), w));
+  v = cross(w, u);
+  return normalize(local.x * u + local.y * v + local.z * w);
+}
+
+// Per-ray state of the pixel's path (Ray + PathState, render/Ray.h:18-99)
+struct PathRay {
+  vec3 org, dir;
+  float tMax;
+  RNGSeed seed;
+  vec3h tp;
+  float misWeight;
+  int numVolumeBounces;
+};
+
+struct ShadeOut {
+  vec3 fragment;
+  bool shadowValid;
+  PathRay shadow;
+};
+
+// bounce() for a volume hit (shadeRays.cu:605-878).  Updates `ray`; a dead
+// ray has tMax = -1.
+__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, int pathDepth,
+                                                  ShadeOut &out) {
+  out.shadowValid = false;
+  const float tHit = h.t;
+  const vec3 albedo = p.multi ? p.scatAlb * h.rgb : .7f * h.rgb;
+  const float g = p.multi ? p.aniso : 0.f;
+  const vec3 incomingThroughput = from_half(ray.tp);
+  Random random = Random::derive(ray.seed, (uint64_t)float_bits(tHit));
+  const vec3 P = h.P;
+  const vec3 wo = -normalize(ray.dir);
+  const float offsetEpsilon = mx(1e-4f, 1e-6f * reduce_max(vabs(P)));
+  LightSample ls;
+  bool needsMIS = false, isDir = false;
+  if (sample_lights(p, random, ls, needsMIS, isDir)) {
+    float density = p.multi ? phase_pdf(p, g, wo, ls.direction) : kOneOverFourPi;
+    vec3 fr = density * albedo;
+    if (!(density > 0.f) || reduce_max(fr) < 1e-4f) {
+      out.shadowValid = false;
+    } else {
+      fr = vmin(fr, vec3(13.f));
+      vec3 tp_sr = incomingThroughput * (isinf(ls.pdf) ? 1.f : 1.f / ls.pdf) * fr * ls.radiance * 1.f;
+      out.shadow.dir = ls.direction;
+      out.shadow.org = P + offsetEpsilon * wo;
+      out.shadow.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
+      out.shadow.tp = to_half(tp_sr);
+      out.shadow.seed = ray.seed;
+      ray.seed.next_h((uint64_t)float_bits(tHit));
+      out.shadow.misWeight = 1.f;
+      out.shadowValid = true;
+      if (!isDir && needsMIS) {
+        float pdf_l = env_pdf(p, ls.direction);
+        float pdf_s = p.multi ? phase_pdf(p, g, wo, ls.direction) : kOneOverFourPi;
+        out.shadow.misWeight = pdf_l / (pdf_l + pdf_s + 1e-10f);
+        if (out.shadow.misWeight < 1e-5f) out.shadowValid = false;
+      }
+    }
+  }
+  if (pathDepth >= 10) {  // MAX_PATH_DEPTH
+    ray.tMax = -1.f;
+    return;
+  }
+  ray.tMax = __int_as_float(0x7f800000);
+  if (!p.multi) {
+    // SCI_VIS_MODE: a volume scatter ends the path after its shadow ray
+    // (the scatter direction is drawn but never used).
+    ray.tMax = -1.f;
+    return;
+  }
+  vec3 wi_in = normalize(-wo);
+  vec3 sdir = sample_hg_direction(wi_in, g, random);
+  float spdf = hg_phase(g, dot(wi_in, sdir));
+  vec3 sf_r = albedo * spdf;
+  if (!(spdf > 0.f) || spdf <= 1e-6f) return;
+  if (!p.volMS || ray.numVolumeBounces >= p.maxVB) {
+    ray.tMax = -1.f;
+    return;
+  }
+  ray.numVolumeBounces = ray.numVolumeBounces + 1;
+  ray.org = P + (1.f * offsetEpsilon) * wo;
+  ray.dir = normalize(sdir);
+  vec3 scatterFactor = sf_r * 1.f / (isinf(spdf) ? 1.f : (spdf + 1e-10f));
+  scatterFactor = vmin(scatterFactor, vec3(2.5f));
+  ray.tp = to_half(from_half(ray.tp) * scatterFactor);
+  if (needsMIS && !isinf(spdf)) {
+    float pdf_s = phase_pdf(p, g, wo, ray.dir);
+    float pdf_l = env_pdf(p, ray.dir);
+    ray.misWeight = pdf_s / (pdf_s + pdf_l);
+  } else {
+    ray.misWeight = 1.f;
+  }
+}
+
+__device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
+  if (frag.x > 0.f) acc.x += frag.x;
+  if (frag.y > 0.f) acc.y += frag.y;
+  if (frag.z > 0.f) acc.z += frag.z;
+}
+
+template <class Store>
+__global__ void __launch_bounds__(128) render_kernel(const RenderParams p, const Store store) {
+  // 16x8 pixels per block; each warp an 8x4 patch
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ix = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const int iy = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  TraceCounters cnt{0, 0, 0, 0};
+  if (ix < p.W && iy < p.H) {
+    const size_t pix = (size_t)iy * p.W + ix;
+    float4 acc = p.accumIdStart == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : p.accum[pix];
+    const float aspect = (float)p.W / (float)p.H;
+    for (int s = 0; s < p.spp; s++) {
+      const int accumID = p.accumIdStart + s;
+      // ---- _generateRays (generateRays.cu:72-243) ----
+      PathRay ray;
+      {
+        Random rand = Random::from_pair((unsigned)(ix + p.W * accumID), (unsigned)(iy + p.H * accumID));
+        ray.seed = seeded((uint32_t)(ix + accumID * p.W), (uint32_t)iy);
+        float pixel_u = (accumID == 0) ? .5f : rand();
+        float pixel_v = (accumID == 0) ? .5f : rand();
+        float image_u = ((float)ix + pixel_u) / (float)p.W;
+        float image_v = ((float)iy + pixel_v) / (float)p.H;
+        vec3 d = p.dir00 + (1.f * aspect * (image_u - .5f)) * p.du + (1.f * (image_v - .5f)) * p.dv;
+        ray.org = p.lens00;
+        ray.dir = normalize(d);
+        ray.tMax = 1e30f;
+        ray.tp = to_half(vec3(1.f));
+        ray.misWeight = 0.f;
+        ray.numVolumeBounces = 0;
+      }
+      float4 miss;
+      {
+        const float t = ((float)iy + .5f) / (float)p.H;
+        miss = p.bg;
+        if (!(p.bg.w >= 0.f)) {
+          miss.x = (1.0f - t) * 0.9f + t * 0.15f;
+          miss.y = (1.0f - t) * 0.9f + t * 0.25f;
+          miss.z = (1.0f - t) * 0.9f + t * .8f;
+          miss.w = (1.0f - t) * 1.f + t * 1.f;
+        }
+      }
+      const float clampMax = 10.f * (float)(1 + accumID);
+      bool rayAlive = true, sValid = false;
+      PathRay sray;
+      for (int gen = 0; (rayAlive || sValid) && gen < 16; gen++) {
+        bool nsValid = false;
+        PathRay nsray;
+        if (sValid) {
+          // shadow ray: adds misWeight*throughput when nothing blocks it
+          Hit sh = trace_volume(p.F, store, p.xf, p.G, sray.org, sray.dir, sray.tMax, sray.seed, cnt);
+          if (!sh.hit) {
+            vec3 frag = vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax));
+            accum_add(acc, frag);
+          }
+          sValid = false;
+        }
+        if (rayAlive) {
+          Hit h = trace_volume(p.F, store, p.xf, p.G, ray.org, ray.dir, ray.tMax, ray.seed, cnt);
+          vec3 frag(0.f);
+          float alpha = 0.f;
+          if (!h.hit) {
+            if (gen == 0) {
+              alpha = miss.w;
+              frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
+            } else {
+              frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
+            }
+            ray.tMax = -1.f;
+          } else {
+            if (gen == 0) alpha = 1.f;
+            ShadeOut so;
+            bounce_volume_hit(p, ray, h, gen, so);
+            if (so.shadowValid && so.shadow.tMax > 0.f) {
+              nsray = so.shadow;
+              nsValid = true;
+            }
+          }
+          frag = vmin(frag, vec3(clampMax));
+          if (accumID == 0 && gen == 0) {
+            acc = make_float4(frag.x, frag.y, frag.z, alpha);
+          } else {
+            if (gen == 0 && alpha > 0.f) acc.w += alpha;
+            accum_add(acc, frag);
+          }
+          rayAlive = ray.tMax > 0.f;
+        }
+        if (nsValid) {
+          sray = nsray;
+          sValid = true;
+        }
+      }
+    }
+    p.accum[pix] = acc;
+  }
+  if (p.counters) {
+    // warp-reduce the counters, one atomic per warp and counter
+    unsigned long long v[4] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      unsigned long long x = v[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0 && x) atomicAdd(p.counters + k, x);
+    }
+  }
+}
+
+// -------------------------------------------------------------------------
+// host side
+// -------------------------------------------------------------------------
+static M3 inverse3(const M3 &m) {
+  vec3 a = cross(m.vy, m.vz), b = cross(m.vz, m.vx), c = cross(m.vx, m.vy);
+  float det = dot(m.vx, a);
+  float r = 1.f / det;
+  M3 t;
+  t.vx = vec3(a.x, b.x, c.x) * r;
+  t.vy = vec3(a.y, b.y, c.y) * r;
+  t.vz = vec3(a.z, b.z, c.z) * r;
+  return t;
+}
+
+bool make_field_geom(const gbv_scene *s, FieldGeom &F) {
+  for (int i = 0; i < 3; i++) {
+    F.N[i] = s->dims[i];
+    F.C[i] = s->dims[i] - 1;
+  }
+  F.origin = vec3(s->origin[0], s->origin[1], s->origin[2]);
+  vec3 spacing(s->spacing[0], s->spacing[1], s->spacing[2]);
+  F.rcpSpacing = rcp(spacing);
+  F.boundsLo = F.origin;
+  F.boundsHi = F.origin + spacing * vec3((float)F.C[0], (float)F.C[1], (float)F.C[2]);
+  return true;
+}
+
+void commit_camera(const float pos[3], const float dir[3], const float up[3], float fovy, vec3 &lens00,
+                   vec3 &dir00, vec3 &du, vec3 &dv) {
+  // PerspectiveCamera::set3f("direction") normalizes; commit() (Camera.cu:83-97)
+  vec3 direction = normalize(vec3(dir[0], dir[1], dir[2]));
+  vec3 vup(up[0], up[1], up[2]);
+  vec3 d00 = normalize(direction);
+  vec3 ddu = normalize(cross(d00, vup));
+  vec3 ddv = normalize(cross(ddu, d00));
+  d00 = d00 * (float)(1.f / (2.0f * tanf((0.5f * fovy) * (float)M_PI / 180.0f)));
+  lens00 = vec3(pos[0], pos[1], pos[2]);
+  dir00 = d00;
+  du = ddu;
+  dv = ddv;
+}
+
+static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
+  make_field_geom(s, p.F);
+  p.xf.v = reinterpret_cast<const float4 *>(s->d_tf);
+  p.xf.n = s->tf_n;
+  p.xf.lo = s->domain[0];
+  p.xf.span = s->domain[1] - s->domain[0];
+  p.xf.baseDensity = s->base_density;
+  int M[3];
+  gbv_status st = gbv_mc_dims(s->dims, s->cells_per_mc, M);
+  if (st != GBV_OK) return st;
+  p.G.maj = s->d_majorants;
+  for (int i = 0; i < 3; i++) p.G.M[i] = M[i];
+  p.G.origin = p.F.boundsLo;
+  p.G.spacing = vec3((float)s->cells_per_mc) * vec3(s->spacing[0], s->spacing[1], s->spacing[2]);
+  commit_camera(s->cam_pos, s->cam_dir, s->cam_up, s->fovy, p.lens00, p.dir00, p.du, p.dv);
+  p.numDir = s->num_dir_lights < 0 ? 0 : (s->num_dir_lights > 4 ? 4 : s->num_dir_lights);
+  for (int i = 0; i < p.numDir; i++) {
+    p.dir[i].direction = normalize(vec3(s->dir_light_dir[i][0], s->dir_light_dir[i][1], s->dir_light_dir[i][2]));
+    p.dir[i].color = vec3(s->dir_light_color[i][0], s->dir_light_color[i][1], s->dir_light_color[i][2]);
+    p.dir[i].radiance = s->dir_light_radiance[i];
+  }
+  p.hasEnv = s->d_env_texels != nullptr;
+  if (p.hasEnv) {
+    if (!s->d_env_cdf_x || !s->d_env_cdf_y || s->env_dims[0] <= 0 || s->env_dims[1] <= 0)
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "env map needs texels, both CDF tables and positive dims");
+    EnvDev &e = p.env;
+    e.tex = reinterpret_cast<const float4 *>(s->d_env_texels);
+    e.cdf_y = s->d_env_cdf_y;
+    e.cdf_x = s->d_env_cdf_x;
+    e.W = s->env_dims[0];
+    e.H = s->env_dims[1];
+    e.addr[0] = s->env_addr[0];
+    e.addr[1] = s->env_addr[1];
+    e.scale = s->env_scale;
+    // EnvMap.cu:164-179
+    vec3 up(s->env_up[0], s->env_up[1], s->env_up[2]);
+    vec3 dir(s->env_dir[0], s->env_dir[1], s->env_dir[2]);
+    e.toWorld.vz = -normalize(up);
+    e.toWorld.vy = -normalize(cross(e.toWorld.vz, dir));
+    e.toWorld.vx = normalize(cross(e.toWorld.vy, e.toWorld.vz));
+    e.toLocal = inverse3(e.toWorld);
+  }
+  p.bg = make_float4(s->bg_color[0], s->bg_color[1], s->bg_color[2], s->bg_color[3]);
+  p.ambient = s->ambient_radiance;
+  p.multi = s->multi_scatter;
+  p.volMS = s->volume_multi_scatter;
+  p.maxVB = s->max_volume_bounces;
+  p.aniso = s->anisotropy;
+  p.scatAlb = s->scattering_albedo;
+  return GBV_OK;
+}
+
+template <class Store>
+static gbv_status launch_render(const RenderParams &p, const Store &store, cudaStream_t stream) {
+  dim3 grid((p.W + 15) / 16, (p.H + 7) / 8), block(128);
+  render_kernel<Store><<<grid, block, 0, stream>>>(p, store);
+  return check_launch("render_kernel");
+}
+
+}  // namespace gbv
+
+using namespace gbv;
+
+extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
+                                 int spp, unsigned long long *d_counters, void *stream) {
+  if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: null pointer or non-positive size");
+  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: scene lacks voxels, majorants or a transfer function");
+  if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: the linear layout holds FP32 voxels only");
+  if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: U8 voxels need the brick scale/offset table");
+  if (spp == 0) return GBV_OK;
+  RenderParams p;
+  gbv_status st = fill_params(s, p);
+  if (st != GBV_OK) return st;
+  p.W = width;
+  p.H = height;
+  p.accum = reinterpret_cast<float4 *>(d_accum);
+  p.accumIdStart = accum_id_start;
+  p.spp = spp;
+  p.counters = d_counters;
+  cudaStream_t cs = (cudaStream_t)stream;
+  if (s->layout == GBV_LAYOUT_LINEAR) {
+    StoreLinearF32 store{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
+    return launch_render(p, store, cs);
+  }
+  if (s->layout != GBV_LAYOUT_BRICK_CORNERS) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown layout");
+  int nb[3];
+  brick_counts(s->dims, nb);
+  switch (s->format) {
+    case GBV_VOXEL_F32:
+      return launch_render(p, StoreBrickCorners<GBV_VOXEL_F32>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
+    case GBV_VOXEL_F16:
+      return launch_render(p, StoreBrickCorners<GBV_VOXEL_F16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
+    case GBV_VOXEL_BF16:
+      return launch_render(p, StoreBrickCorners<GBV_VOXEL_BF16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
+    case GBV_VOXEL_U8_SCALED:
+      return launch_render(p,
+                           StoreBrickCorners<GBV_VOXEL_U8_SCALED>{
+                               s->d_voxels, reinterpret_cast<const float2 *>(s->d_scale_offset), nb[0], nb[1]},
+                           cs);
+  }
+  return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown voxel format");
+}

@@ -1,0 +1,263 @@
+// storage.cu -- brick-corner voxel stores and env-map importance tables.
+#include <cuda_runtime.h>
+#include "gbv_volume.cuh"
+#include "gbv_internal.h"
+
+namespace gbv {
+
+__global__ void mc_ranges_kernel(const float *__restrict__ scalars, int nx, int ny, int nz, int cpm, int mx_,
+                                 int my_, int mz_, float2 *__restrict__ ranges);
+
+// One thread per cell of the padded brick grid, in store order, so each
+// thread writes one contiguous 8-voxel record.
+template <int FMT>
+__global__ void brick_store_kernel(const float *__restrict__ s, int nx, int ny, int nz, int nbx, int nby,
+                                   long long numCells, const float2 *__restrict__ lohi, void *__restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= numCells) return;
+  const long long brick = t >> 9;
+  const int local = (int)(t & 511);
+  const int bx = (int)(brick % nbx), by = (int)((brick / nbx) % nby), bz = (int)(brick / ((long long)nbx * nby));
+  const int cx = bx * 8 + (local & 7), cy = by * 8 + ((local >> 3) & 7), cz = bz * 8 + (local >> 6);
+  float c[8];
+  if (cx < nx - 1 && cy < ny - 1 && cz < nz - 1) {
+    const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+    const size_t b = (size_t)cx + sy * cy + sz * cz;
+    c[0] = s[b];
+    c[1] = s[b + 1];
+    c[2] = s[b + sy];
+    c[3] = s[b + sy + 1];
+    c[4] = s[b + sz];
+    c[5] = s[b + sz + 1];
+    c[6] = s[b + sz + sy];
+    c[7] = s[b + sz + sy + 1];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; k++) c[k] = 0.f;
+  }
+  if (FMT == GBV_VOXEL_F32) {
+    float4 *o = reinterpret_cast<float4 *>(out) + 2 * t;
+    o[0] = make_float4(c[0], c[1], c[2], c[3]);
+    o[1] = make_float4(c[4], c[5], c[6], c[7]);
+  } else if (FMT == GBV_VOXEL_F16) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      w[k] = (uint32_t)__half_as_ushort(__float2half_rn(c[2 * k])) |
+             ((uint32_t)__half_as_ushort(__float2half_rn(c[2 * k + 1])) << 16);
+    reinterpret_cast<uint4 *>(out)[t] = make_uint4(w[0], w[1], w[2], w[3]);
+  } else if (FMT == GBV_VOXEL_BF16) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      w[k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(c[2 * k])) |
+             ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(c[2 * k + 1])) << 16);
+    reinterpret_cast<uint4 *>(out)[t] = make_uint4(w[0], w[1], w[2], w[3]);
+  } else {
+    // u8 = round(255 (v - min_b) / (max_b - min_b)) over the brick's 9^3 voxels
+    const float2 r = lohi[brick];
+    const float span = r.y - r.x;
+    uint32_t w[2] = {0u, 0u};
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      int q = 0;
+      if (span > 0.f) q = (int)floorf((c[k] - r.x) * (255.f / span) + .5f);
+      q = min(255, max(0, q));
+      w[k >> 2] |= (uint32_t)q << (8 * (k & 3));
+    }
+    reinterpret_cast<uint2 *>(out)[t] = make_uint2(w[0], w[1]);
+  }
+}
+
+__global__ void lohi_to_scale_offset(float2 *so, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 r = so[i];
+  float span = r.y - r.x;
+  so[i] = make_float2(span > 0.f ? span / 255.f : 0.f, r.x);
+}
+
+// ---- env map tables (EnvMap.cu:61-137) ----
+struct EnvTex {
+  const float4 *tex;
+  int W, H, ax, ay;
+};
+__device__ __forceinline__ void env_addr(int mode, float tc, int N, int &i0, int &i1, float &f) {
+  i0 = 0; i1 = 0; f = 0.f;
+  if (mode == GBV_ADDR_WRAP) {
+    tc = tc * (float)N - .5f;
+    tc = fmodf(tc, (float)N);
+    if (tc < 0.f) tc += (float)N;
+    float fc = floorf(tc);
+    int ic = (int)fc;
+    f = tc - (float)ic;
+    i0 = ic;
+    i1 = (int)fmodf(tc + 1.f, (float)N);
+  } else if (mode == GBV_ADDR_MIRROR) {
+    tc = tc * (float)N + .5f;
+    float fc = floorf(tc);
+    int ic = (int)fc;
+    f = tc - (float)ic;
+    int a = ic - 1, b = ic;
+    if (a < 0) a = -a;
+    if (b < 0) b = -b;
+    a = a % (2 * N);
+    b = b % (2 * N);
+    if (a >= N) a = 2 * N - 1 - a;
+    if (b >= N) b = 2 * N - 1 - b;
+    i0 = a;
+    i1 = b;
+  } else if (mode == GBV_ADDR_CLAMP) {
+    tc = tc * (float)N;
+    if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; }
+    else if (tc - .5f >= (float)(N - 1)) { i0 = i1 = N - 1; f = 0.f; }
+    else {
+      f = (tc - .5f) - (float)(int)(tc - .5f);
+      i0 = (int)(tc - .5f);
+      i1 = i0 + 1;
+    }
+  }
+}
+__device__ __forceinline__ float4 env_lerp(float f, float4 a, float4 b) {
+  return make_float4((1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
+                     (1.f - f) * a.w + f * b.w);
+}
+__device__ __forceinline__ float4 env_tex2D(const EnvTex &e, float u, float v) {
+  int x0, x1, y0, y1;
+  float fx, fy;
+  env_addr(e.ax, u, e.W, x0, x1, fx);
+  env_addr(e.ay, v, e.H, y0, y1, fy);
+  float4 v00 = e.tex[x0 + (size_t)y0 * e.W], v01 = e.tex[x1 + (size_t)y0 * e.W];
+  float4 v10 = e.tex[x0 + (size_t)y1 * e.W], v11 = e.tex[x1 + (size_t)y1 * e.W];
+  return env_lerp(fy, env_lerp(fx, v00, v01), env_lerp(fx, v10, v11));
+}
+__global__ void env_weights_kernel(EnvTex e, float *cdf_x) {
+  int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= e.W || iy >= e.H) return;
+  float weight = 0.f;
+  for (int iiy = 0; iiy <= 2; iiy++)
+    for (int iix = 0; iix <= 2; iix++) {
+      float4 t = env_tex2D(e, ((float)ix + (float)iix * .5f) / (float)e.W, ((float)iy + (float)iiy * .5f) / (float)e.H);
+      weight = mx(weight, mx(mx(t.x, t.y), t.z));
+    }
+  cdf_x[ix + (size_t)e.W * iy] = weight;
+}
+__global__ void env_lines_kernel(int W, int H, float *cdf_y, float *cdf_x) {
+  int y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= H) return;
+  float *line = cdf_x + (size_t)y * W;
+  float sum = 0.f;
+  for (int ix = 0; ix < W; ix++) sum += line[ix];
+  float rcp_sum = 1.f / sum;
+  sum = 0.f;
+  for (int ix = 0; ix < W; ix++) {
+    sum += line[ix];
+    line[ix] = sum * rcp_sum;
+  }
+  line[W - 1] = 1.f;
+  float rel_y = ((float)y + .5f) / (float)H;
+  const float theta = kPi * rel_y;
+  cdf_y[y] = sum * sinf(theta);
+}
+__global__ void env_normalize_kernel(int H, float *cdf_y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float sum = 0.f;
+  for (int i = 0; i < H; i++) sum += cdf_y[i];
+  float rcp_sum = 1.f / sum;
+  sum = 0.f;
+  for (int i = 0; i < H; i++) {
+    sum += cdf_y[i];
+    cdf_y[i] = sum * rcp_sum;
+  }
+  cdf_y[H - 1] = 1.f;
+}
+
+}  // namespace gbv
+
+using namespace gbv;
+
+extern "C" {
+
+gbv_status gbv_brick_store_bytes(const int dims[3], int format, size_t *voxel_bytes, size_t *scale_offset_bytes) {
+  if (!dims || !voxel_bytes) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_brick_store_bytes: null pointer");
+  int nb[3];
+  brick_counts(dims, nb);
+  size_t bricks = (size_t)nb[0] * nb[1] * nb[2];
+  size_t cells = bricks * kBrickCells;
+  size_t elem = 0;
+  switch (format) {
+    case GBV_VOXEL_F32: elem = 4; break;
+    case GBV_VOXEL_F16:
+    case GBV_VOXEL_BF16: elem = 2; break;
+    case GBV_VOXEL_U8_SCALED: elem = 1; break;
+    default: return set_error(GBV_ERROR_UNSUPPORTED, "gbv_brick_store_bytes: unknown format");
+  }
+  *voxel_bytes = cells * 8 * elem;
+  if (scale_offset_bytes) *scale_offset_bytes = format == GBV_VOXEL_U8_SCALED ? bricks * 2 * sizeof(float) : 0;
+  return GBV_OK;
+}
+
+gbv_status gbv_build_brick_store(const float *d_scalars, const int dims[3], int format, void *d_voxels,
+                                 float *d_scale_offset, void *stream) {
+  if (!d_scalars || !dims || !d_voxels) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: null");
+  if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: a volume needs at least 2 voxels per axis");
+  if (format == GBV_VOXEL_U8_SCALED && !d_scale_offset)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: U8 needs the scale/offset table");
+  int nb[3];
+  brick_counts(dims, nb);
+  long long bricks = (long long)nb[0] * nb[1] * nb[2];
+  long long cells = bricks * kBrickCells;
+  cudaStream_t cs = (cudaStream_t)stream;
+  unsigned blocks = (unsigned)((cells + 255) / 256);
+  float2 *lohi = reinterpret_cast<float2 *>(d_scale_offset);
+  switch (format) {
+    case GBV_VOXEL_F32:
+      brick_store_kernel<GBV_VOXEL_F32><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0], nb[1],
+                                                                cells, nullptr, d_voxels);
+      break;
+    case GBV_VOXEL_F16:
+      brick_store_kernel<GBV_VOXEL_F16><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0], nb[1],
+                                                                cells, nullptr, d_voxels);
+      break;
+    case GBV_VOXEL_BF16:
+      brick_store_kernel<GBV_VOXEL_BF16><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0],
+                                                                 nb[1], cells, nullptr, d_voxels);
+      break;
+    case GBV_VOXEL_U8_SCALED: {
+      // brick (min,max) over 9^3 voxels = the 8-cell macrocell range
+      mc_ranges_kernel<<<(unsigned)((bricks + 7) / 8), 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], 8, nb[0],
+                                                                     nb[1], nb[2], lohi);
+      gbv_status st = check_launch("brick ranges");
+      if (st != GBV_OK) return st;
+      brick_store_kernel<GBV_VOXEL_U8_SCALED><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0],
+                                                                       nb[1], cells, lohi, d_voxels);
+      st = check_launch("brick_store_kernel");
+      if (st != GBV_OK) return st;
+      lohi_to_scale_offset<<<(unsigned)((bricks + 255) / 256), 256, 0, cs>>>(lohi, bricks);
+      break;
+    }
+    default:
+      return set_error(GBV_ERROR_UNSUPPORTED, "gbv_build_brick_store: unknown format");
+  }
+  return check_launch("brick_store_kernel");
+}
+
+gbv_status gbv_env_build_cdfs(const float *d_texels, int width, int height, const int addr[2], float *d_cdf_y,
+                              float *d_cdf_x, void *stream) {
+  if (!d_texels || !d_cdf_y || !d_cdf_x || width <= 0 || height <= 0 || !addr)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_env_build_cdfs: bad argument");
+  cudaStream_t cs = (cudaStream_t)stream;
+  EnvTex e{reinterpret_cast<const float4 *>(d_texels), width, height, addr[0], addr[1]};
+  dim3 bs(16, 16), nb((width + 15) / 16, (height + 15) / 16);
+  env_weights_kernel<<<nb, bs, 0, cs>>>(e, d_cdf_x);
+  gbv_status st = check_launch("env_weights_kernel");
+  if (st != GBV_OK) return st;
+  env_lines_kernel<<<(height + 127) / 128, 128, 0, cs>>>(width, height, d_cdf_y, d_cdf_x);
+  st = check_launch("env_lines_kernel");
+  if (st != GBV_OK) return st;
+  env_normalize_kernel<<<1, 1, 0, cs>>>(height, d_cdf_y);
+  return check_launch("env_normalize_kernel");
+}
+
+}  // extern "C"

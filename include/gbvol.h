@@ -1,0 +1,210 @@
+/* gbvol.h -- low-level C-ABI of the GB300 structured-volume path.
+ *
+ * Plain pointers and sizes only.  Pointers named d_* are device (HBM)
+ * pointers on the current CUDA device; `stream` is a cudaStream_t passed as
+ * void* (0 = legacy default stream).  Every entry point returns a gbv_status
+ * and never throws; gbv_last_error() gives the message of the last failure on
+ * the calling thread.
+ *
+ * These entry points are what the reference's internal volume seam would bind
+ * for this path (one per reference kernel / launcher); the barney-compatible
+ * bn* surface in barney_gb300.h is built on top of them.
+ */
+#ifndef GBVOL_H
+#define GBVOL_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gbv_status {
+  GBV_OK = 0,
+  GBV_ERROR_INVALID_ARGUMENT = 1,
+  GBV_ERROR_CUDA = 2,
+  GBV_ERROR_OUT_OF_MEMORY = 3,
+  /* a device loop hit its iteration cap; results of that launch are partial */
+  GBV_ERROR_LIMIT = 4,
+  GBV_ERROR_UNSUPPORTED = 5
+} gbv_status;
+
+/* voxel storage formats */
+enum {
+  GBV_VOXEL_F32 = 0,
+  GBV_VOXEL_F16 = 1,
+  GBV_VOXEL_BF16 = 2,
+  GBV_VOXEL_U8_SCALED = 3 /* uint8 with a float (scale, offset) per 8^3-cell brick */
+};
+/* voxel layouts */
+enum {
+  GBV_LAYOUT_LINEAR = 0,       /* x-fastest scalars, FP32 only (the reference's texel array) */
+  GBV_LAYOUT_BRICK_CORNERS = 1 /* 8^3-cell bricks; each cell stores its 8 corner voxels */
+};
+/* frame-buffer read formats (BNDataType subset) */
+enum { GBV_FB_FLOAT4 = 0, GBV_FB_RGBA8 = 1, GBV_FB_RGBA8_SRGB = 2 };
+/* texture address modes (BNTextureAddressMode order) */
+enum { GBV_ADDR_WRAP = 0, GBV_ADDR_CLAMP = 1, GBV_ADDR_BORDER = 2, GBV_ADDR_MIRROR = 3 };
+
+const char *gbv_last_error(void);
+int gbv_version(void);
+
+/* ------------------------------------------------------------------------
+ * Macrocells.
+ * ------------------------------------------------------------------------ */
+
+/* Macrocell grid dimensions: ceil((dims-1)/cells_per_mc) per axis.
+   Replaces StructuredData::buildMCs's mcDims computation
+   (barney/volume/StructuredData.cu:73). */
+gbv_status gbv_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
+
+/* Per-macrocell scalar range (min, max) over the (cells_per_mc+1)^3 voxel
+   footprint of each macrocell, from an FP32 x-fastest scalar array.
+   d_ranges: 2 floats per macrocell, x-fastest.
+   Replaces StructuredData_computeMCs (barney/volume/StructuredData.cu:29-61)
+   and MCGrid::clearCells (barney/volume/MCGrid.cu:63-91). */
+gbv_status gbv_build_mc_ranges(const float *d_scalars, const int dims[3],
+                               int cells_per_mc, float *d_ranges, void *stream);
+
+/* Majorant of each macrocell = the transfer function's maximum opacity over
+   its range times base_density.  Bit-identical to the reference's FP32.
+   d_tf: tf_n RGBA float entries.
+   Replaces mapMCs / TransferFunction::DD::majorant
+   (barney/volume/MCGrid.cu:94-116, barney/volume/TransferFunction.h:91-116). */
+gbv_status gbv_map_majorants(const float *d_ranges, int num_mc,
+                             const float *d_tf, int tf_n, float domain_lo,
+                             float domain_hi, float base_density,
+                             float *d_majorants, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Voxel storage.
+ * ------------------------------------------------------------------------ */
+
+/* Bytes needed for the brick-corner store of a volume (voxels; for
+   GBV_VOXEL_U8_SCALED also *scale_offset_bytes for the brick table). */
+gbv_status gbv_brick_store_bytes(const int dims[3], int format,
+                                 size_t *voxel_bytes, size_t *scale_offset_bytes);
+
+/* Re-lays an FP32 x-fastest volume as 8^3-cell bricks in `format`.
+   Replaces the texel upload of StructuredData::setObject("textureData")
+   (barney/volume/StructuredData.cu:154-173, rtcore/cudaCommon/TextureData.cu:59-75). */
+gbv_status gbv_build_brick_store(const float *d_scalars, const int dims[3],
+                                 int format, void *d_voxels,
+                                 float *d_scale_offset, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Scene description for rendering (device pointers where marked d_).
+ * ------------------------------------------------------------------------ */
+typedef struct gbv_scene {
+  /* structured field */
+  const void *d_voxels;          /* per layout/format */
+  const float *d_scale_offset;   /* U8_SCALED only */
+  int format, layout;
+  int dims[3];
+  float origin[3], spacing[3];
+  /* macrocells (from gbv_map_majorants) */
+  const float *d_majorants;
+  int cells_per_mc;
+  /* transfer function */
+  const float *d_tf;
+  int tf_n;
+  float domain[2];
+  float base_density;
+  float anisotropy, scattering_albedo;
+  /* perspective camera parameters */
+  float cam_pos[3], cam_dir[3], cam_up[3];
+  float fovy;
+  /* directional lights (at most 4) */
+  int num_dir_lights;
+  float dir_light_dir[4][3];
+  float dir_light_color[4][3];
+  float dir_light_radiance[4];
+  /* env-map light: d_env_texels == 0 means none */
+  const float *d_env_texels;     /* RGBA float */
+  const float *d_env_cdf_y;      /* env_dims[1] */
+  const float *d_env_cdf_x;      /* env_dims[0]*env_dims[1] */
+  int env_dims[2];
+  int env_addr[2];
+  float env_dir[3], env_up[3];
+  float env_scale;
+  /* renderer */
+  float bg_color[4];
+  float ambient_radiance;
+  int multi_scatter;             /* 0 default build (single scatter), 1 multi-scatter build */
+  int volume_multi_scatter;
+  int max_volume_bounces;
+} gbv_scene;
+
+/* Counters written by gbv_render when d_counters != 0 (uint64 each):
+   [0] density samples, [1] macrocells entered with a non-zero majorant,
+   [2] rays traced, [3] loop-cap events. */
+enum { GBV_COUNTER_SAMPLES = 0, GBV_COUNTER_MC_VISITS = 1, GBV_COUNTER_RAYS = 2,
+       GBV_COUNTER_CAPS = 3, GBV_NUM_COUNTERS = 4 };
+
+/* Env-map importance tables (d_cdf_y: H floats, d_cdf_x: W*H floats) from
+   RGBA float texels.  Replaces EnvMapLight::computeCDFs
+   (barney/light/EnvMap.cu:61-137, 181-238). */
+gbv_status gbv_env_build_cdfs(const float *d_texels, int width, int height,
+                              const int addr[2], float *d_cdf_y, float *d_cdf_x,
+                              void *stream);
+
+/* Renders `spp` accumulation passes (accumIDs accum_id_start ..
+   accum_id_start+spp-1) into d_accum (width*height RGBA float, row-major,
+   row 0 the bottom row), accumulating as the reference does: the first pass
+   of a fresh frame (accum_id_start == 0) overwrites.  d_counters: optional,
+   GBV_NUM_COUNTERS uint64 (accumulated, not cleared).
+   Replaces Context::renderTiles' generate/trace/shade loop
+   (barney/Context.cpp:142-185; barney/kernels/generateRays.cu:44-243,
+   traceRays.dev.cu:20-52, shadeRays.cu:881-1041;
+   barney/volume/MCAccelerator.h:569-708). */
+gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
+                      int height, int accum_id_start, int spp,
+                      unsigned long long *d_counters, void *stream);
+
+/* Frame-buffer read: d_accum * (1/accum_id) into d_out as float4, RGBA8 or
+   sRGB RGBA8.  Replaces linearizeColorAndNormalKernel
+   (barney/fb/TiledFB.cu:13-50) with LocalFB::gatherColorChannel's
+   accumScale (barney/fb/LocalFB.cpp:60-70). */
+gbv_status gbv_tonemap(const float *d_accum, int width, int height,
+                       int accum_id, int format, void *d_out, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Fixed-step emission-absorption march and its adjoint (no counterpart in
+ * the reference, which only delta-tracks).
+ * ------------------------------------------------------------------------ */
+typedef struct gbv_ea_view {
+  float pos[3], dir[3], up[3];
+  float fovy;
+  int width, height;
+} gbv_ea_view;
+
+/* Renders num_views views into d_images (views packed back to back, each
+   width*height RGBA float).  FP32 with compensated optical depth. */
+gbv_status gbv_ea_render(const gbv_scene *scene, const gbv_ea_view *views,
+                         int num_views, float step, float *d_images,
+                         void *stream);
+/* Same march in FP64 (finite-difference check mode); d_images are doubles. */
+gbv_status gbv_ea_render_f64(const gbv_scene *scene, const gbv_ea_view *views,
+                             int num_views, float step, double *d_images,
+                             void *stream);
+/* Adjoint by path replay: given the forward images and dL/dimage, adds
+   dL/dvoxel into d_grad_scalars (FP32, x-fastest, dims) and dL/dTF into
+   d_grad_tf (tf_n*4).  The scene's field must be FP32 LINEAR. */
+gbv_status gbv_ea_backward(const gbv_scene *scene, const gbv_ea_view *views,
+                           int num_views, float step, const float *d_images,
+                           const float *d_grad_images, float *d_grad_scalars,
+                           float *d_grad_tf, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Synthetic inputs (host memory; no GPU needed).
+ * ------------------------------------------------------------------------ */
+/* Blob-plus-noise volume: clamp(sum_i a_i exp(-|x-c_i|^2/(2 s_i^2))
+   + U[0,noise] + fBm, 0, 1) on the unit cube, x-fastest, FP32. */
+gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
+                               float noise_amplitude, int fbm_octaves,
+                               float fbm_amplitude, int nthreads, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBVOL_H */

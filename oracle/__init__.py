@@ -1,0 +1,240 @@
+"""CPU oracle (TEST INFRASTRUCTURE ONLY) for the structured-volume path.
+
+A restatement of the reference renderer's embree (CPU) backend for this path
+(gbv_oracle.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg may use it, and only as the checker.
+
+parity unpinned: the reference ships no golden vectors for this path and its
+sources cannot be built here; see gbv_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+_f3 = C.c_float * 3
+
+
+class OrcScene(C.Structure):
+    _fields_ = [
+        ("scalars", C.c_void_p), ("dims", C.c_int * 3), ("origin", _f3), ("spacing", _f3),
+        ("cells_per_mc", C.c_int), ("majorants", C.c_void_p),
+        ("tf", C.c_void_p), ("tf_n", C.c_int), ("domain", C.c_float * 2), ("base_density", C.c_float),
+        ("anisotropy", C.c_float), ("scattering_albedo", C.c_float),
+        ("cam_pos", _f3), ("cam_dir", _f3), ("cam_up", _f3), ("fovy", C.c_float),
+        ("num_dir_lights", C.c_int), ("dir_light_dir", _f3 * 4), ("dir_light_color", _f3 * 4),
+        ("dir_light_radiance", C.c_float * 4),
+        ("env_texels", C.c_void_p), ("env_dims", C.c_int * 2), ("env_addr", C.c_int * 2),
+        ("env_dir", _f3), ("env_up", _f3), ("env_scale", C.c_float),
+        ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
+        ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
+        ("width", C.c_int), ("height", C.c_int),
+    ]
+
+
+class OrcStats(C.Structure):
+    _fields_ = [("density_samples", C.c_uint64), ("mc_visits", C.c_uint64), ("rays", C.c_uint64)]
+
+
+class OrcEAView(C.Structure):
+    _fields_ = [("pos", _f3), ("dir", _f3), ("up", _f3), ("fovy", C.c_float),
+                ("width", C.c_int), ("height", C.c_int)]
+
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        sp = C.POINTER(OrcScene)
+        sigs = {
+            "orc_rng_sequence": (None, [C.c_uint32, C.c_uint32, i, vp]),
+            "orc_rng_from_seed": (None, [C.c_uint64, C.c_uint64, i, i, vp, C.POINTER(C.c_uint64)]),
+            "orc_fast_log": (f, [f]),
+            "orc_float_to_half": (C.c_uint16, [f]),
+            "orc_half_to_float": (f, [C.c_uint16]),
+            "orc_sample_points": (None, [sp, vp, i, vp]),
+            "orc_tf_map": (None, [sp, vp, i, vp]),
+            "orc_mc_dims": (None, [vp, i, vp]),
+            "orc_mc_ranges": (None, [vp, vp, i, vp]),
+            "orc_majorants": (None, [vp, i, vp, i, f, f, f, vp]),
+            "orc_trace_ray": (i, [sp, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float), vp]),
+            "orc_render": (None, [sp, vp, i, i, i, i, i, i, C.POINTER(OrcStats)]),
+            "orc_tonemap": (None, [vp, i, i, i, i, vp]),
+            "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
+            "orc_ea_render": (None, [sp, C.POINTER(OrcEAView), i, f, i, i, vp]),
+            "orc_ea_backward": (None, [sp, C.POINTER(OrcEAView), i, f, vp, i, vp, vp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """Oracle view of a barney_gb300.scenes.Scene (keeps its arrays alive)."""
+
+    def __init__(self, scene, scalars=None, majorants=None):
+        self.s = scene
+        self.scalars = np.ascontiguousarray(scene.scalars if scalars is None else scalars, dtype=np.float32)
+        self.tf = np.ascontiguousarray(scene.tf, dtype=np.float32)
+        self.majorants = None if majorants is None else np.ascontiguousarray(majorants, dtype=np.float32)
+        self.env = None if scene.env is None else np.ascontiguousarray(scene.env.texels, dtype=np.float32)
+        r = OrcScene()
+        nz, ny, nx = self.scalars.shape
+        r.scalars = self.scalars.ctypes.data
+        r.dims[:] = [nx, ny, nz]
+        origin, spacing = scene.geometry()
+        r.origin[:] = list(origin)
+        r.spacing[:] = list(spacing)
+        r.cells_per_mc = scene.cells_per_mc
+        r.majorants = None if self.majorants is None else self.majorants.ctypes.data
+        r.tf = self.tf.ctypes.data
+        r.tf_n = self.tf.shape[0]
+        r.domain[:] = list(scene.domain)
+        r.base_density = scene.base_density
+        r.anisotropy, r.scattering_albedo = scene.anisotropy, scene.scattering_albedo
+        r.cam_pos[:] = list(scene.cam_pos)
+        r.cam_dir[:] = list(scene.cam_dir)
+        r.cam_up[:] = list(scene.cam_up)
+        r.fovy = scene.fovy
+        r.num_dir_lights = len(scene.dir_lights)
+        for i, (d, c, rad) in enumerate(scene.dir_lights[:4]):
+            r.dir_light_dir[i][:] = list(d)
+            r.dir_light_color[i][:] = list(c)
+            r.dir_light_radiance[i] = rad
+        if self.env is not None:
+            e = scene.env
+            H, W, _ = self.env.shape
+            r.env_texels = self.env.ctypes.data
+            r.env_dims[:] = [W, H]
+            r.env_addr[:] = list(e.addr)
+            r.env_dir[:] = list(e.direction)
+            r.env_up[:] = list(e.up)
+            r.env_scale = e.scale
+        r.bg_color[:] = list(scene.bg_color)
+        r.ambient_radiance = scene.ambient
+        r.multi_scatter = scene.multi_scatter
+        r.volume_multi_scatter = scene.volume_multi_scatter
+        r.max_volume_bounces = scene.max_volume_bounces
+        r.width, r.height = scene.width, scene.height
+        self.rec = r
+
+    # -- macrocells --
+    def mc_dims(self):
+        out = (C.c_int * 3)()
+        lib().orc_mc_dims((C.c_int * 3)(*self.rec.dims), self.s.cells_per_mc, out)
+        return tuple(out)
+
+    def mc_ranges(self) -> np.ndarray:
+        M = self.mc_dims()
+        out = np.empty((M[0] * M[1] * M[2], 2), dtype=np.float32)
+        lib().orc_mc_ranges(_p(self.scalars), (C.c_int * 3)(*self.rec.dims), self.s.cells_per_mc, _p(out))
+        return out
+
+    def majorants_of(self, ranges: np.ndarray) -> np.ndarray:
+        out = np.empty(ranges.shape[0], dtype=np.float32)
+        lib().orc_majorants(_p(np.ascontiguousarray(ranges, dtype=np.float32)), ranges.shape[0], _p(self.tf),
+                            self.tf.shape[0], self.s.domain[0], self.s.domain[1], self.s.base_density, _p(out))
+        return out
+
+    # -- scalar kernels --
+    def sample(self, P: np.ndarray) -> np.ndarray:
+        P = np.ascontiguousarray(P, dtype=np.float32).reshape(-1, 3)
+        out = np.empty(P.shape[0], dtype=np.float32)
+        lib().orc_sample_points(C.byref(self.rec), _p(P), P.shape[0], _p(out))
+        return out
+
+    def tf_map(self, s: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(s, dtype=np.float32).reshape(-1)
+        out = np.empty((s.shape[0], 4), dtype=np.float32)
+        lib().orc_tf_map(C.byref(self.rec), _p(s), s.shape[0], _p(out))
+        return out
+
+    # -- render --
+    def render(self, spp=None, accum=None, accum_id_start=0, use_double=False, nthreads=0, rows=None):
+        W, H = self.s.width, self.s.height
+        if accum is None:
+            accum = np.zeros((H, W, 4), dtype=np.float32)
+        st = OrcStats()
+        r0, r1 = rows if rows is not None else (0, 0)
+        lib().orc_render(C.byref(self.rec), _p(accum), accum_id_start, self.s.spp if spp is None else spp,
+                         1 if use_double else 0, nthreads, r0, r1, C.byref(st))
+        self.stats = dict(density_samples=st.density_samples, mc_visits=st.mc_visits, rays=st.rays)
+        return accum
+
+    def tonemap(self, accum: np.ndarray, accum_id: int, fmt: int = 0) -> np.ndarray:
+        H, W, _ = accum.shape
+        out = np.empty((H, W, 4), np.float32) if fmt == 0 else np.empty((H, W), np.uint32)
+        lib().orc_tonemap(_p(np.ascontiguousarray(accum, np.float32)), W, H, accum_id, fmt, _p(out))
+        return out
+
+    def env_cdfs(self):
+        H, W, _ = self.env.shape
+        cy = np.empty(H, np.float32)
+        cx = np.empty(H * W, np.float32)
+        lib().orc_env_cdfs(_p(self.env), _p(np.array([W, H], np.int32)),
+                           _p(np.array(list(self.s.env.addr), np.int32)), _p(cy), _p(cx))
+        return cy, cx
+
+    # -- emission-absorption --
+    @staticmethod
+    def _views(views):
+        arr = (OrcEAView * len(views))()
+        for a, v in zip(arr, views):
+            a.pos[:] = list(v["pos"])
+            a.dir[:] = list(v["dir"])
+            a.up[:] = list(v["up"])
+            a.fovy = v["fovy"]
+            a.width, a.height = v["width"], v["height"]
+        return arr
+
+    def ea_render(self, views, step: float, use_double=False, nthreads=0) -> np.ndarray:
+        npx = sum(v["width"] * v["height"] for v in views)
+        out = np.empty((npx, 4), np.float32)
+        lib().orc_ea_render(C.byref(self.rec), self._views(views), len(views), step, 1 if use_double else 0,
+                            nthreads, _p(out))
+        return out
+
+    def ea_backward(self, views, step: float, d_images: np.ndarray, nthreads=0):
+        gv = np.zeros(self.scalars.size, np.float64)
+        gt = np.zeros(self.tf.size, np.float64)
+        lib().orc_ea_backward(C.byref(self.rec), self._views(views), len(views), step,
+                              _p(np.ascontiguousarray(d_images, np.float32)), nthreads, _p(gv), _p(gt))
+        return gv.reshape(self.scalars.shape), gt.reshape(self.tf.shape)
+
+
+def rng_sequence(a: int, b: int, n: int) -> np.ndarray:
+    out = np.empty(n, np.float32)
+    lib().orc_rng_sequence(a, b, n, _p(out))
+    return out
+
+
+def fast_log(f: float) -> float:
+    return lib().orc_fast_log(f)
+
+
+def float_to_half(f: float) -> int:
+    return lib().orc_float_to_half(f)

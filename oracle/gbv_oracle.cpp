@@ -1,0 +1,1580 @@
+// gbv_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// CPU oracle for the structured-volume path: a restatement, in plain C++, of
+// what the reference renderer (Barney 1.1.8) computes on its embree (CPU)
+// backend.  It is the checker for the CUDA product and is never shipped or
+// measured as the product.  Only tests/, __graft_entry__.smoke() and the
+// CPU-baseline leg of bench.py may load it.
+//
+// parity unpinned: the reference holds no golden vectors or known-answer tests
+// for this path (its unitTests/ cover umesh iso-surfaces and an omni camera
+// only) and cannot be compiled here (submodules owl/embree/cuBQL/optix are
+// empty).  The oracle is pinned by hand-computed known-answer tests and by an
+// independent pure-Python restatement of its scalar kernels.
+//
+// Every function names the reference file:line it follows.  The third-party
+// owl math library (owl::common, >= 1.2.9, submodule commit unrecorded) is
+// absent; its semantics are restated in the small vector section below:
+//   rcp(x) = 1.f/x componentwise; min/max as std::min/std::max
+//   ((b<a)?b:a and (a<b)?b:a); clamp(v,lo,hi) = min(hi,max(lo,v));
+//   reduce_min/max = min(min(x,y),z); dot = (x*x'+y*y')+z*z';
+//   normalize(v) = v*(1/sqrt(dot(v,v))); length = sqrt(dot);
+//   interval<float> default-constructs empty (+inf,-inf), extend = min/max,
+//   span() = upper-lower.
+//
+// Build with -ffp-contract=off so that x86-64 and aarch64 hosts give
+// identical FP32 results (no fused multiply-add).
+
+#include "gbv_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// owl-equivalent vector math (restated; see header comment)
+// ---------------------------------------------------------------------------
+template <typename T> inline T mn(T a, T b) { return (b < a) ? b : a; }
+template <typename T> inline T mx(T a, T b) { return (a < b) ? b : a; }
+template <typename T> inline T clampv(T v, T lo, T hi) { return mn(hi, mx(lo, v)); }
+
+template <typename R> struct V3 {
+  R x, y, z;
+  V3() : x(0), y(0), z(0) {}
+  V3(R a, R b, R c) : x(a), y(b), z(c) {}
+  explicit V3(R a) : x(a), y(a), z(a) {}
+  R &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  R operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+template <typename R> inline V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename R> inline V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename R> inline V3<R> operator*(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <typename R> inline V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <typename R> inline V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <typename R> inline V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+template <typename R> inline V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <typename R> inline bool operator==(V3<R> a, V3<R> b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+template <typename R> inline V3<R> vmin(V3<R> a, V3<R> b) { return {mn(a.x, b.x), mn(a.y, b.y), mn(a.z, b.z)}; }
+template <typename R> inline V3<R> vmax(V3<R> a, V3<R> b) { return {mx(a.x, b.x), mx(a.y, b.y), mx(a.z, b.z)}; }
+template <typename R> inline V3<R> vabs(V3<R> a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z)}; }
+template <typename R> inline V3<R> rcp(V3<R> a) { return {R(1) / a.x, R(1) / a.y, R(1) / a.z}; }
+template <typename R> inline V3<R> vfloor(V3<R> a) { return {std::floor(a.x), std::floor(a.y), std::floor(a.z)}; }
+template <typename R> inline R reduce_min(V3<R> a) { return mn(mn(a.x, a.y), a.z); }
+template <typename R> inline R reduce_max(V3<R> a) { return mx(mx(a.x, a.y), a.z); }
+template <typename R> inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename R> inline V3<R> cross(V3<R> a, V3<R> b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename R> inline V3<R> normalize(V3<R> v) { return v * (R(1) / std::sqrt(dot(v, v))); }
+template <typename R> inline R length(V3<R> v) { return std::sqrt(dot(v, v)); }
+template <typename R> inline V3<R> vmin_s(V3<R> a, R s) { return vmin(a, V3<R>(s)); }
+template <typename R, typename S> inline V3<R> cvt(V3<S> a) { return {R(a.x), R(a.y), R(a.z)}; }
+
+template <typename R> struct V4 { R x, y, z, w; };
+
+static const float INF = INFINITY;
+static const float ONE_PI = 3.14159265358979323846f;
+static const float TWO_PI = 2.f * 3.14159265358979323846f;
+static const float FOUR_PI = 4.f * 3.14159265358979323846f;
+static const float ONE_OVER_PI = 1.f / 3.14159265358979323846f;
+static const float ONE_OVER_TWO_PI = 1.f / (2.f * 3.14159265358979323846f);
+static const float ONE_OVER_FOUR_PI = 1.f / (4.f * 3.14159265358979323846f);
+
+// ---------------------------------------------------------------------------
+// half precision with the embree backend's rounding (rtcore/embree/Float16.cpp
+// float32ToFloat16: round to nearest, ties away from zero; subnormals kept)
+// ---------------------------------------------------------------------------
+inline uint16_t f2h(float value) {
+  uint32_t bits;
+  std::memcpy(&bits, &value, 4);
+  int i = (int)bits;
+  int s = (i >> 16) & 0x00008000;
+  int e = ((i >> 23) & 0x000000ff) - (127 - 15);
+  int m = i & 0x007fffff;
+  if (e <= 0) {
+    if (e < -10) return uint16_t(s);
+    m = (m | 0x00800000) >> (1 - e);
+    if (m & 0x00001000) m += 0x00002000;
+    return uint16_t(s | (m >> 13));
+  } else if (e == 0xff - (127 - 15)) {
+    if (m == 0) return uint16_t(s | 0x7c00);
+    m >>= 13;
+    return uint16_t(s | 0x7c00 | m | (m == 0));
+  } else {
+    if (m & 0x00001000) {
+      m += 0x00002000;
+      if (m & 0x00800000) { m = 0; e += 1; }
+    }
+    if (e > 30) return uint16_t(s | 0x7c00);
+    return uint16_t(s | (e << 10) | (m >> 13));
+  }
+}
+// rtcore/embree/Float16.cpp float16ToFloat32 (exact widening)
+inline float h2f(uint16_t h) {
+  uint32_t s = (h >> 15) & 1, e = (h >> 10) & 0x1f, m = h & 0x3ff, out;
+  if (e == 0) {
+    if (m == 0) out = s << 31;
+    else {
+      while (!(m & 0x400)) { m <<= 1; e -= 1; }
+      e += 1; m &= ~0x400u;
+      out = (s << 31) | ((e + (127 - 15)) << 23) | (m << 13);
+    }
+  } else if (e == 31) {
+    out = (s << 31) | 0x7f800000u | (m << 13);
+  } else {
+    out = (s << 31) | ((e + (127 - 15)) << 23) | (m << 13);
+  }
+  float f;
+  std::memcpy(&f, &out, 4);
+  return f;
+}
+// vec3h <-> vec3f (barney/common/half.h:47-71)
+struct V3h { uint16_t x, y, z; };
+inline V3h toh(V3<float> v) { return {f2h(v.x), f2h(v.y), f2h(v.z)}; }
+inline V3<float> fromh(V3h v) { return {h2f(v.x), h2f(v.y), h2f(v.z)}; }
+
+// ---------------------------------------------------------------------------
+// RNG (barney/common/barney-common.h:65-152)
+// ---------------------------------------------------------------------------
+struct RNGSeed {
+  uint64_t state = 0xcafef00dd15ea5e5ull;
+  uint32_t next() {                              // :74-82
+    uint64_t x = state;
+    const uint64_t multiplier = 6364136223846793005ull;
+    unsigned count = (unsigned)(x >> 61);
+    state = x * multiplier;
+    x ^= x >> 22;
+    return (uint32_t)(x >> (22 + count));
+  }
+  uint32_t next_h(uint64_t hash) {               // :87-93
+    state ^= (hash << 1);
+    return next();
+  }
+};
+// RNGSeed::seed's arguments are uint32_t: 2*a+1 wraps in 32 bits before the
+// xor with the 64-bit state.  Keep that exact behaviour.
+inline void rng_seed(RNGSeed &r, uint32_t a, uint32_t b) {
+  r.state ^= (uint64_t)(uint32_t)(2u * a + 1u);
+  r.next();
+  r.state ^= (uint64_t)(uint32_t)(2u * b);
+  r.next();
+}
+struct Random2 : RNGSeed {                       // :97-111
+  Random2(uint32_t a, uint32_t b) { rng_seed(*this, a, b); }
+  // Random2(RNGSeed &seed, uint32_t b) and (RNGSeed &seed, uint64_t b): both
+  // end in next((uint64_t)b) after the widening, so one form covers both.
+  Random2(RNGSeed &seed, uint64_t b) {
+    state = seed.state;
+    seed.next();
+    next_h(b ? b : 290374ull);
+  }
+  float operator()() { return (next() & 0x00FFFFFF) * (1.f / (float)0x01000000); }
+};
+inline uint64_t fnv_hash1(uint32_t v) {          // :132-137
+  const uint64_t off = 0xcbf29ce484222325ull, prime = 0x100000001b3ull;
+  return off ^ (prime * (uint64_t)v);
+}
+inline uint64_t fnv_hash2(uint64_t h, uint32_t v) { return (h * 0x100000001b3ull) ^ (uint64_t)v; }
+inline uint64_t fnv_hash3(uint32_t a, uint32_t b, uint32_t c) { return fnv_hash2(fnv_hash2(fnv_hash1(a), b), c); }
+inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+// Volume.h:174-184
+inline float fastLog(float f) {
+  f = (f - 1.f) / (f + 1.f);
+  float f2 = f * f;
+  float s = f;
+  f *= f2;
+  s += (1.f / 3.f) * f;
+  f *= f2;
+  s += (1.f / 5.f) * f;
+  return s + s;
+}
+inline double fastLog(double f) {
+  f = (f - 1.0) / (f + 1.0);
+  double f2 = f * f;
+  double s = f;
+  f *= f2;
+  s += (1.0 / 3.0) * f;
+  f *= f2;
+  s += (1.0 / 5.0) * f;
+  return s + s;
+}
+
+// ---------------------------------------------------------------------------
+// Field and transfer function
+// ---------------------------------------------------------------------------
+struct Field {
+  const float *data;
+  int N[3];          // numScalars
+  int C[3];          // numCells = dims-1 (StructuredData.cu:142-151)
+  V3<float> origin, spacing, rcpSpacing;
+  V3<float> boundsLo, boundsHi;  // StructuredData.cu:176-180
+};
+
+inline Field make_field(const orc_scene *s) {
+  Field f;
+  f.data = s->scalars;
+  for (int i = 0; i < 3; i++) { f.N[i] = s->dims[i]; f.C[i] = s->dims[i] - 1; }
+  f.origin = {s->origin[0], s->origin[1], s->origin[2]};
+  f.spacing = {s->spacing[0], s->spacing[1], s->spacing[2]};
+  f.rcpSpacing = rcp(f.spacing);
+  f.boundsLo = f.origin;
+  f.boundsHi = f.origin + f.spacing * V3<float>((float)f.C[0], (float)f.C[1], (float)f.C[2]);
+  return f;
+}
+
+// rtcore/embree/Texture.cpp:324-336 lerpCoords_notNormalized
+template <typename R> inline void lerpCoords(int N, R tc, int &i0, int &i1, R &f) {
+  if (tc - R(.5) <= R(0)) { i0 = i1 = 0; f = R(0); return; }
+  if (tc - R(.5) >= R(N - 1)) { i0 = i1 = N - 1; f = R(0); return; }
+  f = (tc - R(.5)) - R(int(tc - R(.5)));
+  i0 = int(tc - R(.5));
+  i1 = i0 + 1;
+}
+template <typename R> inline R lerp_l(R f, R a, R b) { return (R(1) - f) * a + f * b; }
+
+struct Tri {  // trilinear stencil, for the adjoint
+  int ix[2], iy[2], iz[2];
+  double fx, fy, fz;
+};
+
+// StructuredData.h:104-115 + rtcore/embree/Texture.cpp:339-411 (LINEAR, CLAMP,
+// unnormalised).  Returns NaN outside [0,numCells).
+template <typename R> inline R sample_field(const Field &F, V3<R> P, Tri *tri = nullptr) {
+  V3<R> rel = (P - cvt<R>(F.origin)) * cvt<R>(F.rcpSpacing);
+  if (rel.x < R(0) || rel.y < R(0) || rel.z < R(0)) return R(NAN);
+  if (rel.x >= R(F.C[0]) || rel.y >= R(F.C[1]) || rel.z >= R(F.C[2])) return R(NAN);
+  V3<R> tc = rel + V3<R>(R(.5));
+  int x0, x1, y0, y1, z0, z1;
+  R fx, fy, fz;
+  lerpCoords<R>(F.N[0], tc.x, x0, x1, fx);
+  lerpCoords<R>(F.N[1], tc.y, y0, y1, fy);
+  lerpCoords<R>(F.N[2], tc.z, z0, z1, fz);
+  const size_t Nx = F.N[0], Ny = F.N[1];
+  auto at = [&](int i, int j, int k) { return R(F.data[i + Nx * (j + Ny * (size_t)k)]); };
+  R v000 = at(x0, y0, z0), v001 = at(x1, y0, z0), v010 = at(x0, y1, z0), v011 = at(x1, y1, z0);
+  R v100 = at(x0, y0, z1), v101 = at(x1, y0, z1), v110 = at(x0, y1, z1), v111 = at(x1, y1, z1);
+  R v00 = lerp_l(fx, v000, v001), v01 = lerp_l(fx, v010, v011);
+  R v10 = lerp_l(fx, v100, v101), v11 = lerp_l(fx, v110, v111);
+  R v0 = lerp_l(fy, v00, v01), v1 = lerp_l(fy, v10, v11);
+  if (tri) {
+    tri->ix[0] = x0; tri->ix[1] = x1; tri->iy[0] = y0; tri->iy[1] = y1;
+    tri->iz[0] = z0; tri->iz[1] = z1;
+    tri->fx = fx; tri->fy = fy; tri->fz = fz;
+  }
+  return lerp_l(fz, v0, v1);
+}
+
+// rtcore/embree/Texture.cpp:249-271 (POINT filter, unnormalised): clamp, then
+// truncate.  Used by the macrocell build at integer coordinates.
+inline float point_field(const float *data, const int N[3], float x, float y, float z) {
+  auto cl = [](float f, float lo, float hi) { return mx(mn(f, hi), lo); };  // Texture.cpp:15-18
+  uint32_t lx = (uint32_t)cl(x, 0.f, N[0] - 1.f);
+  uint32_t ly = (uint32_t)cl(y, 0.f, N[1] - 1.f);
+  uint32_t lz = (uint32_t)cl(z, 0.f, N[2] - 1.f);
+  return data[lx + size_t(N[0]) * (ly + size_t(N[1]) * lz)];
+}
+
+struct XF {
+  const float *v;  // RGBA
+  int n;
+  float lo, hi, span, baseDensity;
+};
+inline XF make_xf(const float *tf, int n, float lo, float hi, float bd) {
+  return XF{tf, n, lo, hi, hi - lo, bd};
+}
+
+// TransferFunction.h:66-86
+template <typename R> inline V4<R> xf_map(const XF &xf, R s, int *idx_out = nullptr, R *f_out = nullptr,
+                                          bool *clamped = nullptr) {
+  R f = (s - R(xf.lo)) / R(xf.span);
+  if (clamped) *clamped = !(f > R(0) && f < R(1));
+  f = clampv(f, R(0), R(1));
+  f *= R(xf.n - 1);
+  int idx = clampv(int(f), 0, xf.n - 2);
+  f -= R(idx);
+  const float *v0 = xf.v + 4 * idx, *v1 = xf.v + 4 * (idx + 1);
+  V4<R> r;
+  r.x = (R(1) - f) * R(v0[0]) + f * R(v1[0]);
+  r.y = (R(1) - f) * R(v0[1]) + f * R(v1[1]);
+  r.z = (R(1) - f) * R(v0[2]) + f * R(v1[2]);
+  r.w = (R(1) - f) * R(v0[3]) + f * R(v1[3]);
+  r.w *= R(xf.baseDensity);
+  if (idx_out) *idx_out = idx;
+  if (f_out) *f_out = f;
+  return r;
+}
+
+// TransferFunction.h:91-116
+inline float xf_majorant(const XF &xf, float lower, float upper) {
+  if (lower > upper) return 0.f;
+  float f_lo = (lower - xf.lo) / xf.span;
+  float f_hi = (upper - xf.lo) / xf.span;
+  f_lo = clampv(f_lo, 0.f, 1.f);
+  f_hi = clampv(f_hi, 0.f, 1.f);
+  f_lo *= (xf.n - 1);
+  f_hi *= (xf.n - 1);
+  int idx0_lo = clampv(int(f_lo), 0, xf.n - 2);
+  int idx0_hi = clampv(int(f_hi), 0, xf.n - 2);
+  f_lo -= idx0_lo;
+  f_hi -= idx0_hi;
+  float lerp_lo = (1.f - f_lo) * xf.v[4 * idx0_lo + 3] + f_lo * xf.v[4 * (idx0_lo + 1) + 3];
+  float lerp_hi = (1.f - f_hi) * xf.v[4 * idx0_hi + 3] + f_hi * xf.v[4 * (idx0_hi + 1) + 3];
+  float m = 0.f;
+  m = mx(m, lerp_lo);
+  m = mx(m, lerp_hi);
+  for (int i = idx0_lo + 1; i <= idx0_hi; i++) m = mx(m, xf.v[4 * i + 3]);
+  return m * xf.baseDensity;
+}
+
+// Volume.h:66-80 (non-principled): NaN -> 0, else TF map
+template <typename R> inline V4<R> sample_and_map(const Field &F, const XF &xf, V3<R> P) {
+  R f = sample_field<R>(F, P);
+  if (std::isnan(f)) return V4<R>{0, 0, 0, 0};
+  return xf_map<R>(xf, f);
+}
+
+// ---------------------------------------------------------------------------
+// Macrocells (StructuredData.cu:29-95, MCGrid.cu:63-116)
+// ---------------------------------------------------------------------------
+inline void mc_dims_of(const int N[3], int cpm, int M[3]) {
+  for (int i = 0; i < 3; i++) {
+    int cells = N[i] - 1;
+    M[i] = cells <= 0 ? 0 : (cells + cpm - 1) / cpm;  // divRoundUp(numCells, cellsPerMC)
+  }
+}
+
+inline void mc_range_one(const float *data, const int N[3], int cpm, int mx_, int my_, int mz_,
+                         float &lo, float &hi) {
+  lo = +INF;
+  hi = -INF;
+  for (int iiz = 0; iiz <= cpm; iiz++)
+    for (int iiy = 0; iiy <= cpm; iiy++)
+      for (int iix = 0; iix <= cpm; iix++) {
+        int sx = mx_ * cpm + iix, sy = my_ * cpm + iiy, sz = mz_ * cpm + iiz;
+        if (sx >= N[0] || sy >= N[1] || sz >= N[2]) continue;
+        float f = point_field(data, N, (float)sx, (float)sy, (float)sz);
+        lo = mn(lo, f);  // interval::extend
+        hi = mx(hi, f);
+      }
+}
+
+// ---------------------------------------------------------------------------
+// Thread pool parallel_for (mirrors rtcore/embree/Compute.cpp:17-25: one
+// worker per hardware thread, dynamic chunks)
+// ---------------------------------------------------------------------------
+template <typename F> void parallel_for(int64_t n, int nthreads, F &&fn, int64_t chunk = 1) {
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  if (nthreads == 1 || n <= chunk) {
+    for (int64_t i = 0; i < n; i++) fn(i);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nthreads; t++)
+    pool.emplace_back([&]() {
+      while (true) {
+        int64_t b = next.fetch_add(chunk);
+        if (b >= n) break;
+        int64_t e = std::min(n, b + chunk);
+        for (int64_t i = b; i < e; i++) fn(i);
+      }
+    });
+  for (auto &th : pool) th.join();
+}
+
+// ---------------------------------------------------------------------------
+// Scene (host-side commits of camera, lights, env map)
+// ---------------------------------------------------------------------------
+struct Camera {  // Camera.cu:83-97
+  V3<float> lens00, dir00, du, dv;
+};
+inline Camera commit_camera(const float pos[3], const float dir[3], const float up[3], float fovy) {
+  Camera c;
+  V3<float> from(pos[0], pos[1], pos[2]);
+  V3<float> direction = normalize(V3<float>(dir[0], dir[1], dir[2]));  // set3f("direction") normalizes
+  V3<float> vup(up[0], up[1], up[2]);
+  V3<float> dir_00 = normalize(direction);
+  V3<float> dir_du = normalize(cross(dir_00, vup));
+  V3<float> dir_dv = normalize(cross(dir_du, dir_00));
+  dir_00 = dir_00 * (float)(1.f / (2.0f * tanf((0.5f * fovy) * (float)M_PI / 180.0f)));
+  c.lens00 = from;
+  c.dir00 = dir_00;
+  c.du = dir_du;
+  c.dv = dir_dv;
+  return c;
+}
+
+struct M3 { V3<float> vx, vy, vz; };  // owl linear3f, columns
+inline V3<float> xfmVector(const M3 &m, V3<float> v) { return m.vx * v.x + m.vy * v.y + m.vz * v.z; }
+// owl linear3f rcp(): inverse = adjoint^T / det
+inline M3 inverse(const M3 &m) {
+  V3<float> a = cross(m.vy, m.vz), b = cross(m.vz, m.vx), c = cross(m.vx, m.vy);
+  float det = dot(m.vx, a);
+  float r = 1.f / det;
+  M3 t;  // rows of the inverse are a,b,c scaled; store as columns
+  t.vx = V3<float>(a.x, b.x, c.x) * r;
+  t.vy = V3<float>(a.y, b.y, c.y) * r;
+  t.vz = V3<float>(a.z, b.z, c.z) * r;
+  return t;
+}
+
+struct Env {
+  bool present = false;
+  const float *tex = nullptr;
+  int W = 0, H = 0;
+  int addr[2] = {0, 0};
+  M3 toWorld, toLocal;
+  float scale = 1.f;
+  std::vector<float> cdf_y, cdf_x;
+};
+
+// rtcore/embree/Texture.cpp:25-93 computeAddress for normalized coordinates
+struct LerpAddr { int idx0, idx1; float f; };
+inline LerpAddr compute_address(int mode, float tc, int N) {
+  LerpAddr out{0, 0, 0.f};
+  switch (mode) {
+    case 0: {  // WRAP
+      tc = tc * (float)N - .5f;
+      tc = fmodf(tc, (float)N);
+      if (tc < 0.f) tc += (float)N;
+      float fc = floorf(tc);
+      int ic = int(fc);
+      out.f = tc - ic;
+      out.idx0 = ic;
+      out.idx1 = int(fmodf(tc + 1.f, (float)N));
+    } break;
+    case 3: {  // MIRROR
+      tc = tc * N + .5f;
+      float fc = floorf(tc);
+      int ic = int(fc);
+      out.f = tc - ic;
+      int i0 = ic - 1, i1 = ic + 0;
+      if (i0 < 0) i0 = -i0;
+      if (i1 < 0) i1 = -i1;
+      i0 = i0 % (2 * N);
+      i1 = i1 % (2 * N);
+      if (i0 >= N) i0 = 2 * N - 1 - i0;
+      if (i1 >= N) i1 = 2 * N - 1 - i1;
+      out.idx0 = i0;
+      out.idx1 = i1;
+    } break;
+    case 2:  // BORDER: the embree backend leaves the address zeroed
+      break;
+    case 1:
+    default: {  // CLAMP
+      tc = tc * N;
+      if (tc - .5f <= 0.f) { out.idx0 = out.idx1 = 0; out.f = 0.f; }
+      else if (tc - .5f >= N - 1) { out.idx0 = out.idx1 = N - 1; out.f = 0.f; }
+      else {
+        out.f = (tc - .5f) - int(tc - .5f);
+        out.idx0 = int(tc - .5f);
+        out.idx1 = out.idx0 + 1;
+      }
+    } break;
+  }
+  return out;
+}
+// rtcore/embree/Texture.cpp:295-321 tex2D LINEAR, normalized coordinates
+inline V4<float> tex2D(const float *tex, int W, int H, const int addr[2], float u, float v) {
+  LerpAddr lx = compute_address(addr[0], u, W), ly = compute_address(addr[1], v, H);
+  auto px = [&](int ix, int iy) -> V4<float> {
+    const float *p = tex + 4 * ((size_t)ix + (size_t)iy * W);
+    return {p[0], p[1], p[2], p[3]};
+  };
+  V4<float> v00 = px(lx.idx0, ly.idx0), v01 = px(lx.idx1, ly.idx0);
+  V4<float> v10 = px(lx.idx0, ly.idx1), v11 = px(lx.idx1, ly.idx1);
+  auto lrp = [](float f, V4<float> a, V4<float> b) -> V4<float> {
+    return {(1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
+            (1.f - f) * a.w + f * b.w};
+  };
+  V4<float> v0 = lrp(lx.f, v00, v01), v1 = lrp(lx.f, v10, v11);
+  return lrp(ly.f, v0, v1);
+}
+
+// EnvMap.cu:61-137 (ComputeWeights_xy, ComputeCDFs_doLine, Normalize_cdf_y)
+inline void env_cdfs(const float *tex, int W, int H, const int addr[2], float *cdf_y, float *cdf_x) {
+  for (int iy = 0; iy < H; iy++)
+    for (int ix = 0; ix < W; ix++) {
+      float weight = 0.f;
+      for (int iiy = 0; iiy <= 2; iiy++)
+        for (int iix = 0; iix <= 2; iix++) {
+          V4<float> t = tex2D(tex, W, H, addr, (ix + iix * .5f) / (W), (iy + iiy * .5f) / (H));
+          weight = mx(weight, mx(mx(t.x, t.y), t.z));
+        }
+      cdf_x[ix + W * iy] = weight;
+    }
+  for (int y = 0; y < H; y++) {
+    float *line = cdf_x + (size_t)y * W;
+    float sum = 0.f;
+    for (int ix = 0; ix < W; ix++) sum += line[ix];
+    float rcp_sum = 1.f / sum;
+    sum = 0.f;
+    for (int ix = 0; ix < W; ix++) {
+      sum += line[ix];
+      line[ix] = sum * rcp_sum;
+    }
+    line[W - 1] = 1.f;
+    float rel_y = (y + .5f) / H;
+    const float theta = ONE_PI * rel_y;
+    cdf_y[y] = sum * sinf(theta);
+  }
+  float sum = 0.f;
+  for (int i = 0; i < H; i++) sum += cdf_y[i];
+  float rcp_sum = 1.f / sum;
+  sum = 0.f;
+  for (int i = 0; i < H; i++) {
+    sum += cdf_y[i];
+    cdf_y[i] = sum * rcp_sum;
+  }
+  cdf_y[H - 1] = 1.f;
+}
+
+struct DirLightDD { V3<float> direction; float radiance; V3<float> color; };
+
+struct Scene {
+  Field F;
+  XF xf;
+  std::vector<float> majorants_own;
+  const float *maj;
+  int M[3];
+  V3<float> mcOrigin, mcSpacing, mcRcpSpacing;
+  Camera cam;
+  int W, H;
+  int numDir;
+  DirLightDD dir[4];
+  Env env;
+  V4<float> bg;
+  float ambient;
+  int multi, volMS, maxVB;
+  float aniso, scatAlb;
+};
+
+inline void build_scene(const orc_scene *s, Scene &S) {
+  S.F = make_field(s);
+  S.xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
+  int cpm = s->cells_per_mc;
+  mc_dims_of(S.F.N, cpm, S.M);
+  // StructuredData.cu:70-76: mc origin = worldBounds.lower, spacing = cpm*gridSpacing
+  S.mcOrigin = S.F.boundsLo;
+  S.mcSpacing = V3<float>((float)cpm) * S.F.spacing;
+  S.mcRcpSpacing = rcp(S.mcSpacing);
+  size_t nmc = (size_t)S.M[0] * S.M[1] * S.M[2];
+  if (s->majorants) S.maj = s->majorants;
+  else {
+    S.majorants_own.resize(nmc);
+    std::vector<float> r(2 * nmc);
+    orc_mc_ranges(s->scalars, s->dims, cpm, r.data());
+    orc_majorants(r.data(), (int)nmc, s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density,
+                  S.majorants_own.data());
+    S.maj = S.majorants_own.data();
+  }
+  S.cam = commit_camera(s->cam_pos, s->cam_dir, s->cam_up, s->fovy);
+  S.W = s->width;
+  S.H = s->height;
+  S.numDir = std::min(4, std::max(0, s->num_dir_lights));
+  for (int i = 0; i < S.numDir; i++) {
+    // DirLight.cu:10-20 with the identity instance transform
+    S.dir[i].direction = normalize(V3<float>(s->dir_light_dir[i][0], s->dir_light_dir[i][1], s->dir_light_dir[i][2]));
+    S.dir[i].color = V3<float>(s->dir_light_color[i][0], s->dir_light_color[i][1], s->dir_light_color[i][2]);
+    S.dir[i].radiance = s->dir_light_radiance[i];
+  }
+  if (s->env_texels) {
+    Env &e = S.env;
+    e.present = true;
+    e.tex = s->env_texels;
+    e.W = s->env_dims[0];
+    e.H = s->env_dims[1];
+    e.addr[0] = s->env_addr[0];
+    e.addr[1] = s->env_addr[1];
+    e.scale = s->env_scale;
+    // EnvMap.cu:164-179
+    V3<float> up(s->env_up[0], s->env_up[1], s->env_up[2]);
+    V3<float> dir(s->env_dir[0], s->env_dir[1], s->env_dir[2]);
+    e.toWorld.vz = -normalize(up);
+    e.toWorld.vy = -normalize(cross(e.toWorld.vz, dir));
+    e.toWorld.vx = normalize(cross(e.toWorld.vy, e.toWorld.vz));
+    e.toLocal = inverse(e.toWorld);
+    e.cdf_y.resize(e.H);
+    e.cdf_x.resize((size_t)e.W * e.H);
+    env_cdfs(e.tex, e.W, e.H, e.addr, e.cdf_y.data(), e.cdf_x.data());
+  }
+  S.bg = {s->bg_color[0], s->bg_color[1], s->bg_color[2], s->bg_color[3]};
+  S.ambient = s->ambient_radiance;
+  S.multi = s->multi_scatter;
+  S.volMS = s->volume_multi_scatter;
+  S.maxVB = s->max_volume_bounces;
+  S.aniso = s->anisotropy;
+  S.scatAlb = s->scattering_albedo;
+}
+
+// DG.h:97-106
+inline float sphericalTheta(V3<float> v) { return acosf(clampv(v.z, -1.f, 1.f)); }
+inline float sphericalPhi(V3<float> v) {
+  float p = atan2f(v.y, v.x);
+  return (p < 0.f) ? (p + float(2.f * M_PI)) : p;
+}
+// EnvMap.h:98-134
+inline float cdfGetPDF(int position, const float *cdf, int N) {
+  float f_at = cdf[position];
+  float f_before = position ? cdf[position - 1] : 0.f;
+  return N * (f_at - f_before);
+}
+inline int sampleCDF(const float *cdf, int N, float v, float &pdf) {
+  int begin = 0, end = N;
+  while ((end - begin) > 1) {
+    int mid = (begin + end) / 2;
+    float f_mid = cdf[mid - 1];
+    if (v < f_mid) end = mid;
+    else begin = mid;
+  }
+  float f_at = cdf[begin];
+  float f_before = begin ? cdf[begin - 1] : 0.f;
+  pdf = N * (f_at - f_before);
+  return begin;
+}
+// EnvMap.h:165-180
+inline void env_worldToPixel(const Env &e, V3<float> worldDir, int &ix, int &iy) {
+  V3<float> localDir = xfmVector(e.toLocal, worldDir);
+  float theta = sphericalTheta(localDir);
+  float phi = sphericalPhi(localDir);
+  float u = phi * ONE_OVER_TWO_PI, v = theta * ONE_OVER_PI;
+  ix = (int)clampv(u * (float)e.W, 0.f, e.W - 1.f);
+  iy = (int)clampv(v * (float)e.H, 0.f, e.H - 1.f);
+}
+// EnvMap.h:136-163
+inline float env_pdf(const Env &e, V3<float> dir) {
+  if (!e.present) return ONE_OVER_FOUR_PI;
+  int px, py;
+  env_worldToPixel(e, dir, px, py);
+  float pdf_y = cdfGetPDF(py, e.cdf_y.data(), e.H);
+  float pdf_x = cdfGetPDF(px, e.cdf_x.data() + (size_t)py * e.W, e.W);
+  float rel_y = (py + .5f) / e.H;
+  const float theta = ONE_PI * rel_y;
+  return pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinf(theta));
+}
+// EnvMap.h:198-210
+inline V3<float> env_uvToWorld(const Env &e, float fx, float fy) {
+  const float phi = TWO_PI * fx;
+  const float theta = ONE_PI * fy;
+  V3<float> d;
+  d.z = cosf(theta);
+  d.x = cosf(phi) * sinf(theta);
+  d.y = sinf(phi) * sinf(theta);
+  return xfmVector(e.toWorld, d);
+}
+
+struct LightSample {  // light/Light.h Light::Sample
+  V3<float> radiance{0.f, 0.f, 0.f};
+  V3<float> direction{0.f, 0.f, 0.f};
+  float distance = 0.f;
+  float pdf = 0.f;
+};
+
+// EnvMap.h:212-250
+inline LightSample env_sample(const Env &e, Random2 &r) {
+  LightSample sample;
+  float r_y = r();
+  float r_x = r();
+  float pdf_y, pdf_x;
+  int iy = sampleCDF(e.cdf_y.data(), e.H, r_y, pdf_y);
+  int ix = sampleCDF(e.cdf_x.data() + (size_t)e.W * iy, e.W, r_x, pdf_x);
+  float sx = (ix + r()) / e.W;
+  float sy = (iy + r()) / e.H;
+  V4<float> t = tex2D(e.tex, e.W, e.H, e.addr, sx, sy);
+  sample.radiance = e.scale * V3<float>(t.x, t.y, t.z);
+  sample.direction = env_uvToWorld(e, sx, sy);
+  float rel_y = sy;
+  const float theta = ONE_PI * rel_y;
+  sample.pdf = pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinf(theta));
+  sample.distance = INF;
+  return sample;
+}
+
+// DG.h:183-193
+inline V3<float> randomDirection(Random2 &rng) {
+  V3<float> v;
+  while (true) {
+    v.x = 1.f - 2.f * rng();
+    v.y = 1.f - 2.f * rng();
+    v.z = 1.f - 2.f * rng();
+    if (dot(v, v) <= 1.f) return normalize(v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Ray record (render/Ray.h:49-99); only the fields this path reads
+// ---------------------------------------------------------------------------
+struct Ray {
+  V3<float> org, dir;
+  float tMax;
+  RNGSeed rngSeed;
+  V3<float> P;
+  bool hit;          // bsdfType != NONE
+  bool isShadowRay;
+  V3<float> albedo;  // Phase data
+  float g;
+  V4<float> missColor;
+};
+struct PathState {   // render/Ray.h:18-26
+  V3h throughput;
+  float misWeight;
+  int numDiffuseBounces;
+  int numVolumeBounces;
+};
+
+struct Counters {
+  uint64_t samples = 0, mcs = 0, rays = 0;
+};
+
+// Woodcock::sampleRange (Volume.h:188-223), templated on the arithmetic type
+// of everything downstream of the 24-bit random numbers.
+template <typename R>
+inline bool woodcock(const Scene &S, V3<R> org, V3<R> dir, R t0, R &t1, R majorant, Random2 &rand,
+                     V4<R> &sample, Counters &cnt) {
+  R t = t0;
+  while (true) {
+    R r = R(rand());
+    R dt = -fastLog(R(1) - r) / majorant;
+    t += dt;
+    if (t >= t1) return false;
+    V3<R> P = org + t * dir;
+    sample = sample_and_map<R>(S.F, S.xf, P);
+    cnt.samples++;
+    if (sample.w >= R(rand()) * majorant) {
+      t1 = t;
+      return true;
+    }
+  }
+}
+
+// Ray.h:175-187 boxTest
+template <typename R> inline bool boxTest(V3<R> org, V3<R> dir, R &t0, R &t1, V3<R> lo, V3<R> hi) {
+  V3<R> t_lo = (lo - org) * rcp(dir);
+  V3<R> t_hi = (hi - org) * rcp(dir);
+  V3<R> t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  t0 = mx(t0, reduce_max(t_nr));
+  t1 = mn(t1, reduce_min(t_fr));
+  return t0 <= t1;
+}
+
+// MCVolumeAccel::isProg (MCAccelerator.h:569-708) + dda::dda3 (DDA.h:65-206)
+// as dispatched by the embree backend (tmin 0, tmax ray.tMax, identity
+// instance transform, one instance and one geometry: hash(0,0,0)).
+// The trace direction has zero components replaced by 1e-6
+// (traceRays.dev.cu:41-44).  On a hit, fills t/rgb/P and returns true.
+template <typename R>
+inline bool trace(const Scene &S, Ray &ray, Counters &cnt, R &t_hit, V3<R> &rgb_hit) {
+  cnt.rays++;
+  V3<float> dirf = ray.dir;
+  if (dirf.x == 0.f) dirf.x = 1e-6f;
+  if (dirf.y == 0.f) dirf.y = 1e-6f;
+  if (dirf.z == 0.f) dirf.z = 1e-6f;
+  if (S.M[0] <= 0 || S.M[1] <= 0 || S.M[2] <= 0) return false;
+  const V3<R> org = cvt<R>(ray.org), dir = cvt<R>(dirf);
+  R tLo = R(0), tHi = R(ray.tMax);
+  if (!boxTest<R>(org, dir, tLo, tHi, cvt<R>(S.F.boundsLo), cvt<R>(S.F.boundsHi))) return false;
+
+  V3<R> dda_org = (org - cvt<R>(S.mcOrigin)) * rcp(cvt<R>(S.mcSpacing));
+  V3<R> dda_dir = dir * rcp(cvt<R>(S.mcSpacing));
+  Random2 rng(ray.rngSeed, fnv_hash3(0, 0, 0));
+  const R tMaxRay = R(ray.tMax);
+  const R tMax = tHi;
+
+  // ---- dda3 ----
+  const V3<R> f_size((R)S.M[0], (R)S.M[1], (R)S.M[2]);
+  const V3<R> rcp_dir = rcp(dda_dir);
+  V3<R> t_lo = (V3<R>(R(0)) - dda_org) * rcp(dda_dir);
+  V3<R> t_hi = (f_size - dda_org) * rcp(dda_dir);
+  V3<R> t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  for (int a = 0; a < 3; a++) {
+    if (dda_dir[a] == R(0)) {
+      if (dda_org[a] < R(0) || dda_org[a] > f_size[a]) return false;
+      t_nr[a] = -R(INFINITY);
+      t_fr[a] = +R(INFINITY);
+    }
+  }
+  R ray_t0 = mx(R(0), reduce_max(t_nr));
+  R ray_t1 = mn(tMax, reduce_min(t_fr));
+  if (ray_t0 > ray_t1) return false;
+  V3<R> org_in_volume = dda_org + ray_t0 * dda_dir;
+  V3<R> f_cell = vmax(V3<R>(R(0)), vmin(f_size - V3<R>(R(1)), vfloor(org_in_volume)));
+  V3<R> f_cell_end(dda_dir.x > R(0) ? f_cell.x + R(1) : f_cell.x, dda_dir.y > R(0) ? f_cell.y + R(1) : f_cell.y,
+                   dda_dir.z > R(0) ? f_cell.z + R(1) : f_cell.z);
+  V3<R> t_step = vabs(rcp_dir);
+  V3<R> t_next;
+  for (int a = 0; a < 3; a++)
+    t_next[a] = (dda_dir[a] == R(0)) ? R(INFINITY) : (std::fabs(f_cell_end[a] - org_in_volume[a]) * t_step[a]);
+  int stop[3], delta[3], cell[3];
+  for (int a = 0; a < 3; a++) {
+    stop[a] = dda_dir[a] > R(0) ? S.M[a] : -1;
+    delta[a] = dda_dir[a] > R(0) ? +1 : -1;
+    cell[a] = int(f_cell[a]);
+  }
+  R next_cell_begin = R(0);
+  const int maxIter = S.M[0] + S.M[1] + S.M[2] + 8;
+  for (int it = 0; it < maxIter; it++) {
+    R t_closest = reduce_min(t_next);
+    const R cell_t0 = ray_t0 + next_cell_begin;
+    const R cell_t1 = ray_t0 + mn(t_closest, tMax);
+    // ---- lambda (MCAccelerator.h:56-146) ----
+    const float majorant = S.maj[cell[0] + S.M[0] * (cell[1] + S.M[1] * cell[2])];
+    if (majorant != 0.f) {
+      cnt.mcs++;
+      R segLo = cell_t0, segHi = mn(cell_t1, tMaxRay);
+      V4<R> sample{0, 0, 0, 0};
+      if (woodcock<R>(S, org, dir, segLo, segHi, R(majorant), rng, sample, cnt)) {
+        t_hit = segHi;
+        rgb_hit = V3<R>(sample.x, sample.y, sample.z);
+        return true;
+      }
+    }
+    next_cell_begin = t_closest;
+    for (int a = 0; a < 3; a++) {
+      if (t_next[a] == t_closest) {
+        t_next[a] += t_step[a];
+        cell[a] += delta[a];
+        if (cell[a] == stop[a]) return false;
+      }
+    }
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Shading (kernels/shadeRays.cu), volume-only world
+// ---------------------------------------------------------------------------
+// shadeRays.cu:141-191
+inline bool sampleDirLights(const Scene &S, V3<float> N, Random2 &random, LightSample &ls) {
+  if (S.numDir == 0) return false;
+  const int RES = 2;
+  int lID[RES];
+  float weights[RES];
+  float sumWeights = 0.f;
+  for (int i = 0; i < RES; i++) {
+    lID[i] = mn(int(random() * S.numDir), S.numDir - 1);
+    weights[i] = 0.f;
+    const DirLightDD &light = S.dir[lID[i]];
+    V3<float> light_radiance = light.color * light.radiance;
+    V3<float> lightDir = -light.direction;
+    float weight = (N == V3<float>(0.f)) ? 1.f : dot(lightDir, N);
+    if (weight <= 1e-3f) continue;
+    weight *= reduce_max(light_radiance);
+    if (weight <= 1e-3f) continue;
+    weights[i] = weight;
+    sumWeights += weight;
+  }
+  if (sumWeights == 0.f) return false;
+  float r = random() * sumWeights;
+  int i = 0;
+  while (i < RES && r >= weights[i]) { r -= weights[i]; ++i; }
+  if (i == RES) return false;
+  const DirLightDD &light = S.dir[lID[i]];
+  ls.direction = -light.direction;
+  ls.distance = INF;
+  ls.radiance = light.color * light.radiance * 1.f / (weights[i] / sumWeights * (float(RES) / float(S.numDir)));
+  ls.pdf = INF;
+  return weights[i] != 0.f;
+}
+
+// shadeRays.cu:268-293
+inline bool sampleEnvLight(const Scene &S, V3<float> N, Random2 &random, LightSample &ls) {
+  if (S.env.present) {
+    ls = env_sample(S.env, random);
+  } else {
+    ls.direction = randomDirection(random);
+    ls.distance = INF;
+    if (!(N == V3<float>(0.f))) {
+      ls.radiance = V3<float>(TWO_PI * S.ambient);
+      if (dot(ls.direction, N) < 0.f) ls.direction = -ls.direction;
+      ls.pdf = ONE_OVER_TWO_PI;
+    } else {
+      ls.radiance = V3<float>(FOUR_PI * S.ambient);
+      ls.pdf = ONE_OVER_FOUR_PI;
+    }
+  }
+  return true;
+}
+
+// shadeRays.cu:295-404 (no area or point lights in this world)
+inline bool sampleLights(const Scene &S, V3<float> Ng, Random2 &random, LightSample &ls, bool &needsMIS,
+                         bool &isDir) {
+  needsMIS = false;
+  LightSample els;
+  float elsWeight = sampleEnvLight(S, Ng, random, els) ? reduce_max(els.radiance) : 0.f;
+  LightSample als;  // no quad lights: sampleAreaLights returns false
+  float alsWeight = 0.f;
+  LightSample dls;
+  float dlsWeight = sampleDirLights(S, Ng, random, dls) ? reduce_max(dls.radiance) : 0.f;
+  float plsWeight = 0.f;
+  float sumWeights = alsWeight + dlsWeight + elsWeight + plsWeight;
+  if (sumWeights == 0.f) return false;
+  elsWeight *= 1.f / sumWeights;
+  alsWeight *= 1.f / sumWeights;
+  dlsWeight *= 1.f / sumWeights;
+  plsWeight *= 1.f / sumWeights;
+  float r = random();
+  if (r <= alsWeight) {
+    // only reachable with r == 0 exactly; the reference then reads an
+    // unfilled sample.  Here that sample is zero, so the pdf test rejects it.
+    ls = als;
+    ls.radiance = ls.radiance * (1.f / alsWeight);
+  } else if (r <= alsWeight + elsWeight) {
+    ls = els;
+    ls.radiance = ls.radiance * (1.f / elsWeight);
+    needsMIS = true;
+  } else if (r <= alsWeight + elsWeight + plsWeight) {
+    return false;  // unreachable: no point lights
+  } else {
+    ls = dls;
+    ls.radiance = ls.radiance * (1.f / dlsWeight);
+    isDir = true;
+  }
+  if (std::isnan(ls.pdf) || (ls.pdf <= 0.f)) return false;
+  return true;
+}
+
+// shadeRays.cu:437-456
+inline V3<float> radianceFromEnv(const Scene &S, const Ray &ray) {
+  const Env &env = S.env;
+  if (env.present) {
+    V3<float> d = xfmVector(env.toLocal, normalize(ray.dir));
+    float theta = sphericalTheta(d);
+    float phi = sphericalPhi(d);
+    const float invPi = 1.f / (float)M_PI;
+    const float inv2Pi = 1.f / (2.f * (float)M_PI);
+    float u = phi * inv2Pi, v = theta * invPi;
+    V4<float> c = tex2D(env.tex, env.W, env.H, env.addr, u, v);
+    return env.scale * V3<float>(c.x, c.y, c.z);
+  }
+  return V3<float>(S.ambient);
+}
+
+// Phase.h:49-57 / 145-146
+inline float phase_pdf(const Scene &S, const Ray &ray, V3<float> wo, V3<float> wi) {
+  if (!S.multi) return ONE_OVER_FOUR_PI;
+  V3<float> wi_in = normalize(-wo);
+  float cosTheta = dot(wi_in, normalize(wi));
+  float g = ray.g;
+  if (fabsf(g) < 1e-3f) return ONE_OVER_FOUR_PI;
+  float g2 = g * g;
+  float denom = 1.f + g2 - 2.f * g * cosTheta;
+  return ONE_OVER_FOUR_PI * (1.f - g2) / (denom * sqrtf(denom));
+}
+inline float hgPhase(float g, float cosTheta) {
+  if (fabsf(g) < 1e-3f) return ONE_OVER_FOUR_PI;
+  float g2 = g * g;
+  float denom = 1.f + g2 - 2.f * g * cosTheta;
+  return ONE_OVER_FOUR_PI * (1.f - g2) / (denom * sqrtf(denom));
+}
+// Phase.h:74-99
+inline V3<float> sampleHGDirection(V3<float> wi_in, float g, Random2 &random) {
+  float u0 = random();
+  float u1 = random();
+  float cosTheta;
+  if (fabsf(g) < 1e-3f) cosTheta = 1.f - 2.f * u0;
+  else {
+    float sqrTerm = (1.f - g * g) / (1.f + g - 2.f * g * u0);
+    cosTheta = (1.f + g * g - sqrTerm * sqrTerm) / (2.f * g);
+  }
+  float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
+  float phi = TWO_PI * u1;
+  V3<float> local(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
+  V3<float> w = normalize(wi_in);
+  V3<float> u, v;
+  if (fabsf(w.x) > 0.1f) u = normalize(cross(V3<float>(0.f, 1.f, 0.f), w));
+  else u = normalize(cross(V3<float>(1.f, 0.f, 0.f), w));
+  v = cross(w, u);
+  return normalize(local.x * u + local.y * v + local.z * w);
+}
+
+struct Fragment { V3<float> rgb; };
+
+// bounce() (shadeRays.cu:477-878), volume-hit and miss branches only.
+// Returns the fragment; updates ray/state; fills the shadow ray.
+inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowRay, PathState &shadowState,
+                        bool &shadowValid, int pathDepth) {
+  const float EPS = 1e-4f;
+  V3<float> fragment(0.f);
+  shadowValid = false;
+  const bool hadNoIntersection = !ray.hit;
+  const V3<float> incomingThroughput = fromh(state.throughput);
+  if (ray.isShadowRay) {
+    if (hadNoIntersection) fragment = state.misWeight * fromh(state.throughput);
+    ray.tMax = -1.f;
+    return fragment;
+  }
+  // Ng = 0 for volume hits (N is never set for this world's hits)
+  if (hadNoIntersection) {
+    if (pathDepth == 0) {
+      fragment = S.env.present ? radianceFromEnv(S, ray) : V3<float>(ray.missColor.x, ray.missColor.y, ray.missColor.z);
+    } else {
+      const V3<float> fromEnv = radianceFromEnv(S, ray);
+      fragment = fromh(state.throughput) * fromEnv * state.misWeight;
+    }
+    ray.tMax = -1.f;
+    return fragment;
+  }
+  // volume hit: isVolumeHit, hitWasOnFront false, Ngff = -Ng = -0
+  const V3<float> Ngff(-0.f, -0.f, -0.f);
+  Random2 random(ray.rngSeed, (uint64_t)fbits(ray.tMax));
+  // DG (shadeRays.cu:625-639)
+  const V3<float> P = ray.P;
+  const V3<float> wo = -normalize(ray.dir);
+  const float offsetEpsilon = mx(EPS, 1e-6f * reduce_max(vabs(P)));  // safe_eps :39-43
+  const V3<float> frontFacingSurfaceOffset = wo;
+
+  LightSample ls;
+  bool needsMIS = false, isDir = false;
+  if (sampleLights(S, Ngff, random, ls, needsMIS, isDir)) {
+    // Phase::eval
+    float density = S.multi ? phase_pdf(S, ray, wo, ls.direction) : ONE_OVER_FOUR_PI;
+    V3<float> fr_value = density * ray.albedo;
+    float fr_pdf = density;
+    if (!(fr_pdf > 0.f) || reduce_max(fr_value) < 1e-4f) {
+      shadowValid = false;
+    } else {
+      fr_value = vmin(fr_value, V3<float>(13.f));  // CLAMP_F_R
+      V3<float> tp_sr = incomingThroughput * (std::isinf(ls.pdf) ? 1.f : 1.f / ls.pdf) * fr_value *
+                        ls.radiance * 1.f;
+      // makeShadowRay (Ray.h:152-163)
+      shadowRay.hit = false;
+      shadowRay.isShadowRay = true;
+      shadowRay.dir = ls.direction;
+      shadowRay.org = P + offsetEpsilon * frontFacingSurfaceOffset;
+      shadowRay.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
+      shadowState.throughput = toh(tp_sr);
+      shadowRay.rngSeed = ray.rngSeed;
+      ray.rngSeed.next_h((uint64_t)fbits(ray.tMax));
+      shadowState.misWeight = 1.f;
+      shadowValid = true;
+      if (!isDir && needsMIS) {
+        float pdf_l = env_pdf(S.env, ls.direction);
+        float pdf_s = S.multi ? phase_pdf(S, ray, wo, ls.direction) : ONE_OVER_FOUR_PI;
+        shadowState.misWeight = pdf_l / (pdf_l + pdf_s + 1e-10f);
+        if (shadowState.misWeight < 1e-5f) shadowValid = false;
+      }
+    }
+  }
+  if (pathDepth >= 10) {  // MAX_PATH_DEPTH
+    ray.tMax = -1.f;
+    return fragment;
+  }
+  ray.hit = false;
+  ray.tMax = INF;
+  // Phase::scatter
+  V3<float> sdir;
+  float spdf;
+  V3<float> sf_r;
+  if (S.multi) {
+    V3<float> wi_in = normalize(-wo);
+    sdir = sampleHGDirection(wi_in, ray.g, random);
+    float density = hgPhase(ray.g, dot(wi_in, sdir));
+    spdf = density;
+    sf_r = ray.albedo * density;
+  } else {
+    float r1 = random();
+    float r2 = random();
+    float x = cosf(TWO_PI * r1) * sqrtf(r2 * (1.f - r2));
+    float y = sinf(TWO_PI * r1) * sqrtf(r2 * (1.f - r2));
+    float z = (1.f - 2.f * r2);
+    spdf = ONE_OVER_FOUR_PI;
+    sf_r = ray.albedo * spdf;
+    sdir = V3<float>(x, y, z);
+  }
+  if (!(spdf > 0.f) || spdf <= 1e-6f) return fragment;  // ray stays alive unchanged
+  // VOLUME scatter
+  if (S.multi) {
+    if (!S.volMS || state.numVolumeBounces >= S.maxVB) {
+      ray.tMax = -1.f;
+      return fragment;
+    }
+    state.numVolumeBounces = state.numVolumeBounces + 1;
+  } else {
+    ray.tMax = -1.f;  // SCI_VIS_MODE: volumes shadow, nothing more
+    return fragment;
+  }
+  ray.org = P + (1.f * offsetEpsilon) * frontFacingSurfaceOffset;
+  ray.dir = normalize(sdir);
+  V3<float> scatterFactor = sf_r * 1.f / (std::isinf(spdf) ? 1.f : (spdf + 1e-10f));
+  scatterFactor = vmin(scatterFactor, V3<float>(2.5f));
+  state.throughput = toh(fromh(state.throughput) * scatterFactor);
+  if (needsMIS && !std::isinf(spdf)) {
+    float pdf_s = S.multi ? phase_pdf(S, ray, wo, ray.dir) : ONE_OVER_FOUR_PI;
+    float pdf_l = env_pdf(S.env, ray.dir);
+    state.misWeight = pdf_s / (pdf_s + pdf_l);
+  } else {
+    state.misWeight = 1.f;
+  }
+  return fragment;
+}
+
+// _generateRays (generateRays.cu:72-243), perspective camera without aperture
+inline void generate(const Scene &S, int ix, int iy, int accumID, Ray &ray, PathState &state) {
+  state.misWeight = 0.f;
+  Random2 rand(unsigned(ix + S.W * accumID), unsigned(iy + S.H * accumID));
+  ray.rngSeed = RNGSeed();
+  rng_seed(ray.rngSeed, (uint32_t)(ix + accumID * S.W), (uint32_t)iy);
+  float pixel_u = ((accumID == 0) ? .5f : rand());
+  float pixel_v = ((accumID == 0) ? .5f : rand());
+  float image_u = ((ix + pixel_u) / float(S.W));
+  float image_v = ((iy + pixel_v) / float(S.H));
+  float aspect = S.W / float(S.H);
+  ray.org = S.cam.lens00;
+  V3<float> ray_dir = S.cam.dir00 + (1.f * aspect * (image_u - .5f)) * S.cam.du + (1.f * (image_v - .5f)) * S.cam.dv;
+  ray.dir = normalize(ray_dir);
+  ray.hit = false;
+  ray.isShadowRay = false;
+  ray.tMax = 1e30f;
+  state.numDiffuseBounces = 0;
+  state.numVolumeBounces = 0;
+  const float t = (iy + .5f) / float(S.H);
+  V4<float> bg = S.bg;
+  if (!(S.bg.w >= 0.f)) {
+    bg.x = (1.0f - t) * 0.9f + t * 0.15f;
+    bg.y = (1.0f - t) * 0.9f + t * 0.25f;
+    bg.z = (1.0f - t) * 0.9f + t * .8f;
+    bg.w = (1.0f - t) * 1.f + t * 1.f;
+  }
+  ray.missColor = bg;
+  state.throughput = toh(V3<float>(1.f));
+}
+
+// trace + setVolumeHit (Ray.h:118-149): albedo = 0.7*rgb (default build) or
+// scatteringAlbedo*rgb with the volume's anisotropy (multi-scatter build).
+template <typename R> inline void trace_and_record(const Scene &S, Ray &ray, Counters &cnt) {
+  R t;
+  V3<R> rgb;
+  if (trace<R>(S, ray, cnt, t, rgb)) {
+    V3<float> dirf = ray.dir;
+    if (dirf.x == 0.f) dirf.x = 1e-6f;
+    if (dirf.y == 0.f) dirf.y = 1e-6f;
+    if (dirf.z == 0.f) dirf.z = 1e-6f;
+    float tf = (float)t;
+    V3<float> rgbf((float)rgb.x, (float)rgb.y, (float)rgb.z);
+    ray.P = cvt<float>(cvt<R>(ray.org) + t * cvt<R>(dirf));
+    ray.tMax = tf;
+    ray.hit = true;
+    if (S.multi) {
+      ray.albedo = S.scatAlb * rgbf;
+      ray.g = S.aniso;
+    } else {
+      ray.albedo = .7f * rgbf;
+      ray.g = 0.f;
+    }
+  }
+}
+
+// One accumulation pass (one value of accumID) for one pixel, following
+// Context::renderTiles (Context.cpp:142-185) and _shadeRays' accumulation
+// (shadeRays.cu:970-1038).  Within a generation the pixel's shadow ray is
+// accumulated before its bounce ray.
+template <typename R> inline void render_pixel(const Scene &S, int ix, int iy, int accumID, float *acc,
+                                               Counters &cnt) {
+  Ray ray;
+  PathState state;
+  generate(S, ix, iy, accumID, ray, state);
+  bool rayAlive = true;
+  Ray sray;
+  PathState sstate;
+  bool sValid = false;
+  const float clampMax = 10.f * (1 + accumID);
+  for (int gen = 0; rayAlive || sValid; gen++) {
+    Ray nsray;
+    PathState nsstate;
+    bool nsValid = false;
+    if (sValid) {
+      trace_and_record<R>(S, sray, cnt);
+      Ray dummy;
+      PathState dstate;
+      bool dv;
+      V3<float> frag = bounce(S, sray, sstate, dummy, dstate, dv, gen);
+      frag = vmin(frag, V3<float>(clampMax));
+      if (frag.x > 0.f) acc[0] += frag.x;
+      if (frag.y > 0.f) acc[1] += frag.y;
+      if (frag.z > 0.f) acc[2] += frag.z;
+      sValid = false;
+    }
+    if (rayAlive) {
+      trace_and_record<R>(S, ray, cnt);
+      float alpha = (gen == 0) ? (ray.hit ? 1.f : ray.missColor.w) : 0.f;
+      V3<float> frag = bounce(S, ray, state, nsray, nsstate, nsValid, gen);
+      frag = vmin(frag, V3<float>(clampMax));
+      if (accumID == 0 && gen == 0) {
+        acc[0] = frag.x;
+        acc[1] = frag.y;
+        acc[2] = frag.z;
+        acc[3] = alpha;
+      } else {
+        if (gen == 0 && alpha > 0.f) acc[3] += alpha;
+        if (frag.x > 0.f) acc[0] += frag.x;
+        if (frag.y > 0.f) acc[1] += frag.y;
+        if (frag.z > 0.f) acc[2] += frag.z;
+      }
+      rayAlive = ray.tMax > 0.f;
+    }
+    if (nsValid && nsray.tMax > 0.f) {
+      sray = nsray;
+      sstate = nsstate;
+      sValid = true;
+    }
+  }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+// ===========================================================================
+// C interface
+// ===========================================================================
+extern "C" {
+
+void orc_rng_sequence(uint32_t a, uint32_t b, int n, float *out) {
+  Random2 r(a, b);
+  for (int i = 0; i < n; i++) out[i] = r();
+}
+
+void orc_rng_from_seed(uint64_t seed_state, uint64_t hash, int use_u64, int n, float *out,
+                       uint64_t *new_seed_state) {
+  (void)use_u64;
+  RNGSeed s;
+  s.state = seed_state;
+  Random2 r(s, hash);
+  for (int i = 0; i < n; i++) out[i] = r();
+  if (new_seed_state) *new_seed_state = s.state;
+}
+
+float orc_fast_log(float f) { return fastLog(f); }
+uint16_t orc_float_to_half(float f) { return f2h(f); }
+float orc_half_to_float(uint16_t h) { return h2f(h); }
+
+void orc_sample_points(const orc_scene *s, const float *P, int n, float *out) {
+  Field F = make_field(s);
+  for (int i = 0; i < n; i++)
+    out[i] = sample_field<float>(F, V3<float>(P[3 * i], P[3 * i + 1], P[3 * i + 2]));
+}
+
+void orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba) {
+  XF xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
+  for (int i = 0; i < n; i++) {
+    V4<float> r = xf_map<float>(xf, scalars[i]);
+    rgba[4 * i + 0] = r.x;
+    rgba[4 * i + 1] = r.y;
+    rgba[4 * i + 2] = r.z;
+    rgba[4 * i + 3] = r.w;
+  }
+}
+
+void orc_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]) { mc_dims_of(dims, cells_per_mc, mc_dims); }
+
+void orc_mc_ranges(const float *scalars, const int dims[3], int cpm, float *ranges) {
+  int M[3];
+  mc_dims_of(dims, cpm, M);
+  int64_t n = (int64_t)M[0] * M[1] * M[2];
+  parallel_for(n, 0, [&](int64_t tid) {
+    int x = int(tid % M[0]), y = int((tid / M[0]) % M[1]), z = int(tid / ((int64_t)M[0] * M[1]));
+    float lo, hi;
+    mc_range_one(scalars, dims, cpm, x, y, z, lo, hi);
+    ranges[2 * tid] = lo;
+    ranges[2 * tid + 1] = hi;
+  }, 64);
+}
+
+void orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n, float lo, float hi,
+                   float base_density, float *out) {
+  XF xf = make_xf(tf, tf_n, lo, hi, base_density);
+  for (int i = 0; i < num_mc; i++) out[i] = xf_majorant(xf, ranges[2 * i], ranges[2 * i + 1]);
+}
+
+int orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3], float tmax, uint64_t *seed_state,
+                  float *t_hit, float rgb[3]) {
+  Scene S;
+  build_scene(s, S);
+  Ray ray;
+  ray.org = V3<float>(org[0], org[1], org[2]);
+  ray.dir = V3<float>(dir[0], dir[1], dir[2]);
+  ray.tMax = tmax;
+  ray.rngSeed.state = *seed_state;
+  Counters c;
+  float t = 0.f;
+  V3<float> c3;
+  bool h = trace<float>(S, ray, c, t, c3);
+  *seed_state = ray.rngSeed.state;
+  if (h) {
+    *t_hit = t;
+    rgb[0] = c3.x;
+    rgb[1] = c3.y;
+    rgb[2] = c3.z;
+  }
+  return h ? 1 : 0;
+}
+
+void orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp, int use_double, int nthreads,
+                int row0, int row1, orc_stats *stats) {
+  Scene S;
+  build_scene(s, S);
+  if (row1 <= 0 || row1 > S.H) row1 = S.H;
+  if (row0 < 0) row0 = 0;
+  const int W = S.W;
+  int64_t n = (int64_t)(row1 - row0) * W;
+  std::atomic<uint64_t> ns{0}, nm{0}, nr{0};
+  parallel_for(n, nthreads, [&](int64_t i) {
+    int ix = int(i % W), iy = row0 + int(i / W);
+    float *acc = accum + 4 * ((size_t)iy * W + ix);
+    Counters c;
+    for (int p = 0; p < spp; p++) {
+      if (use_double) render_pixel<double>(S, ix, iy, accum_id_start + p, acc, c);
+      else render_pixel<float>(S, ix, iy, accum_id_start + p, acc, c);
+    }
+    ns += c.samples;
+    nm += c.mcs;
+    nr += c.rays;
+  }, 16);
+  if (stats) {
+    stats->density_samples = ns;
+    stats->mc_visits = nm;
+    stats->rays = nr;
+  }
+}
+
+// TiledFB.cu:13-50, LocalFB.cpp:60-70 (accumScale = 1/accumID), math.h:52-116
+void orc_tonemap(const float *accum, int W, int H, int accum_id, int format, void *out) {
+  float accumScale = 1.f / accum_id;
+  auto make_8bit = [](float f) -> uint32_t { return (uint32_t)mn(255, mx(0, int(f * 256.f))); };
+  auto srgb = [](float x) -> float {
+    if (x <= 0.0031308f) return 12.92f * x;
+    return 1.055f * powf(x, 1.f / 2.4f) - 0.055f;
+  };
+  for (int64_t i = 0; i < (int64_t)W * H; i++) {
+    float c[4];
+    for (int k = 0; k < 4; k++) c[k] = accum[4 * i + k] * accumScale;
+    if (format == 0) {
+      for (int k = 0; k < 4; k++) ((float *)out)[4 * i + k] = c[k];
+    } else {
+      if (format == 2) for (int k = 0; k < 3; k++) c[k] = srgb(c[k]);
+      ((uint32_t *)out)[i] = (make_8bit(c[0]) << 0) + (make_8bit(c[1]) << 8) + (make_8bit(c[2]) << 16) +
+                             (make_8bit(c[3]) << 24);
+    }
+  }
+}
+
+void orc_env_cdfs(const float *texels, const int dims[2], const int addr[2], float *cdf_y, float *cdf_x) {
+  env_cdfs(texels, dims[0], dims[1], addr, cdf_y, cdf_x);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Fixed-step emission-absorption march (project-defined form; the reference
+// has only delta tracking).  Semantics shared with the CUDA product:
+//   * camera: the perspective camera above at the pixel centre (the
+//     accumID == 0 ray of _generateRays);
+//   * [t0,t1] from boxTest against the field's world bounds, tmin 0, tmax 1e30;
+//   * n = ceil((t1-t0)/dt) steps; step i samples at t = t0+(i+.5)*dt and is
+//     skipped once t >= t1; every step covers a length dt;
+//   * sampleAndMap gives (rgb, sigma) (sigma already times densityAt1);
+//     x_i = sigma_i*dt, alpha_i = -expm1(-x_i), T_i = exp(-tau_i) with
+//     tau_i = sum_{k<i} x_k (compensated sum);
+//   * C = sum_i T_i*alpha_i*rgb_i, A = -expm1(-tau_n); pixel = (C, A).
+// The adjoint uses dC/dx_j = rgb_j*T_{j+1} - (C - C_{<=j}), dA/dx_j = T_n,
+// dC/drgb_j = T_j*alpha_j: a front-to-back replay that stores no per-step
+// state.
+// ===========================================================================
+namespace orc {
+
+struct EAView { Camera cam; int W, H; };
+
+template <typename R> struct EAStep {
+  R t0, t1, dt;
+  int n;
+};
+
+template <typename R>
+inline bool ea_setup(const Field &F, const EAView &v, int ix, int iy, R step, V3<R> &org, V3<R> &dir, EAStep<R> &st) {
+  float image_u = ((ix + .5f) / float(v.W));
+  float image_v = ((iy + .5f) / float(v.H));
+  float aspect = v.W / float(v.H);
+  V3<float> d = v.cam.dir00 + (1.f * aspect * (image_u - .5f)) * v.cam.du + (1.f * (image_v - .5f)) * v.cam.dv;
+  d = normalize(d);
+  org = cvt<R>(v.cam.lens00);
+  dir = cvt<R>(d);
+  R t0 = R(0), t1 = R(1e30f);
+  if (!boxTest<R>(org, dir, t0, t1, cvt<R>(F.boundsLo), cvt<R>(F.boundsHi))) return false;
+  if (!(t1 > t0)) return false;
+  st.t0 = t0;
+  st.t1 = t1;
+  st.dt = step;
+  st.n = (int)std::ceil((t1 - t0) / step);
+  return true;
+}
+
+template <typename R>
+inline void ea_forward_pixel(const Field &F, const XF &xf, const EAView &v, int ix, int iy, R step, R out[4]) {
+  out[0] = out[1] = out[2] = out[3] = R(0);
+  V3<R> org, dir;
+  EAStep<R> st;
+  if (!ea_setup<R>(F, v, ix, iy, step, org, dir, st)) return;
+  R tau = 0, comp = 0;  // Neumaier-compensated optical depth
+  R C[3] = {0, 0, 0};
+  for (int i = 0; i < st.n; i++) {
+    R t = st.t0 + (R(i) + R(.5)) * st.dt;
+    if (t >= st.t1) break;
+    V3<R> P = org + t * dir;
+    V4<R> smp = sample_and_map<R>(F, xf, P);
+    R x = smp.w * st.dt;
+    R T = std::exp(-(tau + comp));
+    R alpha = -std::expm1(-x);
+    R w = T * alpha;
+    C[0] += w * smp.x;
+    C[1] += w * smp.y;
+    C[2] += w * smp.z;
+    R tnew = tau + x;
+    if (std::fabs(tau) >= std::fabs(x)) comp += (tau - tnew) + x;
+    else comp += (x - tnew) + tau;
+    tau = tnew;
+  }
+  out[0] = C[0];
+  out[1] = C[1];
+  out[2] = C[2];
+  out[3] = -std::expm1(-(tau + comp));
+}
+
+inline void ea_backward_pixel(const Field &F, const XF &xf, const EAView &v, int ix, int iy, double step,
+                              const float g[4], double *d_vox, double *d_tf) {
+  V3<double> org, dir;
+  EAStep<double> st;
+  if (!ea_setup<double>(F, v, ix, iy, step, org, dir, st)) return;
+  double Cfin[4];
+  ea_forward_pixel<double>(F, xf, v, ix, iy, step, Cfin);
+  const double Tn = 1.0 - Cfin[3];
+  double tau = 0, comp = 0;
+  double Cacc[3] = {0, 0, 0};
+  const double gs = double(xf.n - 1) / double(xf.span);
+  const size_t Nx = F.N[0], Ny = F.N[1];
+  for (int i = 0; i < st.n; i++) {
+    double t = st.t0 + (double(i) + .5) * st.dt;
+    if (t >= st.t1) break;
+    V3<double> P = org + t * dir;
+    Tri tri;
+    double s = sample_field<double>(F, P, &tri);
+    if (std::isnan(s)) continue;  // sampleAndMap -> 0: no dependence
+    int idx;
+    double f;
+    bool clamped;
+    V4<double> m = xf_map<double>(xf, s, &idx, &f, &clamped);
+    double x = m.w * st.dt;
+    double T = std::exp(-(tau + comp));
+    double alpha = -std::expm1(-x);
+    double w = T * alpha;
+    Cacc[0] += w * m.x;
+    Cacc[1] += w * m.y;
+    Cacc[2] += w * m.z;
+    double tnew = tau + x;
+    if (std::fabs(tau) >= std::fabs(x)) comp += (tau - tnew) + x;
+    else comp += (x - tnew) + tau;
+    tau = tnew;
+    double Tnext = std::exp(-(tau + comp));
+    // dL/dx
+    double dLdx = g[3] * Tn;
+    double rgb[3] = {m.x, m.y, m.z};
+    for (int c = 0; c < 3; c++) dLdx += g[c] * (rgb[c] * Tnext - (Cfin[c] - Cacc[c]));
+    double dLdsigma = dLdx * st.dt;        // sigma = w_tf * baseDensity
+    double dLdrgb[3];
+    for (int c = 0; c < 3; c++) dLdrgb[c] = g[c] * w;
+    // transfer-function entries
+    const float *v0 = xf.v + 4 * idx, *v1 = xf.v + 4 * (idx + 1);
+    double bd = xf.baseDensity;
+    for (int c = 0; c < 3; c++) {
+      d_tf[4 * idx + c] += dLdrgb[c] * (1.0 - f);
+      d_tf[4 * (idx + 1) + c] += dLdrgb[c] * f;
+    }
+    d_tf[4 * idx + 3] += dLdsigma * bd * (1.0 - f);
+    d_tf[4 * (idx + 1) + 3] += dLdsigma * bd * f;
+    // scalar
+    if (clamped) continue;
+    double dLds = dLdsigma * bd * (double(v1[3]) - double(v0[3])) * gs;
+    for (int c = 0; c < 3; c++) dLds += dLdrgb[c] * (double(v1[c]) - double(v0[c])) * gs;
+    double wx[2] = {1.0 - tri.fx, tri.fx}, wy[2] = {1.0 - tri.fy, tri.fy}, wz[2] = {1.0 - tri.fz, tri.fz};
+    for (int kz = 0; kz < 2; kz++)
+      for (int ky = 0; ky < 2; ky++)
+        for (int kx = 0; kx < 2; kx++) {
+          size_t vi = tri.ix[kx] + Nx * (tri.iy[ky] + Ny * (size_t)tri.iz[kz]);
+          d_vox[vi] += dLds * wx[kx] * wy[ky] * wz[kz];
+        }
+  }
+}
+
+}  // namespace orc
+
+extern "C" {
+
+void orc_ea_render(const orc_scene *s, const orc_ea_view *views, int num_views, float step, int use_double,
+                   int nthreads, float *images) {
+  Field F = make_field(s);
+  XF xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
+  size_t off = 0;
+  for (int vi = 0; vi < num_views; vi++) {
+    EAView v{commit_camera(views[vi].pos, views[vi].dir, views[vi].up, views[vi].fovy), views[vi].width,
+             views[vi].height};
+    float *img = images + off;
+    parallel_for((int64_t)v.W * v.H, nthreads, [&](int64_t i) {
+      int ix = int(i % v.W), iy = int(i / v.W);
+      if (use_double) {
+        double o[4];
+        ea_forward_pixel<double>(F, xf, v, ix, iy, (double)step, o);
+        for (int k = 0; k < 4; k++) img[4 * i + k] = (float)o[k];
+      } else {
+        float o[4];
+        ea_forward_pixel<float>(F, xf, v, ix, iy, step, o);
+        for (int k = 0; k < 4; k++) img[4 * i + k] = o[k];
+      }
+    }, 64);
+    off += (size_t)4 * v.W * v.H;
+  }
+}
+
+void orc_ea_backward(const orc_scene *s, const orc_ea_view *views, int num_views, float step, const float *d_images,
+                     int nthreads, double *d_scalars, double *d_tf) {
+  Field F = make_field(s);
+  XF xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
+  size_t nvox = (size_t)s->dims[0] * s->dims[1] * s->dims[2];
+  int nt = nthreads > 0 ? nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
+  // per-thread privatised gradients, reduced at the end (deterministic order)
+  std::vector<std::vector<double>> gv(nt, std::vector<double>(nvox, 0.0));
+  std::vector<std::vector<double>> gt(nt, std::vector<double>((size_t)4 * s->tf_n, 0.0));
+  size_t off = 0;
+  for (int vi = 0; vi < num_views; vi++) {
+    EAView v{commit_camera(views[vi].pos, views[vi].dir, views[vi].up, views[vi].fovy), views[vi].width,
+             views[vi].height};
+    const float *g = d_images + off;
+    int64_t npx = (int64_t)v.W * v.H;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; t++)
+      pool.emplace_back([&, t]() {
+        for (int64_t i = t; i < npx; i += nt)
+          ea_backward_pixel(F, xf, v, int(i % v.W), int(i / v.W), (double)step, g + 4 * i, gv[t].data(),
+                            gt[t].data());
+      });
+    for (auto &th : pool) th.join();
+    off += (size_t)4 * npx;
+  }
+  for (size_t i = 0; i < nvox; i++) {
+    double a = 0;
+    for (int t = 0; t < nt; t++) a += gv[t][i];
+    d_scalars[i] = a;
+  }
+  for (size_t i = 0; i < (size_t)4 * s->tf_n; i++) {
+    double a = 0;
+    for (int t = 0; t < nt; t++) a += gt[t][i];
+    d_tf[i] = a;
+  }
+}
+
+}  // extern "C"

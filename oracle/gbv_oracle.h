@@ -1,0 +1,124 @@
+/* gbv_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * C interface of the CPU oracle: a restatement of the reference renderer's
+ * embree (CPU) backend for the structured-volume path (Barney 1.1.8).  Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
+ * this library.  It is the checker, never the product.
+ *
+ * parity unpinned: the reference ships no golden vectors or known-answer tests
+ * for this path, and its sources cannot be built here (the owl, embree, cuBQL
+ * and optix submodules are empty).  The oracle is pinned only by hand-computed
+ * known-answer tests and by a second, pure-Python restatement of its scalar
+ * kernels (tests/golden/make_golden.py).
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_scene {
+  /* structured field (StructuredData: "dims", "gridOrigin", "gridSpacing") */
+  const float *scalars;      /* x-fastest, dims[0]*dims[1]*dims[2] */
+  int   dims[3];
+  float origin[3];
+  float spacing[3];
+  /* macrocells */
+  int   cells_per_mc;        /* 8 in the reference; 16 for the 512^3 scene */
+  const float *majorants;    /* optional; if null the oracle builds its own */
+  /* transfer function (TransferFunction::set) */
+  const float *tf;           /* n x RGBA */
+  int   tf_n;
+  float domain[2];
+  float base_density;        /* "densityAt1" */
+  /* volume params of the multi-scatter build (Volume.h:158-159) */
+  float anisotropy;
+  float scattering_albedo;
+  /* perspective camera parameters (Camera.cu PerspectiveCamera) */
+  float cam_pos[3], cam_dir[3], cam_up[3];
+  float fovy;
+  /* directional lights (DirLight), at most 4 */
+  int   num_dir_lights;
+  float dir_light_dir[4][3];
+  float dir_light_color[4][3];
+  float dir_light_radiance[4];
+  /* env-map light (EnvMapLight); env_texels == 0 means "no env map" */
+  const float *env_texels;   /* RGBA float, env_dims[0] x env_dims[1] */
+  int   env_dims[2];
+  int   env_addr[2];         /* 0 wrap, 1 clamp, 2 border, 3 mirror */
+  float env_dir[3], env_up[3];
+  float env_scale;
+  /* renderer */
+  float bg_color[4];
+  float ambient_radiance;
+  int   multi_scatter;       /* 0: default build (SCI_VIS_MODE), 1: multi-scatter build */
+  int   volume_multi_scatter;
+  int   max_volume_bounces;
+  /* frame */
+  int   width, height;
+} orc_scene;
+
+typedef struct orc_stats {
+  uint64_t density_samples;  /* sampleAndMap evaluations */
+  uint64_t mc_visits;        /* DDA cells with a non-zero majorant */
+  uint64_t rays;             /* traced rays */
+} orc_stats;
+
+/* --- scalar kernels, exposed for known-answer tests --- */
+void  orc_rng_sequence(uint32_t a, uint32_t b, int n, float *out);
+void  orc_rng_from_seed(uint64_t seed_state, uint64_t hash, int use_u64, int n,
+                        float *out, uint64_t *new_seed_state);
+float orc_fast_log(float f);
+uint16_t orc_float_to_half(float f);
+float orc_half_to_float(uint16_t h);
+void  orc_sample_points(const orc_scene *s, const float *P, int n, float *out);
+void  orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba);
+
+/* --- macrocell build (StructuredData_computeMCs + mapMCs) --- */
+void  orc_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
+void  orc_mc_ranges(const float *scalars, const int dims[3], int cells_per_mc,
+                    float *ranges /* 2 per MC */);
+void  orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n,
+                    float lo, float hi, float base_density, float *out);
+
+/* --- one ray through the volume (MCVolumeAccel::isProg) --- */
+int   orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3],
+                    float tmax, uint64_t *seed_state, float *t_hit, float rgb[3]);
+
+/* --- full render: bnRender's generate/trace/shade loop for `spp`
+       consecutive accumulation passes starting at accum_id_start.
+       accum: width*height RGBA, row-major, y=0 the bottom row.
+       use_double: evaluate everything downstream of the RNG in double.
+       rows: render only rows [row0, row1) (row1<=0 means all). --- */
+void  orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp,
+                 int use_double, int nthreads, int row0, int row1,
+                 orc_stats *stats);
+
+/* --- frame-buffer read (linearizeColorAndNormalKernel); format:
+       0 float4, 1 RGBA8, 2 sRGB RGBA8 --- */
+void  orc_tonemap(const float *accum, int width, int height, int accum_id,
+                  int format, void *out);
+
+/* --- env map importance tables (EnvMap.cu computeCDFs) --- */
+void  orc_env_cdfs(const float *texels, const int dims[2], const int addr[2],
+                   float *cdf_y, float *cdf_x);
+
+/* --- fixed-step emission-absorption (project-defined form) --- */
+typedef struct orc_ea_view {
+  float pos[3], dir[3], up[3];
+  float fovy;
+  int   width, height;
+} orc_ea_view;
+
+void  orc_ea_render(const orc_scene *s, const orc_ea_view *views, int num_views,
+                    float step, int use_double, int nthreads, float *images);
+/* gradient of L = sum(w * image) with respect to voxels and TF entries, in
+   FP64; d_images holds w (dL/dimage). */
+void  orc_ea_backward(const orc_scene *s, const orc_ea_view *views,
+                      int num_views, float step, const float *d_images,
+                      int nthreads, double *d_scalars, double *d_tf);
+
+#ifdef __cplusplus
+}
+#endif
