@@ -1,0 +1,226 @@
+"""Python binding of the barney-compatible bn* C API (include/barney_gb300.h).
+
+Mirrors how an application drives the reference renderer through
+barney/include/barney.h: create a context, a structured scalar field from a
+3D texture, a volume with a transfer function, lights, a group, a model, a
+camera, a renderer and a frame buffer, then bnRender and bnFrameBufferRead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .scenes import Scene
+
+BN_OBJECT = 2
+BN_FLOAT32 = 180
+BN_FLOAT4 = 183
+BN_UFIXED8 = 300
+BN_UFIXED8_RGBA = 301
+BN_UFIXED8_RGBA_SRGB = 302
+BN_FB_COLOR = 1
+BN_TEXTURE_NEAREST, BN_TEXTURE_LINEAR = 0, 1
+
+BN_SYMBOLS = [
+    "bnContextCreate", "bnContextDestroy", "bnRelease", "bnAddReference", "bnCameraCreate",
+    "bnFrameBufferCreate", "bnModelCreate", "bnRendererCreate", "bnDataCreate", "bnTextureData3DCreate",
+    "bnTexture2DCreate", "bnLightCreate", "bnGroupCreate", "bnGroupBuild", "bnScalarFieldCreate",
+    "bnVolumeCreate", "bnVolumeSetXF", "bnCommit", "bnSetString", "bnSetData", "bnSetObject", "bnSetLight",
+    "bnSet1i", "bnSet2i", "bnSet3i", "bnSet4i", "bnSet1f", "bnSet2f", "bnSet3f", "bnSet4f", "bnSet4x3fv",
+    "bnSetInstances", "bnBuild", "bnAccumReset", "bnFrameBufferResize", "bnFrameBufferRead",
+    "bnFrameBufferGetSize", "bnRender", "bnGetLastError", "bnFrameBufferGetStats",
+]
+
+
+class BnFloat2(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float)]
+
+
+_ready = False
+
+
+def lib() -> C.CDLL:
+    global _ready
+    L = N.lib()
+    if not _ready:
+        vp, i, f, cp = C.c_void_p, C.c_int, C.c_float, C.c_char_p
+        sig = {
+            "bnContextCreate": (vp, [vp, i, vp, i]),
+            "bnContextDestroy": (None, [vp]),
+            "bnRelease": (None, [vp]),
+            "bnAddReference": (None, [vp]),
+            "bnCameraCreate": (vp, [vp, cp]),
+            "bnFrameBufferCreate": (vp, [vp, i]),
+            "bnModelCreate": (vp, [vp]),
+            "bnRendererCreate": (vp, [vp, cp]),
+            "bnDataCreate": (vp, [vp, i, i, C.c_size_t, vp]),
+            "bnTextureData3DCreate": (vp, [vp, i, i, i, i, i, vp]),
+            "bnTexture2DCreate": (vp, [vp, i, i, C.c_uint32, C.c_uint32, vp, i, i, i, i]),
+            "bnLightCreate": (vp, [vp, i, cp]),
+            "bnGroupCreate": (vp, [vp, i, vp, i, vp, i]),
+            "bnGroupBuild": (None, [vp]),
+            "bnScalarFieldCreate": (vp, [vp, i, cp]),
+            "bnVolumeCreate": (vp, [vp, i, vp]),
+            "bnVolumeSetXF": (None, [vp, BnFloat2, vp, i, f]),
+            "bnCommit": (None, [vp]),
+            "bnSetData": (None, [vp, cp, vp]),
+            "bnSetObject": (None, [vp, cp, vp]),
+            "bnSet1i": (None, [vp, cp, i]),
+            "bnSet3i": (None, [vp, cp, i, i, i]),
+            "bnSet1f": (None, [vp, cp, f]),
+            "bnSet3f": (None, [vp, cp, f, f, f]),
+            "bnSet4f": (None, [vp, cp, f, f, f, f]),
+            "bnSetInstances": (None, [vp, i, vp, vp, i]),
+            "bnBuild": (None, [vp, i]),
+            "bnAccumReset": (None, [vp]),
+            "bnFrameBufferResize": (None, [vp, i, i, i, C.c_uint32]),
+            "bnFrameBufferRead": (None, [vp, i, vp, i]),
+            "bnFrameBufferGetSize": (None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+            "bnRender": (None, [vp, vp, vp, vp]),
+            "bnGetLastError": (cp, []),
+            "bnFrameBufferGetStats": (None, [vp, C.POINTER(C.c_ulonglong)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _ready = True
+    return L
+
+
+def last_error() -> str:
+    return (lib().bnGetLastError() or b"").decode(errors="replace")
+
+
+def _ok(h, what):
+    if not h:
+        raise N.GbvError(f"{what} failed: {last_error()}")
+    return h
+
+
+class BarneySession:
+    """One context holding one structured-volume scene, driven through bn*.
+
+    `scalars_host` may be any C-contiguous float32 host buffer pointer source
+    (numpy array or pinned torch tensor); set_volume uploads it every call, as
+    bnTextureData3DCreate copies texels at create time.
+    """
+
+    def __init__(self, gpu: int = 0):
+        L = lib()
+        ids = (C.c_int * 1)(gpu)
+        self.ctx = _ok(L.bnContextCreate(None, 1, ids, 1), "bnContextCreate")
+        self.L = L
+        self.keep = []
+
+    def close(self):
+        if self.ctx:
+            self.L.bnContextDestroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
+                    layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4):
+        L, ctx, s = self.L, self.ctx, scene
+        nx, ny, nz = s.dims
+        td = _ok(L.bnTextureData3DCreate(ctx, 0, BN_FLOAT32, nx, ny, nz, C.c_void_p(scalars_ptr)),
+                 "bnTextureData3DCreate")
+        sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"structured"), "bnScalarFieldCreate")
+        L.bnSetObject(sf, b"textureData", td)
+        L.bnSet3i(sf, b"dims", nx, ny, nz)
+        origin, spacing = s.geometry()
+        L.bnSet3f(sf, b"gridOrigin", *origin)
+        L.bnSet3f(sf, b"gridSpacing", *spacing)
+        L.bnSet1i(sf, b"cellsPerMacrocell", s.cells_per_mc)
+        L.bnSet1i(sf, b"voxelFormat", voxel_format)
+        L.bnSet1i(sf, b"voxelLayout", layout)
+        L.bnCommit(sf)
+        vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
+        tf = np.ascontiguousarray(s.tf, np.float32)
+        self.keep.append(tf)
+        L.bnVolumeSetXF(vol, BnFloat2(*s.domain), tf.ctypes.data_as(C.c_void_p), tf.shape[0], s.base_density)
+        L.bnSet1f(vol, b"anisotropy", s.anisotropy)
+        L.bnSet1f(vol, b"scatteringAlbedo", s.scattering_albedo)
+        L.bnCommit(vol)
+        lights = []
+        for d, c, rad in s.dir_lights:
+            l = _ok(L.bnLightCreate(ctx, 0, b"directional"), "bnLightCreate")
+            L.bnSet3f(l, b"direction", *d)
+            L.bnSet3f(l, b"color", *c)
+            L.bnSet1f(l, b"radiance", rad)
+            L.bnCommit(l)
+            lights.append(l)
+        if s.env is not None:
+            e = s.env
+            H, W, _ = e.texels.shape
+            tex = _ok(L.bnTexture2DCreate(ctx, 0, BN_FLOAT4, W, H, e.texels.ctypes.data_as(C.c_void_p),
+                                          BN_TEXTURE_LINEAR, e.addr[0], e.addr[1], 0), "bnTexture2DCreate")
+            l = _ok(L.bnLightCreate(ctx, 0, b"envmap"), "bnLightCreate")
+            L.bnSetObject(l, b"texture", tex)
+            L.bnSet3f(l, b"direction", *e.direction)
+            L.bnSet3f(l, b"up", *e.up)
+            L.bnSet1f(l, b"scale", e.scale)
+            L.bnCommit(l)
+            lights.append(l)
+        vols = (C.c_void_p * 1)(vol)
+        grp = _ok(L.bnGroupCreate(ctx, 0, None, 0, vols, 1), "bnGroupCreate")
+        if lights:
+            arr = (C.c_void_p * len(lights))(*lights)
+            data = _ok(L.bnDataCreate(ctx, 0, BN_OBJECT, len(lights), arr), "bnDataCreate")
+            L.bnSetData(grp, b"lights", data)
+        L.bnCommit(grp)
+        L.bnGroupBuild(grp)
+        model = _ok(L.bnModelCreate(ctx), "bnModelCreate")
+        groups = (C.c_void_p * 1)(grp)
+        L.bnSetInstances(model, 0, groups, None, 1)
+        L.bnBuild(model, 0)
+        cam = _ok(L.bnCameraCreate(ctx, b"perspective"), "bnCameraCreate")
+        L.bnSet3f(cam, b"position", *s.cam_pos)
+        L.bnSet3f(cam, b"direction", *s.cam_dir)
+        L.bnSet3f(cam, b"up", *s.cam_up)
+        L.bnSet1f(cam, b"fovy", s.fovy)
+        L.bnCommit(cam)
+        r = _ok(L.bnRendererCreate(ctx, b"default"), "bnRendererCreate")
+        L.bnSet1i(r, b"pathsPerPixel", s.spp)
+        L.bnSet1f(r, b"ambientRadiance", s.ambient)
+        L.bnSet4f(r, b"bgColor", *s.bg_color)
+        L.bnSet1i(r, b"multiScatter", s.multi_scatter)
+        L.bnSet1i(r, b"volumeMultiScatter", s.volume_multi_scatter)
+        L.bnSet1i(r, b"maxVolumeBounces", s.max_volume_bounces)
+        L.bnCommit(r)
+        fb = _ok(L.bnFrameBufferCreate(ctx, 0), "bnFrameBufferCreate")
+        L.bnFrameBufferResize(fb, color_format, s.width, s.height, BN_FB_COLOR)
+        self.handles = dict(td=td, sf=sf, vol=vol, grp=grp, model=model, cam=cam, renderer=r, fb=fb)
+        self.scene, self.color_format = s, color_format
+        err = last_error()
+        return err
+
+    def render(self) -> None:
+        h = self.handles
+        self.L.bnRender(h["renderer"], h["model"], h["cam"], h["fb"])
+
+    def read(self, out=None):
+        s = self.scene
+        if out is None:
+            out = (np.empty((s.height, s.width, 4), np.float32) if self.color_format == BN_FLOAT4
+                   else np.empty((s.height, s.width), np.uint32))
+        ptr = out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()
+        self.L.bnFrameBufferRead(self.handles["fb"], BN_FB_COLOR, C.c_void_p(ptr), self.color_format)
+        return out
+
+    def stats(self):
+        st = (C.c_ulonglong * 4)()
+        self.L.bnFrameBufferGetStats(self.handles["fb"], st)
+        return list(st)
+
+    def release_scene(self):
+        for k in ("fb", "renderer", "cam", "model", "grp", "vol", "sf", "td"):
+            self.L.bnRelease(self.handles[k])
+        self.handles = {}

@@ -135,7 +135,9 @@ def env_sky(width: int = 512, height: int = 256) -> EnvMap:
     sun = np.array([math.cos(se) * math.cos(sa), math.cos(se) * math.sin(sa), math.sin(se)])
     d = np.stack([np.cos(elev) * np.cos(phi), np.cos(elev) * np.sin(phi), np.sin(elev)], axis=-1)
     ang = np.arccos(np.clip(d @ sun, -1, 1))
-    rgb = np.where((ang < math.radians(1.5))[..., None], np.array([50.0, 47.0, 42.0]), rgb)
+    disk = ang < math.radians(1.5)
+    disk.flat[np.argmin(ang)] = True  # a coarse map still gets its sun texel
+    rgb = np.where(disk[..., None], np.array([50.0, 47.0, 42.0]), rgb)
     tex = np.concatenate([rgb, np.ones_like(rgb[..., :1])], axis=-1).astype(np.float32)
     return EnvMap(texels=np.ascontiguousarray(tex))
 

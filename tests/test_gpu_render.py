@@ -1,4 +1,11 @@
-"""Render parity: the sm_103a frame render against the CPU oracle."""
+"""Render parity: the sm_103a frame render against the CPU oracle.
+
+* single scatter (the reference's default build): no transcendental function
+  on the device path, so frames match the oracle bit for bit;
+* multiple scattering with an env map: sinf/cosf/acosf/atan2f of CUDA and of
+  the host libm differ in the last ulp, so paths can part; frames agree
+  statistically (per-pixel means within 3 sigma, RMSE falling as 1/sqrt(spp)).
+"""
 import numpy as np
 import pytest
 
@@ -10,11 +17,25 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def render_pair(s, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=N.GBV_VOXEL_F32, spp=None, start=0, oracle_vol=None):
+    import torch
+    g = GpuScene(s, layout=layout, fmt=fmt)
+    counters = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    acc_g = g.new_accum()
+    g.render(spp=spp, accum=acc_g, accum_id_start=start, counters=counters)
+    torch.cuda.synchronize()
+    o = oracle.Oracle(s, scalars=oracle_vol)
+    acc_o = np.zeros((s.height, s.width, 4), np.float32)
+    o.render(spp=spp, accum=acc_o, accum_id_start=start)
+    return acc_g.cpu().numpy(), acc_o, counters.cpu().numpy(), o.stats
+
+
 @pytest.mark.parametrize("layout", [N.GBV_LAYOUT_LINEAR, N.GBV_LAYOUT_BRICK_CORNERS])
 def test_single_scatter_bit_exact(cuda, layout):
-    """Single-scatter frames (the reference's default build) touch no
-    transcendental on the device path, so the GPU frame equals the oracle's
-    bit for bit, pass after pass."""
     import torch
     s = scenes.small_scene(dims=64, spp=4, width=128, height=96)
     g = GpuScene(s, layout=layout)
@@ -22,10 +43,156 @@ def test_single_scatter_bit_exact(cuda, layout):
     acc_g = g.render(spp=4)
     torch.cuda.synchronize()
     acc_o = o.render(spp=4)
-    a = acc_g.cpu().numpy()
-    np.testing.assert_array_equal(a.view(np.uint32), acc_o.view(np.uint32))
+    np.testing.assert_array_equal(bits(acc_g.cpu().numpy()), bits(acc_o))
     # progressive accumulation continues exactly
     g.render(spp=3, accum=acc_g, accum_id_start=4)
     o.render(spp=3, accum=acc_o, accum_id_start=4)
     torch.cuda.synchronize()
-    np.testing.assert_array_equal(acc_g.cpu().numpy().view(np.uint32), acc_o.view(np.uint32))
+    np.testing.assert_array_equal(bits(acc_g.cpu().numpy()), bits(acc_o))
+
+
+def test_counters_match_oracle(cuda):
+    s = scenes.small_scene(dims=64, spp=2, width=64, height=64)
+    a, b, c, st = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+    assert c[N.GBV_NUM_COUNTERS - 1] == 0
+    assert c[0] == st["density_samples"] and c[1] == st["mc_visits"] and c[2] == st["rays"]
+
+
+def test_full_small_workload_bit_exact(cuda):
+    # the small workload as named: 64^3, 256x256, 16 spp
+    s = scenes.small_scene()
+    a, b, _, _ = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+
+
+@pytest.mark.parametrize("fmt", [N.GBV_VOXEL_F16, N.GBV_VOXEL_BF16])
+def test_half_storage_matches_oracle_on_rounded_voxels(cuda, fmt):
+    """FP16/BF16 bricks hold the round-to-nearest-even voxels; the oracle on
+    those rounded voxels gives the identical frame."""
+    s = scenes.small_scene(dims=48, spp=2, width=96, height=64)
+    v = s.scalars
+    if fmt == N.GBV_VOXEL_F16:
+        r = v.astype(np.float16).astype(np.float32)
+    else:
+        u = v.view(np.uint32).astype(np.uint64)
+        u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+        r = u.astype(np.uint32).view(np.float32)
+    a, b, _, _ = render_pair(s, fmt=fmt, oracle_vol=r)
+    np.testing.assert_array_equal(bits(a), bits(b))
+
+
+def test_u8_storage_error_bounded(cuda):
+    s = scenes.small_scene(dims=48, spp=8, width=96, height=64)
+    import torch
+    g32 = GpuScene(s, fmt=N.GBV_VOXEL_F32)
+    g8 = GpuScene(s, fmt=N.GBV_VOXEL_U8_SCALED)
+    a = g32.render().cpu().numpy() / s.spp
+    b = g8.render().cpu().numpy() / s.spp
+    torch.cuda.synchronize()
+    rmse = float(np.sqrt(np.mean((a[..., :3] - b[..., :3]) ** 2)))
+    assert rmse < 0.05, rmse
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (17, 9), (33, 65)])
+def test_ragged_frames(cuda, w, h):
+    s = scenes.small_scene(dims=32, spp=2, width=w, height=h)
+    a, b, _, _ = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+
+
+def test_camera_inside_volume_and_looking_away(cuda):
+    s = scenes.small_scene(dims=32, spp=2, width=48, height=32)
+    s.cam_pos, s.cam_dir = (0.05, -0.1, 0.2), (0.3, 0.2, -1.0)
+    a, b, _, _ = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+    s.cam_pos, s.cam_dir = (0.0, 0.0, 2.5), (0.0, 0.0, 1.0)
+    a, b, _, _ = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+    assert np.all(a[..., :3] == 0) and np.all(a[..., 3] == s.spp)
+
+
+def test_degenerate_volume(cuda):
+    vol = scenes.blob_volume((2, 2, 2), 1, seed=9)
+    s = scenes.small_scene(dims=8, spp=2, width=32, height=32)
+    s.scalars = vol
+    a, b, _, _ = render_pair(s)
+    np.testing.assert_array_equal(bits(a), bits(b))
+
+
+def test_tonemap_formats(cuda):
+    import torch
+    s = scenes.small_scene(dims=32, spp=3, width=40, height=24)
+    g = GpuScene(s)
+    acc = g.render()
+    o = oracle.Oracle(s)
+    ref = o.render()
+    for fmt in (N.GBV_FB_FLOAT4, N.GBV_FB_RGBA8, N.GBV_FB_RGBA8_SRGB):
+        out = g.tonemap(acc, 3, fmt).cpu().numpy()
+        exp = o.tonemap(ref, 3, fmt)
+        if fmt == N.GBV_FB_FLOAT4:
+            np.testing.assert_array_equal(bits(out), bits(exp))
+        elif fmt == N.GBV_FB_RGBA8:
+            np.testing.assert_array_equal(out.view(np.uint32), exp)
+        else:  # powf of CUDA and libm may differ by an ulp: allow one code step
+            d = np.abs(out.view(np.uint8).astype(int) - exp.view(np.uint8).astype(int))
+            assert d.max() <= 1
+
+
+def _ms_scene(spp, w=64, h=48, dims=48):
+    s = scenes.frame_scene(dims=dims, width=w, height=h, spp=spp)
+    s.env = scenes.env_sky(64, 32)
+    return s
+
+
+def test_multi_scatter_statistical(cuda):
+    """Per-pixel means of GPU and oracle agree within 3 sigma (sigma from 8
+    independent batches of each) and most pixels are bit-identical."""
+    import torch
+    B, per = 8, 8
+    s = _ms_scene(per)
+    g = GpuScene(s)
+    o = oracle.Oracle(s)
+    ig, io = [], []
+    for b in range(B):
+        acc = g.new_accum()
+        g.render(spp=per, accum=acc, accum_id_start=1 + b * per)
+        ig.append(acc.cpu().numpy()[..., :3] / per)
+        ao = np.zeros((s.height, s.width, 4), np.float32)
+        o.render(spp=per, accum=ao, accum_id_start=1 + b * per)
+        io.append(ao[..., :3] / per)
+    torch.cuda.synchronize()
+    ig, io = np.stack(ig), np.stack(io)
+    mg, mo = ig.mean(0), io.mean(0)
+    sg, so = ig.std(0, ddof=1) / np.sqrt(B), io.std(0, ddof=1) / np.sqrt(B)
+    sig = np.sqrt(sg ** 2 + so ** 2) + 1e-6
+    frac_out = np.mean(np.abs(mg - mo) > 3 * sig)
+    assert frac_out < 0.01, frac_out
+    same = np.mean(np.all(ig == io, axis=-1))
+    assert same > 0.5, same
+
+
+def test_rmse_falls_as_inverse_sqrt_spp(cuda):
+    import torch
+    s = _ms_scene(1, w=48, h=32, dims=32)
+    g = GpuScene(s)
+    ref = g.new_accum()
+    g.render(spp=1024, accum=ref, accum_id_start=100000)
+    ref = ref.cpu().numpy()[..., :3] / 1024
+    rmse = {}
+    for spp in (4, 16, 64):
+        vals = []
+        for rep in range(3):
+            acc = g.new_accum()
+            g.render(spp=spp, accum=acc, accum_id_start=1 + rep * 1000)
+            vals.append(np.sqrt(np.mean((acc.cpu().numpy()[..., :3] / spp - ref) ** 2)))
+        rmse[spp] = float(np.mean(vals))
+    torch.cuda.synchronize()
+    r1, r2 = rmse[4] / rmse[16], rmse[16] / rmse[64]
+    assert 1.5 < r1 < 2.7 and 1.5 < r2 < 2.7, rmse
+    # the oracle converges to the same image
+    o = oracle.Oracle(s)
+    ao = np.zeros((s.height, s.width, 4), np.float32)
+    o.render(spp=16, accum=ao, accum_id_start=1)
+    ro = float(np.sqrt(np.mean((ao[..., :3] / 16 - ref) ** 2)))
+    assert ro < 1.5 * rmse[16], (ro, rmse)

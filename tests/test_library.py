@@ -1,0 +1,101 @@
+"""The native library without a GPU: it loads, exports every entry point its
+headers declare, validates arguments before touching the device, and the
+host-side generator is deterministic."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from barney_gb300 import _native as N
+from barney_gb300 import bn, scenes
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b((?:gbv|bn)[A-Za-z0-9_]*)\s*\(", text):
+            name = m.group(1)
+            if name.startswith("gbv_") or re.match(r"bn[A-Z]", name):
+                names.add(name)
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = N.lib()
+    names = declared_functions()
+    assert len(names) >= 50
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(bn.BN_SYMBOLS) <= names
+
+
+def test_mc_dims():
+    out = (C.c_int * 3)()
+    assert N.lib().gbv_mc_dims(N.ivec(64, 64, 64), 8, out) == N.GBV_OK
+    assert tuple(out) == (8, 8, 8)
+    assert N.lib().gbv_mc_dims(N.ivec(512, 512, 512), 16, out) == N.GBV_OK
+    assert tuple(out) == (32, 32, 32)
+    assert N.lib().gbv_mc_dims(N.ivec(37, 20, 9), 8, out) == N.GBV_OK
+    assert tuple(out) == (5, 3, 1)
+    assert N.lib().gbv_mc_dims(N.ivec(1, 5, 5), 8, out) == N.GBV_OK
+    assert out[0] == 0
+    assert N.lib().gbv_mc_dims(N.ivec(8, 8, 8), 0, out) == 1
+
+
+def test_brick_store_sizes():
+    vb, sb = C.c_size_t(), C.c_size_t()
+    L = N.lib()
+    assert L.gbv_brick_store_bytes(N.ivec(512, 512, 512), N.GBV_VOXEL_F32, C.byref(vb), C.byref(sb)) == 0
+    assert vb.value == 64 ** 3 * 512 * 8 * 4 and sb.value == 0
+    assert L.gbv_brick_store_bytes(N.ivec(512, 512, 512), N.GBV_VOXEL_F16, C.byref(vb), C.byref(sb)) == 0
+    assert vb.value == 64 ** 3 * 512 * 8 * 2
+    assert L.gbv_brick_store_bytes(N.ivec(65, 9, 2), N.GBV_VOXEL_U8_SCALED, C.byref(vb), C.byref(sb)) == 0
+    assert vb.value == 8 * 1 * 1 * 512 * 8 and sb.value == 8 * 8
+    assert L.gbv_brick_store_bytes(N.ivec(8, 8, 8), 9, C.byref(vb), C.byref(sb)) == N.GBV_ERROR_UNSUPPORTED if hasattr(
+        N, "GBV_ERROR_UNSUPPORTED") else 5
+
+
+def test_arguments_checked_before_the_device():
+    L = N.lib()
+    rec = N.GbvScene()
+    assert L.gbv_render(None, None, 4, 4, 0, 1, None, None) == 1
+    assert L.gbv_render(C.byref(rec), C.c_void_p(16), 4, 4, 0, 1, None, None) == 1
+    assert "lacks" in L.gbv_last_error().decode()
+    assert L.gbv_build_mc_ranges(None, N.ivec(8, 8, 8), 8, None, None) == 1
+    assert L.gbv_tonemap(C.c_void_p(16), 4, 4, 0, 0, C.c_void_p(16), None) == 1
+    assert L.gbv_ea_render(C.byref(rec), None, 0, 0.1, None, None) == 1
+    assert L.gbv_build_brick_store(C.c_void_p(16), N.ivec(1, 4, 4), 0, C.c_void_p(16), None, None) == 1
+
+
+def test_generator_deterministic_and_in_range():
+    a = scenes.blob_volume((33, 17, 20), 8, seed=7, noise=0.05, fbm_octaves=2, fbm_amplitude=0.1)
+    b = scenes.blob_volume((33, 17, 20), 8, seed=7, noise=0.05, fbm_octaves=2, fbm_amplitude=0.1, nthreads=1)
+    c = scenes.blob_volume((33, 17, 20), 8, seed=8, noise=0.05, fbm_octaves=2, fbm_amplitude=0.1)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+    assert a.min() >= 0.0 and a.max() <= 1.0 and a.std() > 0.01
+    assert N.lib().gbv_gen_blob_volume(N.ivec(1, 4, 4), 1, 0, 0.0, 0, 0.0, 1, C.c_void_p(16)) == 1
+
+
+def test_bn_context_rejects_cpu_backend_and_multi_gpu():
+    L = bn.lib()
+    ids = (C.c_int * 1)(-1)
+    assert not L.bnContextCreate(None, 1, ids, 1)
+    assert "CPU backend" in bn.last_error()
+    ids2 = (C.c_int * 2)(0, 1)
+    assert not L.bnContextCreate(None, 1, ids2, 2)
+    slots = (C.c_int * 2)(0, 1)
+    assert not L.bnContextCreate(slots, 2, None, -1)
+
+
+def test_env_sky_map():
+    e = scenes.env_sky(64, 32)
+    assert e.texels.shape == (32, 64, 4)
+    assert e.texels[..., :3].max() == 50.0  # the sun disk
+    assert np.all(e.texels[..., 3] == 1.0)

@@ -1,0 +1,104 @@
+"""Oracle-level checks on the CPU: known answers and self-consistency of the
+restated path (no GPU)."""
+import numpy as np
+import pytest
+
+import oracle
+from barney_gb300 import scenes
+
+
+def test_render_deterministic_and_threads_independent():
+    s = scenes.small_scene(dims=32, spp=3, width=48, height=32)
+    o = oracle.Oracle(s)
+    a = o.render(nthreads=1)
+    b = o.render(nthreads=0)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert o.stats["density_samples"] > 0
+
+
+def test_background_only_frame():
+    """Known answer: a camera looking away sees bgColor with alpha bgColor.w
+    on every pass (generateRays.cu:219-230; shadeRays.cu:998-1001)."""
+    s = scenes.small_scene(dims=16, spp=5, width=8, height=8)
+    s.cam_pos, s.cam_dir = (0.0, 0.0, 3.0), (0.0, 0.0, 1.0)
+    s.bg_color = (0.25, 0.5, 0.75, 0.5)
+    o = oracle.Oracle(s)
+    acc = o.render()
+    np.testing.assert_array_equal(acc, np.tile(np.array([1.25, 2.5, 3.75, 2.5], np.float32), (8, 8, 1)))
+    img = o.tonemap(acc, 5)
+    np.testing.assert_allclose(img, np.tile(np.array([0.25, 0.5, 0.75, 0.5], np.float32), (8, 8, 1)))
+    rgba8 = o.tonemap(acc, 5, fmt=1)
+    # make_8bit: min(255, int(c*256))
+    assert rgba8[0, 0] == (64 | (128 << 8) | (192 << 16) | (128 << 24))
+
+
+def test_gradient_background_when_bg_alpha_negative():
+    s = scenes.small_scene(dims=16, spp=1, width=4, height=4)
+    s.cam_pos, s.cam_dir = (0.0, 0.0, 3.0), (0.0, 0.0, 1.0)
+    s.bg_color = (0.0, 0.0, 0.0, -1.0)
+    acc = oracle.Oracle(s).render()
+    t = (np.arange(4) + 0.5) / 4
+    exp_r = (1 - t).astype(np.float32) * np.float32(0.9) + t.astype(np.float32) * np.float32(0.15)
+    np.testing.assert_allclose(acc[:, 0, 0], exp_r, rtol=1e-6)
+
+
+def test_ea_beer_lambert():
+    vol = np.full((16, 16, 16), 0.5, np.float32)
+    tf = np.tile(np.array([[0.2, 0.6, 0.9, 0.4]], np.float32), (4, 1))
+    s = scenes.Scene(scalars=vol, tf=tf, base_density=3.0)
+    views = [dict(pos=(0.0, 0.0, 2.5), dir=(0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0), fovy=20.0, width=8, height=8)]
+    step = 0.01
+    img = oracle.Oracle(s).ea_render(views, step, use_double=True).reshape(8, 8, 4)
+    n = sum(1 for i in range(200) if 2.0 + (i + 0.5) * step < 3.0)
+    a = 1 - np.exp(-n * 1.2 * step)
+    np.testing.assert_allclose(img[3, 3, 3], a, rtol=1e-6)
+    np.testing.assert_allclose(img[3, 3, :3], np.array([0.2, 0.6, 0.9]) * a, rtol=1e-6)
+
+
+def test_ea_gradient_finite_differences():
+    gt = scenes.ea_scene(20)
+    views = scenes.fibonacci_views(2, 2.5, 20)
+    step = 0.5 / 19
+    tgt = oracle.Oracle(gt).ea_render(views, step, use_double=True).astype(np.float64)
+    start = scenes.Scene(scalars=(0.3 + 0.2 * gt.scalars).astype(np.float32), tf=gt.tf, base_density=gt.base_density)
+    o = oracle.Oracle(start)
+    img = o.ea_render(views, step, use_double=True).astype(np.float64)
+    gv, gtf = o.ea_backward(views, step, (2 * (img - tgt)).astype(np.float32))
+
+    def loss(vol):
+        s2 = scenes.Scene(scalars=vol, tf=start.tf, base_density=gt.base_density)
+        return ((oracle.Oracle(s2).ea_render(views, step, use_double=True) - tgt) ** 2).sum()
+
+    rng = np.random.default_rng(44)
+    flat = start.scalars.reshape(-1)
+    sel = np.flatnonzero(np.abs(gv.reshape(-1)) > 1e-2 * np.abs(gv).max())
+    fd, an = [], []
+    for v in rng.choice(sel, 6, replace=False):
+        hi, lo = np.float32(flat[v] + 1e-3), np.float32(flat[v] - 1e-3)
+        p, m = flat.copy(), flat.copy()
+        p[v], m[v] = hi, lo
+        fd.append((loss(p.reshape(start.scalars.shape)) - loss(m.reshape(start.scalars.shape))) /
+                  (float(hi) - float(lo)))
+        an.append(gv.reshape(-1)[v])
+    fd, an = np.array(fd), np.array(an)
+    assert np.linalg.norm(fd - an) <= 1e-3 * np.linalg.norm(fd)
+
+
+def test_env_cdfs_monotone():
+    s = scenes.small_scene(dims=8)
+    s.env = scenes.env_sky(64, 32)
+    cy, cx = oracle.Oracle(s).env_cdfs()
+    assert np.all(np.diff(cy) >= 0) and cy[-1] == 1.0
+    cx = cx.reshape(32, 64)
+    assert np.all(np.diff(cx, axis=1) >= 0) and np.all(cx[:, -1] == 1.0)
+
+
+def test_multi_scatter_adds_light():
+    """Scattering more than once can only add energy to the single-scatter
+    image in expectation (same scene, same lights)."""
+    s = scenes.frame_scene(dims=32, width=24, height=24, spp=32, with_env=False)
+    s.max_volume_bounces = 0
+    a = oracle.Oracle(s).render()[..., :3].mean()
+    s.max_volume_bounces = 4
+    b = oracle.Oracle(s).render()[..., :3].mean()
+    assert b > a
