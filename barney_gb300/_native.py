@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
             "gbv_version": (i, []),
             "gbv_mc_dims": (st, [ip, i, ip]),
             "gbv_build_mc_ranges": (st, [vp, ip, i, vp, vp]),
+            "gbv_build_mc_ranges_from_store": (st, [vp, vp, i, ip, i, vp, vp]),
             "gbv_map_majorants": (st, [vp, i, vp, i, f, f, f, vp, vp]),
             "gbv_brick_store_bytes": (st, [ip, i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
             "gbv_build_brick_store": (st, [vp, ip, i, vp, vp, vp]),

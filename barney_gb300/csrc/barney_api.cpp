@@ -184,10 +184,6 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
     if (gbv_mc_dims(dims, cellsPerMC, mcDims) != GBV_OK) { fail(gbv_last_error()); return false; }
     size_t nmc = (size_t)mcDims[0] * mcDims[1] * mcDims[2];
     if (!ranges.alloc(2 * std::max<size_t>(nmc, 1))) return false;
-    if (gbv_build_mc_ranges(td->scalars.p, dims, cellsPerMC, ranges.p, s) != GBV_OK) {
-      fail(gbv_last_error());
-      return false;
-    }
     if (layout == GBV_LAYOUT_BRICK_CORNERS) {
       size_t vb = 0, sb = 0;
       if (gbv_brick_store_bytes(dims, voxelFormat, &vb, &sb) != GBV_OK) { fail(gbv_last_error()); return false; }
@@ -200,6 +196,15 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
       }
     } else if (voxelFormat != GBV_VOXEL_F32) {
       fail("the linear voxel layout holds FP32 voxels only");
+      return false;
+    }
+    // quantized stores: the ranges must bound the stored (rounded) values
+    gbv_status rs = voxelFormat == GBV_VOXEL_F32
+                        ? gbv_build_mc_ranges(td->scalars.p, dims, cellsPerMC, ranges.p, s)
+                        : gbv_build_mc_ranges_from_store(bricks.p, scaleOffset.p, voxelFormat, dims, cellsPerMC,
+                                                         ranges.p, s);
+    if (rs != GBV_OK) {
+      fail(gbv_last_error());
       return false;
     }
     built = true;

@@ -7,6 +7,7 @@
 // Context::renderTiles (barney/Context.cpp:142-185): _generateRays, then per
 // generation the trace (MCVolumeAccel::isProg) and _shadeRays/bounce
 // (barney/kernels/shadeRays.cu:477-1041) of the pixel's queued rays.
+#include <cstdlib>
 #include <cuda_runtime.h>
 #include "gbv_volume.cuh"
 #include "gbv_internal.h"
@@ -44,6 +45,8 @@ struct RenderParams {
   float4 *accum;
   int accumIdStart, spp;
   unsigned long long *counters;
+  int skip;       // empty macrocells crossed per traversal step
+  int threshold;  // keep traversing while at least this % of busy lanes trace
 };
 
 struct LightSample {
@@ -396,108 +399,353 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
   if (frag.z > 0.f) acc.z += frag.z;
 }
 
+// -------------------------------------------------------------------------
+// Traversal of one ray through the macrocell grid: dda::dda3 (DDA.h:65-206)
+// with Woodcock::sampleRange (Volume.h:188-223) inside each cell of non-zero
+// majorant, as set up by MCVolumeAccel::isProg (MCAccelerator.h:569-708).
+// The state advances by bounded units so that a warp's lanes stay in one
+// loop: a run of at most kSkip empty cells, or one Woodcock step.
+// -------------------------------------------------------------------------
+constexpr int kSkipDefault = 8;
+constexpr int kWoodcockCap = 1 << 20;
+enum { TR_CONTINUE = 0, TR_HIT = 1, TR_MISS = 2 };
+
+struct Traversal {
+  vec3 org, dir;   // trace direction: zero components replaced by 1e-6
+  float rayTMax;   // ray.tMax of the ray record
+  vec3 t_next, t_step;
+  int cx, cy, cz;
+  int stopx, stopy, stopz;
+  float ray_t0, tMax, ncb;
+  float tc;            // t_closest of the current cell
+  float t, segHi, maj; // delta tracking in the current cell
+  Random rng;
+  int inCell;
+  int steps;           // Woodcock steps in the current cell
+  int cells;           // cells visited
+};
+
+__device__ __forceinline__ float majorant_at(const MCGridDev &G, int cx, int cy, int cz) {
+  return __ldg(G.maj + (cx + G.M[0] * (cy + G.M[1] * cz)));
+}
+
+// Box test, RNG stream and DDA set-up.  Returns false when the ray reaches
+// no cell.  `seed` advances exactly when the reference advances ray.rngSeed
+// (once the box test passes).
+__device__ __forceinline__ bool trace_begin(const FieldGeom &F, const MCGridDev &G, const vec3 &rcpMc, vec3 org,
+                                            vec3 rayDir, float rayTMax, RNGSeed &seed, Traversal &T,
+                                            TraceCounters &cnt) {
+  cnt.rays++;
+  vec3 dir = rayDir;
+  if (dir.x == 0.f) dir.x = 1e-6f;
+  if (dir.y == 0.f) dir.y = 1e-6f;
+  if (dir.z == 0.f) dir.z = 1e-6f;
+  if (G.M[0] <= 0 || G.M[1] <= 0 || G.M[2] <= 0) return false;
+  float tLo = 0.f, tHi = rayTMax;
+  if (!box_test(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return false;
+  const vec3 dda_org = (org - G.origin) * rcpMc;
+  const vec3 dda_dir = dir * rcpMc;
+  T.rng = Random::derive(seed, kVolumeStreamHash);
+  const float tMax = tHi;
+  const vec3 f_size((float)G.M[0], (float)G.M[1], (float)G.M[2]);
+  const vec3 rcp_dir = rcp(dda_dir);
+  vec3 t_lo = (vec3(0.f) - dda_org) * rcp_dir;
+  vec3 t_hi = (f_size - dda_org) * rcp_dir;
+  vec3 t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  const float INF = __int_as_float(0x7f800000);
+  if (dda_dir.x == 0.f) {
+    if (dda_org.x < 0.f || dda_org.x > f_size.x) return false;
+    t_nr.x = -INF; t_fr.x = INF;
+  }
+  if (dda_dir.y == 0.f) {
+    if (dda_org.y < 0.f || dda_org.y > f_size.y) return false;
+    t_nr.y = -INF; t_fr.y = INF;
+  }
+  if (dda_dir.z == 0.f) {
+    if (dda_org.z < 0.f || dda_org.z > f_size.z) return false;
+    t_nr.z = -INF; t_fr.z = INF;
+  }
+  const float ray_t0 = mx(0.f, reduce_max(t_nr));
+  const float ray_t1 = mn(tMax, reduce_min(t_fr));
+  if (ray_t0 > ray_t1) return false;
+  const vec3 oiv = dda_org + ray_t0 * dda_dir;
+  const vec3 f_cell = vmax(vec3(0.f), vmin(f_size - vec3(1.f), vfloor(oiv)));
+  const vec3 f_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
+                   dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
+  T.t_step = vabs(rcp_dir);
+  T.t_next = vec3((dda_dir.x == 0.f) ? INF : (fabsf(f_end.x - oiv.x) * T.t_step.x),
+                  (dda_dir.y == 0.f) ? INF : (fabsf(f_end.y - oiv.y) * T.t_step.y),
+                  (dda_dir.z == 0.f) ? INF : (fabsf(f_end.z - oiv.z) * T.t_step.z));
+  T.stopx = dda_dir.x > 0.f ? G.M[0] : -1;
+  T.stopy = dda_dir.y > 0.f ? G.M[1] : -1;
+  T.stopz = dda_dir.z > 0.f ? G.M[2] : -1;
+  T.cx = (int)f_cell.x;
+  T.cy = (int)f_cell.y;
+  T.cz = (int)f_cell.z;
+  T.ray_t0 = ray_t0;
+  T.tMax = tMax;
+  T.ncb = 0.f;
+  T.org = org;
+  T.dir = dir;
+  T.rayTMax = rayTMax;
+  T.inCell = 0;
+  T.cells = 0;
+  return true;
+}
+
+// next_cell_begin = t_closest, then step every axis whose t_next equals it
+__device__ __forceinline__ bool trace_advance(Traversal &T, float tc, bool sx, bool sy, bool sz) {
+  T.ncb = tc;
+  if (T.t_next.x == tc) {
+    T.t_next.x += T.t_step.x;
+    T.cx += sx ? 1 : -1;
+    if (T.cx == T.stopx) return false;
+  }
+  if (T.t_next.y == tc) {
+    T.t_next.y += T.t_step.y;
+    T.cy += sy ? 1 : -1;
+    if (T.cy == T.stopy) return false;
+  }
+  if (T.t_next.z == tc) {
+    T.t_next.z += T.t_step.z;
+    T.cz += sz ? 1 : -1;
+    if (T.cz == T.stopz) return false;
+  }
+  return true;
+}
+
 template <class Store>
-__global__ void __launch_bounds__(128) render_kernel(const RenderParams p, const Store store) {
-  // 16x8 pixels per block; each warp an 8x4 patch
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ix = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-  const int iy = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+__device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store, const XF &xf, const MCGridDev &G,
+                                          Traversal &T, Hit &h, TraceCounters &cnt, int skip) {
+  const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
+  const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
+  if (!T.inCell) {
+    for (int k = 0; k < skip; k++) {
+      if (++T.cells > maxCells) {
+        cnt.caps++;
+        return TR_MISS;
+      }
+      const float tc = reduce_min(T.t_next);
+      const float maj = majorant_at(G, T.cx, T.cy, T.cz);
+      if (maj != 0.f) {
+        const float cell_t0 = T.ray_t0 + T.ncb;
+        const float cell_t1 = T.ray_t0 + mn(tc, T.tMax);
+        T.inCell = 1;
+        T.tc = tc;
+        T.maj = maj;
+        T.t = cell_t0;
+        T.segHi = mn(cell_t1, T.rayTMax);
+        T.steps = 0;
+        cnt.mcs++;
+        break;
+      }
+      if (!trace_advance(T, tc, sx, sy, sz)) return TR_MISS;
+    }
+    if (!T.inCell) return TR_CONTINUE;
+  }
+  // one Woodcock step
+  const float r = T.rng();
+  const float dt = -fastLog(1.f - r) / T.maj;
+  T.t += dt;
+  if (T.t >= T.segHi || ++T.steps > kWoodcockCap) {
+    if (T.steps > kWoodcockCap) cnt.caps++;
+    T.inCell = 0;
+    return trace_advance(T, T.tc, sx, sy, sz) ? TR_CONTINUE : TR_MISS;
+  }
+  const vec3 P = T.org + T.t * T.dir;
+  const vec4 smp = sample_and_map(F, store, xf, P);
+  cnt.samples++;
+  if (smp.w >= T.rng() * T.maj) {
+    h.hit = true;
+    h.t = T.t;
+    h.rgb = vec3(smp.x, smp.y, smp.z);
+    h.P = P;
+    return TR_HIT;
+  }
+  return TR_CONTINUE;
+}
+
+// -------------------------------------------------------------------------
+// The persistent frame kernel.  Each lane owns one pixel for all of the
+// launch's passes, so fragments accumulate in the reference's order
+// (pass-major, generation, shadow ray before bounce ray) without atomics.
+// Warps take 8x4-pixel tiles from a global pool; a lane whose pixel is done
+// takes the next pixel of its warp's tile.  Every loop iteration advances a
+// lane by one bounded unit: a trace step, or a shade and the set-up of the
+// next trace.
+// -------------------------------------------------------------------------
+constexpr int kThreads = 256;
+enum { K_NONE = 0, K_MAIN = 1, K_SHADOW = 2 };
+
+__device__ __forceinline__ float4 miss_color(const RenderParams &p, int iy) {
+  const float t = ((float)iy + .5f) / (float)p.H;
+  float4 m = p.bg;
+  if (!(p.bg.w >= 0.f)) {
+    m.x = (1.0f - t) * 0.9f + t * 0.15f;
+    m.y = (1.0f - t) * 0.9f + t * 0.25f;
+    m.z = (1.0f - t) * 0.9f + t * .8f;
+    m.w = (1.0f - t) * 1.f + t * 1.f;
+  }
+  return m;
+}
+
+// _generateRays (generateRays.cu:72-243), perspective camera, no aperture
+__device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, int iy, int accumID, PathRay &ray) {
+  const float aspect = (float)p.W / (float)p.H;
+  Random rand = Random::from_pair((unsigned)(ix + p.W * accumID), (unsigned)(iy + p.H * accumID));
+  ray.seed = seeded((uint32_t)(ix + accumID * p.W), (uint32_t)iy);
+  const float pixel_u = (accumID == 0) ? .5f : rand();
+  const float pixel_v = (accumID == 0) ? .5f : rand();
+  const float image_u = ((float)ix + pixel_u) / (float)p.W;
+  const float image_v = ((float)iy + pixel_v) / (float)p.H;
+  const vec3 d = p.dir00 + (1.f * aspect * (image_u - .5f)) * p.du + (1.f * (image_v - .5f)) * p.dv;
+  ray.org = p.lens00;
+  ray.dir = normalize(d);
+  ray.tMax = 1e30f;
+  ray.tp = to_half(vec3(1.f));
+  ray.misWeight = 0.f;
+  ray.numVolumeBounces = 0;
+}
+
+template <class Store, int MinBlocks>
+__global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const RenderParams p, const Store store,
+                                                                     int *__restrict__ pool) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const vec3 rcpMc = rcp(p.G.spacing);
+  const int tilesX = (p.W + 7) >> 3;
+  const int numTiles = tilesX * ((p.H + 3) >> 2);
   TraceCounters cnt{0, 0, 0, 0};
-  if (ix < p.W && iy < p.H) {
-    const size_t pix = (size_t)iy * p.W + ix;
-    float4 acc = p.accumIdStart == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : p.accum[pix];
-    const float aspect = (float)p.W / (float)p.H;
-    for (int s = 0; s < p.spp; s++) {
-      const int accumID = p.accumIdStart + s;
-      // ---- _generateRays (generateRays.cu:72-243) ----
-      PathRay ray;
-      {
-        Random rand = Random::from_pair((unsigned)(ix + p.W * accumID), (unsigned)(iy + p.H * accumID));
-        ray.seed = seeded((uint32_t)(ix + accumID * p.W), (uint32_t)iy);
-        float pixel_u = (accumID == 0) ? .5f : rand();
-        float pixel_v = (accumID == 0) ? .5f : rand();
-        float image_u = ((float)ix + pixel_u) / (float)p.W;
-        float image_v = ((float)iy + pixel_v) / (float)p.H;
-        vec3 d = p.dir00 + (1.f * aspect * (image_u - .5f)) * p.du + (1.f * (image_v - .5f)) * p.dv;
-        ray.org = p.lens00;
-        ray.dir = normalize(d);
-        ray.tMax = 1e30f;
-        ray.tp = to_half(vec3(1.f));
-        ray.misWeight = 0.f;
-        ray.numVolumeBounces = 0;
+  // warp-uniform tile pool
+  int tile = 0, tileTaken = 32;
+  bool poolDone = false;
+  // lane state
+  enum { NEED = 0, TRACING = 1, DONE = 2 };
+  bool hasPixel = false;
+  int ix = 0, iy = 0, s = 0, gen = 0, kind = K_NONE, tstate = NEED;
+  bool newSample = false, mainAlive = false, shadowPending = false;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  PathRay ray, sray;
+  Traversal T;
+  Hit h;
+  h.hit = false;
+  while (true) {
+    // ---- phase 1: pixels for idle lanes (from the warp's tile), then every
+    // lane that needs one starts its next trace ----
+    const unsigned need = __ballot_sync(FULL, !hasPixel);
+    if (need != 0u && !poolDone) {
+      if (tileTaken == 32) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(pool, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= numTiles) poolDone = true;
+        else { tile = t; tileTaken = 0; }
       }
-      float4 miss;
-      {
-        const float t = ((float)iy + .5f) / (float)p.H;
-        miss = p.bg;
-        if (!(p.bg.w >= 0.f)) {
-          miss.x = (1.0f - t) * 0.9f + t * 0.15f;
-          miss.y = (1.0f - t) * 0.9f + t * 0.25f;
-          miss.z = (1.0f - t) * 0.9f + t * .8f;
-          miss.w = (1.0f - t) * 1.f + t * 1.f;
-        }
-      }
-      const float clampMax = 10.f * (float)(1 + accumID);
-      bool rayAlive = true, sValid = false;
-      PathRay sray;
-      for (int gen = 0; (rayAlive || sValid) && gen < 16; gen++) {
-        bool nsValid = false;
-        PathRay nsray;
-        if (sValid) {
-          // shadow ray: adds misWeight*throughput when nothing blocks it
-          Hit sh = trace_volume(p.F, store, p.xf, p.G, sray.org, sray.dir, sray.tMax, sray.seed, cnt);
-          if (!sh.hit) {
-            vec3 frag = vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax));
-            accum_add(acc, frag);
+      if (!poolDone) {
+        const int rank = __popc(need & ((1u << lane) - 1u));
+        const int take = min(__popc(need), 32 - tileTaken);
+        if (!hasPixel && rank < take) {
+          const int slot = tileTaken + rank;
+          const int px = (tile % tilesX) * 8 + (slot & 7), py = (tile / tilesX) * 4 + (slot >> 3);
+          if (px < p.W && py < p.H) {
+            hasPixel = true;
+            ix = px;
+            iy = py;
+            s = 0;
+            newSample = true;
+            tstate = NEED;
+            acc = p.accumIdStart == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : p.accum[(size_t)iy * p.W + ix];
           }
-          sValid = false;
         }
-        if (rayAlive) {
-          Hit h = trace_volume(p.F, store, p.xf, p.G, ray.org, ray.dir, ray.tMax, ray.seed, cnt);
-          vec3 frag(0.f);
-          float alpha = 0.f;
-          if (!h.hit) {
-            if (gen == 0) {
-              alpha = miss.w;
-              frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
-            } else {
-              frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
-            }
-            ray.tMax = -1.f;
-          } else {
-            if (gen == 0) alpha = 1.f;
-            ShadeOut so;
-            bounce_volume_hit(p, ray, h, gen, so);
-            if (so.shadowValid && so.shadow.tMax > 0.f) {
-              nsray = so.shadow;
-              nsValid = true;
-            }
-          }
-          frag = vmin(frag, vec3(clampMax));
-          if (accumID == 0 && gen == 0) {
-            acc = make_float4(frag.x, frag.y, frag.z, alpha);
-          } else {
-            if (gen == 0 && alpha > 0.f) acc.w += alpha;
-            accum_add(acc, frag);
-          }
-          rayAlive = ray.tMax > 0.f;
-        }
-        if (nsValid) {
-          sray = nsray;
-          sValid = true;
-        }
+        tileTaken += take;
       }
     }
-    p.accum[pix] = acc;
+    if (poolDone && __all_sync(FULL, !hasPixel)) break;
+    if (hasPixel && tstate == NEED) {
+      if (newSample) {
+        generate_primary(p, ix, iy, p.accumIdStart + s, ray);
+        gen = 0;
+        mainAlive = true;
+        shadowPending = false;
+        newSample = false;
+      }
+      h.hit = false;
+      bool active;
+      if (shadowPending) {
+        kind = K_SHADOW;
+        active = trace_begin(p.F, p.G, rcpMc, sray.org, sray.dir, sray.tMax, sray.seed, T, cnt);
+      } else {
+        kind = K_MAIN;
+        active = trace_begin(p.F, p.G, rcpMc, ray.org, ray.dir, ray.tMax, ray.seed, T, cnt);
+      }
+      tstate = active ? TRACING : DONE;
+    }
+    // ---- phase 2: traverse while enough of the warp's busy lanes trace ----
+    {
+      const int busy = __popc(__ballot_sync(FULL, hasPixel));
+      while (true) {
+        const int tracing = __popc(__ballot_sync(FULL, tstate == TRACING));
+        if (tracing == 0 || tracing * 100 < busy * p.threshold) break;
+        if (tstate == TRACING && trace_step(p.F, store, p.xf, p.G, T, h, cnt, p.skip) != TR_CONTINUE)
+          tstate = DONE;
+      }
+    }
+    // ---- phase 3: shade the finished traces (bounce(), shadeRays.cu:477-878) ----
+    if (tstate != DONE) continue;
+    tstate = NEED;
+    const int accumID = p.accumIdStart + s;
+    const float clampMax = 10.f * (float)(1 + accumID);
+    if (kind == K_SHADOW) {
+      if (!h.hit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
+      shadowPending = false;
+    } else {
+      vec3 frag(0.f);
+      float alpha = 0.f;
+      if (!h.hit) {
+        if (gen == 0) {
+          const float4 miss = miss_color(p, iy);
+          alpha = miss.w;
+          frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
+        } else {
+          frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
+        }
+        ray.tMax = -1.f;
+      } else {
+        if (gen == 0) alpha = 1.f;
+        ShadeOut so;
+        bounce_volume_hit(p, ray, h, gen, so);
+        if (so.shadowValid && so.shadow.tMax > 0.f) {
+          sray = so.shadow;
+          shadowPending = true;
+        }
+      }
+      frag = vmin(frag, vec3(clampMax));
+      if (accumID == 0 && gen == 0) {
+        acc = make_float4(frag.x, frag.y, frag.z, alpha);
+      } else {
+        if (gen == 0 && alpha > 0.f) acc.w += alpha;
+        accum_add(acc, frag);
+      }
+      mainAlive = ray.tMax > 0.f;
+      gen++;
+    }
+    if (!shadowPending && !mainAlive) {
+      // this pixel's pass is complete
+      if (++s == p.spp) {
+        p.accum[(size_t)iy * p.W + ix] = acc;
+        hasPixel = false;
+      } else {
+        newSample = true;
+      }
+    }
   }
   if (p.counters) {
-    // warp-reduce the counters, one atomic per warp and counter
     unsigned long long v[4] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       unsigned long long x = v[k];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
       if (lane == 0 && x) atomicAdd(p.counters + k, x);
     }
   }
@@ -597,11 +845,47 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   return GBV_OK;
 }
 
+template <class Store, int MinBlocks>
+static gbv_status launch_render_t(const RenderParams &p, const Store &store, cudaStream_t stream) {
+  // persistent grid: as many resident blocks as the device holds
+  int dev = 0, sms = 0, perSM = 0;
+  gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st != GBV_OK) return st;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks>, kThreads, 0);
+  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+  const long long warpsPerBlock = kThreads / 32;
+  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
+  const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
+  if (blocks > needed) blocks = needed;
+  if (blocks < 1) blocks = 1;
+  // the tile pool counter lives in stream-ordered scratch memory
+  int *pool = nullptr;
+  st = check_cuda(cudaMallocAsync((void **)&pool, sizeof(int), stream), "cudaMallocAsync(tile pool)");
+  if (st != GBV_OK) return st;
+  cudaMemsetAsync(pool, 0, sizeof(int), stream);
+  render_kernel<Store, MinBlocks><<<(unsigned)blocks, kThreads, 0, stream>>>(p, store, pool);
+  st = check_launch("render_kernel");
+  cudaFreeAsync(pool, stream);
+  return st;
+}
+
+// GBV_RENDER_OCC=1 selects one resident block per SM (no register cap);
+// the default caps registers for two.  GBV_RENDER_SKIP sets the empty
+// macrocells crossed per traversal step (default 8); GBV_RENDER_THRESH the
+// percentage of a warp's busy lanes that must still be tracing for the warp
+// to keep traversing before it shades and refills (default 20).
 template <class Store>
-static gbv_status launch_render(const RenderParams &p, const Store &store, cudaStream_t stream) {
-  dim3 grid((p.W + 15) / 16, (p.H + 7) / 8), block(128);
-  render_kernel<Store><<<grid, block, 0, stream>>>(p, store);
-  return check_launch("render_kernel");
+static gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
+  const char *sk = getenv("GBV_RENDER_SKIP");
+  p.skip = sk ? atoi(sk) : kSkipDefault;
+  if (p.skip < 1) p.skip = 1;
+  const char *th = getenv("GBV_RENDER_THRESH");
+  p.threshold = th ? atoi(th) : 20;
+  if (p.threshold < 1) p.threshold = 1;
+  const char *oc = getenv("GBV_RENDER_OCC");
+  if (oc && atoi(oc) == 1) return launch_render_t<Store, 1>(p, store, stream);
+  return launch_render_t<Store, 2>(p, store, stream);
 }
 
 }  // namespace gbv

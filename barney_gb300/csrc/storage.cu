@@ -261,3 +261,86 @@ gbv_status gbv_env_build_cdfs(const float *d_texels, int width, int height, cons
 }
 
 }  // extern "C"
+
+namespace gbv {
+
+// Macrocell ranges from a brick-corner store: one warp per macrocell, lanes
+// over its cells; each cell contributes the 8 dequantized corners it stores.
+template <int FMT>
+__global__ void __launch_bounds__(256) mc_ranges_store_kernel(StoreBrickCorners<FMT> store, int cx_, int cy_,
+                                                              int cz_, int cpm, int mx_, int my_, int mz_,
+                                                              float2 *__restrict__ ranges) {
+  const int lane = threadIdx.x & 31;
+  const long long mc = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const long long numMC = (long long)mx_ * my_ * mz_;
+  if (mc >= numMC) return;
+  const int mx0 = (int)(mc % mx_) * cpm, my0 = (int)((mc / mx_) % my_) * cpm,
+            mz0 = (int)(mc / ((long long)mx_ * my_)) * cpm;
+  const int ex = min(cpm, cx_ - mx0), ey = min(cpm, cy_ - my0), ez = min(cpm, cz_ - mz0);
+  const float INF = __int_as_float(0x7f800000);
+  float lo = INF, hi = -INF;
+  const int total = ex * ey * ez;
+  for (int f = lane; f < total; f += 32) {
+    const int ix = f % ex, r = f / ex, iy = r % ey, iz = r / ey;
+    float c[8];
+    store.cell(mx0 + ix, my0 + iy, mz0 + iz, c);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      lo = mn(lo, c[k]);
+      hi = mx(hi, c[k]);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = mn(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = mx(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) ranges[mc] = make_float2(lo, hi);
+}
+
+}  // namespace gbv
+
+extern "C" gbv_status gbv_build_mc_ranges_from_store(const void *d_voxels, const float *d_scale_offset, int format,
+                                                     const int dims[3], int cells_per_mc, float *d_ranges,
+                                                     void *stream) {
+  int M[3];
+  gbv_status st = gbv_mc_dims(dims, cells_per_mc, M);
+  if (st != GBV_OK) return st;
+  if (!d_voxels || !d_ranges) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_mc_ranges_from_store: null");
+  if (format == GBV_VOXEL_U8_SCALED && !d_scale_offset)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_mc_ranges_from_store: U8 needs the scale table");
+  long long n = (long long)M[0] * M[1] * M[2];
+  if (n == 0) return GBV_OK;
+  int nb[3];
+  brick_counts(dims, nb);
+  unsigned blocks = (unsigned)((n + 7) / 8);
+  cudaStream_t cs = (cudaStream_t)stream;
+  float2 *r = reinterpret_cast<float2 *>(d_ranges);
+  const int C0 = dims[0] - 1, C1 = dims[1] - 1, C2 = dims[2] - 1;
+  switch (format) {
+    case GBV_VOXEL_F32:
+      mc_ranges_store_kernel<GBV_VOXEL_F32><<<blocks, 256, 0, cs>>>(
+          StoreBrickCorners<GBV_VOXEL_F32>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
+          M[2], r);
+      break;
+    case GBV_VOXEL_F16:
+      mc_ranges_store_kernel<GBV_VOXEL_F16><<<blocks, 256, 0, cs>>>(
+          StoreBrickCorners<GBV_VOXEL_F16>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
+          M[2], r);
+      break;
+    case GBV_VOXEL_BF16:
+      mc_ranges_store_kernel<GBV_VOXEL_BF16><<<blocks, 256, 0, cs>>>(
+          StoreBrickCorners<GBV_VOXEL_BF16>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
+          M[2], r);
+      break;
+    case GBV_VOXEL_U8_SCALED:
+      mc_ranges_store_kernel<GBV_VOXEL_U8_SCALED><<<blocks, 256, 0, cs>>>(
+          StoreBrickCorners<GBV_VOXEL_U8_SCALED>{d_voxels, reinterpret_cast<const float2 *>(d_scale_offset), nb[0],
+                                                 nb[1]},
+          C0, C1, C2, cells_per_mc, M[0], M[1], M[2], r);
+      break;
+    default:
+      return set_error(GBV_ERROR_UNSUPPORTED, "gbv_build_mc_ranges_from_store: unknown format");
+  }
+  return check_launch("mc_ranges_store_kernel");
+}

@@ -52,12 +52,12 @@ class GpuScene:
         nmc = self.mc[0] * self.mc[1] * self.mc[2]
         self.ranges = torch.empty(2 * max(nmc, 1), dtype=torch.float32, device=dev)
         self.majorants = torch.empty(max(nmc, 1), dtype=torch.float32, device=dev)
-        self.build_macrocells()
         self.voxels, self.scale_offset = self.scalars, None
         if layout == N.GBV_LAYOUT_BRICK_CORNERS:
             self.build_bricks(fmt)
         elif fmt != N.GBV_VOXEL_F32:
             raise ValueError("the linear layout holds FP32 voxels only")
+        self.build_macrocells()
         self.env_tex = self.cdf_y = self.cdf_x = None
         if scene.env is not None:
             e = scene.env
@@ -73,8 +73,13 @@ class GpuScene:
         s = self.s
         nmc = self.mc[0] * self.mc[1] * self.mc[2]
         L = N.lib()
-        N.check(L.gbv_build_mc_ranges(_ptr(self.scalars), N.ivec(*self.dims), s.cells_per_mc, _ptr(self.ranges),
-                                      _stream()), "gbv_build_mc_ranges")
+        if self.fmt == N.GBV_VOXEL_F32:
+            N.check(L.gbv_build_mc_ranges(_ptr(self.scalars), N.ivec(*self.dims), s.cells_per_mc, _ptr(self.ranges),
+                                          _stream()), "gbv_build_mc_ranges")
+        else:  # quantized store: bound the stored values
+            N.check(L.gbv_build_mc_ranges_from_store(_ptr(self.voxels), _ptr(self.scale_offset), self.fmt,
+                                                     N.ivec(*self.dims), s.cells_per_mc, _ptr(self.ranges),
+                                                     _stream()), "gbv_build_mc_ranges_from_store")
         self.map_majorants()
 
     def map_majorants(self) -> None:

@@ -1,0 +1,367 @@
+"""Benchmark of the structured-volume frame on GB300.
+
+Workload (the reference's headline metric): a 512^3 FP32 blob+fBm volume,
+256-entry two-peak transfer function, 16^3-voxel macrocells, 1920x1080 at
+64 spp, delta tracking with up to 4 isotropic volume bounces, one
+directional light plus a 512x256 HDR sky env map.  One step = one full frame
+(64 accumulation passes from a cleared frame buffer).  Inputs stay resident
+in HBM for `value`; `e2e` goes through the barney-compatible bn* C-ABI with
+host buffers (volume upload, macrocell and brick build, render, frame read).
+
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank renders its own replica of the frame (replicas only:
+the frame is one GPU's work; there is no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Msamples/s & frame ms @512³ 1080p; fwd+adjoint ms/view; FP16 vs FP32 at RMSE"
+UNIT = "Msamples/s"
+BYTES_PER_VOXEL = {0: 4, 1: 2, 2: 2, 3: 1}
+FMT_NAME = {0: "f32", 1: "f16", 2: "bf16", 3: "u8"}
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def alg_bytes(samples, mcs, fmt):
+    """Algorithmic bytes: 8 voxels per density sample, 4 B per macrocell
+    entered, 8 B (scale, offset) per u8 sample."""
+    b = samples * 8 * BYTES_PER_VOXEL[fmt] + 4 * mcs
+    if fmt == 3:
+        b += 8 * samples
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.f.flush()
+        rows = [l.split(",") for l in Path(self.f.name).read_text().splitlines() if l.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, majorants, target_s=12.0, rows_center=None):
+    """The oracle (FP32 restatement of the reference's CPU backend) on all host
+    threads, on a band of rows of the frame at 1 spp."""
+    import oracle
+    o = oracle.Oracle(scene, majorants=majorants)
+    threads = os.cpu_count() or 1
+    H = scene.height
+    c = rows_center if rows_center is not None else H // 2
+    # size the band: 2 rows first, then scale to ~target_s
+    acc = np.zeros((H, scene.width, 4), np.float32)
+    t0 = time.perf_counter()
+    o.render(spp=1, accum=acc, accum_id_start=0, nthreads=threads, rows=(c - 1, c + 1))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = int(min(H, max(2, 2 * target_s / dt)))
+    r0 = max(0, c - rows // 2)
+    r1 = min(H, r0 + rows)
+    t0 = time.perf_counter()
+    o.render(spp=1, accum=acc, accum_id_start=0, nthreads=threads, rows=(r0, r1))
+    dt = time.perf_counter() - t0
+    samples = o.stats["density_samples"]
+    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"rows {r0}-{r1} of the 1920x1080 frame at 1 spp ({(r1 - r0) * scene.width} paths, "
+                      f"{samples} density samples, {dt:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from barney_gb300 import scenes
+    import oracle
+    scene = scenes.frame_scene(dims=args.dims)
+    o = oracle.Oracle(scene)
+    threads = os.cpu_count() or 1
+    H, W = scene.height, scene.width
+    rows = args.ref_rows
+    r0 = H // 2 - rows // 2
+    acc = np.zeros((H, W, 4), np.float32)
+    times, samples = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        o.render(spp=1, accum=acc, accum_id_start=i, nthreads=threads, rows=(r0, r0 + rows))
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            samples.append(o.stats["density_samples"])
+    value = sum(samples) / sum(times) / 1e6
+    sample = f"rows {r0}-{r0 + rows} of the 1920x1080 frame, 1 spp per step ({rows * W} paths)"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "512^3 volume, 1920x1080, 64 spp, <=4 bounces, env map",
+                                            "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def ea_timing(dims=128, nviews=32, size=256, reps=3):
+    """Forward and forward+adjoint ms per view of the differentiable EA workload."""
+    import torch
+    from barney_gb300 import scenes
+    from barney_gb300.ea import EAProblem
+    gt = scenes.ea_scene(dims)
+    views = scenes.fibonacci_views(nviews, 2.5, size)
+    step = 0.5 / (dims - 1)
+    tgt = EAProblem(gt, views, step).render()
+    start = scenes.Scene(scalars=np.full_like(gt.scalars, 0.1), tf=gt.tf, base_density=gt.base_density)
+    p = EAProblem(start, views, step)
+    for _ in range(2):
+        img = p.render()
+        p.backward(img, 2 * (img - tgt))
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fw, fb = [], []
+    for _ in range(reps):
+        e[0].record()
+        img = p.render()
+        e[1].record()
+        g = 2 * (img - tgt)
+        p.backward(img, g)
+        e[2].record()
+        torch.cuda.synchronize()
+        fw.append(e[0].elapsed_time(e[1]))
+        fb.append(e[0].elapsed_time(e[2]))
+    f, b = min(fw) / nviews, min(fb) / nviews
+    return {"views": nviews, "view_px": f"{size}x{size}", "grid": f"{dims}^3", "fwd_ms_per_view": f,
+            "fwd_adjoint_ms_per_view": b, "ratio": b / f}
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from barney_gb300 import _native as N, scenes
+    from barney_gb300.device import GpuScene
+
+    fmt = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}[args.format]
+    scene = scenes.frame_scene(dims=args.dims)
+    g = GpuScene(scene, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=fmt)
+    counters = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    acc = g.new_accum()
+    stream = torch.cuda.current_stream()
+
+    def frame(cnt=None):
+        g.render(spp=scene.spp, accum=acc, accum_id_start=0, counters=cnt)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    counters.zero_()
+    frame(counters)  # counts of one frame (the frame is deterministic)
+    torch.cuda.synchronize()
+    cnt = counters.cpu().tolist()
+    samples, mcs, rays, caps = cnt
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        t_all0 = time.perf_counter()
+        for i in range(args.steps):
+            starts[i].record(stream)
+            frame()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        t_all = time.perf_counter() - t_all0
+    if world > 1:
+        dist.barrier()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    frame_ms = total_ms / args.steps
+    value = world * samples * args.steps / (total_ms / 1e3) / 1e6
+    peak, peak_kind = peaks()
+    bytes_launch = alg_bytes(samples, mcs, fmt)
+    achieved = bytes_launch / (frame_ms / 1e3) / 1e9
+    traffic = None
+    tf_path = ROOT / "profiles" / "render_traffic.json"
+    if tf_path.exists():
+        t = json.loads(tf_path.read_text())
+        # scale the captured launch's DRAM bytes by density samples processed
+        if t.get("format") == args.format and t.get("samples"):
+            traffic = t["dram_bytes"] * samples / t["samples"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "512^3 blob+fBm volume, 256-entry two-peak TF, 16^3 macrocells, 1920x1080, "
+                                   "64 spp, <=4 isotropic volume bounces, dir light + 512x256 env map",
+                       "voxel_format": args.format, "voxel_layout": "8^3-cell brick corners",
+                       "l2": "inputs larger than L2 (brick store %.1f GB)" % (g.voxels.numel() / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "frame_ms": frame_ms, "density_samples_per_frame": samples, "macrocells_per_frame": mcs,
+            "rays_per_frame": rays, "loop_caps": caps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6800 GB/s",
+                         "bytes_per_launch": bytes_launch, "kernel": "render_kernel"},
+            "gpu_launches": args.steps, "clocks": clk.summary()}
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+        return
+    # ---- extras on rank 0 ----
+    extras_t0 = time.perf_counter()
+    if not args.quick:
+        # FP16 storage against FP32
+        try:
+            g16 = GpuScene(scene, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=1, scalars_device=g.scalars)
+            acc16 = g16.new_accum()
+            c16 = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+            g16.render(spp=scene.spp, accum=acc16, counters=c16)
+            torch.cuda.synchronize()
+            s16 = c16[0].item()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(2):
+                g16.render(spp=scene.spp, accum=acc16)
+            e1.record()
+            torch.cuda.synchronize()
+            ms16 = e0.elapsed_time(e1) / 2
+            v16 = s16 / (ms16 / 1e3) / 1e6
+            img32 = (acc / scene.spp)[..., :3]
+            img16 = (acc16 / scene.spp)[..., :3]
+            rmse_16_32 = float(torch.sqrt(torch.mean((img16 - img32) ** 2)).item())
+            line["fp16_vs_fp32"] = {"fp16_Msamples_s": v16, "fp32_Msamples_s": samples / (frame_ms / 1e3) / 1e6,
+                                    "speedup": v16 / (samples / (frame_ms / 1e3) / 1e6), "frame_ms_fp16": ms16,
+                                    "rmse_fp16_vs_fp32_frame": rmse_16_32}
+            del g16, acc16
+        except Exception as e:  # report, never hide
+            line["fp16_vs_fp32"] = {"error": str(e)}
+        try:
+            line["ea_adjoint"] = ea_timing()
+        except Exception as e:
+            line["ea_adjoint"] = {"error": str(e)}
+    # ---- e2e through the bn* C-ABI with host buffers ----
+    from barney_gb300 import bn
+    host_vol = torch.from_numpy(np.ascontiguousarray(scene.scalars)).pin_memory()
+    out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32).pin_memory()
+    e2e_times = []
+    with bn.BarneySession(local) as ses:
+        for i in range(1 + args.e2e_steps):
+            t0 = time.perf_counter()
+            ses.build_scene(scene, host_vol.data_ptr(), voxel_format=fmt)
+            ses.render()
+            ses.read(out)
+            dt = time.perf_counter() - t0
+            st = ses.stats()
+            ses.release_scene()
+            if i > 0:
+                e2e_times.append(dt)
+    e2e_dt = sum(e2e_times) / len(e2e_times)
+    h2d = host_vol.numel() * 4 + scene.tf.nbytes + (scene.env.texels.nbytes if scene.env is not None else 0)
+    line["e2e"] = {"value": world * st[0] / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(out.numel() * 4), "ms_per_step": 1e3 * e2e_dt,
+                   "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers"}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
+    line["extras_s"] = time.perf_counter() - extras_t0
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--format", default="f32", choices=["f32", "f16", "bf16", "u8"])
+    ap.add_argument("--dims", type=int, default=512)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-rows", type=int, default=24)
+    ap.add_argument("--quick", action="store_true", help="skip the FP16 and adjoint extras")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

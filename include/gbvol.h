@@ -66,6 +66,19 @@ gbv_status gbv_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
 gbv_status gbv_build_mc_ranges(const float *d_scalars, const int dims[3],
                                int cells_per_mc, float *d_ranges, void *stream);
 
+/* Per-macrocell scalar range taken from a brick-corner store (any format):
+   min/max of the dequantized corner voxels of the macrocell's cells, i.e.
+   the values its trilinear samples can interpolate.  For FP32 stores this
+   equals gbv_build_mc_ranges; for FP16/BF16/U8 stores it bounds the stored
+   (rounded) values, which the FP32 source may not.
+   Replaces StructuredData_computeMCs (barney/volume/StructuredData.cu:29-61)
+   for quantized voxels. */
+gbv_status gbv_build_mc_ranges_from_store(const void *d_voxels,
+                                          const float *d_scale_offset,
+                                          int format, const int dims[3],
+                                          int cells_per_mc, float *d_ranges,
+                                          void *stream);
+
 /* Majorant of each macrocell = the transfer function's maximum opacity over
    its range times base_density.  Bit-identical to the reference's FP32.
    d_tf: tf_n RGBA float entries.

@@ -33,7 +33,9 @@ def test_forward_matches_oracle(cuda):
     ref32 = o.ea_render(views, step)
     ref64 = o.ea_render(views, step, use_double=True)
     np.testing.assert_allclose(img, ref32, rtol=RTOL, atol=ATOL)
-    np.testing.assert_allclose(img, ref64, rtol=RTOL, atol=ATOL)
+    # FP32 against FP64: rounding of sample positions, trilinear weights and
+    # steep TF segments; measured max ~3e-4 relative on 0.2% of channels
+    np.testing.assert_allclose(img, ref64, rtol=1e-3, atol=1e-5)
     assert img[:, 3].max() > 0.5
 
 
@@ -64,9 +66,16 @@ def test_constant_density_beer_lambert(cuda):
     np.testing.assert_allclose(c[:3], np.array([0.2, 0.6, 0.9]) * a, rtol=2e-5)
 
 
-def test_adjoint_matches_oracle_and_finite_differences(cuda):
+@pytest.mark.parametrize("tf_kind", ["ramp", "two_peaks"])
+def test_adjoint_matches_oracle_and_finite_differences(cuda, tf_kind):
+    """The two-peak TF has knots (slope changes) inside the data range, where a
+    central difference averages two one-sided slopes; the finite-difference
+    check therefore runs on the knot-free ramp TF, and both TFs are checked
+    against the oracle's FP64 gradient."""
     import torch
     gt, views, step = small_problem(dims=40, nviews=4, size=40)
+    if tf_kind == "ramp":
+        gt.tf = scenes.tf_ramp(256, 0.9)
     p_gt = EAProblem(gt, views, step)
     target = p_gt.render()
     start = scenes.Scene(scalars=np.full_like(gt.scalars, 0.3) + 0.2 * gt.scalars, tf=gt.tf,
@@ -83,6 +92,8 @@ def test_adjoint_matches_oracle_and_finite_differences(cuda):
     sel = np.flatnonzero(np.abs(ov) > 1e-3 * np.abs(ov).max())
     assert np.linalg.norm(gv.reshape(-1)[sel] - ov[sel]) <= 1e-3 * np.linalg.norm(ov[sel])
     assert np.linalg.norm(gt_tf - ot) <= 1e-3 * np.linalg.norm(ot)
+    if tf_kind != "ramp":
+        return
     # central finite differences of the FP64 march, eps = 1e-3
     rng = np.random.default_rng(44)
     tgt64 = target.double()
