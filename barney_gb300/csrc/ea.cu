@@ -12,6 +12,7 @@
 //   C = sum T_i alpha_i rgb_i, A = -expm1(-tau_n).
 // Adjoint (no stored per-step state): dC/dx_j = rgb_j T_{j+1} - (C - C_{<=j}),
 // dA/dx_j = T_n, dC/drgb_j = T_j alpha_j.
+#include <cstdlib>
 #include <cuda_runtime.h>
 #include "gbv_volume.cuh"
 #include "gbv_internal.h"
@@ -184,45 +185,47 @@ __global__ void __launch_bounds__(128) ea_forward_f64_kernel(const EAParams p, d
   out[v.offset + (long long)iy * v.W + ix] = res;
 }
 
-// Warp-aggregated scatter of 8 per-corner gradient contributions.  Lanes
-// whose stencil starts at the same voxel are grouped with __match_any_sync;
-// the group's lowest lane gathers the others' values by shuffles and issues
-// the 8 atomics once for the whole group.  Must be reached by all 32 lanes.
-__device__ __forceinline__ void scatter_stencil(float *__restrict__ grid, bool valid, size_t base, size_t sy,
-                                                size_t sz, int dxs, int dys, int dzs, const float contrib[8]) {
+// Warp-aggregated flush of 8 per-corner (or per-TF-entry) gradient sums.
+// Lanes that flush in the same step and hold the same key are grouped with
+// __match_any_sync; the group's lowest lane gathers the others' sums by
+// shuffles and issues the 8 atomics once.  Called by all 32 lanes.
+template <bool Shared>
+__device__ __forceinline__ void flush8(float *__restrict__ dst, bool flush, unsigned long long key,
+                                       const size_t off[8], const float v[8]) {
   const int lane = threadIdx.x & 31;
-  const unsigned long long key = valid ? (unsigned long long)base : (0xffffffff00000000ull | (unsigned)lane);
-  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const unsigned fm = __ballot_sync(0xffffffffu, flush);
+  if (!flush) return;
+  const unsigned peers = __match_any_sync(fm, key);
   const int leader = __ffs(peers) - 1;
   unsigned rem = (lane == leader) ? (peers & ~(1u << lane)) : 0u;
-  const int rounds = __popc(rem);
-  const int maxRounds = __reduce_max_sync(0xffffffffu, (unsigned)rounds);
+  const int maxRounds = (int)__reduce_max_sync(fm, (unsigned)__popc(rem));
   float acc[8];
 #pragma unroll
-  for (int k = 0; k < 8; k++) acc[k] = contrib[k];
+  for (int k = 0; k < 8; k++) acc[k] = v[k];
   for (int r = 0; r < maxRounds; r++) {
     const int src = rem ? (__ffs(rem) - 1) : lane;
     const bool take = rem != 0u;
     if (rem) rem &= rem - 1u;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      const float v = __shfl_sync(0xffffffffu, contrib[k], src);
-      if (take) acc[k] += v;
+      const float o = __shfl_sync(fm, v[k], src);
+      if (take) acc[k] += o;
     }
   }
-  if (valid && lane == leader) {
+  if (lane == leader) {
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const size_t off = base + (size_t)((k & 1) ? dxs : 0) + ((k & 2) ? (size_t)dys * sy : 0) +
-                         ((k & 4) ? (size_t)dzs * sz : 0);
-      if (acc[k] != 0.f) atomicAdd(grid + off, acc[k]);
-    }
+    for (int k = 0; k < 8; k++)
+      if (acc[k] != 0.f) atomicAdd(dst + off[k], acc[k]);
   }
 }
 
-// FP32 adjoint by path replay.  Every warp runs its lanes in lockstep up to
-// the warp's longest march so the scatter sees all 32 lanes.
-__global__ void __launch_bounds__(128) ea_backward_kernel(const EAParams p, const float4 *__restrict__ img,
+// FP32 adjoint by path replay.  Consecutive steps of a ray mostly stay in
+// the same cell and TF segment, so each lane keeps running sums for its
+// current stencil and TF segment and flushes them (warp-aggregated) only
+// when either changes.  Lanes run in lockstep up to the warp's longest march
+// so the flushes see all 32 lanes.
+template <int MinBlocks>
+__global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAParams p, const float4 *__restrict__ img,
                                                           const float4 *__restrict__ gimg, float *__restrict__ gvox,
                                                           float *__restrict__ gtf) {
   extern __shared__ float s_gtf[];  // tf_n*4, block-private TF gradient
@@ -251,20 +254,37 @@ __global__ void __launch_bounds__(128) ea_backward_kernel(const EAParams p, cons
   const float Tn = 1.f - C.w;
   const float gs = (float)(p.xf.n - 1) / p.xf.span;
   const size_t sy = (size_t)p.F.N[0], sz = (size_t)p.F.N[0] * p.F.N[1];
-  float tau = 0.f, comp = 0.f, A0 = 0.f, A1 = 0.f, A2 = 0.f;
+  const float bd = p.xf.baseDensity;
+  float A0 = 0.f, A1 = 0.f, A2 = 0.f;
+  // transmittance before the current step; the replay advances it as
+  // T_{i+1} = T_i - T_i alpha_i (alpha from expm1, so 1-alpha keeps full
+  // absolute precision): one transcendental per step
+  float T = 1.f;
   bool alive = inside && n > 0;
-  for (int i = 0; i < nMax; i++) {
-    bool valid = false;
-    size_t base = 0;
-    int dxs = 0, dys = 0, dzs = 0;
-    float contrib[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  // running sums: voxel stencil (key = base voxel) and TF segment (key = idx)
+  long long vKey = -1;
+  size_t vOff[8];
+  float vAcc[8];
+  int tIdx = -1;
+  float tAcc[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) { vAcc[k] = 0.f; tAcc[k] = 0.f; vOff[k] = 0; }
+  for (int i = 0; i <= nMax; i++) {
+    // this step's contributions (none past the end of the lane's march)
+    bool have = false;
+    long long key = -1;
+    size_t off[8];
+    float contrib[8];
+    int idx = -1;
+    float tcon[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { contrib[k] = 0.f; tcon[k] = 0.f; off[k] = 0; }
     if (alive && i < n) {
       const float t = t0 + ((float)i + .5f) * p.dt;
       if (t >= t1) {
         alive = false;
       } else {
         const vec3 P = org + t * dir;
-        // sample with the stencil kept for the scatter
         vec3 rel = (P - p.F.origin) * p.F.rcpSpacing;
         const bool in = !(rel.x < 0.f || rel.y < 0.f || rel.z < 0.f || rel.x >= (float)p.F.C[0] ||
                           rel.y >= (float)p.F.C[1] || rel.z >= (float)p.F.C[2]);
@@ -279,44 +299,38 @@ __global__ void __launch_bounds__(128) ea_backward_kernel(const EAParams p, cons
           p.store.corners(x0, x1, y0, y1, z0, z1, c);
           const float v00 = lerp_l(fx, c[0], c[1]), v01 = lerp_l(fx, c[2], c[3]);
           const float v10 = lerp_l(fx, c[4], c[5]), v11 = lerp_l(fx, c[6], c[7]);
-          const float s = lerp_l(fz, lerp_l(fy, v00, v01), lerp_l(fy, v10, v11));
-          // TF map with its segment
-          float f = (s - p.xf.lo) / p.xf.span;
+          const float sv = lerp_l(fz, lerp_l(fy, v00, v01), lerp_l(fy, v10, v11));
+          float f = (sv - p.xf.lo) / p.xf.span;
           const bool clamped = !(f > 0.f && f < 1.f);
           f = clampv(f, 0.f, 1.f);
           f *= (float)(p.xf.n - 1);
-          const int idx = clampv((int)f, 0, p.xf.n - 2);
+          idx = clampv((int)f, 0, p.xf.n - 2);
           f -= (float)idx;
           const float4 e0 = __ldg(p.xf.v + idx), e1 = __ldg(p.xf.v + idx + 1);
           const float r = (1.f - f) * e0.x + f * e1.x, gg = (1.f - f) * e0.y + f * e1.y,
                       b = (1.f - f) * e0.z + f * e1.z;
-          const float sig = ((1.f - f) * e0.w + f * e1.w) * p.xf.baseDensity;
+          const float sig = ((1.f - f) * e0.w + f * e1.w) * bd;
           const float x = sig * p.dt;
-          const float T = expf(-(tau + comp));
           const float w = T * -expm1f(-x);
           A0 += w * r;
           A1 += w * gg;
           A2 += w * b;
-          const float tn = tau + x;
-          if (fabsf(tau) >= fabsf(x)) comp += (tau - tn) + x;
-          else comp += (x - tn) + tau;
-          tau = tn;
-          const float Tnext = expf(-(tau + comp));
+          const float Tnext = T - w;
           float dLdx = g.w * Tn;
           dLdx += g.x * (r * Tnext - (C.x - A0));
           dLdx += g.y * (gg * Tnext - (C.y - A1));
           dLdx += g.z * (b * Tnext - (C.z - A2));
+          T = Tnext;
           const float dLdsig = dLdx * p.dt;
           const float dr = g.x * w, dg = g.y * w, db = g.z * w;
-          const float bd = p.xf.baseDensity;
-          atomicAdd(s_gtf + 4 * idx + 0, dr * (1.f - f));
-          atomicAdd(s_gtf + 4 * idx + 1, dg * (1.f - f));
-          atomicAdd(s_gtf + 4 * idx + 2, db * (1.f - f));
-          atomicAdd(s_gtf + 4 * idx + 3, dLdsig * bd * (1.f - f));
-          atomicAdd(s_gtf + 4 * (idx + 1) + 0, dr * f);
-          atomicAdd(s_gtf + 4 * (idx + 1) + 1, dg * f);
-          atomicAdd(s_gtf + 4 * (idx + 1) + 2, db * f);
-          atomicAdd(s_gtf + 4 * (idx + 1) + 3, dLdsig * bd * f);
+          tcon[0] = dr * (1.f - f);
+          tcon[1] = dg * (1.f - f);
+          tcon[2] = db * (1.f - f);
+          tcon[3] = dLdsig * bd * (1.f - f);
+          tcon[4] = dr * f;
+          tcon[5] = dg * f;
+          tcon[6] = db * f;
+          tcon[7] = dLdsig * bd * f;
           if (!clamped) {
             float dLds = dLdsig * bd * (e1.w - e0.w) * gs;
             dLds += dr * (e1.x - e0.x) * gs + dg * (e1.y - e0.y) * gs + db * (e1.z - e0.z) * gs;
@@ -329,16 +343,42 @@ __global__ void __launch_bounds__(128) ea_backward_kernel(const EAParams p, cons
             contrib[5] = dLds * fx * wy0 * fz;
             contrib[6] = dLds * wx0 * fy * fz;
             contrib[7] = dLds * fx * fy * fz;
-            valid = true;
-            base = (size_t)x0 + sy * y0 + sz * z0;
-            dxs = x1 - x0;
-            dys = y1 - y0;
-            dzs = z1 - z0;
+            const size_t base = (size_t)x0 + sy * y0 + sz * z0;
+            key = (long long)base;
+            const size_t ddx = (size_t)(x1 - x0), ddy = (size_t)(y1 - y0) * sy, ddz = (size_t)(z1 - z0) * sz;
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+              off[k] = base + ((k & 1) ? ddx : 0) + ((k & 2) ? ddy : 0) + ((k & 4) ? ddz : 0);
+            have = true;
           }
         }
       }
     }
-    scatter_stencil(gvox, valid, base, sy, sz, dxs, dys, dzs, contrib);
+    // voxel stencil: flush the running sum when the stencil changes
+    const bool vFlush = vKey >= 0 && (key != vKey);
+    flush8<false>(gvox, vFlush, (unsigned long long)vKey, vOff, vAcc);
+    if (vFlush || vKey < 0) {
+      vKey = have ? key : -1;
+#pragma unroll
+      for (int k = 0; k < 8; k++) { vAcc[k] = have ? contrib[k] : 0.f; vOff[k] = off[k]; }
+    } else if (have) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) vAcc[k] += contrib[k];
+    }
+    // TF segment: same scheme, into the block's shared-memory gradient
+    const bool tFlush = tIdx >= 0 && idx != tIdx;
+    size_t tOff[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) tOff[k] = (size_t)(4 * tIdx + k);
+    flush8<true>(s_gtf, tFlush, (unsigned long long)tIdx, tOff, tAcc);
+    if (tFlush || tIdx < 0) {
+      tIdx = idx;
+#pragma unroll
+      for (int k = 0; k < 8; k++) tAcc[k] = idx >= 0 ? tcon[k] : 0.f;
+    } else if (idx >= 0) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) tAcc[k] += tcon[k];
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < ntf; i += blockDim.x)
@@ -434,9 +474,18 @@ gbv_status gbv_ea_backward(const gbv_scene *s, const gbv_ea_view *views, int num
   if (smem > 48 * 1024) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_ea_backward: transfer function above 3072 entries");
   return for_view_chunks(p, views, num_views, [&](EAParams &q, int cnt, int maxW, int maxH) {
     dim3 grid((maxW + 15) / 16, (maxH + 7) / 8, cnt);
-    ea_backward_kernel<<<grid, 128, smem, (cudaStream_t)stream>>>(
-        q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
-        d_grad_scalars, d_grad_tf);
+    // GBV_EA_OCC: resident 128-thread blocks per SM the adjoint's registers
+    // are capped for (default 4)
+    const char *oc = getenv("GBV_EA_OCC");
+    const int occ = oc ? atoi(oc) : 4;
+    if (occ >= 6)
+      ea_backward_kernel<6><<<grid, 128, smem, (cudaStream_t)stream>>>(
+          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
+          d_grad_scalars, d_grad_tf);
+    else
+      ea_backward_kernel<4><<<grid, 128, smem, (cudaStream_t)stream>>>(
+          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
+          d_grad_scalars, d_grad_tf);
     return check_launch("ea_backward_kernel");
   });
 }

@@ -202,126 +202,17 @@ struct MCGridDev {
   vec3 spacing;     // = cells_per_mc * gridSpacing
 };
 
+// Per-lane event counts (32-bit per lane; summed in 64 bits per launch)
 struct TraceCounters {
-  unsigned long long samples, mcs, rays, caps;
+  unsigned samples, mcs, rays, caps, cells;
 };
 
-// Result of one ray-volume query
+// Result of one ray-volume query (the hit point is recomputed from the
+// traversal's origin and direction when it is shaded)
 struct Hit {
   bool hit;
   float t;
   vec3 rgb;
-  vec3 P;
 };
-
-// MCVolumeAccel::isProg (MCAccelerator.h:569-708) with dda::dda3
-// (DDA.h:65-206) and Woodcock::sampleRange (Volume.h:188-223), dispatched as
-// the CPU backend does: tmin 0, tmax = ray.tMax, identity instance transform,
-// zero direction components replaced by 1e-6 (traceRays.dev.cu:41-44).
-// Advances `seed` exactly as the reference advances ray.rngSeed.
-template <class Store>
-__device__ __forceinline__ Hit trace_volume(const FieldGeom &F, const Store &S, const XF &xf, const MCGridDev &G,
-                                            vec3 org, vec3 rayDir, float rayTMax, RNGSeed &seed,
-                                            TraceCounters &cnt) {
-  Hit h;
-  h.hit = false;
-  cnt.rays++;
-  vec3 dir = rayDir;
-  if (dir.x == 0.f) dir.x = 1e-6f;
-  if (dir.y == 0.f) dir.y = 1e-6f;
-  if (dir.z == 0.f) dir.z = 1e-6f;
-  if (G.M[0] <= 0 || G.M[1] <= 0 || G.M[2] <= 0) return h;
-  float tLo = 0.f, tHi = rayTMax;
-  if (!box_test(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return h;
-
-  const vec3 rcpMc = rcp(G.spacing);
-  const vec3 dda_org = (org - G.origin) * rcpMc;
-  const vec3 dda_dir = dir * rcpMc;
-  Random rng = Random::derive(seed, kVolumeStreamHash);
-  const float tMax = tHi;
-
-  const vec3 f_size((float)G.M[0], (float)G.M[1], (float)G.M[2]);
-  const vec3 rcp_dir = rcp(dda_dir);
-  vec3 t_lo = (vec3(0.f) - dda_org) * rcp(dda_dir);
-  vec3 t_hi = (f_size - dda_org) * rcp(dda_dir);
-  vec3 t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
-  const float INF = __int_as_float(0x7f800000);
-  if (dda_dir.x == 0.f) {
-    if (dda_org.x < 0.f || dda_org.x > f_size.x) return h;
-    t_nr.x = -INF; t_fr.x = INF;
-  }
-  if (dda_dir.y == 0.f) {
-    if (dda_org.y < 0.f || dda_org.y > f_size.y) return h;
-    t_nr.y = -INF; t_fr.y = INF;
-  }
-  if (dda_dir.z == 0.f) {
-    if (dda_org.z < 0.f || dda_org.z > f_size.z) return h;
-    t_nr.z = -INF; t_fr.z = INF;
-  }
-  const float ray_t0 = mx(0.f, reduce_max(t_nr));
-  const float ray_t1 = mn(tMax, reduce_min(t_fr));
-  if (ray_t0 > ray_t1) return h;
-  const vec3 org_in_volume = dda_org + ray_t0 * dda_dir;
-  const vec3 f_cell = vmax(vec3(0.f), vmin(f_size - vec3(1.f), vfloor(org_in_volume)));
-  const vec3 f_cell_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
-                        dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
-  const vec3 t_step = vabs(rcp_dir);
-  vec3 t_next((dda_dir.x == 0.f) ? INF : (fabsf(f_cell_end.x - org_in_volume.x) * t_step.x),
-              (dda_dir.y == 0.f) ? INF : (fabsf(f_cell_end.y - org_in_volume.y) * t_step.y),
-              (dda_dir.z == 0.f) ? INF : (fabsf(f_cell_end.z - org_in_volume.z) * t_step.z));
-  const int stop_x = dda_dir.x > 0.f ? G.M[0] : -1, stop_y = dda_dir.y > 0.f ? G.M[1] : -1,
-            stop_z = dda_dir.z > 0.f ? G.M[2] : -1;
-  const int dx = dda_dir.x > 0.f ? 1 : -1, dy = dda_dir.y > 0.f ? 1 : -1, dz = dda_dir.z > 0.f ? 1 : -1;
-  int cx = (int)f_cell.x, cy = (int)f_cell.y, cz = (int)f_cell.z;
-  float next_cell_begin = 0.f;
-  const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
-  for (int it = 0; it < maxCells; it++) {
-    const float t_closest = reduce_min(t_next);
-    const float cell_t0 = ray_t0 + next_cell_begin;
-    const float cell_t1 = ray_t0 + mn(t_closest, tMax);
-    const float majorant = __ldg(G.maj + (cx + G.M[0] * (cy + G.M[1] * cz)));
-    if (majorant != 0.f) {
-      cnt.mcs++;
-      const float segHi0 = mn(cell_t1, rayTMax);
-      float t = cell_t0;
-      // Woodcock::sampleRange
-      for (int k = 0; k < (1 << 20); k++) {
-        const float r = rng();
-        const float dt = -fastLog(1.f - r) / majorant;
-        t += dt;
-        if (t >= segHi0) break;
-        const vec3 P = org + t * dir;
-        const vec4 smp = sample_and_map(F, S, xf, P);
-        cnt.samples++;
-        if (smp.w >= rng() * majorant) {
-          h.hit = true;
-          h.t = t;
-          h.rgb = vec3(smp.x, smp.y, smp.z);
-          h.P = org + t * dir;
-          return h;
-        }
-        if (k == (1 << 20) - 1) cnt.caps++;
-      }
-    }
-    next_cell_begin = t_closest;
-    if (t_next.x == t_closest) {
-      t_next.x += t_step.x;
-      cx += dx;
-      if (cx == stop_x) return h;
-    }
-    if (t_next.y == t_closest) {
-      t_next.y += t_step.y;
-      cy += dy;
-      if (cy == stop_y) return h;
-    }
-    if (t_next.z == t_closest) {
-      t_next.z += t_step.z;
-      cz += dz;
-      if (cz == stop_z) return h;
-    }
-  }
-  cnt.caps++;
-  return h;
-}
 
 }  // namespace gbv

@@ -47,7 +47,16 @@ struct RenderParams {
   unsigned long long *counters;
   int skip;       // empty macrocells crossed per traversal step
   int threshold;  // keep traversing while at least this % of busy lanes trace
+  // shared-memory staging (offsets in 32-bit words of the dynamic smem)
+  int maskWords;  // >0: bitmask of non-zero majorants staged at offset 0
+  int cdfYOff;    // >=0: env cdf_y staged here
+  int pivOff;     // >=0: per-row pivots of cdf_x staged here
+  int pivPerRow;
+  int profile;    // accumulate per-phase cycle counts
 };
+
+// Dynamic shared memory of the render kernel (layout in RenderParams).
+extern __shared__ uint32_t g_smem[];
 
 struct LightSample {
   vec3 radiance, direction;
@@ -131,6 +140,60 @@ __device__ __forceinline__ int sample_cdf(const float *cdf, int N, float v, floa
   pdf = (float)N * (at - before);
   return begin;
 }
+// cdfGetPDF / sampleCDF on the staged cdf_y (binary search in shared memory)
+__device__ __forceinline__ float cdf_y_at(const RenderParams &p, int i) {
+  return p.cdfYOff >= 0 ? __int_as_float(g_smem[p.cdfYOff + i]) : __ldg(p.env.cdf_y + i);
+}
+__device__ __forceinline__ int sample_cdf_y(const RenderParams &p, float v, float &pdf) {
+  const int N = p.env.H;
+  int begin = 0, end = N;
+  while ((end - begin) > 1) {
+    int mid = (begin + end) / 2;
+    if (v < cdf_y_at(p, mid - 1)) end = mid;
+    else begin = mid;
+  }
+  const float at = cdf_y_at(p, begin);
+  const float before = begin ? cdf_y_at(p, begin - 1) : 0.f;
+  pdf = (float)N * (at - before);
+  return begin;
+}
+// sampleCDF over one row of cdf_x.  The binary search returns the number of
+// entries cdf[0..N-2] that are <= v (the CDF is non-decreasing); with staged
+// pivots (the last counted entry of every 32-entry segment) the same count is
+// the number of segments whose pivot is <= v, times 32, plus a count inside
+// the next segment, whose 32 entries are fetched with independent loads.
+__device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, float v, float &pdf) {
+  const int N = p.env.W;
+  const float *cdf = p.env.cdf_x + (size_t)row * N;
+  if (p.pivOff < 0) return sample_cdf(cdf, N, v, pdf);
+  const float *piv = reinterpret_cast<const float *>(g_smem + p.pivOff) + (size_t)row * p.pivPerRow;
+  const int nseg = p.pivPerRow;
+  int lo = 0, hi = nseg;  // first segment whose pivot is > v
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (piv[mid] <= v) lo = mid + 1;
+    else hi = mid;
+  }
+  int begin;
+  if (lo == nseg) {
+    begin = N - 1;
+  } else {
+    const int s0 = lo * 32;
+    const int last = min(s0 + 31, N - 2);
+    float seg[32];
+#pragma unroll
+    for (int k = 0; k < 32; k++) seg[k] = (s0 + k <= last) ? __ldg(cdf + s0 + k) : 0.f;
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < 32; k++) c += (s0 + k <= last && seg[k] <= v) ? 1 : 0;
+    begin = s0 + c;
+  }
+  const float at = __ldg(cdf + begin);
+  const float before = begin ? __ldg(cdf + begin - 1) : 0.f;
+  pdf = (float)N * (at - before);
+  return begin;
+}
+
 // EnvMap.h:136-180
 __device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   if (!p.hasEnv) return kOneOverFourPi;
@@ -141,7 +204,7 @@ __device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   float u = phi * kOneOverTwoPi, v = theta * kOneOverPi;
   int px = (int)clampv(u * (float)e.W, 0.f, (float)e.W - 1.f);
   int py = (int)clampv(v * (float)e.H, 0.f, (float)e.H - 1.f);
-  float pdf_y = cdf_get_pdf(py, e.cdf_y, e.H);
+  float pdf_y = (float)e.H * (cdf_y_at(p, py) - (py ? cdf_y_at(p, py - 1) : 0.f));
   float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
   float rel_y = ((float)py + .5f) / (float)e.H;
   const float theta2 = kPi * rel_y;
@@ -154,8 +217,8 @@ __device__ __forceinline__ LightSample env_sample(const RenderParams &p, Random 
   float r_y = r();
   float r_x = r();
   float pdf_y, pdf_x;
-  int iy = sample_cdf(e.cdf_y, e.H, r_y, pdf_y);
-  int ix = sample_cdf(e.cdf_x + (size_t)e.W * iy, e.W, r_x, pdf_x);
+  int iy = sample_cdf_y(p, r_y, pdf_y);
+  int ix = sample_cdf_x(p, iy, r_x, pdf_x);
   float sx = ((float)ix + r()) / (float)e.W;
   float sy = ((float)iy + r()) / (float)e.H;
   float4 t = tex2D(e, sx, sy);
@@ -321,15 +384,14 @@ struct ShadeOut {
 
 // bounce() for a volume hit (shadeRays.cu:605-878).  Updates `ray`; a dead
 // ray has tMax = -1.
-__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, int pathDepth,
-                                                  ShadeOut &out) {
+__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
+                                                  int pathDepth, ShadeOut &out) {
   out.shadowValid = false;
   const float tHit = h.t;
   const vec3 albedo = p.multi ? p.scatAlb * h.rgb : .7f * h.rgb;
   const float g = p.multi ? p.aniso : 0.f;
   const vec3 incomingThroughput = from_half(ray.tp);
   Random random = Random::derive(ray.seed, (uint64_t)float_bits(tHit));
-  const vec3 P = h.P;
   const vec3 wo = -normalize(ray.dir);
   const float offsetEpsilon = mx(1e-4f, 1e-6f * reduce_max(vabs(P)));
   LightSample ls;
@@ -516,18 +578,21 @@ __device__ __forceinline__ bool trace_advance(Traversal &T, float tc, bool sx, b
 
 template <class Store>
 __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store, const XF &xf, const MCGridDev &G,
-                                          Traversal &T, Hit &h, TraceCounters &cnt, int skip) {
+                                          Traversal &T, Hit &h, TraceCounters &cnt, int skip, bool staged) {
   const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
   const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
   if (!T.inCell) {
     for (int k = 0; k < skip; k++) {
+      cnt.cells++;
       if (++T.cells > maxCells) {
         cnt.caps++;
         return TR_MISS;
       }
       const float tc = reduce_min(T.t_next);
-      const float maj = majorant_at(G, T.cx, T.cy, T.cz);
-      if (maj != 0.f) {
+      const int ci = T.cx + G.M[0] * (T.cy + G.M[1] * T.cz);
+      const bool nonzero = staged ? ((g_smem[ci >> 5] >> (ci & 31)) & 1u) != 0u : __ldg(G.maj + ci) != 0.f;
+      if (nonzero) {
+        const float maj = __ldg(G.maj + ci);
         const float cell_t0 = T.ray_t0 + T.ncb;
         const float cell_t1 = T.ray_t0 + mn(tc, T.tMax);
         T.inCell = 1;
@@ -559,7 +624,6 @@ __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store
     h.hit = true;
     h.t = T.t;
     h.rgb = vec3(smp.x, smp.y, smp.z);
-    h.P = P;
     return TR_HIT;
   }
   return TR_CONTINUE;
@@ -612,10 +676,32 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const Rende
                                                                      int *__restrict__ pool) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  // ---- stage the majorant bitmask and env-map tables in shared memory ----
+  {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
+    for (int w = warp; w < p.maskWords; w += nwarps) {
+      const int i = w * 32 + lane;
+      const float m = i < nmc ? __ldg(p.G.maj + i) : 0.f;
+      const unsigned b = __ballot_sync(FULL, m != 0.f);
+      if (lane == 0) g_smem[w] = b;
+    }
+    if (p.cdfYOff >= 0)
+      for (int i = threadIdx.x; i < p.env.H; i += blockDim.x) g_smem[p.cdfYOff + i] = __float_as_uint(__ldg(p.env.cdf_y + i));
+    if (p.pivOff >= 0) {
+      const int total = p.env.H * p.pivPerRow;
+      for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int row = i / p.pivPerRow, k = i - row * p.pivPerRow;
+        const int last = min(k * 32 + 31, p.env.W - 2);
+        g_smem[p.pivOff + i] = __float_as_uint(__ldg(p.env.cdf_x + (size_t)row * p.env.W + last));
+      }
+    }
+    __syncthreads();
+  }
   const vec3 rcpMc = rcp(p.G.spacing);
   const int tilesX = (p.W + 7) >> 3;
   const int numTiles = tilesX * ((p.H + 3) >> 2);
-  TraceCounters cnt{0, 0, 0, 0};
+  TraceCounters cnt{0, 0, 0, 0, 0};
   // warp-uniform tile pool
   int tile = 0, tileTaken = 32;
   bool poolDone = false;
@@ -629,6 +715,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const Rende
   Traversal T;
   Hit h;
   h.hit = false;
+  unsigned long long cyc[3] = {0ull, 0ull, 0ull};
   while (true) {
     // ---- phase 1: pixels for idle lanes (from the warp's tile), then every
     // lane that needs one starts its next trace ----
@@ -661,6 +748,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const Rende
       }
     }
     if (poolDone && __all_sync(FULL, !hasPixel)) break;
+    long long c0 = p.profile ? clock64() : 0;
     if (hasPixel && tstate == NEED) {
       if (newSample) {
         generate_primary(p, ix, iy, p.accumIdStart + s, ray);
@@ -681,68 +769,87 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const Rende
       tstate = active ? TRACING : DONE;
     }
     // ---- phase 2: traverse while enough of the warp's busy lanes trace ----
+    long long c1 = 0;
+    if (p.profile) {
+      __syncwarp();
+      c1 = clock64();
+      if (lane == 0) cyc[0] += (unsigned long long)(c1 - c0);
+    }
     {
       const int busy = __popc(__ballot_sync(FULL, hasPixel));
       while (true) {
         const int tracing = __popc(__ballot_sync(FULL, tstate == TRACING));
         if (tracing == 0 || tracing * 100 < busy * p.threshold) break;
-        if (tstate == TRACING && trace_step(p.F, store, p.xf, p.G, T, h, cnt, p.skip) != TR_CONTINUE)
+        if (tstate == TRACING && trace_step(p.F, store, p.xf, p.G, T, h, cnt, p.skip, p.maskWords > 0) != TR_CONTINUE)
           tstate = DONE;
       }
     }
     // ---- phase 3: shade the finished traces (bounce(), shadeRays.cu:477-878) ----
-    if (tstate != DONE) continue;
-    tstate = NEED;
-    const int accumID = p.accumIdStart + s;
-    const float clampMax = 10.f * (float)(1 + accumID);
-    if (kind == K_SHADOW) {
-      if (!h.hit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
-      shadowPending = false;
-    } else {
-      vec3 frag(0.f);
-      float alpha = 0.f;
-      if (!h.hit) {
-        if (gen == 0) {
-          const float4 miss = miss_color(p, iy);
-          alpha = miss.w;
-          frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
-        } else {
-          frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
-        }
-        ray.tMax = -1.f;
-      } else {
-        if (gen == 0) alpha = 1.f;
-        ShadeOut so;
-        bounce_volume_hit(p, ray, h, gen, so);
-        if (so.shadowValid && so.shadow.tMax > 0.f) {
-          sray = so.shadow;
-          shadowPending = true;
-        }
-      }
-      frag = vmin(frag, vec3(clampMax));
-      if (accumID == 0 && gen == 0) {
-        acc = make_float4(frag.x, frag.y, frag.z, alpha);
-      } else {
-        if (gen == 0 && alpha > 0.f) acc.w += alpha;
-        accum_add(acc, frag);
-      }
-      mainAlive = ray.tMax > 0.f;
-      gen++;
+    long long c2 = 0;
+    if (p.profile) {
+      __syncwarp();
+      c2 = clock64();
+      if (lane == 0) cyc[1] += (unsigned long long)(c2 - c1);
     }
-    if (!shadowPending && !mainAlive) {
-      // this pixel's pass is complete
-      if (++s == p.spp) {
-        p.accum[(size_t)iy * p.W + ix] = acc;
-        hasPixel = false;
+    if (tstate == DONE) {
+      tstate = NEED;
+      const int accumID = p.accumIdStart + s;
+      const float clampMax = 10.f * (float)(1 + accumID);
+      if (kind == K_SHADOW) {
+        if (!h.hit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
+        shadowPending = false;
       } else {
-        newSample = true;
+        vec3 frag(0.f);
+        float alpha = 0.f;
+        if (!h.hit) {
+          if (gen == 0) {
+            const float4 miss = miss_color(p, iy);
+            alpha = miss.w;
+            frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
+          } else {
+            frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
+          }
+          ray.tMax = -1.f;
+        } else {
+          if (gen == 0) alpha = 1.f;
+          ShadeOut so;
+          // setVolumeHit's P = obj_org + t * obj_dir (MCAccelerator.h:79)
+        bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, so);
+          if (so.shadowValid && so.shadow.tMax > 0.f) {
+            sray = so.shadow;
+            shadowPending = true;
+          }
+        }
+        frag = vmin(frag, vec3(clampMax));
+        if (accumID == 0 && gen == 0) {
+          acc = make_float4(frag.x, frag.y, frag.z, alpha);
+        } else {
+          if (gen == 0 && alpha > 0.f) acc.w += alpha;
+          accum_add(acc, frag);
+        }
+        mainAlive = ray.tMax > 0.f;
+        gen++;
       }
+      if (!shadowPending && !mainAlive) {
+        // this pixel's pass is complete
+        if (++s == p.spp) {
+          p.accum[(size_t)iy * p.W + ix] = acc;
+          hasPixel = false;
+        } else {
+          newSample = true;
+        }
+      }
+    }
+    if (p.profile) {
+      __syncwarp();
+      if (lane == 0) cyc[2] += (unsigned long long)(clock64() - c2);
     }
   }
   if (p.counters) {
-    unsigned long long v[4] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps};
+    unsigned long long v[8] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps, cnt.cells, cyc[0], cyc[1], cyc[2]};
+    // (per-lane counts are 32-bit; a lane processes far fewer than 2^32 events)
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 8; k++) {
       unsigned long long x = v[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
@@ -852,7 +959,11 @@ static gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st != GBV_OK) return st;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks>, kThreads, 0);
+  const size_t smem = (size_t)(p.maskWords + (p.cdfYOff >= 0 ? p.env.H : 0) +
+                               (p.pivOff >= 0 ? p.env.H * p.pivPerRow : 0)) * sizeof(uint32_t);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(render_kernel<Store, MinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks>, kThreads, smem);
   const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
@@ -864,14 +975,15 @@ static gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   st = check_cuda(cudaMallocAsync((void **)&pool, sizeof(int), stream), "cudaMallocAsync(tile pool)");
   if (st != GBV_OK) return st;
   cudaMemsetAsync(pool, 0, sizeof(int), stream);
-  render_kernel<Store, MinBlocks><<<(unsigned)blocks, kThreads, 0, stream>>>(p, store, pool);
+  render_kernel<Store, MinBlocks><<<(unsigned)blocks, kThreads, smem, stream>>>(p, store, pool);
   st = check_launch("render_kernel");
   cudaFreeAsync(pool, stream);
   return st;
 }
 
-// GBV_RENDER_OCC=1 selects one resident block per SM (no register cap);
-// the default caps registers for two.  GBV_RENDER_SKIP sets the empty
+// GBV_RENDER_OCC=1..4 selects the resident blocks per SM the registers are
+// capped for (default 4: 32 warps per SM; the kernel is latency-bound and
+// gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
 // macrocells crossed per traversal step (default 8); GBV_RENDER_THRESH the
 // percentage of a warp's busy lanes that must still be tracing for the warp
 // to keep traversing before it shades and refills (default 20).
@@ -880,11 +992,44 @@ static gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   const char *sk = getenv("GBV_RENDER_SKIP");
   p.skip = sk ? atoi(sk) : kSkipDefault;
   if (p.skip < 1) p.skip = 1;
+  // Shared-memory staging of the majorant bitmask and env-map CDF pivots
+  // (GBV_RENDER_STAGE=1) gives the same results; it is off by default because
+  // the shared memory it takes comes out of L1, which the kernel's spills,
+  // majorant and CDF loads use (measured slower on GB300).
+  const char *ns = getenv("GBV_RENDER_STAGE");
+  const bool stage = ns && atoi(ns) != 0;
+  const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
+  const int budget = 64 * 1024 / 4;
+  int used = 0;
+  p.maskWords = 0;
+  p.cdfYOff = p.pivOff = -1;
+  p.pivPerRow = 0;
+  if (stage && nmc > 0 && (nmc + 31) / 32 <= budget) {
+    p.maskWords = (int)((nmc + 31) / 32);
+    used = p.maskWords;
+  }
+  if (stage && p.hasEnv && p.env.W >= 2) {
+    if (used + p.env.H <= budget) {
+      p.cdfYOff = used;
+      used += p.env.H;
+    }
+    const int per = (p.env.W - 1 + 31) / 32;  // segments holding entries 0..W-2
+    if ((long long)used + (long long)p.env.H * per <= budget) {
+      p.pivOff = used;
+      p.pivPerRow = per;
+      used += p.env.H * per;
+    }
+  }
+  const char *pf = getenv("GBV_RENDER_PROFILE");
+  p.profile = (pf && atoi(pf) != 0 && p.counters) ? 1 : 0;
   const char *th = getenv("GBV_RENDER_THRESH");
   p.threshold = th ? atoi(th) : 20;
   if (p.threshold < 1) p.threshold = 1;
   const char *oc = getenv("GBV_RENDER_OCC");
-  if (oc && atoi(oc) == 1) return launch_render_t<Store, 1>(p, store, stream);
+  const int occ = oc ? atoi(oc) : 4;
+  if (occ == 3) return launch_render_t<Store, 3>(p, store, stream);
+  if (occ == 4) return launch_render_t<Store, 4>(p, store, stream);
+  if (occ == 1) return launch_render_t<Store, 1>(p, store, stream);
   return launch_render_t<Store, 2>(p, store, stream);
 }
 

@@ -196,3 +196,22 @@ def test_rmse_falls_as_inverse_sqrt_spp(cuda):
     o.render(spp=16, accum=ao, accum_id_start=1)
     ro = float(np.sqrt(np.mean((ao[..., :3] / 16 - ref) ** 2)))
     assert ro < 1.5 * rmse[16], (ro, rmse)
+
+
+def test_shared_memory_staging_is_transparent(cuda):
+    """Staging the majorant bitmask and env-map CDF pivots in shared memory
+    gives the same frame, bit for bit, as reading them from global memory
+    (the pivot search returns the reference binary search's index)."""
+    import os
+    import torch
+    s = _ms_scene(8, w=64, h=48, dims=48)
+    s.env = scenes.env_sky(200, 100)  # W not a multiple of 32
+    g = GpuScene(s)
+    a = g.render(spp=8, accum_id_start=3).cpu().numpy()
+    os.environ["GBV_RENDER_STAGE"] = "1"
+    try:
+        b = g.render(spp=8, accum_id_start=3).cpu().numpy()
+    finally:
+        del os.environ["GBV_RENDER_STAGE"]
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(a), bits(b))
