@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
             "gbv_build_brick_store": (st, [vp, ip, i, vp, vp, vp]),
             "gbv_env_build_cdfs": (st, [vp, i, i, ip, vp, vp, vp]),
             "gbv_render": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
+            "gbv_render_noalloc": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
             "gbv_tonemap": (st, [vp, i, i, i, i, vp, vp]),
             "gbv_ea_render": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),
             "gbv_ea_render_f64": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),

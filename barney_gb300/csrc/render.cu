@@ -8,6 +8,7 @@
 // generation the trace (MCVolumeAccel::isProg) and _shadeRays/bounce
 // (barney/kernels/shadeRays.cu:477-1041) of the pixel's queued rays.
 #include <cstdlib>
+#include <mutex>
 #include <cuda_runtime.h>
 #include "gbv_volume.cuh"
 #include "gbv_internal.h"
@@ -1079,4 +1080,136 @@ extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, 
                            cs);
   }
   return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown voxel format");
+}
+
+// ===========================================================================
+// gbv_render_noalloc: the same frame render with no device allocation.
+//
+// Some callers cannot let a library allocate device memory while they
+// render: an application that hands out all HBM from its own pre-sized pool
+// and requires libraries to work inside the buffers it passes them, or a
+// real-time viewer that forbids allocation and free calls on its frame
+// path (gbv_render takes its one scratch word from cudaMallocAsync and
+// returns it with cudaFreeAsync, which draw on the device's memory pool).
+// This entry point takes that scratch word from a file-scope device array
+// instead.
+// ===========================================================================
+namespace gbv {
+
+// The persistent kernel's only scratch: the tile-pool counter (one 32-bit
+// word).  Every GPU that loads this library holds this array until the
+// process exits.  All calls share it and it keeps the last call's value, so
+// each call clears it first; calls that overlap on the GPU (for example on
+// two streams) race on it.
+static __device__ __align__(256) int g_noalloc_tile_pool[1];
+constexpr long long kNoAllocMaxTiles = 1ll << 30;
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static int *g_noalloc_addr[kNoAllocMaxDevices];
+
+// Device address of the scratch on the current device, looked up once per
+// device (host code may not use the array's name as a device address).
+static gbv_status noalloc_scratch(int **out) {
+  int dev = 0;
+  gbv_status st = check_cuda(cudaGetDevice(&dev), "gbv_render_noalloc: cudaGetDevice");
+  if (st != GBV_OK) return st;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *ptr = nullptr;
+    st = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_tile_pool), "gbv_render_noalloc: cudaGetSymbolAddress");
+    if (st != GBV_OK) return st;
+    g_noalloc_addr[dev] = static_cast<int *>(ptr);
+  }
+  *out = g_noalloc_addr[dev];
+  return GBV_OK;
+}
+
+template <class Store>
+static gbv_status launch_render_noalloc(RenderParams p, const Store &store, cudaStream_t stream, int *pool) {
+  // fixed launch settings (results do not depend on them): 4 resident
+  // blocks per SM, 8 cells per traversal step, no shared-memory staging
+  p.skip = kSkipDefault;
+  p.threshold = 20;
+  p.maskWords = 0;
+  p.cdfYOff = p.pivOff = -1;
+  p.pivPerRow = 0;
+  p.profile = 0;
+  int dev = 0, sms = 0, perSM = 0;
+  gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st != GBV_OK) return st;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4>, kThreads, 0);
+  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+  const long long warpsPerBlock = kThreads / 32;
+  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
+  const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
+  if (blocks > needed) blocks = needed;
+  if (blocks < 1) blocks = 1;
+  st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "gbv_render_noalloc: clearing the tile pool");
+  if (st != GBV_OK) return st;
+  render_kernel<Store, 4><<<(unsigned)blocks, kThreads, 0, stream>>>(p, store, pool);
+  return check_launch("render_kernel (noalloc)");
+}
+
+}  // namespace gbv
+
+extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int width, int height,
+                                         int accum_id_start, int spp, unsigned long long *d_counters,
+                                         void *stream) {
+  if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render_noalloc: null pointer or non-positive size");
+  // the scratch is one 32-bit counter of 8x4-pixel tiles; every warp may take
+  // one tile past the end, so the frame's tiles must leave room for them
+  const long long tiles = (long long)((width + 7) / 8) * ((height + 3) / 4);
+  if (tiles > kNoAllocMaxTiles)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT,
+                     "gbv_render_noalloc: frame exceeds the 2^30 tiles of 8x4 pixels its 32-bit tile counter holds");
+  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT,
+                     "gbv_render_noalloc: scene lacks voxels, majorants or a transfer function");
+  if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: the linear layout holds FP32 voxels only");
+  if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render_noalloc: U8 voxels need the brick scale/offset table");
+  if (spp == 0) return GBV_OK;
+  int *pool = nullptr;
+  gbv_status st = noalloc_scratch(&pool);
+  if (st != GBV_OK) return st;
+  RenderParams p;
+  st = fill_params(s, p);
+  if (st != GBV_OK) return st;
+  p.W = width;
+  p.H = height;
+  p.accum = reinterpret_cast<float4 *>(d_accum);
+  p.accumIdStart = accum_id_start;
+  p.spp = spp;
+  p.counters = d_counters;
+  cudaStream_t cs = (cudaStream_t)stream;
+  if (s->layout == GBV_LAYOUT_LINEAR) {
+    StoreLinearF32 store{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
+    return launch_render_noalloc(p, store, cs, pool);
+  }
+  if (s->layout != GBV_LAYOUT_BRICK_CORNERS)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: unknown layout");
+  int nb[3];
+  brick_counts(s->dims, nb);
+  switch (s->format) {
+    case GBV_VOXEL_F32:
+      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_F32>{s->d_voxels, nullptr, nb[0], nb[1]}, cs, pool);
+    case GBV_VOXEL_F16:
+      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_F16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs, pool);
+    case GBV_VOXEL_BF16:
+      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_BF16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs,
+                                   pool);
+    case GBV_VOXEL_U8_SCALED:
+      return launch_render_noalloc(
+          p,
+          StoreBrickCorners<GBV_VOXEL_U8_SCALED>{s->d_voxels, reinterpret_cast<const float2 *>(s->d_scale_offset),
+                                                 nb[0], nb[1]},
+          cs, pool);
+  }
+  return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: unknown voxel format");
 }

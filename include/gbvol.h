@@ -178,6 +178,23 @@ gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
                       int height, int accum_id_start, int spp,
                       unsigned long long *d_counters, void *stream);
 
+/* gbv_render without any device allocation, for callers that may not
+   allocate device memory while they render (an application that hands out
+   all HBM from its own pre-sized pool, or a real-time viewer that forbids
+   allocation calls on its frame path).  No counterpart in the reference.
+   Same arguments and results as gbv_render.  Its one word of scratch (the
+   persistent kernel's tile-pool counter) lives in a file-scope device array
+   of 4 bytes that every GPU loading this library keeps until exit, instead
+   of a cudaMallocAsync/cudaFreeAsync pair.  The first call on a device looks
+   up that array's device address once (cudaGetSymbolAddress); make that
+   first call before any stream capture.  All calls share the word and each
+   call clears it before its launch, so calls that overlap on the GPU (for
+   example on two streams) race.  Frames above 2^30 tiles of 8x4 pixels are
+   rejected with GBV_ERROR_INVALID_ARGUMENT. */
+gbv_status gbv_render_noalloc(const gbv_scene *scene, float *d_accum, int width,
+                              int height, int accum_id_start, int spp,
+                              unsigned long long *d_counters, void *stream);
+
 /* Frame-buffer read: d_accum * (1/accum_id) into d_out as float4, RGBA8 or
    sRGB RGBA8.  Replaces linearizeColorAndNormalKernel
    (barney/fb/TiledFB.cu:13-50) with LocalFB::gatherColorChannel's
