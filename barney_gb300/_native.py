@@ -69,6 +69,10 @@ def lib() -> C.CDLL:
             "gbv_env_build_cdfs": (st, [vp, i, i, ip, vp, vp, vp]),
             "gbv_render": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
             "gbv_render_noalloc": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
+            "gbv_batch_create": (st, [C.POINTER(GbvScene), vp, ip, ip, i, C.POINTER(vp)]),
+            "gbv_batch_set_launch": (st, [vp, i, i, i]),
+            "gbv_batch_render": (st, [vp, i, i, vp, vp]),
+            "gbv_batch_destroy": (st, [vp]),
             "gbv_tonemap": (st, [vp, i, i, i, i, vp, vp]),
             "gbv_ea_render": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),
             "gbv_ea_render_f64": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),

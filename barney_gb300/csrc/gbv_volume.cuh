@@ -202,11 +202,6 @@ struct MCGridDev {
   vec3 spacing;     // = cells_per_mc * gridSpacing
 };
 
-// Per-lane event counts (32-bit per lane; summed in 64 bits per launch)
-struct TraceCounters {
-  unsigned samples, mcs, rays, caps, cells;
-};
-
 // Result of one ray-volume query (the hit point is recomputed from the
 // traversal's origin and direction when it is shaded)
 struct Hit {

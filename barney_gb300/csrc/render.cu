@@ -1,867 +1,9 @@
-// render.cu -- the structured-volume frame render on sm_103a.
-//
-// One thread owns one pixel for all of a launch's accumulation passes, so
-// the frame buffer needs no atomics and every pixel accumulates its
-// fragments in the reference's order (pass-major, then generation; within a
-// generation the shadow ray before the bounce ray).  A pass follows
-// Context::renderTiles (barney/Context.cpp:142-185): _generateRays, then per
-// generation the trace (MCVolumeAccel::isProg) and _shadeRays/bounce
-// (barney/kernels/shadeRays.cu:477-1041) of the pixel's queued rays.
-#include <cstdlib>
-#include <mutex>
-#include <cuda_runtime.h>
-#include "gbv_volume.cuh"
-#include "gbv_internal.h"
+// render.cu -- host entry points of the frame render: parameter set-up
+// (camera, lights, env map, macrocell grid) and dispatch to the kernels of
+// the scene's voxel store (render_store_*.cu).
+#include "render_kernel.cuh"
 
 namespace gbv {
-
-struct DirLightDev { vec3 direction; float radiance; vec3 color; };
-struct M3 { vec3 vx, vy, vz; };
-__device__ __forceinline__ vec3 xfm_vector(const M3 &m, vec3 v) { return m.vx * v.x + m.vy * v.y + m.vz * v.z; }
-
-struct EnvDev {
-  const float4 *tex;
-  const float *cdf_y, *cdf_x;
-  int W, H;
-  int addr[2];
-  M3 toWorld, toLocal;
-  float scale;
-};
-
-struct RenderParams {
-  FieldGeom F;
-  XF xf;
-  MCGridDev G;
-  // camera (PerspectiveCamera::commit)
-  vec3 lens00, dir00, du, dv;
-  int W, H;
-  int numDir;
-  DirLightDev dir[4];
-  int hasEnv;
-  EnvDev env;
-  float4 bg;
-  float ambient;
-  int multi, volMS, maxVB;
-  float aniso, scatAlb;
-  float4 *accum;
-  int accumIdStart, spp;
-  unsigned long long *counters;
-  int skip;       // empty macrocells crossed per traversal step
-  int threshold;  // keep traversing while at least this % of busy lanes trace
-  // shared-memory staging (offsets in 32-bit words of the dynamic smem)
-  int maskWords;  // >0: bitmask of non-zero majorants staged at offset 0
-  int cdfYOff;    // >=0: env cdf_y staged here
-  int pivOff;     // >=0: per-row pivots of cdf_x staged here
-  int pivPerRow;
-  int profile;    // accumulate per-phase cycle counts
-};
-
-// Dynamic shared memory of the render kernel (layout in RenderParams).
-extern __shared__ uint32_t g_smem[];
-
-struct LightSample {
-  vec3 radiance, direction;
-  float distance, pdf;
-};
-
-// rtcore/embree/Texture.cpp:25-93 (normalized coordinates)
-__device__ __forceinline__ void compute_address(int mode, float tc, int N, int &i0, int &i1, float &f) {
-  i0 = 0; i1 = 0; f = 0.f;
-  if (mode == GBV_ADDR_WRAP) {
-    tc = tc * (float)N - .5f;
-    tc = fmodf(tc, (float)N);
-    if (tc < 0.f) tc += (float)N;
-    float fc = floorf(tc);
-    int ic = (int)fc;
-    f = tc - (float)ic;
-    i0 = ic;
-    i1 = (int)fmodf(tc + 1.f, (float)N);
-  } else if (mode == GBV_ADDR_MIRROR) {
-    tc = tc * (float)N + .5f;
-    float fc = floorf(tc);
-    int ic = (int)fc;
-    f = tc - (float)ic;
-    int a = ic - 1, b = ic;
-    if (a < 0) a = -a;
-    if (b < 0) b = -b;
-    a = a % (2 * N);
-    b = b % (2 * N);
-    if (a >= N) a = 2 * N - 1 - a;
-    if (b >= N) b = 2 * N - 1 - b;
-    i0 = a;
-    i1 = b;
-  } else if (mode == GBV_ADDR_CLAMP) {
-    tc = tc * (float)N;
-    if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; }
-    else if (tc - .5f >= (float)(N - 1)) { i0 = i1 = N - 1; f = 0.f; }
-    else {
-      f = (tc - .5f) - (float)(int)(tc - .5f);
-      i0 = (int)(tc - .5f);
-      i1 = i0 + 1;
-    }
-  }
-}
-__device__ __forceinline__ float4 lerp4(float f, float4 a, float4 b) {
-  return make_float4((1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
-                     (1.f - f) * a.w + f * b.w);
-}
-// rtcore/embree/Texture.cpp:295-321
-__device__ __forceinline__ float4 tex2D(const EnvDev &e, float u, float v) {
-  int x0, x1, y0, y1;
-  float fx, fy;
-  compute_address(e.addr[0], u, e.W, x0, x1, fx);
-  compute_address(e.addr[1], v, e.H, y0, y1, fy);
-  float4 v00 = __ldg(e.tex + (size_t)x0 + (size_t)y0 * e.W), v01 = __ldg(e.tex + (size_t)x1 + (size_t)y0 * e.W);
-  float4 v10 = __ldg(e.tex + (size_t)x0 + (size_t)y1 * e.W), v11 = __ldg(e.tex + (size_t)x1 + (size_t)y1 * e.W);
-  return lerp4(fy, lerp4(fx, v00, v01), lerp4(fx, v10, v11));
-}
-
-// DG.h:97-106
-__device__ __forceinline__ float spherical_theta(vec3 v) { return acosf(clampv(v.z, -1.f, 1.f)); }
-__device__ __forceinline__ float spherical_phi(vec3 v) {
-  float p = atan2f(v.y, v.x);
-  return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
-}
-// EnvMap.h:98-134
-__device__ __forceinline__ float cdf_get_pdf(int position, const float *cdf, int N) {
-  float at = __ldg(cdf + position);
-  float before = position ? __ldg(cdf + position - 1) : 0.f;
-  return (float)N * (at - before);
-}
-__device__ __forceinline__ int sample_cdf(const float *cdf, int N, float v, float &pdf) {
-  int begin = 0, end = N;
-  while ((end - begin) > 1) {
-    int mid = (begin + end) / 2;
-    float f_mid = __ldg(cdf + mid - 1);
-    if (v < f_mid) end = mid;
-    else begin = mid;
-  }
-  float at = __ldg(cdf + begin);
-  float before = begin ? __ldg(cdf + begin - 1) : 0.f;
-  pdf = (float)N * (at - before);
-  return begin;
-}
-// cdfGetPDF / sampleCDF on the staged cdf_y (binary search in shared memory)
-__device__ __forceinline__ float cdf_y_at(const RenderParams &p, int i) {
-  return p.cdfYOff >= 0 ? __int_as_float(g_smem[p.cdfYOff + i]) : __ldg(p.env.cdf_y + i);
-}
-__device__ __forceinline__ int sample_cdf_y(const RenderParams &p, float v, float &pdf) {
-  const int N = p.env.H;
-  int begin = 0, end = N;
-  while ((end - begin) > 1) {
-    int mid = (begin + end) / 2;
-    if (v < cdf_y_at(p, mid - 1)) end = mid;
-    else begin = mid;
-  }
-  const float at = cdf_y_at(p, begin);
-  const float before = begin ? cdf_y_at(p, begin - 1) : 0.f;
-  pdf = (float)N * (at - before);
-  return begin;
-}
-// sampleCDF over one row of cdf_x.  The binary search returns the number of
-// entries cdf[0..N-2] that are <= v (the CDF is non-decreasing); with staged
-// pivots (the last counted entry of every 32-entry segment) the same count is
-// the number of segments whose pivot is <= v, times 32, plus a count inside
-// the next segment, whose 32 entries are fetched with independent loads.
-__device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, float v, float &pdf) {
-  const int N = p.env.W;
-  const float *cdf = p.env.cdf_x + (size_t)row * N;
-  if (p.pivOff < 0) return sample_cdf(cdf, N, v, pdf);
-  const float *piv = reinterpret_cast<const float *>(g_smem + p.pivOff) + (size_t)row * p.pivPerRow;
-  const int nseg = p.pivPerRow;
-  int lo = 0, hi = nseg;  // first segment whose pivot is > v
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (piv[mid] <= v) lo = mid + 1;
-    else hi = mid;
-  }
-  int begin;
-  if (lo == nseg) {
-    begin = N - 1;
-  } else {
-    const int s0 = lo * 32;
-    const int last = min(s0 + 31, N - 2);
-    float seg[32];
-#pragma unroll
-    for (int k = 0; k < 32; k++) seg[k] = (s0 + k <= last) ? __ldg(cdf + s0 + k) : 0.f;
-    int c = 0;
-#pragma unroll
-    for (int k = 0; k < 32; k++) c += (s0 + k <= last && seg[k] <= v) ? 1 : 0;
-    begin = s0 + c;
-  }
-  const float at = __ldg(cdf + begin);
-  const float before = begin ? __ldg(cdf + begin - 1) : 0.f;
-  pdf = (float)N * (at - before);
-  return begin;
-}
-
-// EnvMap.h:136-180
-__device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
-  if (!p.hasEnv) return kOneOverFourPi;
-  const EnvDev &e = p.env;
-  vec3 localDir = xfm_vector(e.toLocal, dir);
-  float theta = spherical_theta(localDir);
-  float phi = spherical_phi(localDir);
-  float u = phi * kOneOverTwoPi, v = theta * kOneOverPi;
-  int px = (int)clampv(u * (float)e.W, 0.f, (float)e.W - 1.f);
-  int py = (int)clampv(v * (float)e.H, 0.f, (float)e.H - 1.f);
-  float pdf_y = (float)e.H * (cdf_y_at(p, py) - (py ? cdf_y_at(p, py - 1) : 0.f));
-  float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
-  float rel_y = ((float)py + .5f) / (float)e.H;
-  const float theta2 = kPi * rel_y;
-  return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta2));
-}
-// EnvMap.h:198-250
-__device__ __forceinline__ LightSample env_sample(const RenderParams &p, Random &r) {
-  const EnvDev &e = p.env;
-  LightSample s;
-  float r_y = r();
-  float r_x = r();
-  float pdf_y, pdf_x;
-  int iy = sample_cdf_y(p, r_y, pdf_y);
-  int ix = sample_cdf_x(p, iy, r_x, pdf_x);
-  float sx = ((float)ix + r()) / (float)e.W;
-  float sy = ((float)iy + r()) / (float)e.H;
-  float4 t = tex2D(e, sx, sy);
-  s.radiance = e.scale * vec3(t.x, t.y, t.z);
-  const float phi = kTwoPi * sx;
-  const float theta = kPi * sy;
-  vec3 d;
-  d.z = cosf(theta);
-  d.x = cosf(phi) * sinf(theta);
-  d.y = sinf(phi) * sinf(theta);
-  s.direction = xfm_vector(e.toWorld, d);
-  s.pdf = pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta));
-  s.distance = __int_as_float(0x7f800000);
-  return s;
-}
-
-// DG.h:183-193
-__device__ __forceinline__ vec3 random_direction(Random &rng) {
-  for (int k = 0; k < 64; k++) {
-    vec3 v;
-    v.x = 1.f - 2.f * rng();
-    v.y = 1.f - 2.f * rng();
-    v.z = 1.f - 2.f * rng();
-    if (dot(v, v) <= 1.f) return normalize(v);
-  }
-  return vec3(0.f, 0.f, 1.f);
-}
-
-// shadeRays.cu:141-191 (the world's only normal here is the volume's N=0)
-__device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random &random, LightSample &ls) {
-  if (p.numDir == 0) return false;
-  int lID[2];
-  float weights[2];
-  float sumWeights = 0.f;
-#pragma unroll
-  for (int i = 0; i < 2; i++) {
-    lID[i] = mn((int)(random() * (float)p.numDir), p.numDir - 1);
-    weights[i] = 0.f;
-    const DirLightDev &light = p.dir[lID[i]];
-    vec3 lr = light.color * light.radiance;
-    float weight = 1.f;  // N == 0
-    weight *= reduce_max(lr);
-    if (weight <= 1e-3f) continue;
-    weights[i] = weight;
-    sumWeights += weight;
-  }
-  if (sumWeights == 0.f) return false;
-  float r = random() * sumWeights;
-  int i = 0;
-  while (i < 2 && r >= weights[i]) { r -= weights[i]; ++i; }
-  if (i == 2) return false;
-  const DirLightDev &light = p.dir[lID[i]];
-  ls.direction = -light.direction;
-  ls.distance = __int_as_float(0x7f800000);
-  ls.radiance = light.color * light.radiance * 1.f / (weights[i] / sumWeights * (2.f / (float)p.numDir));
-  ls.pdf = __int_as_float(0x7f800000);
-  return weights[i] != 0.f;
-}
-
-// shadeRays.cu:268-404 (no area or point lights in this world)
-__device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &random, LightSample &ls,
-                                              bool &needsMIS, bool &isDir) {
-  needsMIS = false;
-  LightSample els;
-  if (p.hasEnv) {
-    els = env_sample(p, random);
-  } else {
-    els.direction = random_direction(random);
-    els.distance = __int_as_float(0x7f800000);
-    els.radiance = vec3(kFourPi * p.ambient);
-    els.pdf = kOneOverFourPi;
-  }
-  float elsWeight = reduce_max(els.radiance);
-  LightSample dls;
-  dls.pdf = 0.f;
-  float dlsWeight = sample_dir_lights(p, random, dls) ? reduce_max(dls.radiance) : 0.f;
-  float alsWeight = 0.f, plsWeight = 0.f;
-  float sumWeights = alsWeight + dlsWeight + elsWeight + plsWeight;
-  if (sumWeights == 0.f) return false;
-  elsWeight *= 1.f / sumWeights;
-  alsWeight *= 1.f / sumWeights;
-  dlsWeight *= 1.f / sumWeights;
-  float r = random();
-  if (r <= alsWeight) {
-    return false;  // empty area-light sample (pdf 0)
-  } else if (r <= alsWeight + elsWeight) {
-    ls = els;
-    ls.radiance = ls.radiance * (1.f / elsWeight);
-    needsMIS = true;
-  } else if (r <= alsWeight + elsWeight + plsWeight) {
-    return false;
-  } else {
-    ls = dls;
-    ls.radiance = ls.radiance * (1.f / dlsWeight);
-    isDir = true;
-  }
-  if (isnan(ls.pdf) || (ls.pdf <= 0.f)) return false;
-  return true;
-}
-
-// shadeRays.cu:437-456
-__device__ __forceinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
-  if (p.hasEnv) {
-    vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
-    float theta = spherical_theta(d);
-    float phi = spherical_phi(d);
-    const float invPi = 1.f / (float)3.14159265358979323846;
-    const float inv2Pi = 1.f / (2.f * (float)3.14159265358979323846);
-    float4 c = tex2D(p.env, phi * inv2Pi, theta * invPi);
-    return p.env.scale * vec3(c.x, c.y, c.z);
-  }
-  return vec3(p.ambient);
-}
-
-// Phase.h:49-57
-__device__ __forceinline__ float hg_phase(float g, float cosTheta) {
-  if (fabsf(g) < 1e-3f) return kOneOverFourPi;
-  float g2 = g * g;
-  float denom = 1.f + g2 - 2.f * g * cosTheta;
-  return kOneOverFourPi * (1.f - g2) / (denom * sqrtf(denom));
-}
-__device__ __forceinline__ float phase_pdf(const RenderParams &p, float g, vec3 wo, vec3 wi) {
-  if (!p.multi) return kOneOverFourPi;
-  vec3 wi_in = normalize(-wo);
-  return hg_phase(g, dot(wi_in, normalize(wi)));
-}
-// Phase.h:74-99
-__device__ __forceinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
-  float u0 = random();
-  float u1 = random();
-  float cosTheta;
-  if (fabsf(g) < 1e-3f) cosTheta = 1.f - 2.f * u0;
-  else {
-    float sqrTerm = (1.f - g * g) / (1.f + g - 2.f * g * u0);
-    cosTheta = (1.f + g * g - sqrTerm * sqrTerm) / (2.f * g);
-  }
-  float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
-  float phi = kTwoPi * u1;
-  vec3 local(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
-  vec3 w = normalize(wi_in);
-  vec3 u, v;
-  if (fabsf(w.x) > 0.1f) u = normalize(cross(vec3(0.f, 1.f, 0.f), w));
-  else u = normalize(cross(vec3(1.f, 0.f, 0.f), w));
-  v = cross(w, u);
-  return normalize(local.x * u + local.y * v + local.z * w);
-}
-
-// Per-ray state of the pixel's path (Ray + PathState, render/Ray.h:18-99)
-struct PathRay {
-  vec3 org, dir;
-  float tMax;
-  RNGSeed seed;
-  vec3h tp;
-  float misWeight;
-  int numVolumeBounces;
-};
-
-struct ShadeOut {
-  vec3 fragment;
-  bool shadowValid;
-  PathRay shadow;
-};
-
-// bounce() for a volume hit (shadeRays.cu:605-878).  Updates `ray`; a dead
-// ray has tMax = -1.
-__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
-                                                  int pathDepth, ShadeOut &out) {
-  out.shadowValid = false;
-  const float tHit = h.t;
-  const vec3 albedo = p.multi ? p.scatAlb * h.rgb : .7f * h.rgb;
-  const float g = p.multi ? p.aniso : 0.f;
-  const vec3 incomingThroughput = from_half(ray.tp);
-  Random random = Random::derive(ray.seed, (uint64_t)float_bits(tHit));
-  const vec3 wo = -normalize(ray.dir);
-  const float offsetEpsilon = mx(1e-4f, 1e-6f * reduce_max(vabs(P)));
-  LightSample ls;
-  bool needsMIS = false, isDir = false;
-  if (sample_lights(p, random, ls, needsMIS, isDir)) {
-    float density = p.multi ? phase_pdf(p, g, wo, ls.direction) : kOneOverFourPi;
-    vec3 fr = density * albedo;
-    if (!(density > 0.f) || reduce_max(fr) < 1e-4f) {
-      out.shadowValid = false;
-    } else {
-      fr = vmin(fr, vec3(13.f));
-      vec3 tp_sr = incomingThroughput * (isinf(ls.pdf) ? 1.f : 1.f / ls.pdf) * fr * ls.radiance * 1.f;
-      out.shadow.dir = ls.direction;
-      out.shadow.org = P + offsetEpsilon * wo;
-      out.shadow.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
-      out.shadow.tp = to_half(tp_sr);
-      out.shadow.seed = ray.seed;
-      ray.seed.next_h((uint64_t)float_bits(tHit));
-      out.shadow.misWeight = 1.f;
-      out.shadowValid = true;
-      if (!isDir && needsMIS) {
-        float pdf_l = env_pdf(p, ls.direction);
-        float pdf_s = p.multi ? phase_pdf(p, g, wo, ls.direction) : kOneOverFourPi;
-        out.shadow.misWeight = pdf_l / (pdf_l + pdf_s + 1e-10f);
-        if (out.shadow.misWeight < 1e-5f) out.shadowValid = false;
-      }
-    }
-  }
-  if (pathDepth >= 10) {  // MAX_PATH_DEPTH
-    ray.tMax = -1.f;
-    return;
-  }
-  ray.tMax = __int_as_float(0x7f800000);
-  if (!p.multi) {
-    // SCI_VIS_MODE: a volume scatter ends the path after its shadow ray
-    // (the scatter direction is drawn but never used).
-    ray.tMax = -1.f;
-    return;
-  }
-  vec3 wi_in = normalize(-wo);
-  vec3 sdir = sample_hg_direction(wi_in, g, random);
-  float spdf = hg_phase(g, dot(wi_in, sdir));
-  vec3 sf_r = albedo * spdf;
-  if (!(spdf > 0.f) || spdf <= 1e-6f) return;
-  if (!p.volMS || ray.numVolumeBounces >= p.maxVB) {
-    ray.tMax = -1.f;
-    return;
-  }
-  ray.numVolumeBounces = ray.numVolumeBounces + 1;
-  ray.org = P + (1.f * offsetEpsilon) * wo;
-  ray.dir = normalize(sdir);
-  vec3 scatterFactor = sf_r * 1.f / (isinf(spdf) ? 1.f : (spdf + 1e-10f));
-  scatterFactor = vmin(scatterFactor, vec3(2.5f));
-  ray.tp = to_half(from_half(ray.tp) * scatterFactor);
-  if (needsMIS && !isinf(spdf)) {
-    float pdf_s = phase_pdf(p, g, wo, ray.dir);
-    float pdf_l = env_pdf(p, ray.dir);
-    ray.misWeight = pdf_s / (pdf_s + pdf_l);
-  } else {
-    ray.misWeight = 1.f;
-  }
-}
-
-__device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
-  if (frag.x > 0.f) acc.x += frag.x;
-  if (frag.y > 0.f) acc.y += frag.y;
-  if (frag.z > 0.f) acc.z += frag.z;
-}
-
-// -------------------------------------------------------------------------
-// Traversal of one ray through the macrocell grid: dda::dda3 (DDA.h:65-206)
-// with Woodcock::sampleRange (Volume.h:188-223) inside each cell of non-zero
-// majorant, as set up by MCVolumeAccel::isProg (MCAccelerator.h:569-708).
-// The state advances by bounded units so that a warp's lanes stay in one
-// loop: a run of at most kSkip empty cells, or one Woodcock step.
-// -------------------------------------------------------------------------
-constexpr int kSkipDefault = 8;
-constexpr int kWoodcockCap = 1 << 20;
-enum { TR_CONTINUE = 0, TR_HIT = 1, TR_MISS = 2 };
-
-struct Traversal {
-  vec3 org, dir;   // trace direction: zero components replaced by 1e-6
-  float rayTMax;   // ray.tMax of the ray record
-  vec3 t_next, t_step;
-  int cx, cy, cz;
-  int stopx, stopy, stopz;
-  float ray_t0, tMax, ncb;
-  float tc;            // t_closest of the current cell
-  float t, segHi, maj; // delta tracking in the current cell
-  Random rng;
-  int inCell;
-  int steps;           // Woodcock steps in the current cell
-  int cells;           // cells visited
-};
-
-__device__ __forceinline__ float majorant_at(const MCGridDev &G, int cx, int cy, int cz) {
-  return __ldg(G.maj + (cx + G.M[0] * (cy + G.M[1] * cz)));
-}
-
-// Box test, RNG stream and DDA set-up.  Returns false when the ray reaches
-// no cell.  `seed` advances exactly when the reference advances ray.rngSeed
-// (once the box test passes).
-__device__ __forceinline__ bool trace_begin(const FieldGeom &F, const MCGridDev &G, const vec3 &rcpMc, vec3 org,
-                                            vec3 rayDir, float rayTMax, RNGSeed &seed, Traversal &T,
-                                            TraceCounters &cnt) {
-  cnt.rays++;
-  vec3 dir = rayDir;
-  if (dir.x == 0.f) dir.x = 1e-6f;
-  if (dir.y == 0.f) dir.y = 1e-6f;
-  if (dir.z == 0.f) dir.z = 1e-6f;
-  if (G.M[0] <= 0 || G.M[1] <= 0 || G.M[2] <= 0) return false;
-  float tLo = 0.f, tHi = rayTMax;
-  if (!box_test(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return false;
-  const vec3 dda_org = (org - G.origin) * rcpMc;
-  const vec3 dda_dir = dir * rcpMc;
-  T.rng = Random::derive(seed, kVolumeStreamHash);
-  const float tMax = tHi;
-  const vec3 f_size((float)G.M[0], (float)G.M[1], (float)G.M[2]);
-  const vec3 rcp_dir = rcp(dda_dir);
-  vec3 t_lo = (vec3(0.f) - dda_org) * rcp_dir;
-  vec3 t_hi = (f_size - dda_org) * rcp_dir;
-  vec3 t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
-  const float INF = __int_as_float(0x7f800000);
-  if (dda_dir.x == 0.f) {
-    if (dda_org.x < 0.f || dda_org.x > f_size.x) return false;
-    t_nr.x = -INF; t_fr.x = INF;
-  }
-  if (dda_dir.y == 0.f) {
-    if (dda_org.y < 0.f || dda_org.y > f_size.y) return false;
-    t_nr.y = -INF; t_fr.y = INF;
-  }
-  if (dda_dir.z == 0.f) {
-    if (dda_org.z < 0.f || dda_org.z > f_size.z) return false;
-    t_nr.z = -INF; t_fr.z = INF;
-  }
-  const float ray_t0 = mx(0.f, reduce_max(t_nr));
-  const float ray_t1 = mn(tMax, reduce_min(t_fr));
-  if (ray_t0 > ray_t1) return false;
-  const vec3 oiv = dda_org + ray_t0 * dda_dir;
-  const vec3 f_cell = vmax(vec3(0.f), vmin(f_size - vec3(1.f), vfloor(oiv)));
-  const vec3 f_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
-                   dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
-  T.t_step = vabs(rcp_dir);
-  T.t_next = vec3((dda_dir.x == 0.f) ? INF : (fabsf(f_end.x - oiv.x) * T.t_step.x),
-                  (dda_dir.y == 0.f) ? INF : (fabsf(f_end.y - oiv.y) * T.t_step.y),
-                  (dda_dir.z == 0.f) ? INF : (fabsf(f_end.z - oiv.z) * T.t_step.z));
-  T.stopx = dda_dir.x > 0.f ? G.M[0] : -1;
-  T.stopy = dda_dir.y > 0.f ? G.M[1] : -1;
-  T.stopz = dda_dir.z > 0.f ? G.M[2] : -1;
-  T.cx = (int)f_cell.x;
-  T.cy = (int)f_cell.y;
-  T.cz = (int)f_cell.z;
-  T.ray_t0 = ray_t0;
-  T.tMax = tMax;
-  T.ncb = 0.f;
-  T.org = org;
-  T.dir = dir;
-  T.rayTMax = rayTMax;
-  T.inCell = 0;
-  T.cells = 0;
-  return true;
-}
-
-// next_cell_begin = t_closest, then step every axis whose t_next equals it
-__device__ __forceinline__ bool trace_advance(Traversal &T, float tc, bool sx, bool sy, bool sz) {
-  T.ncb = tc;
-  if (T.t_next.x == tc) {
-    T.t_next.x += T.t_step.x;
-    T.cx += sx ? 1 : -1;
-    if (T.cx == T.stopx) return false;
-  }
-  if (T.t_next.y == tc) {
-    T.t_next.y += T.t_step.y;
-    T.cy += sy ? 1 : -1;
-    if (T.cy == T.stopy) return false;
-  }
-  if (T.t_next.z == tc) {
-    T.t_next.z += T.t_step.z;
-    T.cz += sz ? 1 : -1;
-    if (T.cz == T.stopz) return false;
-  }
-  return true;
-}
-
-template <class Store>
-__device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store, const XF &xf, const MCGridDev &G,
-                                          Traversal &T, Hit &h, TraceCounters &cnt, int skip, bool staged) {
-  const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
-  const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
-  if (!T.inCell) {
-    for (int k = 0; k < skip; k++) {
-      cnt.cells++;
-      if (++T.cells > maxCells) {
-        cnt.caps++;
-        return TR_MISS;
-      }
-      const float tc = reduce_min(T.t_next);
-      const int ci = T.cx + G.M[0] * (T.cy + G.M[1] * T.cz);
-      const bool nonzero = staged ? ((g_smem[ci >> 5] >> (ci & 31)) & 1u) != 0u : __ldg(G.maj + ci) != 0.f;
-      if (nonzero) {
-        const float maj = __ldg(G.maj + ci);
-        const float cell_t0 = T.ray_t0 + T.ncb;
-        const float cell_t1 = T.ray_t0 + mn(tc, T.tMax);
-        T.inCell = 1;
-        T.tc = tc;
-        T.maj = maj;
-        T.t = cell_t0;
-        T.segHi = mn(cell_t1, T.rayTMax);
-        T.steps = 0;
-        cnt.mcs++;
-        break;
-      }
-      if (!trace_advance(T, tc, sx, sy, sz)) return TR_MISS;
-    }
-    if (!T.inCell) return TR_CONTINUE;
-  }
-  // one Woodcock step
-  const float r = T.rng();
-  const float dt = -fastLog(1.f - r) / T.maj;
-  T.t += dt;
-  if (T.t >= T.segHi || ++T.steps > kWoodcockCap) {
-    if (T.steps > kWoodcockCap) cnt.caps++;
-    T.inCell = 0;
-    return trace_advance(T, T.tc, sx, sy, sz) ? TR_CONTINUE : TR_MISS;
-  }
-  const vec3 P = T.org + T.t * T.dir;
-  const vec4 smp = sample_and_map(F, store, xf, P);
-  cnt.samples++;
-  if (smp.w >= T.rng() * T.maj) {
-    h.hit = true;
-    h.t = T.t;
-    h.rgb = vec3(smp.x, smp.y, smp.z);
-    return TR_HIT;
-  }
-  return TR_CONTINUE;
-}
-
-// -------------------------------------------------------------------------
-// The persistent frame kernel.  Each lane owns one pixel for all of the
-// launch's passes, so fragments accumulate in the reference's order
-// (pass-major, generation, shadow ray before bounce ray) without atomics.
-// Warps take 8x4-pixel tiles from a global pool; a lane whose pixel is done
-// takes the next pixel of its warp's tile.  Every loop iteration advances a
-// lane by one bounded unit: a trace step, or a shade and the set-up of the
-// next trace.
-// -------------------------------------------------------------------------
-constexpr int kThreads = 256;
-enum { K_NONE = 0, K_MAIN = 1, K_SHADOW = 2 };
-
-__device__ __forceinline__ float4 miss_color(const RenderParams &p, int iy) {
-  const float t = ((float)iy + .5f) / (float)p.H;
-  float4 m = p.bg;
-  if (!(p.bg.w >= 0.f)) {
-    m.x = (1.0f - t) * 0.9f + t * 0.15f;
-    m.y = (1.0f - t) * 0.9f + t * 0.25f;
-    m.z = (1.0f - t) * 0.9f + t * .8f;
-    m.w = (1.0f - t) * 1.f + t * 1.f;
-  }
-  return m;
-}
-
-// _generateRays (generateRays.cu:72-243), perspective camera, no aperture
-__device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, int iy, int accumID, PathRay &ray) {
-  const float aspect = (float)p.W / (float)p.H;
-  Random rand = Random::from_pair((unsigned)(ix + p.W * accumID), (unsigned)(iy + p.H * accumID));
-  ray.seed = seeded((uint32_t)(ix + accumID * p.W), (uint32_t)iy);
-  const float pixel_u = (accumID == 0) ? .5f : rand();
-  const float pixel_v = (accumID == 0) ? .5f : rand();
-  const float image_u = ((float)ix + pixel_u) / (float)p.W;
-  const float image_v = ((float)iy + pixel_v) / (float)p.H;
-  const vec3 d = p.dir00 + (1.f * aspect * (image_u - .5f)) * p.du + (1.f * (image_v - .5f)) * p.dv;
-  ray.org = p.lens00;
-  ray.dir = normalize(d);
-  ray.tMax = 1e30f;
-  ray.tp = to_half(vec3(1.f));
-  ray.misWeight = 0.f;
-  ray.numVolumeBounces = 0;
-}
-
-template <class Store, int MinBlocks>
-__global__ void __launch_bounds__(kThreads, MinBlocks) render_kernel(const RenderParams p, const Store store,
-                                                                     int *__restrict__ pool) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  // ---- stage the majorant bitmask and env-map tables in shared memory ----
-  {
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
-    for (int w = warp; w < p.maskWords; w += nwarps) {
-      const int i = w * 32 + lane;
-      const float m = i < nmc ? __ldg(p.G.maj + i) : 0.f;
-      const unsigned b = __ballot_sync(FULL, m != 0.f);
-      if (lane == 0) g_smem[w] = b;
-    }
-    if (p.cdfYOff >= 0)
-      for (int i = threadIdx.x; i < p.env.H; i += blockDim.x) g_smem[p.cdfYOff + i] = __float_as_uint(__ldg(p.env.cdf_y + i));
-    if (p.pivOff >= 0) {
-      const int total = p.env.H * p.pivPerRow;
-      for (int i = threadIdx.x; i < total; i += blockDim.x) {
-        const int row = i / p.pivPerRow, k = i - row * p.pivPerRow;
-        const int last = min(k * 32 + 31, p.env.W - 2);
-        g_smem[p.pivOff + i] = __float_as_uint(__ldg(p.env.cdf_x + (size_t)row * p.env.W + last));
-      }
-    }
-    __syncthreads();
-  }
-  const vec3 rcpMc = rcp(p.G.spacing);
-  const int tilesX = (p.W + 7) >> 3;
-  const int numTiles = tilesX * ((p.H + 3) >> 2);
-  TraceCounters cnt{0, 0, 0, 0, 0};
-  // warp-uniform tile pool
-  int tile = 0, tileTaken = 32;
-  bool poolDone = false;
-  // lane state
-  enum { NEED = 0, TRACING = 1, DONE = 2 };
-  bool hasPixel = false;
-  int ix = 0, iy = 0, s = 0, gen = 0, kind = K_NONE, tstate = NEED;
-  bool newSample = false, mainAlive = false, shadowPending = false;
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-  PathRay ray, sray;
-  Traversal T;
-  Hit h;
-  h.hit = false;
-  unsigned long long cyc[3] = {0ull, 0ull, 0ull};
-  while (true) {
-    // ---- phase 1: pixels for idle lanes (from the warp's tile), then every
-    // lane that needs one starts its next trace ----
-    const unsigned need = __ballot_sync(FULL, !hasPixel);
-    if (need != 0u && !poolDone) {
-      if (tileTaken == 32) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(pool, 1);
-        t = __shfl_sync(FULL, t, 0);
-        if (t >= numTiles) poolDone = true;
-        else { tile = t; tileTaken = 0; }
-      }
-      if (!poolDone) {
-        const int rank = __popc(need & ((1u << lane) - 1u));
-        const int take = min(__popc(need), 32 - tileTaken);
-        if (!hasPixel && rank < take) {
-          const int slot = tileTaken + rank;
-          const int px = (tile % tilesX) * 8 + (slot & 7), py = (tile / tilesX) * 4 + (slot >> 3);
-          if (px < p.W && py < p.H) {
-            hasPixel = true;
-            ix = px;
-            iy = py;
-            s = 0;
-            newSample = true;
-            tstate = NEED;
-            acc = p.accumIdStart == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : p.accum[(size_t)iy * p.W + ix];
-          }
-        }
-        tileTaken += take;
-      }
-    }
-    if (poolDone && __all_sync(FULL, !hasPixel)) break;
-    long long c0 = p.profile ? clock64() : 0;
-    if (hasPixel && tstate == NEED) {
-      if (newSample) {
-        generate_primary(p, ix, iy, p.accumIdStart + s, ray);
-        gen = 0;
-        mainAlive = true;
-        shadowPending = false;
-        newSample = false;
-      }
-      h.hit = false;
-      bool active;
-      if (shadowPending) {
-        kind = K_SHADOW;
-        active = trace_begin(p.F, p.G, rcpMc, sray.org, sray.dir, sray.tMax, sray.seed, T, cnt);
-      } else {
-        kind = K_MAIN;
-        active = trace_begin(p.F, p.G, rcpMc, ray.org, ray.dir, ray.tMax, ray.seed, T, cnt);
-      }
-      tstate = active ? TRACING : DONE;
-    }
-    // ---- phase 2: traverse while enough of the warp's busy lanes trace ----
-    long long c1 = 0;
-    if (p.profile) {
-      __syncwarp();
-      c1 = clock64();
-      if (lane == 0) cyc[0] += (unsigned long long)(c1 - c0);
-    }
-    {
-      const int busy = __popc(__ballot_sync(FULL, hasPixel));
-      while (true) {
-        const int tracing = __popc(__ballot_sync(FULL, tstate == TRACING));
-        if (tracing == 0 || tracing * 100 < busy * p.threshold) break;
-        if (tstate == TRACING && trace_step(p.F, store, p.xf, p.G, T, h, cnt, p.skip, p.maskWords > 0) != TR_CONTINUE)
-          tstate = DONE;
-      }
-    }
-    // ---- phase 3: shade the finished traces (bounce(), shadeRays.cu:477-878) ----
-    long long c2 = 0;
-    if (p.profile) {
-      __syncwarp();
-      c2 = clock64();
-      if (lane == 0) cyc[1] += (unsigned long long)(c2 - c1);
-    }
-    if (tstate == DONE) {
-      tstate = NEED;
-      const int accumID = p.accumIdStart + s;
-      const float clampMax = 10.f * (float)(1 + accumID);
-      if (kind == K_SHADOW) {
-        if (!h.hit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
-        shadowPending = false;
-      } else {
-        vec3 frag(0.f);
-        float alpha = 0.f;
-        if (!h.hit) {
-          if (gen == 0) {
-            const float4 miss = miss_color(p, iy);
-            alpha = miss.w;
-            frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
-          } else {
-            frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
-          }
-          ray.tMax = -1.f;
-        } else {
-          if (gen == 0) alpha = 1.f;
-          ShadeOut so;
-          // setVolumeHit's P = obj_org + t * obj_dir (MCAccelerator.h:79)
-        bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, so);
-          if (so.shadowValid && so.shadow.tMax > 0.f) {
-            sray = so.shadow;
-            shadowPending = true;
-          }
-        }
-        frag = vmin(frag, vec3(clampMax));
-        if (accumID == 0 && gen == 0) {
-          acc = make_float4(frag.x, frag.y, frag.z, alpha);
-        } else {
-          if (gen == 0 && alpha > 0.f) acc.w += alpha;
-          accum_add(acc, frag);
-        }
-        mainAlive = ray.tMax > 0.f;
-        gen++;
-      }
-      if (!shadowPending && !mainAlive) {
-        // this pixel's pass is complete
-        if (++s == p.spp) {
-          p.accum[(size_t)iy * p.W + ix] = acc;
-          hasPixel = false;
-        } else {
-          newSample = true;
-        }
-      }
-    }
-    if (p.profile) {
-      __syncwarp();
-      if (lane == 0) cyc[2] += (unsigned long long)(clock64() - c2);
-    }
-  }
-  if (p.counters) {
-    unsigned long long v[8] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps, cnt.cells, cyc[0], cyc[1], cyc[2]};
-    // (per-lane counts are 32-bit; a lane processes far fewer than 2^32 events)
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      unsigned long long x = v[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
-      if (lane == 0 && x) atomicAdd(p.counters + k, x);
-    }
-  }
-}
-
-// -------------------------------------------------------------------------
-// host side
-// -------------------------------------------------------------------------
 static M3 inverse3(const M3 &m) {
   vec3 a = cross(m.vy, m.vz), b = cross(m.vz, m.vx), c = cross(m.vx, m.vy);
   float det = dot(m.vx, a);
@@ -915,6 +57,15 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   for (int i = 0; i < 3; i++) p.G.M[i] = M[i];
   p.G.origin = p.F.boundsLo;
   p.G.spacing = vec3((float)s->cells_per_mc) * vec3(s->spacing[0], s->spacing[1], s->spacing[2]);
+  p.rcpMc = rcp(p.G.spacing);
+  p.vox = s->d_voxels;
+  p.so = reinterpret_cast<const float2 *>(s->d_scale_offset);
+  {
+    int nb[3];
+    brick_counts(s->dims, nb);
+    p.nbx = nb[0];
+    p.nby = nb[1];
+  }
   commit_camera(s->cam_pos, s->cam_dir, s->cam_up, s->fovy, p.lens00, p.dir00, p.du, p.dv);
   p.numDir = s->num_dir_lights < 0 ? 0 : (s->num_dir_lights > 4 ? 4 : s->num_dir_lights);
   for (int i = 0; i < p.numDir; i++) {
@@ -953,87 +104,6 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   return GBV_OK;
 }
 
-template <class Store, int MinBlocks>
-static gbv_status launch_render_t(const RenderParams &p, const Store &store, cudaStream_t stream) {
-  // persistent grid: as many resident blocks as the device holds
-  int dev = 0, sms = 0, perSM = 0;
-  gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-  if (st != GBV_OK) return st;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = (size_t)(p.maskWords + (p.cdfYOff >= 0 ? p.env.H : 0) +
-                               (p.pivOff >= 0 ? p.env.H * p.pivPerRow : 0)) * sizeof(uint32_t);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(render_kernel<Store, MinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks>, kThreads, smem);
-  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
-  const long long warpsPerBlock = kThreads / 32;
-  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
-  const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
-  if (blocks > needed) blocks = needed;
-  if (blocks < 1) blocks = 1;
-  // the tile pool counter lives in stream-ordered scratch memory
-  int *pool = nullptr;
-  st = check_cuda(cudaMallocAsync((void **)&pool, sizeof(int), stream), "cudaMallocAsync(tile pool)");
-  if (st != GBV_OK) return st;
-  cudaMemsetAsync(pool, 0, sizeof(int), stream);
-  render_kernel<Store, MinBlocks><<<(unsigned)blocks, kThreads, smem, stream>>>(p, store, pool);
-  st = check_launch("render_kernel");
-  cudaFreeAsync(pool, stream);
-  return st;
-}
-
-// GBV_RENDER_OCC=1..4 selects the resident blocks per SM the registers are
-// capped for (default 4: 32 warps per SM; the kernel is latency-bound and
-// gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
-// macrocells crossed per traversal step (default 8); GBV_RENDER_THRESH the
-// percentage of a warp's busy lanes that must still be tracing for the warp
-// to keep traversing before it shades and refills (default 20).
-template <class Store>
-static gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
-  const char *sk = getenv("GBV_RENDER_SKIP");
-  p.skip = sk ? atoi(sk) : kSkipDefault;
-  if (p.skip < 1) p.skip = 1;
-  // Shared-memory staging of the majorant bitmask and env-map CDF pivots
-  // (GBV_RENDER_STAGE=1) gives the same results; it is off by default because
-  // the shared memory it takes comes out of L1, which the kernel's spills,
-  // majorant and CDF loads use (measured slower on GB300).
-  const char *ns = getenv("GBV_RENDER_STAGE");
-  const bool stage = ns && atoi(ns) != 0;
-  const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
-  const int budget = 64 * 1024 / 4;
-  int used = 0;
-  p.maskWords = 0;
-  p.cdfYOff = p.pivOff = -1;
-  p.pivPerRow = 0;
-  if (stage && nmc > 0 && (nmc + 31) / 32 <= budget) {
-    p.maskWords = (int)((nmc + 31) / 32);
-    used = p.maskWords;
-  }
-  if (stage && p.hasEnv && p.env.W >= 2) {
-    if (used + p.env.H <= budget) {
-      p.cdfYOff = used;
-      used += p.env.H;
-    }
-    const int per = (p.env.W - 1 + 31) / 32;  // segments holding entries 0..W-2
-    if ((long long)used + (long long)p.env.H * per <= budget) {
-      p.pivOff = used;
-      p.pivPerRow = per;
-      used += p.env.H * per;
-    }
-  }
-  const char *pf = getenv("GBV_RENDER_PROFILE");
-  p.profile = (pf && atoi(pf) != 0 && p.counters) ? 1 : 0;
-  const char *th = getenv("GBV_RENDER_THRESH");
-  p.threshold = th ? atoi(th) : 20;
-  if (p.threshold < 1) p.threshold = 1;
-  const char *oc = getenv("GBV_RENDER_OCC");
-  const int occ = oc ? atoi(oc) : 4;
-  if (occ == 3) return launch_render_t<Store, 3>(p, store, stream);
-  if (occ == 4) return launch_render_t<Store, 4>(p, store, stream);
-  if (occ == 1) return launch_render_t<Store, 1>(p, store, stream);
-  return launch_render_t<Store, 2>(p, store, stream);
-}
-
 }  // namespace gbv
 
 using namespace gbv;
@@ -1059,25 +129,13 @@ extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, 
   p.spp = spp;
   p.counters = d_counters;
   cudaStream_t cs = (cudaStream_t)stream;
-  if (s->layout == GBV_LAYOUT_LINEAR) {
-    StoreLinearF32 store{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
-    return launch_render(p, store, cs);
-  }
+  if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_linear(p, cs);
   if (s->layout != GBV_LAYOUT_BRICK_CORNERS) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown layout");
-  int nb[3];
-  brick_counts(s->dims, nb);
   switch (s->format) {
-    case GBV_VOXEL_F32:
-      return launch_render(p, StoreBrickCorners<GBV_VOXEL_F32>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
-    case GBV_VOXEL_F16:
-      return launch_render(p, StoreBrickCorners<GBV_VOXEL_F16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
-    case GBV_VOXEL_BF16:
-      return launch_render(p, StoreBrickCorners<GBV_VOXEL_BF16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs);
-    case GBV_VOXEL_U8_SCALED:
-      return launch_render(p,
-                           StoreBrickCorners<GBV_VOXEL_U8_SCALED>{
-                               s->d_voxels, reinterpret_cast<const float2 *>(s->d_scale_offset), nb[0], nb[1]},
-                           cs);
+    case GBV_VOXEL_F32: return render_launch_f32(p, cs);
+    case GBV_VOXEL_F16: return render_launch_f16(p, cs);
+    case GBV_VOXEL_BF16: return render_launch_bf16(p, cs);
+    case GBV_VOXEL_U8_SCALED: return render_launch_u8(p, cs);
   }
   return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown voxel format");
 }
@@ -1127,32 +185,6 @@ static gbv_status noalloc_scratch(int **out) {
   return GBV_OK;
 }
 
-template <class Store>
-static gbv_status launch_render_noalloc(RenderParams p, const Store &store, cudaStream_t stream, int *pool) {
-  // fixed launch settings (results do not depend on them): 4 resident
-  // blocks per SM, 8 cells per traversal step, no shared-memory staging
-  p.skip = kSkipDefault;
-  p.threshold = 20;
-  p.maskWords = 0;
-  p.cdfYOff = p.pivOff = -1;
-  p.pivPerRow = 0;
-  p.profile = 0;
-  int dev = 0, sms = 0, perSM = 0;
-  gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-  if (st != GBV_OK) return st;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4>, kThreads, 0);
-  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
-  const long long warpsPerBlock = kThreads / 32;
-  long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
-  const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
-  if (blocks > needed) blocks = needed;
-  if (blocks < 1) blocks = 1;
-  st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "gbv_render_noalloc: clearing the tile pool");
-  if (st != GBV_OK) return st;
-  render_kernel<Store, 4><<<(unsigned)blocks, kThreads, 0, stream>>>(p, store, pool);
-  return check_launch("render_kernel (noalloc)");
-}
 
 }  // namespace gbv
 
@@ -1188,28 +220,122 @@ extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int
   p.spp = spp;
   p.counters = d_counters;
   cudaStream_t cs = (cudaStream_t)stream;
-  if (s->layout == GBV_LAYOUT_LINEAR) {
-    StoreLinearF32 store{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
-    return launch_render_noalloc(p, store, cs, pool);
-  }
+  if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_noalloc_linear(p, cs, pool);
   if (s->layout != GBV_LAYOUT_BRICK_CORNERS)
     return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: unknown layout");
-  int nb[3];
-  brick_counts(s->dims, nb);
   switch (s->format) {
-    case GBV_VOXEL_F32:
-      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_F32>{s->d_voxels, nullptr, nb[0], nb[1]}, cs, pool);
-    case GBV_VOXEL_F16:
-      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_F16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs, pool);
-    case GBV_VOXEL_BF16:
-      return launch_render_noalloc(p, StoreBrickCorners<GBV_VOXEL_BF16>{s->d_voxels, nullptr, nb[0], nb[1]}, cs,
-                                   pool);
-    case GBV_VOXEL_U8_SCALED:
-      return launch_render_noalloc(
-          p,
-          StoreBrickCorners<GBV_VOXEL_U8_SCALED>{s->d_voxels, reinterpret_cast<const float2 *>(s->d_scale_offset),
-                                                 nb[0], nb[1]},
-          cs, pool);
+    case GBV_VOXEL_F32: return render_launch_noalloc_f32(p, cs, pool);
+    case GBV_VOXEL_F16: return render_launch_noalloc_f16(p, cs, pool);
+    case GBV_VOXEL_BF16: return render_launch_noalloc_bf16(p, cs, pool);
+    case GBV_VOXEL_U8_SCALED: return render_launch_noalloc_u8(p, cs, pool);
   }
   return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: unknown voxel format");
+}
+
+// ===========================================================================
+// Batched rendering: many independent scenes of uneven sizes in one
+// persistent launch.  All items share a voxel format and layout.
+// ===========================================================================
+
+
+extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_accums, const int *widths,
+                                       const int *heights, int count, gbv_batch **out) {
+  if (!scenes || !d_accums || !widths || !heights || count <= 0 || !out)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: bad argument");
+  *out = nullptr;
+  std::vector<RenderParams> items(count);
+  std::vector<long long> starts(count + 1, 0);
+  for (int i = 0; i < count; i++) {
+    const gbv_scene *s = scenes + i;
+    if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0 || !d_accums[i] ||
+        widths[i] <= 0 || heights[i] <= 0)
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: an item lacks data or has an empty frame");
+    if (s->format != scenes[0].format || s->layout != scenes[0].layout)
+      return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: items must share voxel format and layout");
+    if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
+      return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: the linear layout holds FP32 voxels only");
+    if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: U8 voxels need the brick scale table");
+    gbv_status st = fill_params(s, items[i]);
+    if (st != GBV_OK) return st;
+    RenderParams &p = items[i];
+    p.W = widths[i];
+    p.H = heights[i];
+    p.accum = reinterpret_cast<float4 *>(d_accums[i]);
+    p.maskWords = 0;
+    p.cdfYOff = p.pivOff = -1;
+    p.pivPerRow = 0;
+    starts[i + 1] = starts[i] + (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+  }
+  if (starts[count] >= (1ll << 31) - (1ll << 20))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: more tiles than the 32-bit tile counter holds");
+  gbv_batch *b = new gbv_batch();
+  b->count = count;
+  b->format = scenes[0].format;
+  b->layout = scenes[0].layout;
+  b->totalTiles = starts[count];
+  b->occ = 4;
+  b->threshold = 5;
+  b->skip = kSkipDefault;
+  cudaGetDevice(&b->device);
+  gbv_status st = check_cuda(cudaMalloc((void **)&b->d_items, sizeof(RenderParams) * count), "gbv_batch_create");
+  if (st == GBV_OK)
+    st = check_cuda(cudaMalloc((void **)&b->d_tileStart, sizeof(long long) * (count + 1)), "gbv_batch_create");
+  if (st == GBV_OK) st = check_cuda(cudaMalloc((void **)&b->d_pool, sizeof(int)), "gbv_batch_create");
+  if (st == GBV_OK)
+    st = check_cuda(cudaMemcpy(b->d_items, items.data(), sizeof(RenderParams) * count, cudaMemcpyHostToDevice),
+                    "gbv_batch_create: upload");
+  if (st == GBV_OK)
+    st = check_cuda(cudaMemcpy(b->d_tileStart, starts.data(), sizeof(long long) * (count + 1),
+                               cudaMemcpyHostToDevice),
+                    "gbv_batch_create: upload");
+  if (st != GBV_OK) {
+    gbv_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return GBV_OK;
+}
+
+extern "C" gbv_status gbv_batch_set_launch(gbv_batch *b, int blocks_per_sm, int threshold_pct, int skip_cells) {
+  if (!b || blocks_per_sm < 3 || blocks_per_sm > 4 || threshold_pct < 1 || threshold_pct > 100 || skip_cells < 1)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_set_launch: blocks 3..4, threshold 1..100, skip >= 1");
+  b->occ = blocks_per_sm;
+  b->threshold = threshold_pct;
+  b->skip = skip_cells;
+  return GBV_OK;
+}
+
+extern "C" gbv_status gbv_batch_render(gbv_batch *b, int accum_id_start, int spp, unsigned long long *d_counters,
+                                       void *stream) {
+  if (!b || spp < 0 || accum_id_start < 0) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_render: bad argument");
+  if (spp == 0) return GBV_OK;
+  RenderParams L;
+  memset(&L, 0, sizeof(L));
+  L.accumIdStart = accum_id_start;
+  L.spp = spp;
+  L.counters = d_counters;
+  L.skip = b->skip;
+  L.threshold = b->threshold;
+  L.maskWords = 0;
+  L.cdfYOff = L.pivOff = -1;
+  L.profile = 0;
+  cudaStream_t cs = (cudaStream_t)stream;
+  if (b->layout == GBV_LAYOUT_LINEAR) return batch_launch_linear(b, L, cs);
+  switch (b->format) {
+    case GBV_VOXEL_F32: return batch_launch_f32(b, L, cs);
+    case GBV_VOXEL_F16: return batch_launch_f16(b, L, cs);
+    case GBV_VOXEL_BF16: return batch_launch_bf16(b, L, cs);
+    case GBV_VOXEL_U8_SCALED: return batch_launch_u8(b, L, cs);
+  }
+  return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_render: unknown voxel format");
+}
+
+extern "C" gbv_status gbv_batch_destroy(gbv_batch *b) {
+  if (!b) return GBV_OK;
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->d_tileStart) cudaFree(b->d_tileStart);
+  if (b->d_pool) cudaFree(b->d_pool);
+  delete b;
+  return GBV_OK;
 }

@@ -227,7 +227,7 @@ def run_ours(args):
     frame(counters)  # counts of one frame (the frame is deterministic)
     torch.cuda.synchronize()
     cnt = counters.cpu().tolist()
-    samples, mcs, rays, caps = cnt
+    samples, mcs, rays, caps = cnt[:4]
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()

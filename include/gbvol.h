@@ -195,6 +195,27 @@ gbv_status gbv_render_noalloc(const gbv_scene *scene, float *d_accum, int width,
                               int height, int accum_id_start, int spp,
                               unsigned long long *d_counters, void *stream);
 
+/* Batched rendering: many independent scenes of uneven sizes (each with its
+   own field, TF, camera, lights and frame) rendered by one persistent launch
+   whose warps take 8x4-pixel tiles from all items.  No counterpart in the
+   reference (which renders one model per bnRender).
+   gbv_batch_create uploads the items' parameters (allocates and copies; call
+   it outside stream capture); gbv_batch_render is one memset and one kernel
+   launch on `stream`, so a capture of it replays as a CUDA graph;
+   gbv_batch_set_launch sets the launch shape (resident 256-thread blocks per
+   SM, 3 or 4; traversal threshold %; empty macrocells per traversal step),
+   which changes speed, never results.  Items must share the voxel format and
+   layout; each item's frame accumulates exactly as gbv_render would. */
+typedef struct gbv_batch gbv_batch;
+gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_accums,
+                            const int *widths, const int *heights, int count,
+                            gbv_batch **out);
+gbv_status gbv_batch_set_launch(gbv_batch *batch, int blocks_per_sm,
+                                int threshold_pct, int skip_cells);
+gbv_status gbv_batch_render(gbv_batch *batch, int accum_id_start, int spp,
+                            unsigned long long *d_counters, void *stream);
+gbv_status gbv_batch_destroy(gbv_batch *batch);
+
 /* Frame-buffer read: d_accum * (1/accum_id) into d_out as float4, RGBA8 or
    sRGB RGBA8.  Replaces linearizeColorAndNormalKernel
    (barney/fb/TiledFB.cu:13-50) with LocalFB::gatherColorChannel's
