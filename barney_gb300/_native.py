@@ -11,6 +11,7 @@ from pathlib import Path
 _LIB = Path(__file__).resolve().parent / "_lib" / "libbarney_gb300.so"
 
 GBV_OK = 0
+GBV_ERROR_INVALID_ARGUMENT, GBV_ERROR_CUDA, GBV_ERROR_OUT_OF_MEMORY, GBV_ERROR_LIMIT, GBV_ERROR_UNSUPPORTED = 1, 2, 3, 4, 5
 GBV_VOXEL_F32, GBV_VOXEL_F16, GBV_VOXEL_BF16, GBV_VOXEL_U8_SCALED = 0, 1, 2, 3
 GBV_LAYOUT_LINEAR, GBV_LAYOUT_BRICK_CORNERS = 0, 1
 GBV_FB_FLOAT4, GBV_FB_RGBA8, GBV_FB_RGBA8_SRGB = 0, 1, 2
@@ -37,6 +38,7 @@ class GbvScene(C.Structure):
         ("env_scale", C.c_float),
         ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
+        ("brick_log2", _i3),
     ]
 
 
@@ -66,6 +68,9 @@ def lib() -> C.CDLL:
             "gbv_map_majorants": (st, [vp, i, vp, i, f, f, f, vp, vp]),
             "gbv_brick_store_bytes": (st, [ip, i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
             "gbv_build_brick_store": (st, [vp, ip, i, vp, vp, vp]),
+            "gbv_brick_store_bytes_shaped": (st, [ip, i, ip, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+            "gbv_build_brick_store_shaped": (st, [vp, ip, i, ip, vp, vp, vp]),
+            "gbv_build_mc_ranges_from_store_shaped": (st, [vp, vp, i, ip, ip, i, vp, vp]),
             "gbv_env_build_cdfs": (st, [vp, i, i, ip, vp, vp, vp]),
             "gbv_render": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
             "gbv_render_noalloc": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),

@@ -14,8 +14,11 @@ from .device import GpuScene, _ptr, _stream
 
 
 class GpuBatch:
-    def __init__(self, scenes, fmt: int = N.GBV_VOXEL_F32, layout: int = N.GBV_LAYOUT_BRICK_CORNERS):
-        self.items = [GpuScene(s, layout=layout, fmt=fmt) for s in scenes]
+    def __init__(self, scenes, fmt: int = N.GBV_VOXEL_F32, layout: int = N.GBV_LAYOUT_BRICK_CORNERS,
+                 brick=(3, 3, 3)):
+        self.scenes = list(scenes)
+        self.fmt, self.layout, self.brick = fmt, layout, tuple(brick)
+        self.items = [GpuScene(s, layout=layout, fmt=fmt, brick=brick) for s in self.scenes]
         self.accums = [g.new_accum() for g in self.items]
         n = len(self.items)
         recs = (N.GbvScene * n)(*[g.record() for g in self.items])

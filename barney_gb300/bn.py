@@ -127,7 +127,7 @@ class BarneySession:
         self.close()
 
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
-                    layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4):
+                    layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None):
         L, ctx, s = self.L, self.ctx, scene
         nx, ny, nz = s.dims
         td = _ok(L.bnTextureData3DCreate(ctx, 0, BN_FLOAT32, nx, ny, nz, C.c_void_p(scalars_ptr)),
@@ -141,6 +141,8 @@ class BarneySession:
         L.bnSet1i(sf, b"cellsPerMacrocell", s.cells_per_mc)
         L.bnSet1i(sf, b"voxelFormat", voxel_format)
         L.bnSet1i(sf, b"voxelLayout", layout)
+        if brick is not None:
+            L.bnSet3i(sf, b"brickLog2", *brick)
         L.bnCommit(sf)
         vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
         tf = np.ascontiguousarray(s.tf, np.float32)

@@ -140,6 +140,7 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
   int cellsPerMC = 8;
   int voxelFormat = GBV_VOXEL_F32;
   int layout = GBV_LAYOUT_BRICK_CORNERS;
+  int brickLog2[3] = {3, 3, 3};
   // built state
   bool built = false;
   int mcDims[3] = {0, 0, 0};
@@ -149,6 +150,11 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
   bool set3i(const std::string &m, int x, int y, int z) override {
     if (m == "dims") {
       dims[0] = x; dims[1] = y; dims[2] = z;
+      built = false;
+      return true;
+    }
+    if (m == "brickLog2") {  // brick shape of the brick-corner store (this library's knob)
+      brickLog2[0] = x; brickLog2[1] = y; brickLog2[2] = z;
       built = false;
       return true;
     }
@@ -186,11 +192,14 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
     if (!ranges.alloc(2 * std::max<size_t>(nmc, 1))) return false;
     if (layout == GBV_LAYOUT_BRICK_CORNERS) {
       size_t vb = 0, sb = 0;
-      if (gbv_brick_store_bytes(dims, voxelFormat, &vb, &sb) != GBV_OK) { fail(gbv_last_error()); return false; }
+      if (gbv_brick_store_bytes_shaped(dims, voxelFormat, brickLog2, &vb, &sb) != GBV_OK) {
+        fail(gbv_last_error());
+        return false;
+      }
       if (!bricks.alloc(vb)) return false;
       if (sb && !scaleOffset.alloc(sb / sizeof(float))) return false;
-      if (gbv_build_brick_store(td->scalars.p, dims, voxelFormat, bricks.p, sb ? scaleOffset.p : nullptr, s) !=
-          GBV_OK) {
+      if (gbv_build_brick_store_shaped(td->scalars.p, dims, voxelFormat, brickLog2, bricks.p,
+                                       sb ? scaleOffset.p : nullptr, s) != GBV_OK) {
         fail(gbv_last_error());
         return false;
       }
@@ -201,8 +210,8 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
     // quantized stores: the ranges must bound the stored (rounded) values
     gbv_status rs = voxelFormat == GBV_VOXEL_F32
                         ? gbv_build_mc_ranges(td->scalars.p, dims, cellsPerMC, ranges.p, s)
-                        : gbv_build_mc_ranges_from_store(bricks.p, scaleOffset.p, voxelFormat, dims, cellsPerMC,
-                                                         ranges.p, s);
+                        : gbv_build_mc_ranges_from_store_shaped(bricks.p, scaleOffset.p, voxelFormat, dims,
+                                                                brickLog2, cellsPerMC, ranges.p, s);
     if (rs != GBV_OK) {
       fail(gbv_last_error());
       return false;
@@ -783,6 +792,7 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   s.d_voxels = sf.layout == GBV_LAYOUT_BRICK_CORNERS ? (const void *)sf.bricks.p : (const void *)sf.td->scalars.p;
   s.d_scale_offset = sf.scaleOffset.p;
   for (int a = 0; a < 3; a++) {
+    s.brick_log2[a] = sf.brickLog2[a];
     s.dims[a] = sf.dims[a];
     s.origin[a] = sf.origin[a];
     s.spacing[a] = sf.spacing[a];

@@ -8,8 +8,9 @@
 
 namespace gbv {
 
-constexpr int kBrick = 8;          // cells per brick edge
-constexpr int kBrickCells = 512;   // 8^3
+// U8 stores keep one (scale, offset) pair per 8^3 cells ("scale brick"),
+// whatever the brick shape of the layout.
+constexpr int kScaleBrickLog2 = 3;
 
 // Field geometry shared by every voxel store (StructuredData: numScalars,
 // numCells = dims-1, gridOrigin, rcp(gridSpacing); StructuredData.cu:127-180).
@@ -45,21 +46,59 @@ struct StoreLinearF32 {
   static constexpr bool kCellStore = false;
 };
 
-// 8^3-cell bricks, each cell holding its 8 corner voxels contiguously: one
-// stencil is one aligned vector load (32 B FP32, 16 B FP16/BF16, 8 B U8).
+// Index constants of a brick-corner store: bricks of 2^lx x 2^ly x 2^lz
+// cells, x-fastest; cells within a brick x-fastest.  Kept precomputed (masks
+// and shift sums) so that kernels read them as constants.
+struct BrickGeom {
+  int nbx, nby;      // bricks along x and y
+  int lx, ly, lz;    // log2 of the brick edge in cells
+  int lxy, lxyz;     // lx + ly, lx + ly + lz
+  int mx, my, mz;    // (1 << l) - 1 per axis
+  int nsx, nsy;      // U8: 8^3-cell scale bricks along x and y
+};
+// dims: voxels per axis; l: log2 brick edges (validated by the caller)
+__host__ __device__ inline BrickGeom make_brick_geom(const int dims[3], const int l[3]) {
+  BrickGeom g;
+  int nb[3], ns[3];
+  for (int i = 0; i < 3; i++) {
+    const int cells = dims[i] - 1;
+    nb[i] = cells <= 0 ? 0 : (cells + (1 << l[i]) - 1) >> l[i];
+    ns[i] = cells <= 0 ? 0 : (cells + (1 << kScaleBrickLog2) - 1) >> kScaleBrickLog2;
+  }
+  g.nbx = nb[0];
+  g.nby = nb[1];
+  g.lx = l[0];
+  g.ly = l[1];
+  g.lz = l[2];
+  g.lxy = l[0] + l[1];
+  g.lxyz = l[0] + l[1] + l[2];
+  g.mx = (1 << l[0]) - 1;
+  g.my = (1 << l[1]) - 1;
+  g.mz = (1 << l[2]) - 1;
+  g.nsx = ns[0];
+  g.nsy = ns[1];
+  return g;
+}
+
+// Each cell of a brick holds its 8 corner voxels contiguously: one stencil
+// is one aligned vector load (32 B FP32, 16 B FP16/BF16, 8 B U8).
 template <int FMT> struct StoreBrickCorners {
   const void *v;
-  const float2 *so;  // U8: (scale, offset) per brick
-  int nbx, nby;
+  const float2 *so;  // U8: (scale, offset) per 8^3-cell scale brick
+  BrickGeom g;
   static constexpr bool kCellStore = true;
-  __device__ __forceinline__ size_t cell_index(int cx, int cy, int cz, size_t &brick) const {
-    brick = (size_t)(cx >> 3) + (size_t)nbx * ((size_t)(cy >> 3) + (size_t)nby * (size_t)(cz >> 3));
-    int local = (cx & 7) + 8 * ((cy & 7) + 8 * (cz & 7));
-    return brick * kBrickCells + (size_t)local;
+  __device__ __forceinline__ size_t cell_index(int cx, int cy, int cz) const {
+    const size_t brick =
+        (size_t)(cx >> g.lx) + (size_t)g.nbx * ((size_t)(cy >> g.ly) + (size_t)g.nby * (size_t)(cz >> g.lz));
+    const int local = (cx & g.mx) | ((cy & g.my) << g.lx) | ((cz & g.mz) << g.lxy);
+    return (brick << g.lxyz) | (size_t)local;
+  }
+  __device__ __forceinline__ size_t scale_index(int cx, int cy, int cz) const {
+    return (size_t)(cx >> kScaleBrickLog2) +
+           (size_t)g.nsx * ((size_t)(cy >> kScaleBrickLog2) + (size_t)g.nsy * (size_t)(cz >> kScaleBrickLog2));
   }
   __device__ __forceinline__ void cell(int cx, int cy, int cz, float c[8]) const {
-    size_t brick;
-    size_t idx = cell_index(cx, cy, cz, brick);
+    const size_t idx = cell_index(cx, cy, cz);
     if (FMT == GBV_VOXEL_F32) {
       const float4 *p = reinterpret_cast<const float4 *>(v) + 2 * idx;
       float4 a = __ldg(p), b = __ldg(p + 1);
@@ -83,7 +122,7 @@ template <int FMT> struct StoreBrickCorners {
       }
     } else {  // U8_SCALED
       uint2 q = __ldg(reinterpret_cast<const uint2 *>(v) + idx);
-      float2 s = __ldg(so + brick);
+      float2 s = __ldg(so + scale_index(cx, cy, cz));
       uint32_t w[2] = {q.x, q.y};
 #pragma unroll
       for (int k = 0; k < 8; k++) {

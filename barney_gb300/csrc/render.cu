@@ -61,10 +61,10 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   p.vox = s->d_voxels;
   p.so = reinterpret_cast<const float2 *>(s->d_scale_offset);
   {
-    int nb[3];
-    brick_counts(s->dims, nb);
-    p.nbx = nb[0];
-    p.nby = nb[1];
+    int l[3];
+    if (!resolve_brick_shape(s->brick_log2, l))
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "brick_log2: each 1..6 (0 = 3), sum at most 15");
+    p.brick = make_brick_geom(s->dims, l);
   }
   commit_camera(s->cam_pos, s->cam_dir, s->cam_up, s->fovy, p.lens00, p.dir00, p.du, p.dv);
   p.numDir = s->num_dir_lights < 0 ? 0 : (s->num_dir_lights > 4 ? 4 : s->num_dir_lights);

@@ -62,7 +62,7 @@ struct RenderParams {
   // voxel store of this scene (see make_store)
   const void *vox;
   const float2 *so;
-  int nbx, nby;
+  BrickGeom brick;
   vec3 rcpMc;     // 1 / macrocell spacing
 };
 
@@ -73,7 +73,7 @@ template <> __device__ __forceinline__ StoreLinearF32 make_store<StoreLinearF32>
 #define GBV_BRICK_STORE(FMT)                                                                         \
   template <> __device__ __forceinline__ StoreBrickCorners<FMT> make_store<StoreBrickCorners<FMT>>(  \
       const RenderParams &p) {                                                                       \
-    return StoreBrickCorners<FMT>{p.vox, p.so, p.nbx, p.nby};                                        \
+    return StoreBrickCorners<FMT>{p.vox, p.so, p.brick};                                             \
   }
 GBV_BRICK_STORE(GBV_VOXEL_F32)
 GBV_BRICK_STORE(GBV_VOXEL_F16)

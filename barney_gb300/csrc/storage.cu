@@ -9,18 +9,23 @@ __global__ void mc_ranges_kernel(const float *__restrict__ scalars, int nx, int 
                                  int my_, int mz_, float2 *__restrict__ ranges);
 
 // One thread per cell of the padded brick grid, in store order, so each
-// thread writes one contiguous 8-voxel record.
+// thread writes one contiguous 8-voxel record.  Bricks have 2^lx x 2^ly x
+// 2^lz cells; U8 quantizes with the (min, max) of the cell's 8^3 scale brick
+// (lohi: nsx x nsy x ... scale bricks).
 template <int FMT>
-__global__ void brick_store_kernel(const float *__restrict__ s, int nx, int ny, int nz, int nbx, int nby,
-                                   long long numCells, const float2 *__restrict__ lohi, void *__restrict__ out) {
+__global__ void brick_store_kernel(const float *__restrict__ s, int nx, int ny, int nz, int nbx, int nby, int lx,
+                                   int ly, int lz, int nsx, int nsy, long long numCells,
+                                   const float2 *__restrict__ lohi, void *__restrict__ out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= numCells) return;
-  const long long brick = t >> 9;
-  const int local = (int)(t & 511);
+  const long long brick = t >> (lx + ly + lz);
+  const int local = (int)(t & ((1ll << (lx + ly + lz)) - 1));
   const int bx = (int)(brick % nbx), by = (int)((brick / nbx) % nby), bz = (int)(brick / ((long long)nbx * nby));
-  const int cx = bx * 8 + (local & 7), cy = by * 8 + ((local >> 3) & 7), cz = bz * 8 + (local >> 6);
+  const int cx = (bx << lx) | (local & ((1 << lx) - 1)), cy = (by << ly) | ((local >> lx) & ((1 << ly) - 1)),
+            cz = (bz << lz) | (local >> (lx + ly));
+  const bool inside = cx < nx - 1 && cy < ny - 1 && cz < nz - 1;
   float c[8];
-  if (cx < nx - 1 && cy < ny - 1 && cz < nz - 1) {
+  if (inside) {
     const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
     const size_t b = (size_t)cx + sy * cy + sz * cz;
     c[0] = s[b];
@@ -54,16 +59,20 @@ __global__ void brick_store_kernel(const float *__restrict__ s, int nx, int ny, 
              ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(c[2 * k + 1])) << 16);
     reinterpret_cast<uint4 *>(out)[t] = make_uint4(w[0], w[1], w[2], w[3]);
   } else {
-    // u8 = round(255 (v - min_b) / (max_b - min_b)) over the brick's 9^3 voxels
-    const float2 r = lohi[brick];
-    const float span = r.y - r.x;
+    // u8 = round(255 (v - min_b) / (max_b - min_b)) over the scale brick's
+    // 9^3 voxels; padding cells (never sampled) store 0
     uint32_t w[2] = {0u, 0u};
+    if (inside) {
+      const float2 r = lohi[(size_t)(cx >> kScaleBrickLog2) +
+                            (size_t)nsx * ((size_t)(cy >> kScaleBrickLog2) + (size_t)nsy * (cz >> kScaleBrickLog2))];
+      const float span = r.y - r.x;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      int q = 0;
-      if (span > 0.f) q = (int)floorf((c[k] - r.x) * (255.f / span) + .5f);
-      q = min(255, max(0, q));
-      w[k >> 2] |= (uint32_t)q << (8 * (k & 3));
+      for (int k = 0; k < 8; k++) {
+        int q = 0;
+        if (span > 0.f) q = (int)floorf((c[k] - r.x) * (255.f / span) + .5f);
+        q = min(255, max(0, q));
+        w[k >> 2] |= (uint32_t)q << (8 * (k & 3));
+      }
     }
     reinterpret_cast<uint2 *>(out)[t] = make_uint2(w[0], w[1]);
   }
@@ -178,12 +187,16 @@ using namespace gbv;
 
 extern "C" {
 
-gbv_status gbv_brick_store_bytes(const int dims[3], int format, size_t *voxel_bytes, size_t *scale_offset_bytes) {
+gbv_status gbv_brick_store_bytes_shaped(const int dims[3], int format, const int brick_log2[3], size_t *voxel_bytes,
+                                        size_t *scale_offset_bytes) {
   if (!dims || !voxel_bytes) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_brick_store_bytes: null pointer");
-  int nb[3];
-  brick_counts(dims, nb);
-  size_t bricks = (size_t)nb[0] * nb[1] * nb[2];
-  size_t cells = bricks * kBrickCells;
+  int l[3];
+  if (!resolve_brick_shape(brick_log2, l))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "brick_log2: each 1..6 (0 = 3), sum at most 15");
+  int nb[3], ns[3];
+  brick_counts(dims, nb, l);
+  brick_counts(dims, ns);
+  const size_t cells = ((size_t)nb[0] * nb[1] * nb[2]) << (l[0] + l[1] + l[2]);
   size_t elem = 0;
   switch (format) {
     case GBV_VOXEL_F32: elem = 4; break;
@@ -193,54 +206,66 @@ gbv_status gbv_brick_store_bytes(const int dims[3], int format, size_t *voxel_by
     default: return set_error(GBV_ERROR_UNSUPPORTED, "gbv_brick_store_bytes: unknown format");
   }
   *voxel_bytes = cells * 8 * elem;
-  if (scale_offset_bytes) *scale_offset_bytes = format == GBV_VOXEL_U8_SCALED ? bricks * 2 * sizeof(float) : 0;
+  if (scale_offset_bytes)
+    *scale_offset_bytes = format == GBV_VOXEL_U8_SCALED ? (size_t)ns[0] * ns[1] * ns[2] * 2 * sizeof(float) : 0;
   return GBV_OK;
 }
 
-gbv_status gbv_build_brick_store(const float *d_scalars, const int dims[3], int format, void *d_voxels,
-                                 float *d_scale_offset, void *stream) {
+gbv_status gbv_brick_store_bytes(const int dims[3], int format, size_t *voxel_bytes, size_t *scale_offset_bytes) {
+  return gbv_brick_store_bytes_shaped(dims, format, nullptr, voxel_bytes, scale_offset_bytes);
+}
+
+gbv_status gbv_build_brick_store_shaped(const float *d_scalars, const int dims[3], int format, const int brick_log2[3],
+                                        void *d_voxels, float *d_scale_offset, void *stream) {
   if (!d_scalars || !dims || !d_voxels) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: null");
   if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: a volume needs at least 2 voxels per axis");
   if (format == GBV_VOXEL_U8_SCALED && !d_scale_offset)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_brick_store: U8 needs the scale/offset table");
-  int nb[3];
-  brick_counts(dims, nb);
-  long long bricks = (long long)nb[0] * nb[1] * nb[2];
-  long long cells = bricks * kBrickCells;
+  int l[3];
+  if (!resolve_brick_shape(brick_log2, l))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "brick_log2: each 1..6 (0 = 3), sum at most 15");
+  int nb[3], ns[3];
+  brick_counts(dims, nb, l);
+  brick_counts(dims, ns);
+  const long long cells = ((long long)nb[0] * nb[1] * nb[2]) << (l[0] + l[1] + l[2]);
+  const long long scaleBricks = (long long)ns[0] * ns[1] * ns[2];
   cudaStream_t cs = (cudaStream_t)stream;
   unsigned blocks = (unsigned)((cells + 255) / 256);
   float2 *lohi = reinterpret_cast<float2 *>(d_scale_offset);
+#define GBV_STORE_ARGS dims[0], dims[1], dims[2], nb[0], nb[1], l[0], l[1], l[2], ns[0], ns[1], cells
   switch (format) {
     case GBV_VOXEL_F32:
-      brick_store_kernel<GBV_VOXEL_F32><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0], nb[1],
-                                                                cells, nullptr, d_voxels);
+      brick_store_kernel<GBV_VOXEL_F32><<<blocks, 256, 0, cs>>>(d_scalars, GBV_STORE_ARGS, nullptr, d_voxels);
       break;
     case GBV_VOXEL_F16:
-      brick_store_kernel<GBV_VOXEL_F16><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0], nb[1],
-                                                                cells, nullptr, d_voxels);
+      brick_store_kernel<GBV_VOXEL_F16><<<blocks, 256, 0, cs>>>(d_scalars, GBV_STORE_ARGS, nullptr, d_voxels);
       break;
     case GBV_VOXEL_BF16:
-      brick_store_kernel<GBV_VOXEL_BF16><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0],
-                                                                 nb[1], cells, nullptr, d_voxels);
+      brick_store_kernel<GBV_VOXEL_BF16><<<blocks, 256, 0, cs>>>(d_scalars, GBV_STORE_ARGS, nullptr, d_voxels);
       break;
     case GBV_VOXEL_U8_SCALED: {
-      // brick (min,max) over 9^3 voxels = the 8-cell macrocell range
-      mc_ranges_kernel<<<(unsigned)((bricks + 7) / 8), 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], 8, nb[0],
-                                                                     nb[1], nb[2], lohi);
+      // scale brick (min,max) over 9^3 voxels = the 8-cell macrocell range
+      mc_ranges_kernel<<<(unsigned)((scaleBricks + 7) / 8), 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], 8,
+                                                                          ns[0], ns[1], ns[2], lohi);
       gbv_status st = check_launch("brick ranges");
       if (st != GBV_OK) return st;
-      brick_store_kernel<GBV_VOXEL_U8_SCALED><<<blocks, 256, 0, cs>>>(d_scalars, dims[0], dims[1], dims[2], nb[0],
-                                                                       nb[1], cells, lohi, d_voxels);
+      brick_store_kernel<GBV_VOXEL_U8_SCALED><<<blocks, 256, 0, cs>>>(d_scalars, GBV_STORE_ARGS, lohi, d_voxels);
       st = check_launch("brick_store_kernel");
       if (st != GBV_OK) return st;
-      lohi_to_scale_offset<<<(unsigned)((bricks + 255) / 256), 256, 0, cs>>>(lohi, bricks);
+      lohi_to_scale_offset<<<(unsigned)((scaleBricks + 255) / 256), 256, 0, cs>>>(lohi, scaleBricks);
       break;
     }
     default:
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_build_brick_store: unknown format");
   }
+#undef GBV_STORE_ARGS
   return check_launch("brick_store_kernel");
+}
+
+gbv_status gbv_build_brick_store(const float *d_scalars, const int dims[3], int format, void *d_voxels,
+                                 float *d_scale_offset, void *stream) {
+  return gbv_build_brick_store_shaped(d_scalars, dims, format, nullptr, d_voxels, d_scale_offset, stream);
 }
 
 gbv_status gbv_env_build_cdfs(const float *d_texels, int width, int height, const int addr[2], float *d_cdf_y,
@@ -300,47 +325,44 @@ __global__ void __launch_bounds__(256) mc_ranges_store_kernel(StoreBrickCorners<
 
 }  // namespace gbv
 
-extern "C" gbv_status gbv_build_mc_ranges_from_store(const void *d_voxels, const float *d_scale_offset, int format,
-                                                     const int dims[3], int cells_per_mc, float *d_ranges,
-                                                     void *stream) {
+extern "C" gbv_status gbv_build_mc_ranges_from_store_shaped(const void *d_voxels, const float *d_scale_offset,
+                                                            int format, const int dims[3], const int brick_log2[3],
+                                                            int cells_per_mc, float *d_ranges, void *stream) {
   int M[3];
   gbv_status st = gbv_mc_dims(dims, cells_per_mc, M);
   if (st != GBV_OK) return st;
   if (!d_voxels || !d_ranges) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_mc_ranges_from_store: null");
   if (format == GBV_VOXEL_U8_SCALED && !d_scale_offset)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_build_mc_ranges_from_store: U8 needs the scale table");
+  int l[3];
+  if (!resolve_brick_shape(brick_log2, l))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "brick_log2: each 1..6 (0 = 3), sum at most 15");
   long long n = (long long)M[0] * M[1] * M[2];
   if (n == 0) return GBV_OK;
-  int nb[3];
-  brick_counts(dims, nb);
   unsigned blocks = (unsigned)((n + 7) / 8);
   cudaStream_t cs = (cudaStream_t)stream;
   float2 *r = reinterpret_cast<float2 *>(d_ranges);
   const int C0 = dims[0] - 1, C1 = dims[1] - 1, C2 = dims[2] - 1;
+  const float2 *so = reinterpret_cast<const float2 *>(d_scale_offset);
+#define GBV_RANGES(FMT)                                                                                        \
+  mc_ranges_store_kernel<FMT><<<blocks, 256, 0, cs>>>(                                                         \
+      StoreBrickCorners<FMT>{d_voxels, so, make_brick_geom(dims, l)}, C0, C1, C2, cells_per_mc,             \
+      M[0], M[1], M[2], r)
   switch (format) {
-    case GBV_VOXEL_F32:
-      mc_ranges_store_kernel<GBV_VOXEL_F32><<<blocks, 256, 0, cs>>>(
-          StoreBrickCorners<GBV_VOXEL_F32>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
-          M[2], r);
-      break;
-    case GBV_VOXEL_F16:
-      mc_ranges_store_kernel<GBV_VOXEL_F16><<<blocks, 256, 0, cs>>>(
-          StoreBrickCorners<GBV_VOXEL_F16>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
-          M[2], r);
-      break;
-    case GBV_VOXEL_BF16:
-      mc_ranges_store_kernel<GBV_VOXEL_BF16><<<blocks, 256, 0, cs>>>(
-          StoreBrickCorners<GBV_VOXEL_BF16>{d_voxels, nullptr, nb[0], nb[1]}, C0, C1, C2, cells_per_mc, M[0], M[1],
-          M[2], r);
-      break;
-    case GBV_VOXEL_U8_SCALED:
-      mc_ranges_store_kernel<GBV_VOXEL_U8_SCALED><<<blocks, 256, 0, cs>>>(
-          StoreBrickCorners<GBV_VOXEL_U8_SCALED>{d_voxels, reinterpret_cast<const float2 *>(d_scale_offset), nb[0],
-                                                 nb[1]},
-          C0, C1, C2, cells_per_mc, M[0], M[1], M[2], r);
-      break;
+    case GBV_VOXEL_F32: GBV_RANGES(GBV_VOXEL_F32); break;
+    case GBV_VOXEL_F16: GBV_RANGES(GBV_VOXEL_F16); break;
+    case GBV_VOXEL_BF16: GBV_RANGES(GBV_VOXEL_BF16); break;
+    case GBV_VOXEL_U8_SCALED: GBV_RANGES(GBV_VOXEL_U8_SCALED); break;
     default:
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_build_mc_ranges_from_store: unknown format");
   }
+#undef GBV_RANGES
   return check_launch("mc_ranges_store_kernel");
+}
+
+extern "C" gbv_status gbv_build_mc_ranges_from_store(const void *d_voxels, const float *d_scale_offset, int format,
+                                                     const int dims[3], int cells_per_mc, float *d_ranges,
+                                                     void *stream) {
+  return gbv_build_mc_ranges_from_store_shaped(d_voxels, d_scale_offset, format, dims, nullptr, cells_per_mc,
+                                               d_ranges, stream);
 }

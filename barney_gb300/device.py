@@ -34,13 +34,15 @@ class GpuScene:
 
     layout: GBV_LAYOUT_LINEAR (FP32 only) or GBV_LAYOUT_BRICK_CORNERS.
     fmt:    voxel format of the brick store.
+    brick:  log2 of the brick edge in cells per axis (default (3, 3, 3)).
     """
 
     def __init__(self, scene: Scene, layout: int = N.GBV_LAYOUT_BRICK_CORNERS, fmt: int = N.GBV_VOXEL_F32,
-                 scalars_device=None):
+                 scalars_device=None, brick=(3, 3, 3)):
         import torch
         self.s = scene
         self.layout, self.fmt = layout, fmt
+        self.brick = tuple(int(b) for b in brick)
         dev = torch.device("cuda")
         if scalars_device is not None:
             self.scalars = scalars_device
@@ -77,9 +79,10 @@ class GpuScene:
             N.check(L.gbv_build_mc_ranges(_ptr(self.scalars), N.ivec(*self.dims), s.cells_per_mc, _ptr(self.ranges),
                                           _stream()), "gbv_build_mc_ranges")
         else:  # quantized store: bound the stored values
-            N.check(L.gbv_build_mc_ranges_from_store(_ptr(self.voxels), _ptr(self.scale_offset), self.fmt,
-                                                     N.ivec(*self.dims), s.cells_per_mc, _ptr(self.ranges),
-                                                     _stream()), "gbv_build_mc_ranges_from_store")
+            N.check(L.gbv_build_mc_ranges_from_store_shaped(_ptr(self.voxels), _ptr(self.scale_offset), self.fmt,
+                                                            N.ivec(*self.dims), N.ivec(*self.brick), s.cells_per_mc,
+                                                            _ptr(self.ranges), _stream()),
+                    "gbv_build_mc_ranges_from_store_shaped")
         self.map_majorants()
 
     def map_majorants(self) -> None:
@@ -92,12 +95,14 @@ class GpuScene:
     def build_bricks(self, fmt: int) -> None:
         import torch
         vb, sb = C.c_size_t(), C.c_size_t()
-        N.check(N.lib().gbv_brick_store_bytes(N.ivec(*self.dims), fmt, C.byref(vb), C.byref(sb)), "bytes")
+        N.check(N.lib().gbv_brick_store_bytes_shaped(N.ivec(*self.dims), fmt, N.ivec(*self.brick), C.byref(vb),
+                                                     C.byref(sb)), "gbv_brick_store_bytes_shaped")
         # 32-byte aligned storage (torch allocations are 512-byte aligned)
         self.voxels = torch.empty(max(vb.value, 32), dtype=torch.uint8, device="cuda")
         self.scale_offset = torch.empty(max(sb.value, 8), dtype=torch.uint8, device="cuda") if sb.value else None
-        N.check(N.lib().gbv_build_brick_store(_ptr(self.scalars), N.ivec(*self.dims), fmt, _ptr(self.voxels),
-                                              _ptr(self.scale_offset), _stream()), "gbv_build_brick_store")
+        N.check(N.lib().gbv_build_brick_store_shaped(_ptr(self.scalars), N.ivec(*self.dims), fmt,
+                                                     N.ivec(*self.brick), _ptr(self.voxels), _ptr(self.scale_offset),
+                                                     _stream()), "gbv_build_brick_store_shaped")
         self.fmt = fmt
 
     # -- scene record ---------------------------------------------------------
@@ -108,6 +113,7 @@ class GpuScene:
         r.d_scale_offset = self.scale_offset.data_ptr() if self.scale_offset is not None else None
         r.format, r.layout = self.fmt, self.layout
         r.dims[:] = list(self.dims)
+        r.brick_log2[:] = list(self.brick)
         origin, spacing = s.geometry()
         r.origin[:] = list(origin)
         r.spacing[:] = list(spacing)

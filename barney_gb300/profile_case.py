@@ -3,9 +3,12 @@
   python -m barney_gb300.profile_case --dims 512 --width 480 --height 270 --spp 1 --format f32
 
 Builds the frame scene (512^3 volume by default), renders `--warmup` untimed
-launches, then `--launches` profiled launches of the render kernel, and
-writes the per-launch counters to gpurun_out/profile_case.json so that ncu
-DRAM bytes can be related to density samples.
+launches, then `--launches` launches of the render kernel as timed runs make
+them (no event counting), then one launch with event counting, and writes its
+counters to the --out JSON so that ncu DRAM bytes of the uncounted launches
+can be related to density samples (the frame is deterministic, so every
+launch processes the same samples).  To capture the uncounted launches:
+ncu -k regex:render_kernel -s <warmup> -c <launches>.
 """
 from __future__ import annotations
 
@@ -25,7 +28,7 @@ def main():
     ap.add_argument("--layout", default="brick", choices=["brick", "linear"])
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--launches", type=int, default=1)
-    ap.add_argument("--out", default="gpurun_out/profile_case.json")
+    ap.add_argument("--out", default="profile_case.json")
     a = ap.parse_args()
     import torch
     from . import _native as N, scenes
@@ -35,13 +38,12 @@ def main():
     layout = N.GBV_LAYOUT_BRICK_CORNERS if a.layout == "brick" else N.GBV_LAYOUT_LINEAR
     g = GpuScene(s, layout=layout, fmt=fmt)
     acc = g.new_accum()
-    for _ in range(a.warmup):
+    for _ in range(a.warmup + a.launches):
         g.render(accum=acc)
     cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
-    for _ in range(a.launches):
-        g.render(accum=acc, counters=cnt)
+    g.render(accum=acc, counters=cnt)
     torch.cuda.synchronize()
-    c = [int(x) // a.launches for x in cnt.cpu().tolist()]
+    c = [int(x) for x in cnt.cpu().tolist()]
     rec = dict(dims=a.dims, width=a.width, height=a.height, spp=a.spp, format=a.format, layout=a.layout,
                samples_per_launch=c[0], mc_visits_per_launch=c[1], rays_per_launch=c[2])
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)

@@ -35,6 +35,8 @@ METRIC = "Msamples/s & frame ms @512³ 1080p; fwd+adjoint ms/view; FP16 vs FP32 
 UNIT = "Msamples/s"
 BYTES_PER_VOXEL = {0: 4, 1: 2, 2: 2, 3: 1}
 FMT_NAME = {0: "f32", 1: "f16", 2: "bf16", 3: "u8"}
+WORKLOAD = ("512^3 blob+fBm volume, 256-entry two-peak TF, 16^3 macrocells, 1920x1080, 64 spp, "
+            "<=4 isotropic volume bounces, dir light + 512x256 env map")
 
 
 def dist_info():
@@ -110,32 +112,39 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, majorants, target_s=12.0, rows_center=None):
-    """The oracle (FP32 restatement of the reference's CPU backend) on all host
-    threads, on a band of rows of the frame at 1 spp."""
+def _full_frame_passes(o, scene, threads, first_accum_id, target_s, max_passes):
+    """Renders full 1-spp passes of the frame with the oracle (accumIDs
+    first_accum_id, first_accum_id+1, ...) until target_s seconds or
+    max_passes passes; returns (passes, density samples, seconds per pass)."""
+    acc = np.zeros((scene.height, scene.width, 4), np.float32)
+    times, samples = [], []
+    while len(times) < max_passes and (not times or sum(times) < target_s):
+        t0 = time.perf_counter()
+        o.render(spp=1, accum=acc, accum_id_start=first_accum_id + len(times), nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        samples.append(o.stats["density_samples"])
+    return samples, times
+
+
+def cpu_baseline(scene, majorants, target_s=10.0):
+    """The oracle (FP32 restatement of the reference's CPU backend, one
+    std::thread per host core) on full 1920x1080 frames at 1 spp (accumIDs
+    1, 2, ...; accumID 0 has no pixel jitter), repeated for about target_s."""
     import oracle
     o = oracle.Oracle(scene, majorants=majorants)
     threads = os.cpu_count() or 1
-    H = scene.height
-    c = rows_center if rows_center is not None else H // 2
-    # size the band: 2 rows first, then scale to ~target_s
-    acc = np.zeros((H, scene.width, 4), np.float32)
-    t0 = time.perf_counter()
-    o.render(spp=1, accum=acc, accum_id_start=0, nthreads=threads, rows=(c - 1, c + 1))
-    dt = max(time.perf_counter() - t0, 1e-3)
-    rows = int(min(H, max(2, 2 * target_s / dt)))
-    r0 = max(0, c - rows // 2)
-    r1 = min(H, r0 + rows)
-    t0 = time.perf_counter()
-    o.render(spp=1, accum=acc, accum_id_start=0, nthreads=threads, rows=(r0, r1))
-    dt = time.perf_counter() - t0
-    samples = o.stats["density_samples"]
-    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"rows {r0}-{r1} of the 1920x1080 frame at 1 spp ({(r1 - r0) * scene.width} paths, "
-                      f"{samples} density samples, {dt:.1f} s)"}
+    samples, times = _full_frame_passes(o, scene, threads, 1, target_s, 64)
+    value = sum(samples) / sum(times) / 1e6
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full {scene.width}x{scene.height} passes at 1 spp (accumID 1..{len(times)}), "
+                      f"{sum(samples)} density samples in {sum(times):.1f} s",
+            "frame_ms_extrapolated": 1e3 * sum(times) / len(times) * scene.spp}
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle's restatement of the embree
+    backend) on all host cores: one step = one full 1920x1080 pass at 1 spp
+    of the 64-spp frame (accumID 1 + step)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
@@ -144,25 +153,16 @@ def run_reference(args):
     scene = scenes.frame_scene(dims=args.dims)
     o = oracle.Oracle(scene)
     threads = os.cpu_count() or 1
-    H, W = scene.height, scene.width
-    rows = args.ref_rows
-    r0 = H // 2 - rows // 2
-    acc = np.zeros((H, W, 4), np.float32)
-    times, samples = [], []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        o.render(spp=1, accum=acc, accum_id_start=i, nthreads=threads, rows=(r0, r0 + rows))
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
-            samples.append(o.stats["density_samples"])
+    samples, times = _full_frame_passes(o, scene, threads, 1, float("inf"), args.warmup + args.steps)
+    samples, times = samples[args.warmup:], times[args.warmup:]
     value = sum(samples) / sum(times) / 1e6
-    sample = f"rows {r0}-{r0 + rows} of the 1920x1080 frame, 1 spp per step ({rows * W} paths)"
+    sample = (f"full {scene.width}x{scene.height} pass at 1 spp per step (accumID {1 + args.warmup}.."
+              f"{args.warmup + args.steps}), {sum(samples) // len(samples)} density samples per step")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": "512^3 volume, 1920x1080, 64 spp, <=4 bounces, env map",
-                                            "sample": sample},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": sample},
+            "frame_ms_extrapolated": 1e3 * sum(times) / len(times) * scene.spp,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -198,6 +198,57 @@ def ea_timing(dims=128, nviews=32, size=256, reps=3):
     f, b = min(fw) / nviews, min(fb) / nviews
     return {"views": nviews, "view_px": f"{size}x{size}", "grid": f"{dims}^3", "fwd_ms_per_view": f,
             "fwd_adjoint_ms_per_view": b, "ratio": b / f}
+
+
+def batch_timing(count=64, reps=3):
+    """The batched uneven workload: `count` volumes (sides log-uniform in
+    [32, 256] per axis), each with its own TF, camera and image size from
+    {128^2, 256^2, 512^2}, 8 spp; one persistent launch replayed from a CUDA
+    graph against one gbv_render launch per item on the same stream."""
+    import torch
+    from barney_gb300 import _native as N, scenes
+    from barney_gb300.batch import GpuBatch
+    from barney_gb300.autotune import tuned_batch
+    items = scenes.batch_items(count)
+    spp = items[0].spp
+    b, tuned = tuned_batch(items, spp)
+    cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    b.render(spp, counters=cnt)
+    torch.cuda.synchronize()
+    samples = int(cnt[0].item())
+    graph = b.capture(spp)
+    stream = torch.cuda.current_stream()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for _ in range(reps):
+        graph.replay()
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    batched = [a.clone() for a in b.accums]
+    for _ in range(2):
+        for g, a in zip(b.items, b.accums):
+            g.render(spp=spp, accum=a)
+    torch.cuda.synchronize()
+    e[2].record(stream)
+    for _ in range(reps):
+        for g, a in zip(b.items, b.accums):
+            g.render(spp=spp, accum=a)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    identical = all(torch.equal(x, y) for x, y in zip(batched, b.accums))
+    ms_b = e[0].elapsed_time(e[1]) / reps
+    ms_s = e[2].elapsed_time(e[3]) / reps
+    out = {"items": count, "spp": spp, "pixels": sum(s.width * s.height for s in items),
+           "voxels": int(sum(s.scalars.size for s in items)), "density_samples": samples,
+           "batch_graph_ms": ms_b, "separate_launches_ms": ms_s, "speedup": ms_s / ms_b,
+           "batch_Msamples_s": samples / (ms_b / 1e3) / 1e6, "images_identical": identical}
+    out["tuned"] = {"brick_log2": list(tuned["brick"]), "launch_blocks_threshold_skip": list(tuned["launch"]),
+                    "cached": tuned["cached"], "brick_ms": tuned.get("brick_ms")}
+    b.close()
+    return out
 
 
 def run_ours(args):
@@ -264,8 +315,7 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "512^3 blob+fBm volume, 256-entry two-peak TF, 16^3 macrocells, 1920x1080, "
-                                   "64 spp, <=4 isotropic volume bounces, dir light + 512x256 env map",
+            "config": {"workload": WORKLOAD,
                        "voxel_format": args.format, "voxel_layout": "8^3-cell brick corners",
                        "l2": "inputs larger than L2 (brick store %.1f GB)" % (g.voxels.numel() / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -310,6 +360,10 @@ def run_ours(args):
         except Exception as e:  # report, never hide
             line["fp16_vs_fp32"] = {"error": str(e)}
         try:
+            line["batch"] = batch_timing()
+        except Exception as e:
+            line["batch"] = {"error": str(e)}
+        try:
             line["ea_adjoint"] = ea_timing()
         except Exception as e:
             line["ea_adjoint"] = {"error": str(e)}
@@ -351,7 +405,6 @@ def main():
     ap.add_argument("--format", default="f32", choices=["f32", "f16", "bf16", "u8"])
     ap.add_argument("--dims", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--ref-rows", type=int, default=24)
     ap.add_argument("--quick", action="store_true", help="skip the FP16 and adjoint extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()

@@ -34,12 +34,12 @@ enum {
   GBV_VOXEL_F32 = 0,
   GBV_VOXEL_F16 = 1,
   GBV_VOXEL_BF16 = 2,
-  GBV_VOXEL_U8_SCALED = 3 /* uint8 with a float (scale, offset) per 8^3-cell brick */
+  GBV_VOXEL_U8_SCALED = 3 /* uint8 with a float (scale, offset) per 8^3 cells */
 };
 /* voxel layouts */
 enum {
   GBV_LAYOUT_LINEAR = 0,       /* x-fastest scalars, FP32 only (the reference's texel array) */
-  GBV_LAYOUT_BRICK_CORNERS = 1 /* 8^3-cell bricks; each cell stores its 8 corner voxels */
+  GBV_LAYOUT_BRICK_CORNERS = 1 /* bricks of cells (8^3 unless shaped); each cell stores its 8 corner voxels */
 };
 /* frame-buffer read formats (BNDataType subset) */
 enum { GBV_FB_FLOAT4 = 0, GBV_FB_RGBA8 = 1, GBV_FB_RGBA8_SRGB = 2 };
@@ -94,16 +94,40 @@ gbv_status gbv_map_majorants(const float *d_ranges, int num_mc,
  * ------------------------------------------------------------------------ */
 
 /* Bytes needed for the brick-corner store of a volume (voxels; for
-   GBV_VOXEL_U8_SCALED also *scale_offset_bytes for the brick table). */
+   GBV_VOXEL_U8_SCALED also *scale_offset_bytes for the scale table). */
 gbv_status gbv_brick_store_bytes(const int dims[3], int format,
                                  size_t *voxel_bytes, size_t *scale_offset_bytes);
 
-/* Re-lays an FP32 x-fastest volume as 8^3-cell bricks in `format`.
+/* Re-lays an FP32 x-fastest volume as 8^3-cell bricks in `format`; each
+   cell stores its 8 corner voxels (one vector load per trilinear sample).
+   U8: one float (scale, offset) per 8^3 cells, u8 = round(255 (v - min) /
+   (max - min)) over their 9^3 voxels.
    Replaces the texel upload of StructuredData::setObject("textureData")
    (barney/volume/StructuredData.cu:154-173, rtcore/cudaCommon/TextureData.cu:59-75). */
 gbv_status gbv_build_brick_store(const float *d_scalars, const int dims[3],
                                  int format, void *d_voxels,
                                  float *d_scale_offset, void *stream);
+
+/* The same with a chosen brick shape: brick_log2[i] = log2 of the brick
+   edge in cells along axis i, each 1..6 (0 or a null pointer: 3) and at most
+   15 in sum.  The shape changes only the order of cells in HBM (locality),
+   never a sampled value: U8 scales stay per 8^3 cells.  A scene rendering
+   such a store sets gbv_scene.brick_log2 to the same shape.  No counterpart
+   in the reference (its texels are a cudaArray or an x-fastest array). */
+gbv_status gbv_brick_store_bytes_shaped(const int dims[3], int format,
+                                        const int brick_log2[3],
+                                        size_t *voxel_bytes,
+                                        size_t *scale_offset_bytes);
+gbv_status gbv_build_brick_store_shaped(const float *d_scalars, const int dims[3],
+                                        int format, const int brick_log2[3],
+                                        void *d_voxels, float *d_scale_offset,
+                                        void *stream);
+gbv_status gbv_build_mc_ranges_from_store_shaped(const void *d_voxels,
+                                                 const float *d_scale_offset,
+                                                 int format, const int dims[3],
+                                                 const int brick_log2[3],
+                                                 int cells_per_mc, float *d_ranges,
+                                                 void *stream);
 
 /* ------------------------------------------------------------------------
  * Scene description for rendering (device pointers where marked d_).
@@ -146,6 +170,9 @@ typedef struct gbv_scene {
   int multi_scatter;             /* 0 default build (single scatter), 1 multi-scatter build */
   int volume_multi_scatter;
   int max_volume_bounces;
+  /* brick shape of a GBV_LAYOUT_BRICK_CORNERS store (as passed to
+     gbv_build_brick_store_shaped; {0,0,0} = 8^3 cells) */
+  int brick_log2[3];
 } gbv_scene;
 
 /* Counters written by gbv_render when d_counters != 0 (uint64 each):

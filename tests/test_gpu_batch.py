@@ -72,3 +72,25 @@ def test_batch_graph_replay(cuda):
     torch.cuda.synchronize()
     for a, r in zip(b.accums, ref):
         assert torch.equal(a, r)
+
+
+def test_autotuner_picks_shapes_caches_them_and_keeps_images(cuda, tmp_path, monkeypatch):
+    import torch
+    from barney_gb300 import autotune
+    monkeypatch.setenv("GBV_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    items = small_items()
+    ref = GpuBatch(items)
+    ref.render(spp=3)
+    bricks = [(3, 3, 3), (2, 2, 2), (4, 3, 2)]
+    launches = [(3, 5, 8), (4, 30, 4)]
+    b, rec = autotune.tuned_batch(items, 3, bricks=bricks, reps=1)
+    assert not rec["cached"] and rec["brick"] in bricks
+    assert (tmp_path / "tune.json").exists()
+    b.render(spp=3)
+    torch.cuda.synchronize()
+    for a, r in zip(b.accums, ref.accums):
+        assert torch.equal(a, r)
+    b2, rec2 = autotune.tuned_batch(items, 3, bricks=bricks, reps=1)
+    assert rec2["cached"] and rec2["brick"] == rec["brick"] and rec2["launch"] == rec["launch"]
+    got = autotune.tune_batch(b2, 3, candidates=launches, reps=1, use_cache=False)
+    assert got["launch"] in launches and len(got["timed"]) == 2

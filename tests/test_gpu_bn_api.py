@@ -43,12 +43,13 @@ def test_bn_fixed8_formats(cuda, fmt):
         assert d.max() <= (0 if fmt == bn.BN_UFIXED8_RGBA else 1)
 
 
-def test_bn_multi_scatter_env_matches_gbv_path(cuda):
+@pytest.mark.parametrize("brick", [None, (4, 4, 2)])
+def test_bn_multi_scatter_env_matches_gbv_path(cuda, brick):
     import torch
     s = scenes.frame_scene(dims=40, width=48, height=32, spp=4)
     s.env = scenes.env_sky(64, 32)
     with bn.BarneySession() as ses:
-        ses.build_scene(s, s.scalars.ctypes.data, voxel_format=N.GBV_VOXEL_F16)
+        ses.build_scene(s, s.scalars.ctypes.data, voxel_format=N.GBV_VOXEL_F16, brick=brick)
         ses.render()
         img = ses.read()
     g = GpuScene(s, fmt=N.GBV_VOXEL_F16)

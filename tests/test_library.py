@@ -99,3 +99,32 @@ def test_env_sky_map():
     assert e.texels.shape == (32, 64, 4)
     assert e.texels[..., :3].max() == 50.0  # the sun disk
     assert np.all(e.texels[..., 3] == 1.0)
+
+
+def test_brick_store_bytes_for_shapes():
+    L = N.lib()
+    vb, sb = C.c_size_t(), C.c_size_t()
+    # 99 x 59 x 32 cells in 16 x 8 x 4-cell bricks: 7 x 8 x 8 bricks of 512 cells
+    assert L.gbv_brick_store_bytes_shaped(N.ivec(100, 60, 33), N.GBV_VOXEL_F32, N.ivec(4, 3, 2), C.byref(vb),
+                                          C.byref(sb)) == N.GBV_OK
+    assert vb.value == 7 * 8 * 8 * 512 * 32 and sb.value == 0
+    # U8 keeps one (scale, offset) per 8^3 cells whatever the brick shape
+    assert L.gbv_brick_store_bytes_shaped(N.ivec(100, 60, 33), N.GBV_VOXEL_U8_SCALED, N.ivec(4, 3, 2), C.byref(vb),
+                                          C.byref(sb)) == N.GBV_OK
+    assert vb.value == 7 * 8 * 8 * 512 * 8 and sb.value == 13 * 8 * 4 * 8
+    # zeros and a null shape mean 8^3 bricks, as the unshaped call
+    ref = C.c_size_t()
+    assert L.gbv_brick_store_bytes(N.ivec(100, 60, 33), N.GBV_VOXEL_F16, C.byref(ref), None) == N.GBV_OK
+    assert L.gbv_brick_store_bytes_shaped(N.ivec(100, 60, 33), N.GBV_VOXEL_F16, N.ivec(0, 0, 0), C.byref(vb),
+                                          None) == N.GBV_OK
+    assert vb.value == ref.value == 13 * 8 * 4 * 512 * 16
+    assert L.gbv_brick_store_bytes_shaped(N.ivec(100, 60, 33), N.GBV_VOXEL_F16, None, C.byref(vb), None) == N.GBV_OK
+    assert vb.value == ref.value
+
+
+@pytest.mark.parametrize("shape", [(7, 3, 3), (-1, 3, 3), (6, 6, 6), (3, 3, 10)])
+def test_brick_shape_out_of_range_is_rejected(shape):
+    vb = C.c_size_t()
+    st = N.lib().gbv_brick_store_bytes_shaped(N.ivec(64, 64, 64), N.GBV_VOXEL_F32, N.ivec(*shape), C.byref(vb), None)
+    assert st == N.GBV_ERROR_INVALID_ARGUMENT
+    assert "brick_log2" in N.lib().gbv_last_error().decode()
