@@ -32,7 +32,11 @@ struct EAViewDev {
 };
 struct EAParams {
   FieldGeom F;
-  StoreLinearF32 store;
+  StoreLinearF32 store;  // linear FP32 field (the adjoint and FP64 modes read this)
+  // brick-corner field of the forward march (any format), see ea_store
+  const void *vox;
+  const float2 *so;
+  BrickGeom brick;
   XF xf;
   float dt;
   int numViews;
@@ -57,8 +61,24 @@ __device__ __forceinline__ bool ea_ray(const EAParams &p, const EAViewDev &v, in
   return true;
 }
 
-// FP32 forward
+template <class Store> __device__ __forceinline__ Store ea_store(const EAParams &p);
+template <> __device__ __forceinline__ StoreLinearF32 ea_store<StoreLinearF32>(const EAParams &p) { return p.store; }
+#define GBV_EA_BRICK_STORE(FMT)                                                                           \
+  template <> __device__ __forceinline__ StoreBrickCorners<FMT> ea_store<StoreBrickCorners<FMT>>(        \
+      const EAParams &p) {                                                                                \
+    return StoreBrickCorners<FMT>{p.vox, p.so, p.brick};                                                  \
+  }
+GBV_EA_BRICK_STORE(GBV_VOXEL_F32)
+GBV_EA_BRICK_STORE(GBV_VOXEL_F16)
+GBV_EA_BRICK_STORE(GBV_VOXEL_BF16)
+GBV_EA_BRICK_STORE(GBV_VOXEL_U8_SCALED)
+#undef GBV_EA_BRICK_STORE
+
+// FP32 forward; the voxels come from any store (a brick-corner FP32 store
+// samples the same values as the linear one)
+template <class Store>
 __global__ void __launch_bounds__(128) ea_forward_kernel(const EAParams p, float4 *__restrict__ out) {
+  const Store store = ea_store<Store>(p);
   const EAViewDev &v = p.views[blockIdx.z];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ix = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -74,7 +94,7 @@ __global__ void __launch_bounds__(128) ea_forward_kernel(const EAParams p, float
       const float t = t0 + ((float)i + .5f) * p.dt;
       if (t >= t1) break;
       const vec3 P = org + t * dir;
-      const vec4 m = sample_and_map(p.F, p.store, p.xf, P);
+      const vec4 m = sample_and_map(p.F, store, p.xf, P);
       const float x = m.w * p.dt;
       const float T = expf(-(tau + comp));
       const float alpha = -expm1f(-x);
@@ -189,9 +209,10 @@ __global__ void __launch_bounds__(128) ea_forward_f64_kernel(const EAParams p, d
 // Lanes that flush in the same step and hold the same key are grouped with
 // __match_any_sync; the group's lowest lane gathers the others' sums by
 // shuffles and issues the 8 atomics once.  Called by all 32 lanes.
-template <bool Shared>
-__device__ __forceinline__ void flush8(float *__restrict__ dst, bool flush, unsigned long long key,
-                                       const size_t off[8], const float v[8]) {
+// off(k) gives the destination index of sum k (evaluated by the leader only).
+template <class Off>
+__device__ __forceinline__ void flush8(float *__restrict__ dst, bool flush, unsigned long long key, Off off,
+                                       const float v[8]) {
   const int lane = threadIdx.x & 31;
   const unsigned fm = __ballot_sync(0xffffffffu, flush);
   if (!flush) return;
@@ -215,7 +236,7 @@ __device__ __forceinline__ void flush8(float *__restrict__ dst, bool flush, unsi
   if (lane == leader) {
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      if (acc[k] != 0.f) atomicAdd(dst + off[k], acc[k]);
+      if (acc[k] != 0.f) atomicAdd(dst + off(k), acc[k]);
   }
 }
 
@@ -223,7 +244,8 @@ __device__ __forceinline__ void flush8(float *__restrict__ dst, bool flush, unsi
 // the same cell and TF segment, so each lane keeps running sums for its
 // current stencil and TF segment and flushes them (warp-aggregated) only
 // when either changes.  Lanes run in lockstep up to the warp's longest march
-// so the flushes see all 32 lanes.
+// (one extra iteration without steps flushes the last sums) so the flushes
+// see all 32 lanes.
 template <int MinBlocks>
 __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAParams p, const float4 *__restrict__ img,
                                                           const float4 *__restrict__ gimg, float *__restrict__ gvox,
@@ -261,24 +283,20 @@ __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAPar
   // absolute precision): one transcendental per step
   float T = 1.f;
   bool alive = inside && n > 0;
-  // running sums: voxel stencil (key = base voxel) and TF segment (key = idx)
+  // running sums: voxel stencil (key = 8 * base voxel + which axes are not
+  // clamped) and TF segment (key = idx)
   long long vKey = -1;
-  size_t vOff[8];
   float vAcc[8];
   int tIdx = -1;
   float tAcc[8];
 #pragma unroll
-  for (int k = 0; k < 8; k++) { vAcc[k] = 0.f; tAcc[k] = 0.f; vOff[k] = 0; }
+  for (int k = 0; k < 8; k++) { vAcc[k] = 0.f; tAcc[k] = 0.f; }
   for (int i = 0; i <= nMax; i++) {
     // this step's contributions (none past the end of the lane's march)
     bool have = false;
     long long key = -1;
-    size_t off[8];
-    float contrib[8];
     int idx = -1;
-    float tcon[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) { contrib[k] = 0.f; tcon[k] = 0.f; off[k] = 0; }
+    float fx = 0.f, fy = 0.f, fz = 0.f, dLds = 0.f, f = 0.f, dr = 0.f, dg = 0.f, db = 0.f, dsb = 0.f;
     if (alive && i < n) {
       const float t = t0 + ((float)i + .5f) * p.dt;
       if (t >= t1) {
@@ -291,7 +309,6 @@ __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAPar
         if (in) {
           const vec3 tc = rel + vec3(.5f);
           int x0, x1, y0, y1, z0, z1;
-          float fx, fy, fz;
           lerp_coords(p.F.N[0], tc.x, x0, x1, fx);
           lerp_coords(p.F.N[1], tc.y, y0, y1, fy);
           lerp_coords(p.F.N[2], tc.z, z0, z1, fz);
@@ -300,7 +317,7 @@ __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAPar
           const float v00 = lerp_l(fx, c[0], c[1]), v01 = lerp_l(fx, c[2], c[3]);
           const float v10 = lerp_l(fx, c[4], c[5]), v11 = lerp_l(fx, c[6], c[7]);
           const float sv = lerp_l(fz, lerp_l(fy, v00, v01), lerp_l(fy, v10, v11));
-          float f = (sv - p.xf.lo) / p.xf.span;
+          f = (sv - p.xf.lo) / p.xf.span;
           const bool clamped = !(f > 0.f && f < 1.f);
           f = clampv(f, 0.f, 1.f);
           f *= (float)(p.xf.n - 1);
@@ -322,62 +339,62 @@ __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAPar
           dLdx += g.z * (b * Tnext - (C.z - A2));
           T = Tnext;
           const float dLdsig = dLdx * p.dt;
-          const float dr = g.x * w, dg = g.y * w, db = g.z * w;
-          tcon[0] = dr * (1.f - f);
-          tcon[1] = dg * (1.f - f);
-          tcon[2] = db * (1.f - f);
-          tcon[3] = dLdsig * bd * (1.f - f);
-          tcon[4] = dr * f;
-          tcon[5] = dg * f;
-          tcon[6] = db * f;
-          tcon[7] = dLdsig * bd * f;
+          dr = g.x * w;
+          dg = g.y * w;
+          db = g.z * w;
+          dsb = dLdsig * bd;
           if (!clamped) {
-            float dLds = dLdsig * bd * (e1.w - e0.w) * gs;
+            dLds = dLdsig * bd * (e1.w - e0.w) * gs;
             dLds += dr * (e1.x - e0.x) * gs + dg * (e1.y - e0.y) * gs + db * (e1.z - e0.z) * gs;
-            const float wx0 = 1.f - fx, wy0 = 1.f - fy, wz0 = 1.f - fz;
-            contrib[0] = dLds * wx0 * wy0 * wz0;
-            contrib[1] = dLds * fx * wy0 * wz0;
-            contrib[2] = dLds * wx0 * fy * wz0;
-            contrib[3] = dLds * fx * fy * wz0;
-            contrib[4] = dLds * wx0 * wy0 * fz;
-            contrib[5] = dLds * fx * wy0 * fz;
-            contrib[6] = dLds * wx0 * fy * fz;
-            contrib[7] = dLds * fx * fy * fz;
             const size_t base = (size_t)x0 + sy * y0 + sz * z0;
-            key = (long long)base;
-            const size_t ddx = (size_t)(x1 - x0), ddy = (size_t)(y1 - y0) * sy, ddz = (size_t)(z1 - z0) * sz;
-#pragma unroll
-            for (int k = 0; k < 8; k++)
-              off[k] = base + ((k & 1) ? ddx : 0) + ((k & 2) ? ddy : 0) + ((k & 4) ? ddz : 0);
+            key = 8 * (long long)base + (x1 != x0 ? 1 : 0) + (y1 != y0 ? 2 : 0) + (z1 != z0 ? 4 : 0);
             have = true;
           }
         }
       }
     }
-    // voxel stencil: flush the running sum when the stencil changes
+    // voxel stencil: flush the running sums when the stencil changes
     const bool vFlush = vKey >= 0 && (key != vKey);
-    flush8<false>(gvox, vFlush, (unsigned long long)vKey, vOff, vAcc);
+    flush8(gvox, vFlush, (unsigned long long)vKey,
+           [&](int k) {
+             const size_t base = (size_t)(vKey >> 3);
+             const int m = (int)(vKey & 7) & k;
+             return base + ((m & 1) ? 1 : 0) + ((m & 2) ? sy : 0) + ((m & 4) ? sz : 0);
+           },
+           vAcc);
     if (vFlush || vKey < 0) {
       vKey = have ? key : -1;
 #pragma unroll
-      for (int k = 0; k < 8; k++) { vAcc[k] = have ? contrib[k] : 0.f; vOff[k] = off[k]; }
-    } else if (have) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) vAcc[k] += contrib[k];
+      for (int k = 0; k < 8; k++) vAcc[k] = 0.f;
+    }
+    if (have) {
+      const float wx0 = 1.f - fx, wy0 = 1.f - fy, wz0 = 1.f - fz;
+      vAcc[0] += dLds * wx0 * wy0 * wz0;
+      vAcc[1] += dLds * fx * wy0 * wz0;
+      vAcc[2] += dLds * wx0 * fy * wz0;
+      vAcc[3] += dLds * fx * fy * wz0;
+      vAcc[4] += dLds * wx0 * wy0 * fz;
+      vAcc[5] += dLds * fx * wy0 * fz;
+      vAcc[6] += dLds * wx0 * fy * fz;
+      vAcc[7] += dLds * fx * fy * fz;
     }
     // TF segment: same scheme, into the block's shared-memory gradient
     const bool tFlush = tIdx >= 0 && idx != tIdx;
-    size_t tOff[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) tOff[k] = (size_t)(4 * tIdx + k);
-    flush8<true>(s_gtf, tFlush, (unsigned long long)tIdx, tOff, tAcc);
+    flush8(s_gtf, tFlush, (unsigned long long)tIdx, [&](int k) { return 4 * tIdx + k; }, tAcc);
     if (tFlush || tIdx < 0) {
       tIdx = idx;
 #pragma unroll
-      for (int k = 0; k < 8; k++) tAcc[k] = idx >= 0 ? tcon[k] : 0.f;
-    } else if (idx >= 0) {
-#pragma unroll
-      for (int k = 0; k < 8; k++) tAcc[k] += tcon[k];
+      for (int k = 0; k < 8; k++) tAcc[k] = 0.f;
+    }
+    if (idx >= 0) {
+      tAcc[0] += dr * (1.f - f);
+      tAcc[1] += dg * (1.f - f);
+      tAcc[2] += db * (1.f - f);
+      tAcc[3] += dsb * (1.f - f);
+      tAcc[4] += dr * f;
+      tAcc[5] += dg * f;
+      tAcc[6] += db * f;
+      tAcc[7] += dsb * f;
     }
   }
   __syncthreads();
@@ -385,16 +402,34 @@ __global__ void __launch_bounds__(128, MinBlocks) ea_backward_kernel(const EAPar
     if (s_gtf[i] != 0.f) atomicAdd(gtf + i, s_gtf[i]);
 }
 
-static gbv_status ea_prepare(const gbv_scene *s, float step, EAParams &p) {
+// forward_any_store: the caller is the forward march, which also reads
+// brick-corner stores (any format); the adjoint and the FP64 march read the
+// linear FP32 field only.
+static gbv_status ea_prepare(const gbv_scene *s, float step, EAParams &p, bool forward_any_store = false) {
   if (!s || !s->d_voxels || !s->d_tf || s->tf_n < 2)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "ea: scene lacks voxels or transfer function");
-  if (s->layout != GBV_LAYOUT_LINEAR || s->format != GBV_VOXEL_F32)
-    return set_error(GBV_ERROR_UNSUPPORTED, "ea: the march reads an FP32 linear field");
+  const bool linear = s->layout == GBV_LAYOUT_LINEAR && s->format == GBV_VOXEL_F32;
+  const bool bricks = s->layout == GBV_LAYOUT_BRICK_CORNERS && s->format >= GBV_VOXEL_F32 &&
+                      s->format <= GBV_VOXEL_U8_SCALED;
+  if (!linear && !(forward_any_store && bricks))
+    return set_error(GBV_ERROR_UNSUPPORTED, forward_any_store
+                                                ? "ea: unknown voxel layout or format"
+                                                : "ea: the adjoint and FP64 marches read an FP32 linear field");
+  if (bricks && s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "ea: U8 voxels need the scale/offset table");
   if (!(step > 0.f)) return set_error(GBV_ERROR_INVALID_ARGUMENT, "ea: step must be positive");
   if (s->dims[0] < 2 || s->dims[1] < 2 || s->dims[2] < 2)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "ea: a field needs at least 2 voxels per axis");
   make_field_geom(s, p.F);
   p.store = StoreLinearF32{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
+  p.vox = s->d_voxels;
+  p.so = reinterpret_cast<const float2 *>(s->d_scale_offset);
+  if (bricks) {
+    int l[3];
+    if (!resolve_brick_shape(s->brick_log2, l))
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "brick_log2: each 1..6 (0 = 3), sum at most 15");
+    p.brick = make_brick_geom(s->dims, l);
+  }
   p.xf.v = reinterpret_cast<const float4 *>(s->d_tf);
   p.xf.n = s->tf_n;
   p.xf.lo = s->domain[0];
@@ -439,12 +474,20 @@ extern "C" {
 gbv_status gbv_ea_render(const gbv_scene *s, const gbv_ea_view *views, int num_views, float step, float *d_images,
                          void *stream) {
   EAParams p;
-  gbv_status st = ea_prepare(s, step, p);
+  gbv_status st = ea_prepare(s, step, p, true);
   if (st != GBV_OK) return st;
   if (!views || num_views <= 0 || !d_images) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_ea_render: views");
+  const int layout = s->layout, format = s->format;
   return for_view_chunks(p, views, num_views, [&](EAParams &q, int cnt, int maxW, int maxH) {
     dim3 grid((maxW + 15) / 16, (maxH + 7) / 8, cnt);
-    ea_forward_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(q, reinterpret_cast<float4 *>(d_images));
+    float4 *out = reinterpret_cast<float4 *>(d_images);
+    cudaStream_t cs = (cudaStream_t)stream;
+    if (layout == GBV_LAYOUT_LINEAR) ea_forward_kernel<StoreLinearF32><<<grid, 128, 0, cs>>>(q, out);
+    else if (format == GBV_VOXEL_F32) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F32>><<<grid, 128, 0, cs>>>(q, out);
+    else if (format == GBV_VOXEL_F16) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F16>><<<grid, 128, 0, cs>>>(q, out);
+    else if (format == GBV_VOXEL_BF16)
+      ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_BF16>><<<grid, 128, 0, cs>>>(q, out);
+    else ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_U8_SCALED>><<<grid, 128, 0, cs>>>(q, out);
     return check_launch("ea_forward_kernel");
   });
 }
@@ -475,10 +518,14 @@ gbv_status gbv_ea_backward(const gbv_scene *s, const gbv_ea_view *views, int num
   return for_view_chunks(p, views, num_views, [&](EAParams &q, int cnt, int maxW, int maxH) {
     dim3 grid((maxW + 15) / 16, (maxH + 7) / 8, cnt);
     // GBV_EA_OCC: resident 128-thread blocks per SM the adjoint's registers
-    // are capped for (default 4)
+    // are capped for (4, 6 or 8; default 6: 80 registers, no spills)
     const char *oc = getenv("GBV_EA_OCC");
-    const int occ = oc ? atoi(oc) : 4;
-    if (occ >= 6)
+    const int occ = oc ? atoi(oc) : 6;
+    if (occ >= 8)
+      ea_backward_kernel<8><<<grid, 128, smem, (cudaStream_t)stream>>>(
+          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
+          d_grad_scalars, d_grad_tf);
+    else if (occ >= 6)
       ea_backward_kernel<6><<<grid, 128, smem, (cudaStream_t)stream>>>(
           q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
           d_grad_scalars, d_grad_tf);

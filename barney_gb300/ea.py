@@ -20,9 +20,14 @@ from .scenes import Scene
 
 
 class EAProblem:
-    def __init__(self, scene: Scene, views, step: float, scalars=None, tf=None):
+    """store: optional GpuScene whose brick-corner store (any format and brick
+    shape) the forward march reads instead of the FP32 linear field; the
+    adjoint and the FP64 march always read the FP32 linear field."""
+
+    def __init__(self, scene: Scene, views, step: float, scalars=None, tf=None, store=None):
         import torch
         self.s = scene
+        self.store = store
         self.views = list(views)
         self.step = float(step)
         self._views_c = ea_views(self.views)
@@ -52,6 +57,12 @@ class EAProblem:
         import torch
         out = torch.empty((self.npx, 4), dtype=torch.float32, device="cuda")
         rec = self.record(scalars, tf)
+        if self.store is not None and scalars is None:
+            g = self.store
+            rec.d_voxels = g.voxels.data_ptr()
+            rec.d_scale_offset = g.scale_offset.data_ptr() if g.scale_offset is not None else None
+            rec.format, rec.layout = g.fmt, g.layout
+            rec.brick_log2[:] = list(g.brick)
         N.check(N.lib().gbv_ea_render(C.byref(rec), self._views_c, len(self.views), self.step, _ptr(out),
                                       _stream()), "gbv_ea_render")
         return out

@@ -200,6 +200,146 @@ def ea_timing(dims=128, nviews=32, size=256, reps=3):
             "fwd_adjoint_ms_per_view": b, "ratio": b / f}
 
 
+def ea_steps(scene, view, step):
+    """March steps of the EA views (pixel-centre rays, box test, n = ceil of
+    the chord over the step), counted in float64 on the host."""
+    W, H = view["width"], view["height"]
+    pos = np.asarray(view["pos"], np.float64)
+    d = np.asarray(view["dir"], np.float64)
+    d = d / np.linalg.norm(d)
+    up = np.asarray(view["up"], np.float64)
+    du = np.cross(d, up)
+    du /= np.linalg.norm(du)
+    dv = np.cross(du, d)
+    dv /= np.linalg.norm(dv)
+    scale = 1.0 / (2.0 * math.tan(math.radians(view["fovy"]) / 2.0))
+    u = ((np.arange(W) + 0.5) / W - 0.5) * (W / H)
+    v = (np.arange(H) + 0.5) / H - 0.5
+    dirs = d[None, None, :] * scale + u[None, :, None] * du + v[:, None, None] * dv
+    dirs /= np.linalg.norm(dirs, axis=-1, keepdims=True)
+    origin, spacing = scene.geometry()
+    lo = np.asarray(origin, np.float64)
+    hi = lo + np.asarray(spacing, np.float64) * (np.asarray(scene.dims, np.float64) - 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        a = (lo - pos) / dirs
+        b = (hi - pos) / dirs
+    t0 = np.maximum(np.nanmax(np.minimum(a, b), axis=-1), 0.0)
+    t1 = np.nanmin(np.maximum(a, b), axis=-1)
+    n = np.where(t1 > t0, np.ceil((t1 - t0) / step), 0.0)
+    return int(n.sum())
+
+
+def precision_study(scene, g32, rows=(523, 557), reps=2):
+    """Voxel storage precision, two ways.
+
+    ea: the fixed-step emission-absorption march (deterministic) of the
+    512^3 volume through the frame's camera, per format: samples/s at
+    1920x1080 and the error of a 240x135 view against the oracle's FP64 march
+    of the FP32 source voxels.  `linear_f32` is the plain form (the
+    reference's x-fastest FP32 texels).
+
+    delta_tracking: each format's full frame (samples/s, frame ms) and its
+    error on a band of rows against the oracle's FP64 render from the FP32
+    source voxels.  All formats and the oracle use the FP32 source's majorant
+    grid, so every pixel draws the same random numbers; still, a decision
+    that flips between precisions changes the rest of that path, so these
+    errors are dominated by path divergence: `oracle_fp32_vs_fp64` is that
+    floor for the FP32 arithmetic itself."""
+    import torch
+    import oracle
+    from barney_gb300 import _native as N
+    from barney_gb300.device import GpuScene
+    from barney_gb300.ea import EAProblem
+    maj = g32.majorants.cpu().numpy()
+    o = oracle.Oracle(scene, majorants=maj)
+    threads = os.cpu_count() or 1
+    H, W, spp = scene.height, scene.width, scene.spp
+    out = {"delta_tracking": {}, "ea": {}}
+    # ---- EA march ----
+    step = 0.5 / (scene.dims[0] - 1)
+    cam = dict(pos=tuple(scene.cam_pos), dir=tuple(scene.cam_dir), up=tuple(scene.cam_up), fovy=scene.fovy)
+    big = dict(cam, width=W, height=H)
+    small = dict(cam, width=240, height=135)
+    t0 = time.perf_counter()
+    ea64 = o.ea_render([small], step, use_double=True, nthreads=threads)
+    out["ea"] = {"step": "0.5 voxel", "timed_view": f"{W}x{H}", "error_view": "240x135 (same camera)",
+                 "oracle_fp64_s": time.perf_counter() - t0, "samples_per_view": ea_steps(scene, big, step),
+                 "formats": {}}
+    nsamp = out["ea"]["samples_per_view"]
+    stores = [("linear_f32", None)] + [(name, fmt) for fmt, name in FMT_NAME.items()]
+    for name, fmt in stores:
+        g = None if fmt is None else (g32 if fmt == 0 else GpuScene(scene, fmt=fmt, scalars_device=g32.scalars))
+        pb = EAProblem(scene, [big], step, scalars=g32.scalars, store=g)
+        ps = EAProblem(scene, [small], step, scalars=g32.scalars, store=g)
+        pb.render()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            pb.render()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        d = ps.render().cpu().numpy() - ea64
+        out["ea"]["formats"][name] = {"Msamples_s": nsamp / (ms / 1e3) / 1e6, "ms": ms,
+                                      "rmse_vs_fp64": float(np.sqrt(np.mean(d ** 2))),
+                                      "max_err_vs_fp64": float(np.abs(d).max())}
+        if fmt not in (None, 0):
+            del g
+        del pb, ps
+        torch.cuda.empty_cache()
+    base = out["ea"]["formats"]["linear_f32"]["Msamples_s"]
+    for v in out["ea"]["formats"].values():
+        v["vs_linear_f32"] = v["Msamples_s"] / base
+    # ---- delta tracking ----
+    t0 = time.perf_counter()
+    ref64 = o.render(spp=spp, use_double=True, nthreads=threads, rows=rows)[rows[0]:rows[1], :, :3] / spp
+    t64 = time.perf_counter() - t0
+    ref32 = o.render(spp=spp, use_double=False, nthreads=threads, rows=rows)[rows[0]:rows[1], :, :3] / spp
+    dt = out["delta_tracking"]
+    dt.update({"crop": f"rows {rows[0]}-{rows[1]} x {W} columns ({(rows[1] - rows[0]) * W} pixels), {spp} spp",
+               "majorants": "FP32 source majorant grid for every format", "oracle_fp64_s": t64,
+               "oracle_fp32_vs_fp64": {"rmse": float(np.sqrt(np.mean((ref32 - ref64) ** 2))),
+                                       "max_err": float(np.abs(ref32 - ref64).max())},
+               "formats": {}})
+    cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    img32 = None
+    for fmt, name in FMT_NAME.items():
+        g = g32 if fmt == 0 else GpuScene(scene, fmt=fmt, scalars_device=g32.scalars)
+        if fmt != 0:
+            g.majorants.copy_(g32.majorants)
+        acc = g.new_accum()
+        cnt.zero_()
+        g.render(spp=spp, accum=acc, counters=cnt)
+        torch.cuda.synchronize()
+        samples = int(cnt[0].item())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            g.render(spp=spp, accum=acc)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        full = acc.cpu().numpy()
+        img = full[rows[0]:rows[1], :, :3] / spp
+        d = img - ref64
+        rec = {"Msamples_s": samples / (ms / 1e3) / 1e6, "frame_ms": ms, "store_GB": g.voxels.numel() / 1e9,
+               "rmse_vs_fp64": float(np.sqrt(np.mean(d ** 2))), "max_err_vs_fp64": float(np.abs(d).max())}
+        if img32 is None:
+            img32 = full
+        else:
+            rec["pixels_identical_to_f32"] = float(np.mean(np.all(full == img32, axis=-1)))
+        dt["formats"][name] = rec
+        if fmt != 0:
+            del g
+        del acc
+        torch.cuda.empty_cache()
+    f32 = dt["formats"]["f32"]["Msamples_s"]
+    for v in dt["formats"].values():
+        v["vs_f32"] = v["Msamples_s"] / f32
+    return out
+
+
 def batch_timing(count=64, reps=3):
     """The batched uneven workload: `count` volumes (sides log-uniform in
     [32, 256] per axis), each with its own TF, camera and image size from
@@ -334,31 +474,11 @@ def run_ours(args):
     # ---- extras on rank 0 ----
     extras_t0 = time.perf_counter()
     if not args.quick:
-        # FP16 storage against FP32
+        # voxel storage formats against the FP64 oracle
         try:
-            g16 = GpuScene(scene, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=1, scalars_device=g.scalars)
-            acc16 = g16.new_accum()
-            c16 = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
-            g16.render(spp=scene.spp, accum=acc16, counters=c16)
-            torch.cuda.synchronize()
-            s16 = c16[0].item()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(2):
-                g16.render(spp=scene.spp, accum=acc16)
-            e1.record()
-            torch.cuda.synchronize()
-            ms16 = e0.elapsed_time(e1) / 2
-            v16 = s16 / (ms16 / 1e3) / 1e6
-            img32 = (acc / scene.spp)[..., :3]
-            img16 = (acc16 / scene.spp)[..., :3]
-            rmse_16_32 = float(torch.sqrt(torch.mean((img16 - img32) ** 2)).item())
-            line["fp16_vs_fp32"] = {"fp16_Msamples_s": v16, "fp32_Msamples_s": samples / (frame_ms / 1e3) / 1e6,
-                                    "speedup": v16 / (samples / (frame_ms / 1e3) / 1e6), "frame_ms_fp16": ms16,
-                                    "rmse_fp16_vs_fp32_frame": rmse_16_32}
-            del g16, acc16
+            line["precision"] = precision_study(scene, g)
         except Exception as e:  # report, never hide
-            line["fp16_vs_fp32"] = {"error": str(e)}
+            line["precision"] = {"error": repr(e)}
         try:
             line["batch"] = batch_timing()
         except Exception as e:

@@ -261,11 +261,15 @@ typedef struct gbv_ea_view {
 } gbv_ea_view;
 
 /* Renders num_views views into d_images (views packed back to back, each
-   width*height RGBA float).  FP32 with compensated optical depth. */
+   width*height RGBA float).  FP32 interpolation and transmittance with
+   compensated optical depth.  The field is FP32 LINEAR or a brick-corner
+   store of any format and brick shape (FP16/BF16/U8 voxels are widened to
+   FP32 before interpolation). */
 gbv_status gbv_ea_render(const gbv_scene *scene, const gbv_ea_view *views,
                          int num_views, float step, float *d_images,
                          void *stream);
-/* Same march in FP64 (finite-difference check mode); d_images are doubles. */
+/* Same march in FP64 (finite-difference check mode); d_images are doubles.
+   The field must be FP32 LINEAR. */
 gbv_status gbv_ea_render_f64(const gbv_scene *scene, const gbv_ea_view *views,
                              int num_views, float step, double *d_images,
                              void *stream);

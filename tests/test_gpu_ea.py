@@ -132,3 +132,57 @@ def test_autograd_function(cuda):
     # the adjoint's atomics sum in no fixed order: equal up to FP32 reassociation
     torch.testing.assert_close(vox.grad.reshape(-1), gv.reshape(-1), rtol=1e-4, atol=1e-6)
     torch.testing.assert_close(tf.grad.reshape(-1), gtf.reshape(-1), rtol=1e-4, atol=1e-5)
+
+
+def _rounded(v, fmt):
+    if fmt == N.GBV_VOXEL_F16:
+        return v.astype(np.float16).astype(np.float32)
+    u = v.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("fmt,brick", [(N.GBV_VOXEL_F32, (3, 3, 3)), (N.GBV_VOXEL_F32, (4, 2, 2)),
+                                       (N.GBV_VOXEL_F16, (3, 3, 3)), (N.GBV_VOXEL_BF16, (2, 2, 2))])
+def test_forward_on_brick_stores(cuda, fmt, brick):
+    """The forward march over a brick-corner store equals the march over the
+    linear FP32 field holding the same (rounded) voxel values, bit for bit."""
+    from barney_gb300.device import GpuScene
+    gt, views, step = small_problem(nviews=3)
+    g = GpuScene(gt, fmt=fmt, brick=brick)
+    got = EAProblem(gt, views, step, store=g).render().cpu().numpy()
+    rounded = gt.scalars if fmt == N.GBV_VOXEL_F32 else _rounded(gt.scalars, fmt)
+    import copy
+    gr = copy.copy(gt)
+    gr.scalars = np.ascontiguousarray(rounded)
+    ref = EAProblem(gr, views, step).render().cpu().numpy()
+    np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_forward_on_u8_store_error_against_fp64(cuda):
+    from barney_gb300.device import GpuScene
+    gt, views, step = small_problem(nviews=3)
+    g = GpuScene(gt, fmt=N.GBV_VOXEL_U8_SCALED)
+    got = EAProblem(gt, views, step, store=g).render().cpu().numpy().reshape(-1, 4)
+    ref64 = oracle.Oracle(gt).ea_render(views, step, use_double=True)
+    err = np.abs(got - ref64)
+    # 8-bit voxels per 8^3 cells: a few 1e-3 on the image
+    assert float(np.sqrt(np.mean(err ** 2))) < 5e-3 and err.max() < 0.05, (np.sqrt(np.mean(err ** 2)), err.max())
+
+
+def test_adjoint_rejects_brick_stores(cuda):
+    import ctypes as C
+    from barney_gb300.device import GpuScene, _ptr, _stream
+    gt, views, step = small_problem(nviews=1)
+    g = GpuScene(gt, fmt=N.GBV_VOXEL_F16)
+    p = EAProblem(gt, views, step, store=g)
+    rec = p.record()
+    rec.d_voxels = g.voxels.data_ptr()
+    rec.format, rec.layout = g.fmt, g.layout
+    import torch
+    img = p.render()
+    gv = torch.zeros(p.scalars.numel(), device="cuda")
+    gtf = torch.zeros(p.tf.numel(), device="cuda")
+    st = N.lib().gbv_ea_backward(C.byref(rec), p._views_c, 1, step, _ptr(img), _ptr(img), _ptr(gv), _ptr(gtf),
+                                 _stream())
+    assert st == N.GBV_ERROR_UNSUPPORTED
