@@ -74,6 +74,8 @@ def lib() -> C.CDLL:
             "gbv_env_build_cdfs": (st, [vp, i, i, ip, vp, vp, vp]),
             "gbv_render": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
             "gbv_render_noalloc": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
+            "gbv_render_tiles": (st, [C.POINTER(GbvScene), vp, i, i, i, i, i, i, vp, vp]),
+            "gbv_tile_partition": (st, [i, i, i, i, ip, ip]),
             "gbv_batch_create": (st, [C.POINTER(GbvScene), vp, ip, ip, i, C.POINTER(vp)]),
             "gbv_batch_set_launch": (st, [vp, i, i, i]),
             "gbv_batch_render": (st, [vp, i, i, vp, vp]),

@@ -1,6 +1,7 @@
 // render.cu -- host entry points of the frame render: parameter set-up
 // (camera, lights, env map, macrocell grid) and dispatch to the kernels of
 // the scene's voxel store (render_store_*.cu).
+#include <cstdio>
 #include "render_kernel.cuh"
 
 namespace gbv {
@@ -101,6 +102,8 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   p.maxVB = s->max_volume_bounces;
   p.aniso = s->anisotropy;
   p.scatAlb = s->scattering_albedo;
+  p.rank = 0;
+  p.numRanks = 1;
   return GBV_OK;
 }
 
@@ -108,16 +111,32 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
 
 using namespace gbv;
 
-extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
-                                 int spp, unsigned long long *d_counters, void *stream) {
-  if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0)
-    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: null pointer or non-positive size");
-  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0)
-    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: scene lacks voxels, majorants or a transfer function");
-  if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
-    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: the linear layout holds FP32 voxels only");
-  if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)
-    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render: U8 voxels need the brick scale/offset table");
+namespace gbv {
+
+static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accum, int width, int height,
+                               int accum_id_start, int spp, int rank, int num_ranks, unsigned long long *d_counters,
+                               void *stream) {
+  char msg[160];
+  if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0) {
+    snprintf(msg, sizeof msg, "%s: null pointer or non-positive size", fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
+  if (num_ranks < 1 || rank < 0 || rank >= num_ranks) {
+    snprintf(msg, sizeof msg, "%s: rank must be in [0, num_ranks) and num_ranks >= 1", fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
+  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0) {
+    snprintf(msg, sizeof msg, "%s: scene lacks voxels, majorants or a transfer function", fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
+  if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32) {
+    snprintf(msg, sizeof msg, "%s: the linear layout holds FP32 voxels only", fn);
+    return set_error(GBV_ERROR_UNSUPPORTED, msg);
+  }
+  if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset) {
+    snprintf(msg, sizeof msg, "%s: U8 voxels need the brick scale/offset table", fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
   if (spp == 0) return GBV_OK;
   RenderParams p;
   gbv_status st = fill_params(s, p);
@@ -128,16 +147,59 @@ extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, 
   p.accumIdStart = accum_id_start;
   p.spp = spp;
   p.counters = d_counters;
+  p.rank = rank;
+  p.numRanks = num_ranks;
+  if (warp_tile_count(p) == 0) return GBV_OK;  // a rank that owns no tile
+  if (warp_tile_count(p) >= (1ll << 31) - (1ll << 24)) {
+    snprintf(msg, sizeof msg, "%s: more 8x4-pixel tiles than the 32-bit tile counter holds", fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
   cudaStream_t cs = (cudaStream_t)stream;
   if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_linear(p, cs);
-  if (s->layout != GBV_LAYOUT_BRICK_CORNERS) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown layout");
+  if (s->layout != GBV_LAYOUT_BRICK_CORNERS) {
+    snprintf(msg, sizeof msg, "%s: unknown layout", fn);
+    return set_error(GBV_ERROR_UNSUPPORTED, msg);
+  }
   switch (s->format) {
     case GBV_VOXEL_F32: return render_launch_f32(p, cs);
     case GBV_VOXEL_F16: return render_launch_f16(p, cs);
     case GBV_VOXEL_BF16: return render_launch_bf16(p, cs);
     case GBV_VOXEL_U8_SCALED: return render_launch_u8(p, cs);
   }
-  return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render: unknown voxel format");
+  snprintf(msg, sizeof msg, "%s: unknown voxel format", fn);
+  return set_error(GBV_ERROR_UNSUPPORTED, msg);
+}
+
+}  // namespace gbv
+
+extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
+                                 int spp, unsigned long long *d_counters, void *stream) {
+  return render_frame("gbv_render", s, d_accum, width, height, accum_id_start, spp, 0, 1, d_counters, stream);
+}
+
+extern "C" gbv_status gbv_render_tiles(const gbv_scene *s, float *d_accum, int width, int height,
+                                       int accum_id_start, int spp, int rank, int num_ranks,
+                                       unsigned long long *d_counters, void *stream) {
+  return render_frame("gbv_render_tiles", s, d_accum, width, height, accum_id_start, spp, rank, num_ranks,
+                      d_counters, stream);
+}
+
+extern "C" gbv_status gbv_tile_partition(int width, int height, int rank, int num_ranks, int *num_tiles,
+                                         int *tile_lower) {
+  if (width <= 0 || height <= 0 || num_ranks < 1 || rank < 0 || rank >= num_ranks || !num_tiles)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_tile_partition: bad size, rank or null count");
+  const long long n = owned_ref_tiles(width, height, rank, num_ranks);
+  if (n > (1ll << 31) - 1) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_tile_partition: too many tiles");
+  *num_tiles = (int)n;
+  if (tile_lower) {
+    const int tilesX = (width + kRefTile - 1) / kRefTile;
+    for (long long k = 0; k < n; k++) {
+      const long long id = (long long)rank + k * num_ranks;
+      tile_lower[2 * k] = (int)(id % tilesX) * kRefTile;
+      tile_lower[2 * k + 1] = (int)(id / tilesX) * kRefTile;
+    }
+  }
+  return GBV_OK;
 }
 
 // ===========================================================================

@@ -64,7 +64,25 @@ struct RenderParams {
   const float2 *so;
   BrickGeom brick;
   vec3 rcpMc;     // 1 / macrocell spacing
+  // frame partition across ranks (TiledFB.cu:226-255): with numRanks > 1
+  // this launch renders only the 32x32-pixel tiles rank, rank + numRanks, ...
+  int rank, numRanks;
 };
+
+// The reference frame buffer's tiles (TiledFB tileSize) and their
+// round-robin assignment to ranks: rank r owns tiles r, r + R, r + 2R, ...
+// of the row-major tile grid (TiledFB::resize numActiveTilesThisGPU and
+// setTileCoordsKernel, barney/fb/TiledFB.cu:226-255).
+constexpr int kRefTile = 32;
+__host__ __device__ inline long long owned_ref_tiles(int W, int H, int rank, int numRanks) {
+  const long long total = (long long)((W + kRefTile - 1) / kRefTile) * ((H + kRefTile - 1) / kRefTile);
+  return total > rank ? (total - rank + numRanks - 1) / numRanks : 0;
+}
+// 8x4-pixel warp tiles one (non-batched) launch hands out
+__host__ __device__ inline long long warp_tile_count(const RenderParams &p) {
+  if (p.numRanks > 1) return owned_ref_tiles(p.W, p.H, p.rank, p.numRanks) * 32;
+  return (long long)((p.W + 7) >> 3) * ((p.H + 3) >> 2);
+}
 
 template <class Store> __device__ __forceinline__ Store make_store(const RenderParams &p);
 template <> __device__ __forceinline__ StoreLinearF32 make_store<StoreLinearF32>(const RenderParams &p) {
@@ -743,7 +761,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
     }
     __syncthreads();
   }
-  const long long numTiles = Batch ? tileStart[numItems] : (long long)((p0.W + 7) >> 3) * ((p0.H + 3) >> 2);
+  const long long numTiles = Batch ? tileStart[numItems] : warp_tile_count(p0);
   Ctr<Count> cnt;
   // warp-uniform tile pool
   int tile = 0, tileTaken = 32, tileItem = 0;
@@ -789,12 +807,23 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       }
       if (!poolDone) {
         const RenderParams &tp = Batch ? items[tileItem] : p0;
-        const int tilesX = (tp.W + 7) >> 3;
+        // the warp tile's upper-left pixel
+        int tx, ty;
+        if (!Batch && L.numRanks > 1) {  // the k-th 32x32 tile this rank owns, 4x8 warp tiles in it
+          const long long big = (long long)L.rank + (long long)(tile >> 5) * L.numRanks;
+          const int bigX = (tp.W + kRefTile - 1) / kRefTile;
+          tx = (int)(big % bigX) * kRefTile + (tile & 3) * 8;
+          ty = (int)(big / bigX) * kRefTile + ((tile >> 2) & 7) * 4;
+        } else {
+          const int tilesX = (tp.W + 7) >> 3;
+          tx = (tile % tilesX) * 8;
+          ty = (tile / tilesX) * 4;
+        }
         const int rank = __popc(need & ((1u << lane) - 1u));
         const int take = min(__popc(need), 32 - tileTaken);
         if (!hasPixel && rank < take) {
           const int slot = tileTaken + rank;
-          const int px = (tile % tilesX) * 8 + (slot & 7), py = (tile / tilesX) * 4 + (slot >> 3);
+          const int px = tx + (slot & 7), py = ty + (slot >> 3);
           if (px < tp.W && py < tp.H) {
             hasPixel = true;
             item = tileItem;
@@ -941,7 +970,7 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks, false, true>, kThreads,
                                                 smem);
-  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+  const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
   const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
@@ -1028,7 +1057,7 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   if (st != GBV_OK) return st;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>, kThreads, 0);
-  const long long tiles = (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+  const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
   const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;

@@ -168,6 +168,20 @@ class GpuScene:
                                    self.s.spp if spp is None else spp, _ptr(counters), _stream()), "gbv_render")
         return accum
 
+    def render_tiles(self, rank: int, world: int, spp: Optional[int] = None, accum=None, accum_id_start: int = 0,
+                     counters=None):
+        """render() of only the 32x32 tiles `rank` of `world` owns (the
+        reference's round-robin partition); other pixels of accum are left
+        as they are."""
+        w, h = self.s.width, self.s.height
+        if accum is None:
+            accum = self.new_accum(w, h)
+        rec = self.record()
+        N.check(N.lib().gbv_render_tiles(C.byref(rec), _ptr(accum), w, h, accum_id_start,
+                                         self.s.spp if spp is None else spp, rank, world, _ptr(counters),
+                                         _stream()), "gbv_render_tiles")
+        return accum
+
     def tonemap(self, accum, accum_id: int, fmt: int = N.GBV_FB_FLOAT4):
         import torch
         h, w, _ = accum.shape

@@ -205,6 +205,29 @@ gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
                       int height, int accum_id_start, int spp,
                       unsigned long long *d_counters, void *stream);
 
+/* Frame partition across ranks (one GPU each), as the reference's tiled
+   frame buffer does it: the frame is cut into 32x32-pixel tiles, row-major,
+   and rank r of num_ranks owns tiles r, r + num_ranks, r + 2*num_ranks, ...
+   gbv_tile_partition (host only) gives the number of tiles rank `rank` owns
+   and, if tile_lower is not null, each tile's lower-left pixel (x, y) in
+   that order.  Replaces TiledFB::resize's numActiveTilesThisGPU and
+   setTileCoordsKernel (barney/fb/TiledFB.cu:226-255). */
+gbv_status gbv_tile_partition(int width, int height, int rank, int num_ranks,
+                              int *num_tiles, int *tile_lower);
+
+/* gbv_render restricted to the tiles rank `rank` of num_ranks owns: those
+   pixels of d_accum (the full width*height frame) are written exactly as
+   gbv_render writes them; all other pixels are left untouched.  A rank that
+   owns no tile returns at once.  The owners' tiles together are the frame;
+   gathering them to one rank is the caller's exchange step (the reference's
+   LocalFB::gatherColorChannel / DistFB, barney/fb/LocalFB.cpp:60-70).
+   Replaces the per-device part of Context::renderTiles
+   (barney/Context.cpp:142-185) on a multi-device context. */
+gbv_status gbv_render_tiles(const gbv_scene *scene, float *d_accum, int width,
+                            int height, int accum_id_start, int spp, int rank,
+                            int num_ranks, unsigned long long *d_counters,
+                            void *stream);
+
 /* gbv_render without any device allocation, for callers that may not
    allocate device memory while they render (an application that hands out
    all HBM from its own pre-sized pool, or a real-time viewer that forbids
