@@ -16,7 +16,7 @@ GBV_VOXEL_F32, GBV_VOXEL_F16, GBV_VOXEL_BF16, GBV_VOXEL_U8_SCALED = 0, 1, 2, 3
 GBV_LAYOUT_LINEAR, GBV_LAYOUT_BRICK_CORNERS = 0, 1
 GBV_FB_FLOAT4, GBV_FB_RGBA8, GBV_FB_RGBA8_SRGB = 0, 1, 2
 GBV_ADDR_WRAP, GBV_ADDR_CLAMP, GBV_ADDR_BORDER, GBV_ADDR_MIRROR = 0, 1, 2, 3
-GBV_NUM_COUNTERS = 8
+GBV_NUM_COUNTERS = 12
 
 _f3 = C.c_float * 3
 _i3 = C.c_int * 3

@@ -238,8 +238,16 @@ __device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, floa
   return begin;
 }
 
+// Code size.  The render kernel is limited as much by instruction fetch as
+// by memory: warps of one SM sit in different phases (start, traverse,
+// shade) at once, so the whole loop body is the instruction working set, and
+// ncu attributes almost half of the stall samples of a 1080p launch to
+// "no instruction".  The shading helpers below are therefore compiled out
+// of line (__noinline__, one copy each instead of one per call site), and
+// the kernel has one call site each for trace_begin and the env lookup of a
+// miss.  Measured on the 512^3 frame: +7% samples/s.
 // EnvMap.h:136-180
-__device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
+static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   if (!p.hasEnv) return kOneOverFourPi;
   const EnvDev &e = p.env;
   vec3 localDir = xfm_vector(e.toLocal, dir);
@@ -255,7 +263,7 @@ __device__ __forceinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta2));
 }
 // EnvMap.h:198-250
-__device__ __forceinline__ LightSample env_sample(const RenderParams &p, Random &r) {
+static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Random &r) {
   const EnvDev &e = p.env;
   LightSample s;
   float r_y = r();
@@ -281,6 +289,7 @@ __device__ __forceinline__ LightSample env_sample(const RenderParams &p, Random 
 
 // DG.h:183-193
 __device__ __forceinline__ vec3 random_direction(Random &rng) {
+#pragma unroll 1
   for (int k = 0; k < 64; k++) {
     vec3 v;
     v.x = 1.f - 2.f * rng();
@@ -364,7 +373,7 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
 }
 
 // shadeRays.cu:437-456
-__device__ __forceinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
+static __device__ __noinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
   if (p.hasEnv) {
     vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
     float theta = spherical_theta(d);
@@ -390,7 +399,7 @@ __device__ __forceinline__ float phase_pdf(const RenderParams &p, float g, vec3 
   return hg_phase(g, dot(wi_in, normalize(wi)));
 }
 // Phase.h:74-99
-__device__ __forceinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
+static __device__ __noinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
   float u0 = random();
   float u1 = random();
   float cosTheta;
@@ -428,7 +437,7 @@ struct ShadeOut {
 
 // bounce() for a volume hit (shadeRays.cu:605-878).  Updates `ray`; a dead
 // ray has tMax = -1.
-__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
+static __device__ __noinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
                                                   int pathDepth, ShadeOut &out) {
   out.shadowValid = false;
   const float tHit = h.t;
@@ -731,9 +740,11 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
 // lane reads the scene of the pixel it owns.  Otherwise the launch renders
 // the one scene `p0`.  Launch-wide settings (passes, thresholds, counters)
 // always come from p0.  Count: whether to count events (see Ctr).
+// p0 is __grid_constant__ so that out-of-line helpers can take it by
+// reference without a copy to local memory.
 template <class Store, int MinBlocks, bool Batch, bool Count>
 __global__ void __launch_bounds__(kThreads, MinBlocks)
-    render_kernel(const RenderParams p0, const RenderParams *__restrict__ items,
+    render_kernel(const __grid_constant__ RenderParams p0, const RenderParams *__restrict__ items,
                   const long long *__restrict__ tileStart, int numItems, int *__restrict__ pool) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -778,6 +789,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
   Hit h;
   h.hit = false;
   unsigned long long cyc[3] = {0ull, 0ull, 0ull};
+  // profile: traversal iterations and tracing lanes summed over them, shading
+  // passes and shaded lanes summed over them (lane 0 of each warp counts)
+  unsigned long long simt[4] = {0ull, 0ull, 0ull, 0ull};
   while (true) {
     // ---- phase 1: pixels for idle lanes (from the warp's tile), then every
     // lane that needs one starts its next trace ----
@@ -850,14 +864,13 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         newSample = false;
       }
       h.hit = false;
-      bool active;
-      if (shadowPending) {
-        kind = K_SHADOW;
-        active = trace_begin(p.F, p.G, p.rcpMc, sray.org, sray.dir, sray.tMax, sray.seed, T, cnt);
-      } else {
-        kind = K_MAIN;
-        active = trace_begin(p.F, p.G, p.rcpMc, ray.org, ray.dir, ray.tMax, ray.seed, T, cnt);
-      }
+      kind = shadowPending ? K_SHADOW : K_MAIN;
+      RNGSeed seed = shadowPending ? sray.seed : ray.seed;
+      const bool active = trace_begin(p.F, p.G, p.rcpMc, shadowPending ? sray.org : ray.org,
+                                      shadowPending ? sray.dir : ray.dir, shadowPending ? sray.tMax : ray.tMax, seed,
+                                      T, cnt);
+      if (shadowPending) sray.seed = seed;
+      else ray.seed = seed;
       tstate = active ? TRACING : DONE;
     }
     // ---- phase 2: traverse while enough of the warp's busy lanes trace ----
@@ -872,6 +885,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       while (true) {
         const int tracing = __popc(__ballot_sync(FULL, tstate == TRACING));
         if (tracing == 0 || tracing * 100 < busy * L.threshold) break;
+        if (L.profile && lane == 0) {
+          simt[0]++;
+          simt[1] += (unsigned)tracing;
+        }
         if (tstate == TRACING && trace_step(p.F, make_store<Store>(p), p.xf, p.G, T, h, cnt, L.skip,
                                             !Batch && L.maskWords > 0) != TR_CONTINUE)
           tstate = DONE;
@@ -884,6 +901,13 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       c2 = clock64();
       if (lane == 0) cyc[1] += (unsigned long long)(c2 - c1);
     }
+    if (L.profile) {
+      const unsigned shading = __popc(__ballot_sync(FULL, tstate == DONE));
+      if (lane == 0 && shading) {
+        simt[2]++;
+        simt[3] += shading;
+      }
+    }
     if (tstate == DONE) {
       tstate = NEED;
       const int accumID = L.accumIdStart + s;
@@ -895,12 +919,13 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         vec3 frag(0.f);
         float alpha = 0.f;
         if (!h.hit) {
+          const float4 miss = miss_color(p, iy);
+          const vec3 env = (gen != 0 || p.hasEnv) ? radiance_from_env(p, ray.dir) : vec3(0.f);
           if (gen == 0) {
-            const float4 miss = miss_color(p, iy);
             alpha = miss.w;
-            frag = p.hasEnv ? radiance_from_env(p, ray.dir) : vec3(miss.x, miss.y, miss.z);
+            frag = p.hasEnv ? env : vec3(miss.x, miss.y, miss.z);
           } else {
-            frag = from_half(ray.tp) * radiance_from_env(p, ray.dir) * ray.misWeight;
+            frag = from_half(ray.tp) * env * ray.misWeight;
           }
           ray.tMax = -1.f;
         } else {
@@ -939,10 +964,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
     }
   }
   if (Count && L.counters) {
-    unsigned long long v[8] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps, cnt.cells, cyc[0], cyc[1], cyc[2]};
+    unsigned long long v[12] = {cnt.samples, cnt.mcs, cnt.rays, cnt.caps, cnt.cells, cyc[0], cyc[1], cyc[2],
+                                simt[0], simt[1], simt[2], simt[3]};
     // (per-lane counts are 32-bit; a lane processes far fewer than 2^32 events)
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 12; k++) {
       unsigned long long x = v[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);

@@ -179,11 +179,16 @@ typedef struct gbv_scene {
    [0] density samples, [1] macrocells entered with a non-zero majorant,
    [2] rays traced, [3] loop-cap events, [4] macrocells crossed (all),
    [5..7] SM cycles spent starting traces, traversing and shading, summed
-   over warps (only with GBV_RENDER_PROFILE=1 in the environment, else 0). */
+   over warps, [8] traversal iterations of warps and [9] tracing lanes
+   summed over them, [10] shading passes of warps and [11] shaded lanes
+   summed over them ([5..11] only with GBV_RENDER_PROFILE=1 in the
+   environment, else 0). */
 enum { GBV_COUNTER_SAMPLES = 0, GBV_COUNTER_MC_VISITS = 1, GBV_COUNTER_RAYS = 2,
        GBV_COUNTER_CAPS = 3, GBV_COUNTER_CELLS = 4, GBV_COUNTER_CYCLES_START = 5,
        GBV_COUNTER_CYCLES_TRAVERSE = 6, GBV_COUNTER_CYCLES_SHADE = 7,
-       GBV_NUM_COUNTERS = 8 };
+       GBV_COUNTER_TRAVERSE_ITERS = 8, GBV_COUNTER_TRAVERSE_LANES = 9,
+       GBV_COUNTER_SHADE_PASSES = 10, GBV_COUNTER_SHADE_LANES = 11,
+       GBV_NUM_COUNTERS = 12 };
 
 /* Env-map importance tables (d_cdf_y: H floats, d_cdf_x: W*H floats) from
    RGBA float texels.  Replaces EnvMapLight::computeCDFs
