@@ -7,8 +7,8 @@ and tests/test_gpu_bricks.py check both bit for bit):
 
 * brick         -- log2 of the brick edge in cells per axis of the voxel
   stores (where neighbouring cells sit in HBM);
-* blocks_per_sm -- resident 256-thread blocks per SM (3 or 4: the kernel is
-  compiled for both register budgets);
+* blocks_per_sm -- resident 256-thread blocks per SM (4, 5 or 6: the kernel
+  is compiled for each register budget);
 * threshold     -- a warp keeps traversing while at least this percentage of
   its busy lanes still traces, then shades together;
 * skip          -- empty macrocells a lane may cross in one traversal unit.
@@ -28,7 +28,7 @@ import json
 import os
 from pathlib import Path
 
-LAUNCH_CANDIDATES = [(b, t, k) for b in (3, 4) for t in (5, 15, 30) for k in (4, 8, 16)]
+LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (2, 5, 15) for k in (4, 8, 16)]
 BRICK_CANDIDATES = [(3, 3, 3), (2, 2, 2), (4, 4, 4), (4, 4, 2), (5, 3, 2)]
 
 

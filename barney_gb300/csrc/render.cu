@@ -336,7 +336,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
   b->format = scenes[0].format;
   b->layout = scenes[0].layout;
   b->totalTiles = starts[count];
-  b->occ = 4;
+  b->occ = 5;
   b->threshold = 5;
   b->skip = kSkipDefault;
   cudaGetDevice(&b->device);
@@ -360,8 +360,8 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
 }
 
 extern "C" gbv_status gbv_batch_set_launch(gbv_batch *b, int blocks_per_sm, int threshold_pct, int skip_cells) {
-  if (!b || blocks_per_sm < 3 || blocks_per_sm > 4 || threshold_pct < 1 || threshold_pct > 100 || skip_cells < 1)
-    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_set_launch: blocks 3..4, threshold 1..100, skip >= 1");
+  if (!b || blocks_per_sm < 4 || blocks_per_sm > 6 || threshold_pct < 1 || threshold_pct > 100 || skip_cells < 1)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_set_launch: blocks 4..6, threshold 1..100, skip >= 1");
   b->occ = blocks_per_sm;
   b->threshold = threshold_pct;
   b->skip = skip_cells;

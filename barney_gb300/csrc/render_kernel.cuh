@@ -1018,9 +1018,9 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   return st;
 }
 
-// GBV_RENDER_OCC=3 or 4 selects the resident blocks per SM the registers are
-// capped for (default 4: 32 warps per SM; the kernel is latency-bound and
-// gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
+// GBV_RENDER_OCC=4, 5 or 6 selects the resident blocks per SM the registers
+// are capped for (default 5: 40 warps per SM at 51 registers; the kernel is
+// latency-bound and gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
 // macrocells crossed per traversal step (default 8); GBV_RENDER_THRESH the
 // percentage of a warp's busy lanes that must still be tracing for the warp
 // to keep traversing before it shades and refills (default 5).
@@ -1063,14 +1063,15 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   p.threshold = th ? atoi(th) : 5;
   if (p.threshold < 1) p.threshold = 1;
   const char *oc = getenv("GBV_RENDER_OCC");
-  const int occ = oc ? atoi(oc) : 4;
-  if (occ == 3) return launch_render_t<Store, 3>(p, store, stream);
-  return launch_render_t<Store, 4>(p, store, stream);
+  const int occ = oc ? atoi(oc) : 5;
+  if (occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
+  if (occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
+  return launch_render_t<Store, 5>(p, store, stream);
 }
 
 template <class Store>
 inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cudaStream_t stream, int *pool) {
-  // fixed launch settings (results do not depend on them): 4 resident
+  // fixed launch settings (results do not depend on them): 5 resident
   // blocks per SM, 8 cells per traversal step, no shared-memory staging
   p.skip = kSkipDefault;
   p.threshold = 5;
@@ -1082,7 +1083,7 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st != GBV_OK) return st;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 5, false, true>, kThreads, 0);
   const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
@@ -1092,9 +1093,9 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "gbv_render_noalloc: clearing the tile pool");
   if (st != GBV_OK) return st;
   if (p.counters)
-    render_kernel<Store, 4, false, true><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
+    render_kernel<Store, 5, false, true><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
   else
-    render_kernel<Store, 4, false, false><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
+    render_kernel<Store, 5, false, false><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
   return check_launch("render_kernel (noalloc)");
 }
 
@@ -1135,8 +1136,9 @@ inline gbv_status batch_launch(const gbv_batch *b, RenderParams L, cudaStream_t 
           L, b->d_items, b->d_tileStart, b->count, b->d_pool);                                             \
   }
   switch (b->occ) {
-    case 3: GBV_BATCH_LAUNCH(3) break;
-    default: GBV_BATCH_LAUNCH(4) break;
+    case 4: GBV_BATCH_LAUNCH(4) break;
+    case 6: GBV_BATCH_LAUNCH(6) break;
+    default: GBV_BATCH_LAUNCH(5) break;
   }
 #undef GBV_BATCH_LAUNCH
   return check_launch("render_kernel (batch)");

@@ -37,7 +37,7 @@ def test_batch_equals_separate_renders(cuda):
         np.testing.assert_array_equal(acc.cpu().numpy().view(np.uint32), ref.cpu().numpy().view(np.uint32))
 
 
-@pytest.mark.parametrize("shape", [(3, 30, 4), (3, 5, 8), (4, 90, 16)])
+@pytest.mark.parametrize("shape", [(4, 30, 4), (5, 5, 8), (6, 90, 16)])
 def test_launch_shapes_do_not_change_results(cuda, shape):
     import torch
     items = small_items()
@@ -82,7 +82,7 @@ def test_autotuner_picks_shapes_caches_them_and_keeps_images(cuda, tmp_path, mon
     ref = GpuBatch(items)
     ref.render(spp=3)
     bricks = [(3, 3, 3), (2, 2, 2), (4, 3, 2)]
-    launches = [(3, 5, 8), (4, 30, 4)]
+    launches = [(5, 5, 8), (4, 30, 4)]
     b, rec = autotune.tuned_batch(items, 3, bricks=bricks, reps=1)
     assert not rec["cached"] and rec["brick"] in bricks
     assert (tmp_path / "tune.json").exists()
