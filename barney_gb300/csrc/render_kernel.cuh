@@ -165,6 +165,11 @@ __device__ __forceinline__ float spherical_phi(vec3 v) {
   float p = atan2f(v.y, v.x);
   return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
 }
+// (theta, phi) of a direction in the env map's frame; one out-of-line copy
+// of acosf and atan2f for the env-map pdf and the env lookup
+static __device__ __noinline__ float2 spherical_theta_phi(vec3 v) {
+  return make_float2(spherical_theta(v), spherical_phi(v));
+}
 // EnvMap.h:98-134
 __device__ __forceinline__ float cdf_get_pdf(int position, const float *cdf, int N) {
   float at = __ldg(cdf + position);
@@ -250,9 +255,9 @@ __device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, floa
 static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   if (!p.hasEnv) return kOneOverFourPi;
   const EnvDev &e = p.env;
-  vec3 localDir = xfm_vector(e.toLocal, dir);
-  float theta = spherical_theta(localDir);
-  float phi = spherical_phi(localDir);
+  const float2 tp = spherical_theta_phi(xfm_vector(e.toLocal, dir));
+  float theta = tp.x;
+  float phi = tp.y;
   float u = phi * kOneOverTwoPi, v = theta * kOneOverPi;
   int px = (int)clampv(u * (float)e.W, 0.f, (float)e.W - 1.f);
   int py = (int)clampv(v * (float)e.H, 0.f, (float)e.H - 1.f);
@@ -277,12 +282,15 @@ static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Ran
   s.radiance = e.scale * vec3(t.x, t.y, t.z);
   const float phi = kTwoPi * sx;
   const float theta = kPi * sy;
+  float sinTheta, cosTheta, sinPhi, cosPhi;
+  sincosf(theta, &sinTheta, &cosTheta);
+  sincosf(phi, &sinPhi, &cosPhi);
   vec3 d;
-  d.z = cosf(theta);
-  d.x = cosf(phi) * sinf(theta);
-  d.y = sinf(phi) * sinf(theta);
+  d.z = cosTheta;
+  d.x = cosPhi * sinTheta;
+  d.y = sinPhi * sinTheta;
   s.direction = xfm_vector(e.toWorld, d);
-  s.pdf = pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta));
+  s.pdf = pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinTheta);
   s.distance = __int_as_float(0x7f800000);
   return s;
 }
@@ -376,8 +384,9 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
 static __device__ __noinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
   if (p.hasEnv) {
     vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
-    float theta = spherical_theta(d);
-    float phi = spherical_phi(d);
+    const float2 tp = spherical_theta_phi(d);
+    float theta = tp.x;
+    float phi = tp.y;
     const float invPi = 1.f / (float)3.14159265358979323846;
     const float inv2Pi = 1.f / (2.f * (float)3.14159265358979323846);
     float4 c = tex2D(p.env, phi * inv2Pi, theta * invPi);
@@ -410,7 +419,9 @@ static __device__ __noinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Ran
   }
   float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
   float phi = kTwoPi * u1;
-  vec3 local(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
+  float sinPhi, cosPhi;
+  sincosf(phi, &sinPhi, &cosPhi);
+  vec3 local(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
   vec3 w = normalize(wi_in);
   vec3 u, v;
   if (fabsf(w.x) > 0.1f) u = normalize(cross(vec3(0.f, 1.f, 0.f), w));
