@@ -98,6 +98,16 @@ __global__ void tonemap_kernel(const float4 *__restrict__ accum, long long n, fl
       (make_8bit(c.x) << 0) + (make_8bit(c.y) << 8) + (make_8bit(c.z) << 16) + (make_8bit(c.w) << 24);
 }
 
+__global__ void sincos_angle_kernel(const float *__restrict__ x, long long n, float *__restrict__ sn,
+                                    float *__restrict__ cs) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s, c;
+  sincos_angle(x[i], s, c);
+  sn[i] = s;
+  cs[i] = c;
+}
+
 }  // namespace gbv
 
 using namespace gbv;
@@ -158,6 +168,17 @@ gbv_status gbv_tonemap(const float *d_accum, int width, int height, int accum_id
   tonemap_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float4 *>(d_accum), n, accumScale, format, d_out);
   return check_launch("tonemap_kernel");
+}
+
+gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn, float *cs, int on_device, void *stream) {
+  if (!x || !sn || !cs || n < 0) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_selftest_sincos: bad argument");
+  if (n == 0) return GBV_OK;
+  if (!on_device) {
+    for (long long i = 0; i < n; i++) sincos_angle(x[i], sn[i], cs[i]);
+    return GBV_OK;
+  }
+  sincos_angle_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, n, sn, cs);
+  return check_launch("sincos_angle_kernel");
 }
 
 }  // extern "C"

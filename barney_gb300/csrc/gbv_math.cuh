@@ -188,6 +188,35 @@ GBV_HD float fastLog(float f) {
 
 GBV_HD float lerp_l(float f, float a, float b) { return (1.f - f) * a + f * b; }
 
+// Sine and cosine of x in [-pi/4, 2pi + pi/4], the range of the angles the
+// renderer forms from [0, 1) random numbers (env-map directions and pdfs,
+// phase-function azimuths).  Cody-Waite reduction (Cody & Waite, Software
+// Manual for the Elementary Functions, 1980): r = x - k pi/2 with pi/2 split
+// into three floats, the first two short enough that k times them is exact,
+// so r is accurate to its last bit even next to a multiple of pi/2; then the
+// Taylor polynomials of sin and cos on |r| <= pi/4 (truncation error below
+// 3e-9) in Horner form.  No large-argument path: a few dozen instructions
+// where a general sincosf carries a long one.  Same arithmetic on host and
+// device (no contraction), so both give identical results.
+GBV_HD void sincos_angle(float x, float &sn, float &cs) {
+  const float kTwoOverPi = 0.636619772f;
+  const float kPio2A = 0x1.92p+0f;       // 201/128
+  const float kPio2B = 0x1.fb544p-12f;   // next 21 bits of pi/2
+  const float kPio2C = 0x1.0b4612p-34f;  // the rest, rounded to float
+  const float k = rintf(x * kTwoOverPi);
+  const float r = ((x - k * kPio2A) - k * kPio2B) - k * kPio2C;
+  const float r2 = r * r;
+  const float ps = r + (r * r2) * (-1.f / 6.f + r2 * (1.f / 120.f + r2 * (-1.f / 5040.f + r2 * (1.f / 362880.f))));
+  const float pc =
+      1.f - .5f * r2 + (r2 * r2) * (1.f / 24.f + r2 * (-1.f / 720.f + r2 * (1.f / 40320.f + r2 * (-1.f / 3628800.f))));
+  switch ((int)k & 3) {
+    case 0: sn = ps; cs = pc; break;
+    case 1: sn = pc; cs = -ps; break;
+    case 2: sn = -ps; cs = -pc; break;
+    default: sn = -pc; cs = ps; break;
+  }
+}
+
 // rtcore/embree/Texture.cpp:324-336
 GBV_HD void lerp_coords(int N, float tc, int &i0, int &i1, float &f) {
   if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; return; }

@@ -265,7 +265,9 @@ static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
   float rel_y = ((float)py + .5f) / (float)e.H;
   const float theta2 = kPi * rel_y;
-  return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinf(theta2));
+  float sinTheta2, cosTheta2;
+  sincos_angle(theta2, sinTheta2, cosTheta2);
+  return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinTheta2);
 }
 // EnvMap.h:198-250
 static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Random &r) {
@@ -283,8 +285,8 @@ static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Ran
   const float phi = kTwoPi * sx;
   const float theta = kPi * sy;
   float sinTheta, cosTheta, sinPhi, cosPhi;
-  sincosf(theta, &sinTheta, &cosTheta);
-  sincosf(phi, &sinPhi, &cosPhi);
+  sincos_angle(theta, sinTheta, cosTheta);  // theta in [0, pi]
+  sincos_angle(phi, sinPhi, cosPhi);        // phi in [0, 2 pi]
   vec3 d;
   d.z = cosTheta;
   d.x = cosPhi * sinTheta;
@@ -420,7 +422,7 @@ static __device__ __noinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Ran
   float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
   float phi = kTwoPi * u1;
   float sinPhi, cosPhi;
-  sincosf(phi, &sinPhi, &cosPhi);
+  sincos_angle(phi, sinPhi, cosPhi);  // phi in [0, 2 pi)
   vec3 local(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
   vec3 w = normalize(wi_in);
   vec3 u, v;

@@ -319,6 +319,17 @@ gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
                                float noise_amplitude, int fbm_octaves,
                                float fbm_amplitude, int nthreads, float *out);
 
+/* ------------------------------------------------------------------------
+ * Self-test (no counterpart in the reference).
+ * ------------------------------------------------------------------------ */
+
+/* The renderer's bounded sine/cosine (angles in [-pi/4, 2pi + pi/4]) for n
+   arguments: on the host (on_device = 0; host pointers) or in a kernel on
+   `stream` (on_device = 1; device pointers).  Both give identical results;
+   tests check them against float64 sine and cosine. */
+gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn,
+                               float *cs, int on_device, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

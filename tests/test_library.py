@@ -128,3 +128,31 @@ def test_brick_shape_out_of_range_is_rejected(shape):
     st = N.lib().gbv_brick_store_bytes_shaped(N.ivec(64, 64, 64), N.GBV_VOXEL_F32, N.ivec(*shape), C.byref(vb), None)
     assert st == N.GBV_ERROR_INVALID_ARGUMENT
     assert "brick_log2" in N.lib().gbv_last_error().decode()
+
+
+def _angle_sweep():
+    # a dense sweep of [-pi/4, 2 pi + pi/4] plus every float within 2000 ulp
+    # of each multiple of pi/2 in it (where sine or cosine crosses zero)
+    x = np.linspace(-np.pi / 4, 2 * np.pi + np.pi / 4, 2_000_001, dtype=np.float64).astype(np.float32)
+    near = []
+    for k in range(5):
+        c = np.float32(k * np.pi / 2)
+        i = c.view(np.int32) if c != 0 else np.int32(0)
+        ints = np.arange(max(int(i) - 2000, 0), int(i) + 2000, dtype=np.int32)
+        near.append(ints.view(np.float32))
+        if k == 0:
+            near.append(-ints[1:].view(np.float32))
+    return np.concatenate([x] + near)
+
+
+def test_bounded_sincos_within_two_ulp():
+    x = _angle_sweep()
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    assert N.lib().gbv_selftest_sincos(x.ctypes.data, x.size, s.ctypes.data, c.ctypes.data, 0, None) == N.GBV_OK
+    for got, ref in ((s, np.sin(x.astype(np.float64))), (c, np.cos(x.astype(np.float64)))):
+        r32 = np.abs(ref).astype(np.float32)
+        ulp = np.spacing(r32).astype(np.float64)
+        ulp[r32 == 0] = np.float64(np.finfo(np.float32).smallest_subnormal)
+        err = np.abs(got.astype(np.float64) - ref) / ulp
+        assert err.max() <= 2.0, (err.max(), x[err.argmax()])
