@@ -752,7 +752,9 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
 // tiles are numbered consecutively (tileStart[] holds the prefix sums); a
 // lane reads the scene of the pixel it owns.  Otherwise the launch renders
 // the one scene `p0`.  Launch-wide settings (passes, thresholds, counters)
-// always come from p0.  Count: whether to count events (see Ctr).
+// always come from p0.  Count: whether to count events (see Ctr) and, with
+// GBV_RENDER_PROFILE, cycles and lanes per phase (the timed kernel, Count =
+// false, carries no profiling code).
 // p0 is __grid_constant__ so that out-of-line helpers can take it by
 // reference without a copy to local memory.
 template <class Store, int MinBlocks, bool Batch, bool Count>
@@ -867,7 +869,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
     }
     if (poolDone && __all_sync(FULL, !hasPixel)) break;
     const RenderParams &p = Batch ? items[item] : p0;
-    long long c0 = L.profile ? clock64() : 0;
+    long long c0 = (Count && L.profile) ? clock64() : 0;
     if (hasPixel && tstate == NEED) {
       if (newSample) {
         generate_primary(p, ix, iy, L.accumIdStart + s, ray);
@@ -888,7 +890,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
     }
     // ---- phase 2: traverse while enough of the warp's busy lanes trace ----
     long long c1 = 0;
-    if (L.profile) {
+    if (Count && L.profile) {
       __syncwarp();
       c1 = clock64();
       if (lane == 0) cyc[0] += (unsigned long long)(c1 - c0);
@@ -898,7 +900,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       while (true) {
         const int tracing = __popc(__ballot_sync(FULL, tstate == TRACING));
         if (tracing == 0 || tracing * 100 < busy * L.threshold) break;
-        if (L.profile && lane == 0) {
+        if (Count && L.profile && lane == 0) {
           simt[0]++;
           simt[1] += (unsigned)tracing;
         }
@@ -909,12 +911,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
     }
     // ---- phase 3: shade the finished traces (bounce(), shadeRays.cu:477-878) ----
     long long c2 = 0;
-    if (L.profile) {
+    if (Count && L.profile) {
       __syncwarp();
       c2 = clock64();
       if (lane == 0) cyc[1] += (unsigned long long)(c2 - c1);
     }
-    if (L.profile) {
+    if (Count && L.profile) {
       const unsigned shading = __popc(__ballot_sync(FULL, tstate == DONE));
       if (lane == 0 && shading) {
         simt[2]++;
@@ -971,7 +973,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         }
       }
     }
-    if (L.profile) {
+    if (Count && L.profile) {
       __syncwarp();
       if (lane == 0) cyc[2] += (unsigned long long)(clock64() - c2);
     }

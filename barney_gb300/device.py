@@ -182,6 +182,18 @@ class GpuScene:
                                          _stream()), "gbv_render_tiles")
         return accum
 
+    def iso_intersect(self, rays, iso: float):
+        """First crossings of the iso value by rays, a (n, 8) float32 CUDA
+        tensor (org xyz, tmax, dir xyz, unused); returns (n, 8): t, P xyz,
+        N xyz, hit (1/0)."""
+        import torch
+        rays = rays.contiguous().float()
+        hits = torch.empty_like(rays)
+        rec = self.record()
+        N.check(N.lib().gbv_iso_intersect(C.byref(rec), _ptr(self.ranges), float(iso), _ptr(rays), rays.shape[0],
+                                          _ptr(hits), _stream()), "gbv_iso_intersect")
+        return hits
+
     def tonemap(self, accum, accum_id: int, fmt: int = N.GBV_FB_FLOAT4):
         import torch
         h, w, _ = accum.shape

@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--format", default="f32", choices=["f32", "f16", "bf16", "u8"])
     ap.add_argument("--dims", type=int, default=512)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--quick", action="store_true", help="skip the FP16 and adjoint extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()

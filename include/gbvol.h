@@ -320,6 +320,27 @@ gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
                                float fbm_amplitude, int nthreads, float *out);
 
 /* ------------------------------------------------------------------------
+ * Iso-surface ray queries.
+ * ------------------------------------------------------------------------ */
+
+/* For each of num_rays rays, the first crossing of the scene field's
+   iso_value, found as the reference's iso-surface geometry finds it: the
+   macrocell DDA, cells whose scalar range (d_ranges, from
+   gbv_build_mc_ranges or gbv_build_mc_ranges_from_store) holds the value cut
+   into 10 sub-steps, linear interpolation inside the first bracketing
+   sub-step, and a central-difference normal.  Any voxel layout, format and
+   brick shape of the scene.
+   d_rays: two float4 per ray, (org.xyz, tmax) and (dir.xyz, unused).
+   d_hits: two float4 per ray, (t, P.xyz) and (N.xyz, 1) on a hit (N unit
+   length), all zero on a miss.
+   Replaces MCIsoSurfaceAccel::isProg up to the hit record
+   (barney/volume/MCAccelerator.h:338-503); the material, opacity and hit-ID
+   parts of it belong to the surface path, which is not on this path. */
+gbv_status gbv_iso_intersect(const gbv_scene *scene, const float *d_ranges,
+                             float iso_value, const float *d_rays,
+                             long long num_rays, float *d_hits, void *stream);
+
+/* ------------------------------------------------------------------------
  * Self-test (no counterpart in the reference).
  * ------------------------------------------------------------------------ */
 

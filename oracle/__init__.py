@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
             "orc_mc_ranges": (None, [vp, vp, i, vp]),
             "orc_majorants": (None, [vp, i, vp, i, f, f, f, vp]),
             "orc_trace_ray": (i, [sp, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float), vp]),
+            "orc_iso_intersect": (i, [sp, vp, f, vp, vp, f, vp]),
             "orc_render": (None, [sp, vp, i, i, i, i, i, i, C.POINTER(OrcStats)]),
             "orc_tonemap": (None, [vp, i, i, i, i, vp]),
             "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
@@ -152,6 +153,21 @@ class Oracle:
         M = self.mc_dims()
         out = np.empty((M[0] * M[1] * M[2], 2), dtype=np.float32)
         lib().orc_mc_ranges(_p(self.scalars), (C.c_int * 3)(*self.rec.dims), self.s.cells_per_mc, _p(out))
+        return out
+
+    def iso_intersect(self, rays: np.ndarray, iso: float, ranges=None) -> np.ndarray:
+        """rays: (n, 8) float32 (org xyz, tmax, dir xyz, unused).  Returns (n, 8):
+        t, P xyz, N xyz, hit (1/0) -- the layout of gbv_iso_intersect."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros((rays.shape[0], 8), np.float32)
+        rp = None if ranges is None else _p(np.ascontiguousarray(ranges, np.float32))
+        o7 = np.zeros(7, np.float32)
+        for k in range(rays.shape[0]):
+            h = lib().orc_iso_intersect(C.byref(self.rec), rp, iso, _p(rays[k, 0:3].copy()), _p(rays[k, 4:7].copy()),
+                                        float(rays[k, 3]), _p(o7))
+            if h:
+                out[k, :7] = o7
+                out[k, 7] = 1.0
         return out
 
     def majorants_of(self, ranges: np.ndarray) -> np.ndarray:

@@ -1316,6 +1316,144 @@ int orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3], fl
   return h ? 1 : 0;
 }
 
+// MCIsoSurfaceAccel::isProg (barney/volume/MCAccelerator.h:338-567) over
+// dda::dda3 (DDA.h:65-206), as the embree backend dispatches it (tmin 0,
+// tmax ray.tMax, identity instance).  The trace direction has zero
+// components replaced by 1e-6 (traceRays.dev.cu:41-44).  Per macrocell whose
+// scalar range holds the iso value, the cell's t range is cut into 10
+// sub-steps; the first sub-step whose end values bracket the iso value gives
+// t by linear interpolation.  The normal is the central difference of the
+// field at +-delta per axis (a one-sided difference where a sample falls
+// outside the field).  out: t, P[3], N[3] (N normalized).
+int orc_iso_intersect(const orc_scene *s, const float *ranges, float iso, const float org_[3], const float dir_[3],
+                      float tmax, float out[7]) {
+  const Field F = make_field(s);
+  int M[3];
+  mc_dims_of(F.N, s->cells_per_mc, M);
+  if (M[0] <= 0 || M[1] <= 0 || M[2] <= 0) return 0;
+  std::vector<float> own;
+  if (!ranges) {
+    own.resize((size_t)2 * M[0] * M[1] * M[2]);
+    orc_mc_ranges(s->scalars, s->dims, s->cells_per_mc, own.data());
+    ranges = own.data();
+  }
+  const V3<float> org(org_[0], org_[1], org_[2]);
+  V3<float> dir(dir_[0], dir_[1], dir_[2]);
+  if (dir.x == 0.f) dir.x = 1e-6f;
+  if (dir.y == 0.f) dir.y = 1e-6f;
+  if (dir.z == 0.f) dir.z = 1e-6f;
+  float tLo = 0.f, tHi = tmax;
+  if (!boxTest<float>(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return 0;
+  const V3<float> mcOrigin = F.boundsLo;
+  const V3<float> mcSpacing = V3<float>((float)s->cells_per_mc) * F.spacing;
+  const V3<float> dda_org = (org - mcOrigin) * rcp(mcSpacing);
+  const V3<float> dda_dir = dir * rcp(mcSpacing);
+  const float tMax = tHi;
+  // ---- dda3 ----
+  const V3<float> f_size((float)M[0], (float)M[1], (float)M[2]);
+  const V3<float> rcp_dir = rcp(dda_dir);
+  V3<float> t_lo = (V3<float>(0.f) - dda_org) * rcp(dda_dir);
+  V3<float> t_hi = (f_size - dda_org) * rcp(dda_dir);
+  V3<float> t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  for (int a = 0; a < 3; a++) {
+    if (dda_dir[a] == 0.f) {
+      if (dda_org[a] < 0.f || dda_org[a] > f_size[a]) return 0;
+      t_nr[a] = -INF;
+      t_fr[a] = +INF;
+    }
+  }
+  const float ray_t0 = mx(0.f, reduce_max(t_nr));
+  const float ray_t1 = mn(tMax, reduce_min(t_fr));
+  if (ray_t0 > ray_t1) return 0;
+  const V3<float> oiv = dda_org + ray_t0 * dda_dir;
+  const V3<float> f_cell = vmax(V3<float>(0.f), vmin(f_size - V3<float>(1.f), vfloor(oiv)));
+  const V3<float> f_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
+                        dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
+  const V3<float> t_step = vabs(rcp_dir);
+  V3<float> t_next;
+  for (int a = 0; a < 3; a++)
+    t_next[a] = (dda_dir[a] == 0.f) ? INF : (std::fabs(f_end[a] - oiv[a]) * t_step[a]);
+  int stop[3], delta[3], cell[3];
+  for (int a = 0; a < 3; a++) {
+    stop[a] = dda_dir[a] > 0.f ? M[a] : -1;
+    delta[a] = dda_dir[a] > 0.f ? +1 : -1;
+    cell[a] = int(f_cell[a]);
+  }
+  float tHit = tmax;
+  float next_cell_begin = 0.f;
+  const int maxIter = M[0] + M[1] + M[2] + 8;
+  bool stopped = false;
+  for (int it = 0; it < maxIter && !stopped; it++) {
+    const float t_closest = reduce_min(t_next);
+    const float t0 = ray_t0 + next_cell_begin;
+    const float t1 = ray_t0 + mn(t_closest, tMax);
+    // ---- the iso lambda (MCAccelerator.h:405-471) ----
+    [&]() {
+      if (t0 >= mn(t1, tmax)) return;
+      const size_t ci = (size_t)cell[0] + (size_t)M[0] * ((size_t)cell[1] + (size_t)M[1] * cell[2]);
+      const float vlo = ranges[2 * ci], vhi = ranges[2 * ci + 1];
+      if (!(iso >= vlo && iso <= vhi)) return;
+      float tt1 = t0;
+      float ff1 = sample_field<float>(F, org + tt1 * dir);
+      for (int i = 1; i <= 10; i++) {
+        const float tt0 = tt1;
+        const float ff0 = ff1;
+        tt1 = lerp_l((float)i / 10.f, t0, t1);
+        ff1 = sample_field<float>(F, org + tt1 * dir);
+        if (std::isnan(ff0) || std::isnan(ff1)) continue;
+        const float lo = mn(ff0, ff1), hi = mx(ff0, ff1);
+        if (iso >= lo && iso <= hi) {
+          float t = (iso - ff0) / (ff1 - ff0);
+          t = lerp_l(t, tt0, tt1);
+          tHit = mn(tHit, t);
+          if (tHit < tmax) {
+            stopped = true;
+            return;
+          }
+        }
+      }
+    }();
+    if (stopped) break;
+    next_cell_begin = t_closest;
+    bool done = false;
+    for (int a = 0; a < 3 && !done; a++) {
+      if (t_next[a] == t_closest) {
+        t_next[a] += t_step[a];
+        cell[a] += delta[a];
+        if (cell[a] == stop[a]) done = true;
+      }
+    }
+    if (done) break;
+  }
+  if (!(tHit < tmax)) return 0;
+  // ---- normal (MCAccelerator.h:476-503) ----
+  const V3<float> P = org + tHit * dir;
+  const V3<float> size = F.boundsHi - F.boundsLo;
+  const float d = length(size) * .1f / float(M[0] + M[1] + M[2]);
+  const float fP = sample_field<float>(F, P);
+  float fx0 = sample_field<float>(F, P + V3<float>(-d, 0.f, 0.f));
+  float fx1 = sample_field<float>(F, P + V3<float>(+d, 0.f, 0.f));
+  float fy0 = sample_field<float>(F, P + V3<float>(0.f, -d, 0.f));
+  float fy1 = sample_field<float>(F, P + V3<float>(0.f, +d, 0.f));
+  float fz0 = sample_field<float>(F, P + V3<float>(0.f, 0.f, -d));
+  float fz1 = sample_field<float>(F, P + V3<float>(0.f, 0.f, +d));
+  float dx = 2.f, dy = 2.f, dz = 2.f;
+  if (std::isnan(fx0)) { dx -= 1.f; fx0 = fP; }
+  if (std::isnan(fx1)) { dx -= 1.f; fx1 = fP; }
+  if (std::isnan(fy0)) { dy -= 1.f; fy0 = fP; }
+  if (std::isnan(fy1)) { dy -= 1.f; fy1 = fP; }
+  if (std::isnan(fz0)) { dz -= 1.f; fz0 = fP; }
+  if (std::isnan(fz1)) { dz -= 1.f; fz1 = fP; }
+  V3<float> N(dx == 0.f ? 0.f : (fx1 - fx0) / dx, dy == 0.f ? 0.f : (fy1 - fy0) / dy,
+              dz == 0.f ? 0.f : (fz1 - fz0) / dz);
+  if (N == V3<float>(0.f)) N = -normalize(dir);
+  N = normalize(N);
+  out[0] = tHit;
+  out[1] = P.x; out[2] = P.y; out[3] = P.z;
+  out[4] = N.x; out[5] = N.y; out[6] = N.z;
+  return 1;
+}
+
 void orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp, int use_double, int nthreads,
                 int row0, int row1, orc_stats *stats) {
   Scene S;

@@ -86,6 +86,12 @@ void  orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n,
 int   orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3],
                     float tmax, uint64_t *seed_state, float *t_hit, float rgb[3]);
 
+/* --- iso-surface ray query (MCIsoSurfaceAccel::isProg); ranges: per-MC
+       (min, max) or null; out: t, P[3], N[3]; returns 1 on a hit --- */
+int   orc_iso_intersect(const orc_scene *s, const float *ranges, float iso,
+                        const float org[3], const float dir[3], float tmax,
+                        float out[7]);
+
 /* --- full render: bnRender's generate/trace/shade loop for `spp`
        consecutive accumulation passes starting at accum_id_start.
        accum: width*height RGBA, row-major, y=0 the bottom row.

@@ -102,3 +102,31 @@ def test_multi_scatter_adds_light():
     s.max_volume_bounces = 4
     b = oracle.Oracle(s).render()[..., :3].mean()
     assert b > a
+
+
+def test_iso_plane_of_a_linear_field():
+    """v(x, y, z) = x + 0.5 on the unit cube: the iso surface v = c is the
+    plane x = c - 0.5, and trilinear interpolation of a linear field is
+    exact, so rays hit it at the analytic t with normal +x."""
+    n = 33
+    x = np.linspace(-0.5, 0.5, n, dtype=np.float64)
+    vol = np.broadcast_to((x + 0.5)[None, None, :], (n, n, n)).astype(np.float32).copy()
+    s = scenes.Scene(scalars=vol, tf=scenes.tf_ramp(16), cells_per_mc=8)
+    o = oracle.Oracle(s)
+    rng = np.random.default_rng(0)
+    k = 200
+    # rays from x = -0.7 that stay inside |y|, |z| < 0.5 up to the far face
+    org = np.stack([np.full(k, -0.7), rng.uniform(-0.3, 0.3, k), rng.uniform(-0.3, 0.3, k)], 1)
+    d = np.stack([np.ones(k), rng.uniform(-0.1, 0.1, k), rng.uniform(-0.1, 0.1, k)], 1)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((k, 8), np.float32)
+    rays[:, 0:3], rays[:, 3], rays[:, 4:7] = org, 1e30, d
+    for c in (0.25, 0.5, 0.8):
+        h = o.iso_intersect(rays, c, ranges=o.mc_ranges())
+        assert h[:, 7].all()
+        t_exact = ((c - 0.5) - org[:, 0]) / d[:, 0]
+        np.testing.assert_allclose(h[:, 0], t_exact, rtol=2e-6, atol=2e-6)
+        np.testing.assert_allclose(h[:, 1], c - 0.5, atol=2e-6)
+        np.testing.assert_allclose(h[:, 4:7], np.tile([1.0, 0.0, 0.0], (k, 1)), atol=1e-5)
+    # the plane lies outside [0, 1]: no hit
+    assert not o.iso_intersect(rays, 1.5, ranges=o.mc_ranges())[:, 7].any()
