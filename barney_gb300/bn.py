@@ -17,9 +17,12 @@ from .scenes import Scene
 BN_OBJECT = 2
 BN_FLOAT32 = 180
 BN_FLOAT4 = 183
+BN_UINT8 = 110
+BN_UINT16 = 130
 BN_UFIXED8 = 300
 BN_UFIXED8_RGBA = 301
 BN_UFIXED8_RGBA_SRGB = 302
+BN_UFIXED16 = 303
 BN_FB_COLOR = 1
 BN_TEXTURE_NEAREST, BN_TEXTURE_LINEAR = 0, 1
 
@@ -127,10 +130,11 @@ class BarneySession:
         self.close()
 
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
-                    layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None):
+                    layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None,
+                    texel_format: int = BN_FLOAT32):
         L, ctx, s = self.L, self.ctx, scene
         nx, ny, nz = s.dims
-        td = _ok(L.bnTextureData3DCreate(ctx, 0, BN_FLOAT32, nx, ny, nz, C.c_void_p(scalars_ptr)),
+        td = _ok(L.bnTextureData3DCreate(ctx, 0, texel_format, nx, ny, nz, C.c_void_p(scalars_ptr)),
                  "bnTextureData3DCreate")
         sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"structured"), "bnScalarFieldCreate")
         L.bnSetObject(sf, b"textureData", td)

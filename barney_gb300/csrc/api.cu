@@ -98,6 +98,17 @@ __global__ void tonemap_kernel(const float4 *__restrict__ accum, long long n, fl
       (make_8bit(c.x) << 0) + (make_8bit(c.y) << 8) + (make_8bit(c.z) << 16) + (make_8bit(c.w) << 24);
 }
 
+// Normalised integer texels (cudaReadModeNormalizedFloat of the reference's
+// CUDA texture objects, rtcore/cudaCommon/TextureData.cu:34-39; the CPU
+// backend's getTexel<unsigned char>, rtcore/embree/Texture.cpp:216-225):
+// v / 255 or v / 65535, one IEEE division per texel.
+template <typename T>
+__global__ void normalize_texels_kernel(const T *__restrict__ in, long long n, float scale_max,
+                                        float *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i] / scale_max;
+}
+
 __global__ void sincos_angle_kernel(const float *__restrict__ x, long long n, float *__restrict__ sn,
                                     float *__restrict__ cs) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -179,6 +190,20 @@ gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn, float *cs
   }
   sincos_angle_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, n, sn, cs);
   return check_launch("sincos_angle_kernel");
+}
+
+gbv_status gbv_normalize_texels(const void *d_texels, int bits, long long n, float *d_scalars, void *stream) {
+  if (!d_texels || !d_scalars || n < 0 || (bits != 8 && bits != 16))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_normalize_texels: bad argument (bits must be 8 or 16)");
+  if (n == 0) return GBV_OK;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (bits == 8)
+    normalize_texels_kernel<uint8_t><<<blocks, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const uint8_t *>(d_texels), n, 255.f, d_scalars);
+  else
+    normalize_texels_kernel<uint16_t><<<blocks, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const uint16_t *>(d_texels), n, 65535.f, d_scalars);
+  return check_launch("normalize_texels_kernel");
 }
 
 }  // extern "C"

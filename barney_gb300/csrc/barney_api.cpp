@@ -534,13 +534,13 @@ BNTextureData bnTextureData3DCreate(BNContext context, int, BNDataType texelForm
     cudaStreamSynchronize(c->stream);
   } else if (texelFormat == BN_UFIXED8 || texelFormat == BN_UINT8 || texelFormat == BN_UFIXED16 ||
              texelFormat == BN_UINT16) {
-    // normalised integer texels read as v/max (rtcore/cudaCommon/TextureData.cu:34-39)
-    std::vector<float> f(n);
-    if (texelFormat == BN_UFIXED8 || texelFormat == BN_UINT8)
-      for (size_t i = 0; i < n; i++) f[i] = (float)((const uint8_t *)items)[i] / 255.f;
-    else
-      for (size_t i = 0; i < n; i++) f[i] = (float)((const uint16_t *)items)[i] / 65535.f;
-    if (cudaMemcpy(td->scalars.p, f.data(), n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+    // normalised integer texels: upload the raw texels, normalise on the device
+    const int bits = (texelFormat == BN_UFIXED8 || texelFormat == BN_UINT8) ? 8 : 16;
+    DevBuf<unsigned char> raw;
+    if (!raw.alloc(n * (bits / 8))) return nullptr;
+    if (cudaMemcpyAsync(raw.p, items, n * (bits / 8), cudaMemcpyDefault, c->stream) != cudaSuccess ||
+        gbv_normalize_texels(raw.p, bits, (long long)n, td->scalars.p, c->stream) != GBV_OK ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
       fail("texel upload failed");
       return nullptr;
     }

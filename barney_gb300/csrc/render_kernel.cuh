@@ -743,7 +743,7 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
   ray.org = p.lens00;
   ray.dir = normalize(d);
   ray.tMax = 1e30f;
-  ray.tp = to_half(vec3(1.f));
+  ray.tp = vec3h{0x3c00, 0x3c00, 0x3c00};  // 1.0 in half
   ray.misWeight = 0.f;
   ray.numVolumeBounces = 0;
 }

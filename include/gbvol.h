@@ -129,6 +129,13 @@ gbv_status gbv_build_mc_ranges_from_store_shaped(const void *d_voxels,
                                                  int cells_per_mc, float *d_ranges,
                                                  void *stream);
 
+/* Normalised 8- or 16-bit unsigned texels (bits = 8 or 16) to FP32 scalars
+   v / 255 or v / 65535, on the device.  Replaces the normalised-float texture
+   reads of integer texel formats (rtcore/cudaCommon/TextureData.cu:34-39,
+   rtcore/embree/Texture.cpp:216-225) for BN_UFIXED8 / BN_UFIXED16 fields. */
+gbv_status gbv_normalize_texels(const void *d_texels, int bits, long long n,
+                                float *d_scalars, void *stream);
+
 /* ------------------------------------------------------------------------
  * Scene description for rendering (device pointers where marked d_).
  * ------------------------------------------------------------------------ */

@@ -67,3 +67,23 @@ def test_bn_errors_are_recorded(cuda):
         fb = L.bnFrameBufferCreate(ses.ctx, 0)
         L.bnFrameBufferResize(fb, 123, 8, 8, 1)
         assert "unsupported color format" in bn.last_error()
+
+
+@pytest.mark.parametrize("bits", [8, 16])
+def test_bn_integer_texels_normalised_on_device(cuda, bits):
+    """UFIXED8/UFIXED16 fields read v/255 or v/65535 (normalised texture
+    reads): the frame equals the one of the FP32 field holding those values."""
+    s = scenes.small_scene(dims=40, spp=2, width=48, height=40)
+    top = 255 if bits == 8 else 65535
+    q = np.round(s.scalars * top).astype(np.uint8 if bits == 8 else np.uint16)
+    f = (q.astype(np.float32) / np.float32(top)).astype(np.float32)
+    fmt = bn.BN_UFIXED8 if bits == 8 else bn.BN_UFIXED16
+    with bn.BarneySession() as ses:
+        ses.build_scene(s, q.ctypes.data, texel_format=fmt)
+        ses.render()
+        got = ses.read()
+        ses.release_scene()
+        ses.build_scene(s, np.ascontiguousarray(f).ctypes.data)
+        ses.render()
+        ref = ses.read()
+    np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
