@@ -1044,23 +1044,27 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   const char *sk = getenv("GBV_RENDER_SKIP");
   p.skip = sk ? atoi(sk) : kSkipDefault;
   if (p.skip < 1) p.skip = 1;
-  // Shared-memory staging of the majorant bitmask and env-map CDF pivots
-  // (GBV_RENDER_STAGE=1) gives the same results; it is off by default because
-  // the shared memory it takes comes out of L1, which the kernel's spills,
-  // majorant and CDF loads use (measured slower on GB300).
+  // Shared-memory staging (same results either way).  GBV_RENDER_STAGE=1
+  // (default): the bitmask of non-zero majorants, one bit per macrocell, when
+  // it takes at most 8 KB per block (64 Ki macrocells; 4 KB for the 32^3
+  // grid of the 512^3 frame): the empty-cell test of the traversal becomes a
+  // shared-memory load (measured +1.8%).  =2 also stages the env-map cdf_y
+  // and the per-row pivots of cdf_x (up to 64 KB per block; measured slower:
+  // the shared memory comes out of L1, which spills and CDF loads use).
+  // =0 stages nothing.
   const char *ns = getenv("GBV_RENDER_STAGE");
-  const bool stage = ns && atoi(ns) != 0;
+  const int stage = ns ? atoi(ns) : 1;
   const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
-  const int budget = 64 * 1024 / 4;
+  const int budget = (stage >= 2 ? 64 : 8) * 1024 / 4;
   int used = 0;
   p.maskWords = 0;
   p.cdfYOff = p.pivOff = -1;
   p.pivPerRow = 0;
-  if (stage && nmc > 0 && (nmc + 31) / 32 <= budget) {
+  if (stage >= 1 && nmc > 0 && (nmc + 31) / 32 <= budget) {
     p.maskWords = (int)((nmc + 31) / 32);
     used = p.maskWords;
   }
-  if (stage && p.hasEnv && p.env.W >= 2) {
+  if (stage >= 2 && p.hasEnv && p.env.W >= 2) {
     if (used + p.env.H <= budget) {
       p.cdfYOff = used;
       used += p.env.H;

@@ -198,18 +198,21 @@ def test_rmse_falls_as_inverse_sqrt_spp(cuda):
     assert ro < 1.5 * rmse[16], (ro, rmse)
 
 
-def test_shared_memory_staging_is_transparent(cuda):
-    """Staging the majorant bitmask and env-map CDF pivots in shared memory
-    gives the same frame, bit for bit, as reading them from global memory
-    (the pivot search returns the reference binary search's index)."""
+@pytest.mark.parametrize("stage", ["1", "2"])
+def test_shared_memory_staging_is_transparent(cuda, stage):
+    """Staging the majorant bitmask (GBV_RENDER_STAGE=1, the default) and
+    also the env-map CDF pivots (=2) in shared memory gives the same frame,
+    bit for bit, as reading them from global memory (=0; the pivot search
+    returns the reference binary search's index)."""
     import os
     import torch
     s = _ms_scene(8, w=64, h=48, dims=48)
     s.env = scenes.env_sky(200, 100)  # W not a multiple of 32
     g = GpuScene(s)
-    a = g.render(spp=8, accum_id_start=3).cpu().numpy()
-    os.environ["GBV_RENDER_STAGE"] = "1"
+    os.environ["GBV_RENDER_STAGE"] = "0"
     try:
+        a = g.render(spp=8, accum_id_start=3).cpu().numpy()
+        os.environ["GBV_RENDER_STAGE"] = stage
         b = g.render(spp=8, accum_id_start=3).cpu().numpy()
     finally:
         del os.environ["GBV_RENDER_STAGE"]
