@@ -78,6 +78,9 @@ def lib() -> C.CDLL:
             "gbv_tile_partition": (st, [i, i, i, i, ip, ip]),
             "gbv_selftest_sincos": (st, [vp, C.c_longlong, vp, vp, i, vp]),
             "gbv_normalize_texels": (st, [vp, i, C.c_longlong, vp, vp]),
+            "gbv_compressed_tile_bytes": (C.c_size_t, []),
+            "gbv_compress_tiles": (st, [vp, i, i, i, i, i, vp, vp]),
+            "gbv_unpack_tiles": (st, [vp, i, i, i, i, i, vp, vp]),
             "gbv_iso_intersect": (st, [C.POINTER(GbvScene), vp, C.c_float, vp, C.c_longlong, vp, vp]),
             "gbv_batch_create": (st, [C.POINTER(GbvScene), vp, ip, ip, i, C.POINTER(vp)]),
             "gbv_batch_set_launch": (st, [vp, i, i, i]),

@@ -71,14 +71,8 @@ __global__ void majorants_kernel(const float2 *__restrict__ ranges, long long nu
   out[i] = xf_majorant(tf, n, lo, span, bd, r.x, r.y);
 }
 
-// linearizeColorAndNormalKernel (TiledFB.cu:13-50) + math.h:52-116
-__device__ __forceinline__ uint32_t make_8bit(float f) {
-  return (uint32_t)min(255, max(0, (int)(f * 256.f)));
-}
-__device__ __forceinline__ float linear_to_srgb(float x) {
-  if (x <= 0.0031308f) return 12.92f * x;
-  return 1.055f * powf(x, 1.f / 2.4f) - 0.055f;
-}
+// linearizeColorAndNormalKernel (TiledFB.cu:13-50); make_8bit and
+// linear_to_srgb (math.h:52-116) are in gbv_math.cuh
 __global__ void tonemap_kernel(const float4 *__restrict__ accum, long long n, float accumScale, int format,
                                void *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

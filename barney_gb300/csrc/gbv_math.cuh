@@ -188,6 +188,21 @@ GBV_HD float fastLog(float f) {
 
 GBV_HD float lerp_l(float f, float a, float b) { return (1.f - f) * a + f * b; }
 
+// barney/common/math.h:52-116: 8-bit channel min(255, max(0, int(f * 256)))
+// (a NaN converts to 0 on the device and is mapped to 0 on the host, as the
+// device's conversion does) and the sRGB transfer curve
+GBV_HD uint32_t make_8bit(float f) {
+#if !defined(__CUDA_ARCH__)
+  if (f != f) return 0u;
+#endif
+  const int v = (int)(f * 256.f);
+  return (uint32_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+}
+GBV_HD float linear_to_srgb(float x) {
+  if (x <= 0.0031308f) return 12.92f * x;
+  return 1.055f * powf(x, 1.f / 2.4f) - 0.055f;
+}
+
 // Sine and cosine of x in [-pi/4, 2pi + pi/4], the range of the angles the
 // renderer forms from [0, 1) random numbers (env-map directions and pdfs,
 // phase-function azimuths).  Cody-Waite reduction (Cody & Waite, Software

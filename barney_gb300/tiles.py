@@ -52,14 +52,57 @@ def unpack_tiles(frame, tiles, lowers) -> None:
         frame[y:y + h, x:x + w] = tiles[k, :h, :w]
 
 
-def gather_frame(frame, rank: int, world: int, root: int = 0, group=None):
+def compress_tiles(accum, accum_id: int, rank: int, world: int):
+    """The tiles `rank` owns of a (H, W, 4) CUDA accumulation frame in the
+    compressed tile format (gbv_compress_tiles): a (k, 6144) uint8 tensor."""
+    import torch
+    from .device import _ptr, _stream
+    H, W, _ = accum.shape
+    k = len(tile_partition(W, H, rank, world))
+    nb = int(N.lib().gbv_compressed_tile_bytes())
+    out = torch.empty((max(k, 1), nb), dtype=torch.uint8, device=accum.device)
+    N.check(N.lib().gbv_compress_tiles(_ptr(accum.contiguous()), W, H, accum_id, rank, world, _ptr(out), _stream()),
+            "gbv_compress_tiles")
+    return out[:k]
+
+
+def unpack_tiles_into(out, tiles, rank: int, world: int, fmt: int = N.GBV_FB_FLOAT4) -> None:
+    """Writes `rank`'s compressed tiles into the (H, W, 4) float32 (FLOAT4) or
+    (H, W) int32 (RGBA8) CUDA frame `out` (gbv_unpack_tiles)."""
+    from .device import _ptr, _stream
+    H, W = out.shape[0], out.shape[1]
+    if len(tiles) == 0:
+        return
+    N.check(N.lib().gbv_unpack_tiles(_ptr(tiles.contiguous()), W, H, rank, world, fmt, _ptr(out), _stream()),
+            "gbv_unpack_tiles")
+
+
+def gather_frame(frame, rank: int, world: int, root: int = 0, group=None, compress: bool = False,
+                 accum_id: int = 1):
     """Brings every rank's owned tiles of its (H, W, 4) frame to `root`,
     which returns the assembled frame; other ranks return None.  One gather
     of fixed-size buffers (each rank pads its tile list to the largest
-    rank's), so it runs on any torch.distributed backend that has gather."""
+    rank's), so it runs on any torch.distributed backend that has gather.
+    compress=True (CUDA frames): ships the compressed tile format (6 bytes a
+    pixel instead of 16) and returns the read colour, accumulation / accum_id,
+    as DistFB's gather does."""
     import torch
     import torch.distributed as dist
     H, W, ch = frame.shape
+    if compress:
+        most = len(tile_partition(W, H, 0, world))
+        mine = compress_tiles(frame, accum_id, rank, world)
+        buf = torch.zeros((max(most, 1), int(N.lib().gbv_compressed_tile_bytes())), dtype=torch.uint8,
+                          device=frame.device)
+        buf[: len(mine)] = mine
+        bufs = [torch.empty_like(buf) for _ in range(world)] if rank == root else None
+        dist.gather(buf, bufs, dst=root, group=group)
+        if rank != root:
+            return None
+        out = torch.zeros((H, W, 4), dtype=torch.float32, device=frame.device)
+        for r in range(world):
+            unpack_tiles_into(out, bufs[r][: len(tile_partition(W, H, r, world))], r, world)
+        return out
     most = len(tile_partition(W, H, 0, world))  # rank 0 owns the most tiles
     mine = tile_partition(W, H, rank, world)
     buf = torch.zeros((most, TILE, TILE, ch), dtype=frame.dtype, device=frame.device)

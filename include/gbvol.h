@@ -240,6 +240,25 @@ gbv_status gbv_render_tiles(const gbv_scene *scene, float *d_accum, int width,
                             int num_ranks, unsigned long long *d_counters,
                             void *stream);
 
+/* The compressed tile format of the gather (DistFB's CompressedColorTile,
+   barney/fb/DistFB.h:43-48): per 32x32 tile, 1024 uint32 RGBA8 (rgb divided
+   by the pixel's largest channel, alpha unscaled) followed by 1024 uint16
+   half-precision scales (that largest channel), gbv_compressed_tile_bytes()
+   = 6144 bytes per tile.
+   gbv_compress_tiles writes the tiles rank `rank` of num_ranks owns
+   (gbv_tile_partition order) of the frame d_accum (width*height RGBA float
+   accumulation, accum_id passes) to d_tiles; gbv_unpack_tiles writes that
+   rank's tiles from d_tiles into d_out (width*height float4, RGBA8 or sRGB
+   RGBA8, GBV_FB_*), leaving other pixels alone.  Replace CompressTiles and
+   UnpackTiles (barney/fb/DistFB.cu:25-108). */
+size_t gbv_compressed_tile_bytes(void);
+gbv_status gbv_compress_tiles(const float *d_accum, int width, int height,
+                              int accum_id, int rank, int num_ranks,
+                              void *d_tiles, void *stream);
+gbv_status gbv_unpack_tiles(const void *d_tiles, int width, int height,
+                            int rank, int num_ranks, int format, void *d_out,
+                            void *stream);
+
 /* gbv_render without any device allocation, for callers that may not
    allocate device memory while they render (an application that hands out
    all HBM from its own pre-sized pool, or a real-time viewer that forbids
