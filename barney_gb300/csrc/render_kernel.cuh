@@ -532,7 +532,8 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
 // with Woodcock::sampleRange (Volume.h:188-223) inside each cell of non-zero
 // majorant, as set up by MCVolumeAccel::isProg (MCAccelerator.h:569-708).
 // The state advances by bounded units so that a warp's lanes stay in one
-// loop: a run of at most kSkip empty cells, or one Woodcock step.
+// loop: a run of at most `skip` (default kSkipDefault) empty cells, or one
+// Woodcock step.
 // -------------------------------------------------------------------------
 constexpr int kSkipDefault = 8;
 
