@@ -131,7 +131,7 @@ class BarneySession:
 
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
                     layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None,
-                    texel_format: int = BN_FLOAT32):
+                    texel_format: int = BN_FLOAT32, frame_stats: bool = False):
         L, ctx, s = self.L, self.ctx, scene
         nx, ny, nz = s.dims
         td = _ok(L.bnTextureData3DCreate(ctx, 0, texel_format, nx, ny, nz, C.c_void_p(scalars_ptr)),
@@ -195,6 +195,8 @@ class BarneySession:
         L.bnCommit(cam)
         r = _ok(L.bnRendererCreate(ctx, b"default"), "bnRendererCreate")
         L.bnSet1i(r, b"pathsPerPixel", s.spp)
+        if frame_stats:  # event counts for bnFrameBufferGetStats (a slower kernel)
+            L.bnSet1i(r, b"frameStats", 1)
         L.bnSet1f(r, b"ambientRadiance", s.ambient)
         L.bnSet4f(r, b"bgColor", *s.bg_color)
         L.bnSet1i(r, b"multiScatter", s.multi_scatter)

@@ -21,6 +21,7 @@
 
 #include "../../include/barney_gb300.h"
 #include "../../include/gbvol.h"
+#include "gbv_internal.h"
 
 namespace bnimpl {
 
@@ -357,6 +358,7 @@ struct Renderer : Object {  // render/Renderer.{h,cpp}; staged until commit
     int maxVolumeBounces = 0;
     int volumeMultiScatter = 0;
     int multiScatterBuild = 0;
+    int frameStats = 0;  // this library's: count events for bnFrameBufferGetStats
   } staged, live;
   Renderer() {
     // The reference picks single or multiple scattering at compile time
@@ -372,6 +374,7 @@ struct Renderer : Object {  // render/Renderer.{h,cpp}; staged until commit
     if (m == "maxVolumeBounces") { staged.maxVolumeBounces = v; return true; }
     if (m == "volumeMultiScatter") { staged.volumeMultiScatter = v; return true; }
     if (m == "multiScatter") { staged.multiScatterBuild = v ? 1 : 0; return true; }
+    if (m == "frameStats") { staged.frameStats = v ? 1 : 0; return true; }
     return false;
   }
   bool set1f(const std::string &m, float v) override {
@@ -839,17 +842,27 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   s.multi_scatter = rp.multiScatterBuild;
   s.volume_multi_scatter = rp.volumeMultiScatter;
   s.max_volume_bounces = rp.maxVolumeBounces;
-  if (!f->counters.alloc(GBV_NUM_COUNTERS)) return;
-  cudaMemsetAsync(f->counters.p, 0, GBV_NUM_COUNTERS * sizeof(unsigned long long), c->stream);
-  if (gbv_render(&s, f->accum.p, f->W, f->H, f->accumID, rp.spp, f->counters.p, c->stream) != GBV_OK)
-    return fail(gbv_last_error());
+  // counters: [0..GBV_NUM_COUNTERS) event counts (renderer "frameStats" = 1),
+  // else only a loop-cap flag, kept in the word after them (the counting
+  // kernel is some 3% slower)
+  if (!f->counters.alloc(GBV_NUM_COUNTERS + 1)) return;
+  cudaMemsetAsync(f->counters.p, 0, (GBV_NUM_COUNTERS + 1) * sizeof(unsigned long long), c->stream);
+  int *capFlag = reinterpret_cast<int *>(f->counters.p + GBV_NUM_COUNTERS);
+  const gbv_status rs = rp.frameStats
+                            ? gbv_render(&s, f->accum.p, f->W, f->H, f->accumID, rp.spp, f->counters.p, c->stream)
+                            : gbv::render_cap_flagged(&s, f->accum.p, f->W, f->H, f->accumID, rp.spp, capFlag,
+                                                      c->stream);
+  if (rs != GBV_OK) return fail(gbv_last_error());
   f->accumID += rp.spp;
   // FrameBuffer::finalizeFrame: linearize with accumScale = 1/accumID
   if (f->accumID > 0 &&
       gbv_tonemap(f->accum.p, f->W, f->H, f->accumID, fbFormat(f->colorFormat), f->color.p, c->stream) != GBV_OK)
     return fail(gbv_last_error());
   cudaMemcpyAsync(f->lastStats, f->counters.p, sizeof(f->lastStats), cudaMemcpyDeviceToHost, c->stream);
+  unsigned long long capWord = 0;
+  cudaMemcpyAsync(&capWord, f->counters.p + GBV_NUM_COUNTERS, sizeof(capWord), cudaMemcpyDeviceToHost, c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail("bnRender: CUDA error during the frame");
+  if (capWord) f->lastStats[3] = 1;
   if (f->lastStats[3]) fail("bnRender: a device loop hit its iteration cap; the frame is partial");
 }
 

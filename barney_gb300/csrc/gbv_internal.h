@@ -11,6 +11,11 @@ gbv_status set_error(gbv_status st, const char *msg);
 gbv_status check_launch(const char *what);
 gbv_status check_cuda(cudaError_t e, const char *what);
 
+// gbv_render without event counting whose loop-cap events store 1 in
+// *d_cap_flag (render.cu; the bn* frame path).
+gbv_status render_cap_flagged(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
+                              int spp, int *d_cap_flag, void *stream);
+
 // Number of bricks of 2^l[i] cells per axis of a volume with `dims` voxels
 // (l == nullptr: 8^3-cell bricks).
 inline void brick_counts(const int dims[3], int nb[3], const int *l = nullptr) {

@@ -104,6 +104,7 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   p.scatAlb = s->scattering_albedo;
   p.rank = 0;
   p.numRanks = 1;
+  p.capFlag = nullptr;
   return GBV_OK;
 }
 
@@ -115,7 +116,7 @@ namespace gbv {
 
 static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accum, int width, int height,
                                int accum_id_start, int spp, int rank, int num_ranks, unsigned long long *d_counters,
-                               void *stream) {
+                               void *stream, int *d_cap_flag = nullptr) {
   char msg[160];
   if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0) {
     snprintf(msg, sizeof msg, "%s: null pointer or non-positive size", fn);
@@ -147,6 +148,7 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   p.accumIdStart = accum_id_start;
   p.spp = spp;
   p.counters = d_counters;
+  p.capFlag = d_cap_flag;
   p.rank = rank;
   p.numRanks = num_ranks;
   if (warp_tile_count(p) == 0) return GBV_OK;  // a rank that owns no tile
@@ -168,6 +170,14 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   }
   snprintf(msg, sizeof msg, "%s: unknown voxel format", fn);
   return set_error(GBV_ERROR_UNSUPPORTED, msg);
+}
+
+// gbv_render without event counting whose loop-cap events store 1 in
+// *d_cap_flag (the bn* frame path: frame statistics only when asked for).
+gbv_status render_cap_flagged(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
+                              int spp, int *d_cap_flag, void *stream) {
+  return render_frame("bnRender", s, d_accum, width, height, accum_id_start, spp, 0, 1, nullptr, stream,
+                      d_cap_flag);
 }
 
 }  // namespace gbv

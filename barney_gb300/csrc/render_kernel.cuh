@@ -51,6 +51,7 @@ struct RenderParams {
   float4 *accum;
   int accumIdStart, spp;
   unsigned long long *counters;
+  int *capFlag;   // if set, a loop-cap event stores 1 here (no counting needed)
   int skip;       // empty macrocells crossed per traversal step
   int threshold;  // keep traversing while at least this % of busy lanes trace
   // shared-memory staging (offsets in 32-bit words of the dynamic smem)
@@ -656,7 +657,8 @@ __device__ __forceinline__ bool trace_advance(Traversal &T, float tc, bool sx, b
 
 template <class Store, class Cnt>
 __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store, const XF &xf, const MCGridDev &G,
-                                          Traversal &T, Hit &h, Cnt &cnt, int skip, bool staged) {
+                                          Traversal &T, Hit &h, Cnt &cnt, int skip, bool staged,
+                                          int *capFlag) {
   const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
   const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
   if (!T.inCell) {
@@ -664,6 +666,7 @@ __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store
       GBV_COUNT(cnt, cells);
       if (++T.cells > maxCells) {
         GBV_COUNT(cnt, caps);
+        if (capFlag) *capFlag = 1;
         return TR_MISS;
       }
       const float tc = reduce_min(T.t_next);
@@ -691,7 +694,10 @@ __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store
   const float dt = -fastLog(1.f - r) / T.maj;
   T.t += dt;
   if (T.t >= T.segHi || ++T.steps > kWoodcockCap) {
-    if (T.steps > kWoodcockCap) GBV_COUNT(cnt, caps);
+    if (T.steps > kWoodcockCap) {
+      GBV_COUNT(cnt, caps);
+      if (capFlag) *capFlag = 1;
+    }
     T.inCell = 0;
     return trace_advance(T, T.tc, sx, sy, sz) ? TR_CONTINUE : TR_MISS;
   }
@@ -906,7 +912,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
           simt[1] += (unsigned)tracing;
         }
         if (tstate == TRACING && trace_step(p.F, make_store<Store>(p), p.xf, p.G, T, h, cnt, L.skip,
-                                            !Batch && L.maskWords > 0) != TR_CONTINUE)
+                                            !Batch && L.maskWords > 0, L.capFlag) != TR_CONTINUE)
           tstate = DONE;
       }
     }

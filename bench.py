@@ -499,15 +499,17 @@ def run_ours(args):
             ses.render()
             ses.read(out)
             dt = time.perf_counter() - t0
-            st = ses.stats()
             ses.release_scene()
             if i > 0:
                 e2e_times.append(dt)
     e2e_dt = sum(e2e_times) / len(e2e_times)
+    # the bn* frame is the device frame read out: same samples, same pixels
+    same = bool(torch.equal(out.cuda(), g.tonemap(acc, scene.spp)))
     h2d = host_vol.numel() * 4 + scene.tf.nbytes + (scene.env.texels.nbytes if scene.env is not None else 0)
-    line["e2e"] = {"value": world * st[0] / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    line["e2e"] = {"value": world * samples / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(out.numel() * 4), "ms_per_step": 1e3 * e2e_dt,
-                   "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers"}
+                   "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers",
+                   "frame_identical_to_device_frame": same}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
     line["extras_s"] = time.perf_counter() - extras_t0

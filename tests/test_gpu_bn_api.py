@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 def test_bn_render_matches_oracle(cuda):
     s = scenes.small_scene(dims=48, spp=4, width=64, height=48)
     with bn.BarneySession() as ses:
-        err = ses.build_scene(s, s.scalars.ctypes.data)
+        err = ses.build_scene(s, s.scalars.ctypes.data, frame_stats=True)
         assert err == "", err
         ses.render()
         img = ses.read()
