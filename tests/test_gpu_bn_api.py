@@ -87,3 +87,27 @@ def test_bn_integer_texels_normalised_on_device(cuda, bits):
         ses.render()
         ref = ses.read()
     np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_bn_progressive_accumulation_and_reset(cuda):
+    """Two bnRender calls of 3 paths each accumulate like one 6-pass frame
+    (accumIDs 0..5); bnAccumReset starts over (the reference's
+    FrameBuffer::accumID bookkeeping)."""
+    import torch
+    s = scenes.small_scene(dims=40, spp=3, width=48, height=40)
+    with bn.BarneySession() as ses:
+        ses.build_scene(s, s.scalars.ctypes.data)
+        ses.render()
+        ses.render()
+        two = ses.read()
+        ses.L.bnAccumReset(ses.handles["fb"])
+        ses.render()
+        one = ses.read()
+    g = GpuScene(s)
+    acc = g.render(spp=3)
+    g.render(spp=3, accum=acc, accum_id_start=3)
+    ref6 = g.tonemap(acc, 6).cpu().numpy()
+    ref3 = g.tonemap(g.render(spp=3), 3).cpu().numpy()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(two.view(np.uint32), ref6.view(np.uint32))
+    np.testing.assert_array_equal(one.view(np.uint32), ref3.view(np.uint32))
