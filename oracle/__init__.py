@@ -34,7 +34,7 @@ class OrcScene(C.Structure):
         ("env_dir", _f3), ("env_up", _f3), ("env_scale", C.c_float),
         ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
-        ("width", C.c_int), ("height", C.c_int),
+        ("width", C.c_int), ("height", C.c_int), ("u8_scaled", C.c_int),
     ]
 
 
@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
             "orc_tf_map": (None, [sp, vp, i, vp]),
             "orc_mc_dims": (None, [vp, i, vp]),
             "orc_mc_ranges": (None, [vp, vp, i, vp]),
+            "orc_scene_mc_ranges": (None, [sp, vp]),
             "orc_majorants": (None, [vp, i, vp, i, f, f, f, vp]),
             "orc_trace_ray": (i, [sp, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float), vp]),
             "orc_iso_intersect": (i, [sp, vp, f, vp, vp, f, vp]),
@@ -97,8 +98,12 @@ def _p(a: np.ndarray) -> C.c_void_p:
 class Oracle:
     """Oracle view of a barney_gb300.scenes.Scene (keeps its arrays alive)."""
 
-    def __init__(self, scene, scalars=None, majorants=None):
+    def __init__(self, scene, scalars=None, majorants=None, u8=False):
+        """u8=True samples the field as the library's U8 brick store holds it
+        (8-bit per 8^3-cell scale brick) and bounds macrocells by the
+        dequantized corners -- float arithmetic only."""
         self.s = scene
+        self.u8 = bool(u8)
         self.scalars = np.ascontiguousarray(scene.scalars if scalars is None else scalars, dtype=np.float32)
         self.tf = np.ascontiguousarray(scene.tf, dtype=np.float32)
         self.majorants = None if majorants is None else np.ascontiguousarray(majorants, dtype=np.float32)
@@ -141,6 +146,7 @@ class Oracle:
         r.volume_multi_scatter = scene.volume_multi_scatter
         r.max_volume_bounces = scene.max_volume_bounces
         r.width, r.height = scene.width, scene.height
+        r.u8_scaled = 1 if self.u8 else 0
         self.rec = r
 
     # -- macrocells --
@@ -152,7 +158,7 @@ class Oracle:
     def mc_ranges(self) -> np.ndarray:
         M = self.mc_dims()
         out = np.empty((M[0] * M[1] * M[2], 2), dtype=np.float32)
-        lib().orc_mc_ranges(_p(self.scalars), (C.c_int * 3)(*self.rec.dims), self.s.cells_per_mc, _p(out))
+        lib().orc_scene_mc_ranges(C.byref(self.rec), _p(out))
         return out
 
     def iso_intersect(self, rays: np.ndarray, iso: float, ranges=None) -> np.ndarray:
@@ -192,6 +198,8 @@ class Oracle:
     # -- render --
     def render(self, spp=None, accum=None, accum_id_start=0, use_double=False, nthreads=0, rows=None):
         W, H = self.s.width, self.s.height
+        if use_double and self.u8:
+            raise ValueError("the U8 storage form is sampled in float only")
         if accum is None:
             accum = np.zeros((H, W, 4), dtype=np.float32)
         st = OrcStats()
@@ -228,6 +236,8 @@ class Oracle:
         return arr
 
     def ea_render(self, views, step: float, use_double=False, nthreads=0) -> np.ndarray:
+        if use_double and self.u8:
+            raise ValueError("the U8 storage form is sampled in float only")
         npx = sum(v["width"] * v["height"] for v in views)
         out = np.empty((npx, 4), np.float32)
         lib().orc_ea_render(C.byref(self.rec), self._views(views), len(views), step, 1 if use_double else 0,
@@ -235,6 +245,8 @@ class Oracle:
         return out
 
     def ea_backward(self, views, step: float, d_images: np.ndarray, nthreads=0):
+        if self.u8:
+            raise ValueError("the adjoint is defined on the FP32 linear grid only")
         gv = np.zeros(self.scalars.size, np.float64)
         gt = np.zeros(self.tf.size, np.float64)
         lib().orc_ea_backward(C.byref(self.rec), self._views(views), len(views), step,

@@ -215,7 +215,31 @@ struct Field {
   int C[3];          // numCells = dims-1 (StructuredData.cu:142-151)
   V3<float> origin, spacing, rcpSpacing;
   V3<float> boundsLo, boundsHi;  // StructuredData.cu:176-180
+  // U8 storage form (orc_scene.u8_scaled): (min, max) per 8^3-cell scale brick
+  const float *u8lohi = nullptr;
+  int ns[3] = {0, 0, 0};
 };
+
+// The library's U8 store: the corner voxel v of a cell in scale brick
+// (min, max) reads back as min + (span/255) * round(255 (v - min) / span).
+inline float u8_dequant(float v, float lo, float hi) {
+  const float span = hi - lo;
+  int q = 0;
+  if (span > 0.f) q = (int)std::floor((v - lo) * (255.f / span) + .5f);
+  q = std::min(255, std::max(0, q));
+  const float scale = span > 0.f ? span / 255.f : 0.f;
+  return lo + scale * (float)q;
+}
+// The 8 dequantized corners of cell (cx, cy, cz), in the store's order.
+inline void u8_cell_corners(const Field &F, int cx, int cy, int cz, float c[8]) {
+  const size_t sb = (size_t)(cx >> 3) + (size_t)F.ns[0] * ((size_t)(cy >> 3) + (size_t)F.ns[1] * (size_t)(cz >> 3));
+  const float lo = F.u8lohi[2 * sb], hi = F.u8lohi[2 * sb + 1];
+  const size_t Nx = F.N[0], Ny = F.N[1];
+  for (int k = 0; k < 8; k++) {
+    const int x = cx + (k & 1), y = cy + ((k >> 1) & 1), z = cz + (k >> 2);
+    c[k] = u8_dequant(F.data[x + Nx * (y + Ny * (size_t)z)], lo, hi);
+  }
+}
 
 inline Field make_field(const orc_scene *s) {
   Field f;
@@ -246,7 +270,35 @@ struct Tri {  // trilinear stencil, for the adjoint
 
 // StructuredData.h:104-115 + rtcore/embree/Texture.cpp:339-411 (LINEAR, CLAMP,
 // unnormalised).  Returns NaN outside [0,numCells).
-template <typename R> inline R sample_field(const Field &F, V3<R> P, Tri *tri = nullptr) {
+template <typename R> inline R sample_field(const Field &F, V3<R> P, Tri *tri = nullptr);
+// sample_field of the U8 storage form: the cell holding the stencil (a
+// clamped axis uses cell 0 with weight 0 or cell N-2 with weight 1, as a
+// cell store must) and its dequantized corners
+inline float sample_field_u8(const Field &F, V3<float> P) {
+  V3<float> rel = (P - F.origin) * F.rcpSpacing;
+  if (rel.x < 0.f || rel.y < 0.f || rel.z < 0.f) return NAN;
+  if (rel.x >= (float)F.C[0] || rel.y >= (float)F.C[1] || rel.z >= (float)F.C[2]) return NAN;
+  V3<float> tc = rel + V3<float>(.5f);
+  int x0, x1, y0, y1, z0, z1;
+  float fx, fy, fz;
+  lerpCoords<float>(F.N[0], tc.x, x0, x1, fx);
+  lerpCoords<float>(F.N[1], tc.y, y0, y1, fy);
+  lerpCoords<float>(F.N[2], tc.z, z0, z1, fz);
+  if (x0 == x1 && x0 > 0) { x0 -= 1; fx = 1.f; }
+  if (y0 == y1 && y0 > 0) { y0 -= 1; fy = 1.f; }
+  if (z0 == z1 && z0 > 0) { z0 -= 1; fz = 1.f; }
+  float c[8];
+  u8_cell_corners(F, x0, y0, z0, c);
+  float v00 = lerp_l(fx, c[0], c[1]), v01 = lerp_l(fx, c[2], c[3]);
+  float v10 = lerp_l(fx, c[4], c[5]), v11 = lerp_l(fx, c[6], c[7]);
+  float v0 = lerp_l(fy, v00, v01), v1 = lerp_l(fy, v10, v11);
+  return lerp_l(fz, v0, v1);
+}
+
+template <typename R> inline R sample_field(const Field &F, V3<R> P, Tri *tri) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (F.u8lohi) return sample_field_u8(F, P);
+  }
   V3<R> rel = (P - cvt<R>(F.origin)) * cvt<R>(F.rcpSpacing);
   if (rel.x < R(0) || rel.y < R(0) || rel.z < R(0)) return R(NAN);
   if (rel.x >= R(F.C[0]) || rel.y >= R(F.C[1]) || rel.z >= R(F.C[2])) return R(NAN);
@@ -538,10 +590,42 @@ inline void env_cdfs(const float *tex, int W, int H, const int addr[2], float *c
 
 struct DirLightDD { V3<float> direction; float radiance; V3<float> color; };
 
+// U8 storage form: the (min, max) of each 8^3-cell scale brick over its 9^3
+// voxels (the 8-cell macrocell range), and macrocell ranges bounding the
+// dequantized corners of the macrocell's cells.
+inline void u8_build(Field &F, std::vector<float> &lohi) {
+  for (int i = 0; i < 3; i++) F.ns[i] = (F.C[i] + 7) >> 3;
+  const size_t n = (size_t)F.ns[0] * F.ns[1] * F.ns[2];
+  lohi.resize(2 * n);
+  for (size_t b = 0; b < n; b++) {
+    const int bx = (int)(b % F.ns[0]), by = (int)((b / F.ns[0]) % F.ns[1]), bz = (int)(b / ((size_t)F.ns[0] * F.ns[1]));
+    mc_range_one(F.data, F.N, 8, bx, by, bz, lohi[2 * b], lohi[2 * b + 1]);
+  }
+  F.u8lohi = lohi.data();
+}
+inline void u8_mc_ranges(const Field &F, int cpm, const int M[3], float *out) {
+  const size_t nmc = (size_t)M[0] * M[1] * M[2];
+  for (size_t m = 0; m < nmc; m++) {
+    const int x0 = (int)(m % M[0]) * cpm, y0 = (int)((m / M[0]) % M[1]) * cpm,
+              z0 = (int)(m / ((size_t)M[0] * M[1])) * cpm;
+    float lo = INF, hi = -INF;
+    for (int z = z0; z < std::min(z0 + cpm, F.C[2]); z++)
+      for (int y = y0; y < std::min(y0 + cpm, F.C[1]); y++)
+        for (int x = x0; x < std::min(x0 + cpm, F.C[0]); x++) {
+          float c[8];
+          u8_cell_corners(F, x, y, z, c);
+          for (int k = 0; k < 8; k++) { lo = mn(lo, c[k]); hi = mx(hi, c[k]); }
+        }
+    out[2 * m] = lo;
+    out[2 * m + 1] = hi;
+  }
+}
+
 struct Scene {
   Field F;
   XF xf;
   std::vector<float> majorants_own;
+  std::vector<float> u8lohi;  // U8 storage form: (min, max) per scale brick
   const float *maj;
   int M[3];
   V3<float> mcOrigin, mcSpacing, mcRcpSpacing;
@@ -566,11 +650,13 @@ inline void build_scene(const orc_scene *s, Scene &S) {
   S.mcSpacing = V3<float>((float)cpm) * S.F.spacing;
   S.mcRcpSpacing = rcp(S.mcSpacing);
   size_t nmc = (size_t)S.M[0] * S.M[1] * S.M[2];
+  if (s->u8_scaled) u8_build(S.F, S.u8lohi);
   if (s->majorants) S.maj = s->majorants;
   else {
     S.majorants_own.resize(nmc);
     std::vector<float> r(2 * nmc);
-    orc_mc_ranges(s->scalars, s->dims, cpm, r.data());
+    if (s->u8_scaled) u8_mc_ranges(S.F, cpm, S.M, r.data());
+    else orc_mc_ranges(s->scalars, s->dims, cpm, r.data());
     orc_majorants(r.data(), (int)nmc, s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density,
                   S.majorants_own.data());
     S.maj = S.majorants_own.data();
@@ -1257,6 +1343,8 @@ float orc_half_to_float(uint16_t h) { return h2f(h); }
 
 void orc_sample_points(const orc_scene *s, const float *P, int n, float *out) {
   Field F = make_field(s);
+  std::vector<float> lohi;
+  if (s->u8_scaled) u8_build(F, lohi);
   for (int i = 0; i < n; i++)
     out[i] = sample_field<float>(F, V3<float>(P[3 * i], P[3 * i + 1], P[3 * i + 2]));
 }
@@ -1285,6 +1373,19 @@ void orc_mc_ranges(const float *scalars, const int dims[3], int cpm, float *rang
     ranges[2 * tid] = lo;
     ranges[2 * tid + 1] = hi;
   }, 64);
+}
+
+void orc_scene_mc_ranges(const orc_scene *s, float *ranges) {
+  Field F = make_field(s);
+  int M[3];
+  mc_dims_of(F.N, s->cells_per_mc, M);
+  if (!s->u8_scaled) {
+    orc_mc_ranges(s->scalars, s->dims, s->cells_per_mc, ranges);
+    return;
+  }
+  std::vector<float> lohi;
+  u8_build(F, lohi);
+  u8_mc_ranges(F, s->cells_per_mc, M, ranges);
 }
 
 void orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n, float lo, float hi,
@@ -1327,14 +1428,16 @@ int orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3], fl
 // outside the field).  out: t, P[3], N[3] (N normalized).
 int orc_iso_intersect(const orc_scene *s, const float *ranges, float iso, const float org_[3], const float dir_[3],
                       float tmax, float out[7]) {
-  const Field F = make_field(s);
+  Field F = make_field(s);
+  std::vector<float> lohi;
+  if (s->u8_scaled) u8_build(F, lohi);
   int M[3];
   mc_dims_of(F.N, s->cells_per_mc, M);
   if (M[0] <= 0 || M[1] <= 0 || M[2] <= 0) return 0;
   std::vector<float> own;
   if (!ranges) {
     own.resize((size_t)2 * M[0] * M[1] * M[2]);
-    orc_mc_ranges(s->scalars, s->dims, s->cells_per_mc, own.data());
+    orc_scene_mc_ranges(s, own.data());
     ranges = own.data();
   }
   const V3<float> org(org_[0], org_[1], org_[2]);
@@ -1656,6 +1759,8 @@ extern "C" {
 void orc_ea_render(const orc_scene *s, const orc_ea_view *views, int num_views, float step, int use_double,
                    int nthreads, float *images) {
   Field F = make_field(s);
+  std::vector<float> lohi;
+  if (s->u8_scaled) u8_build(F, lohi);
   XF xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
   size_t off = 0;
   for (int vi = 0; vi < num_views; vi++) {

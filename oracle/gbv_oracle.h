@@ -57,6 +57,12 @@ typedef struct orc_scene {
   int   max_volume_bounces;
   /* frame */
   int   width, height;
+  /* 1: sample the field as the library's U8 brick store holds it -- per
+     8^3-cell scale brick, u8 = round(255 (v - min) / (max - min)) over its
+     9^3 voxels, dequantized as min + (max - min)/255 * u8 per cell corner --
+     and bound macrocells by the dequantized corners (the library's own
+     storage form; the reference has none) */
+  int   u8_scaled;
 } orc_scene;
 
 typedef struct orc_stats {
@@ -79,6 +85,8 @@ void  orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba);
 void  orc_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
 void  orc_mc_ranges(const float *scalars, const int dims[3], int cells_per_mc,
                     float *ranges /* 2 per MC */);
+/* ranges of the scene's field in its storage form (orc_scene.u8_scaled) */
+void  orc_scene_mc_ranges(const orc_scene *s, float *ranges /* 2 per MC */);
 void  orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n,
                     float lo, float hi, float base_density, float *out);
 

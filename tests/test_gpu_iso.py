@@ -64,6 +64,18 @@ def test_iso_half_store_matches_oracle_on_rounded_voxels(cuda):
     _compare(got, ref)
 
 
+def test_iso_u8_store_matches_oracle_u8_form(cuda):
+    import torch
+    s = scenes.small_scene(dims=40)
+    g = GpuScene(s, fmt=N.GBV_VOXEL_U8_SCALED)
+    rays = make_rays(1500, seed=6)
+    got = g.iso_intersect(torch.from_numpy(rays).cuda(), 0.45).cpu().numpy()
+    o = oracle.Oracle(s, u8=True)
+    ref = o.iso_intersect(rays, 0.45, ranges=o.mc_ranges())
+    assert 0.2 < ref[:, 7].mean() < 0.9
+    _compare(got, ref)
+
+
 def test_iso_outside_the_data_range_never_hits(cuda):
     import torch
     s = scenes.small_scene(dims=32)

@@ -94,6 +94,23 @@ def test_u8_storage_error_bounded(cuda):
     assert rmse < 0.05, rmse
 
 
+@pytest.mark.parametrize("brick", [(3, 3, 3), (4, 2, 2)])
+def test_u8_storage_matches_oracle_u8_form(cuda, brick):
+    """The U8 brick store against the oracle's U8 storage form (same scale
+    bricks, same dequantized corners): macrocell ranges, majorants and the
+    single-scatter frame match bit for bit."""
+    import torch
+    s = scenes.small_scene(dims=48, spp=2, width=96, height=64)
+    g = GpuScene(s, fmt=N.GBV_VOXEL_U8_SCALED, brick=brick)
+    o = oracle.Oracle(s, u8=True)
+    r = o.mc_ranges()
+    np.testing.assert_array_equal(bits(g.ranges.cpu().numpy().reshape(-1, 2)), bits(r))
+    np.testing.assert_array_equal(bits(g.majorants.cpu().numpy().reshape(-1)), bits(o.majorants_of(r)))
+    acc = g.render()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(acc.cpu().numpy()), bits(o.render()))
+
+
 @pytest.mark.parametrize("w,h", [(1, 1), (17, 9), (33, 65)])
 def test_ragged_frames(cuda, w, h):
     s = scenes.small_scene(dims=32, spp=2, width=w, height=h)

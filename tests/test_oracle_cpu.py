@@ -130,3 +130,40 @@ def test_iso_plane_of_a_linear_field():
         np.testing.assert_allclose(h[:, 4:7], np.tile([1.0, 0.0, 0.0], (k, 1)), atol=1e-5)
     # the plane lies outside [0, 1]: no hit
     assert not o.iso_intersect(rays, 1.5, ranges=o.mc_ranges())[:, 7].any()
+
+
+def test_u8_storage_form_of_the_oracle():
+    """The oracle's U8 storage form: every corner is within half a step of
+    its scale brick (span/510) of the voxel, so samples are too; macrocell
+    ranges bound every sample inside the macrocell; a constant scale brick
+    (span 0) reads back exactly."""
+    s = scenes.small_scene(dims=37, spp=1, width=24, height=16)
+    o, o8 = oracle.Oracle(s), oracle.Oracle(s, u8=True)
+    rng = np.random.default_rng(1)
+    P = rng.uniform(-0.55, 0.55, (6000, 3)).astype(np.float32)
+    a, b = o.sample(P), o8.sample(P)
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(a)
+    v = s.scalars
+    span = 0.0
+    for z in range(0, 36, 8):
+        for y in range(0, 36, 8):
+            for x in range(0, 36, 8):
+                blk = v[z:z + 9, y:y + 9, x:x + 9]
+                span = max(span, float(blk.max() - blk.min()))
+    assert np.abs(a[m] - b[m]).max() <= span / 510 * (1 + 1e-5) + 1e-6
+    # ranges bound the U8 samples of each macrocell
+    r8 = o8.mc_ranges()
+    origin, spacing = s.geometry()
+    cell = np.floor((P[m] - np.asarray(origin, np.float32)) / np.asarray(spacing, np.float32)).astype(int)
+    M = o8.mc_dims()
+    mc = np.minimum(cell // s.cells_per_mc, np.asarray(M) - 1)
+    idx = mc[:, 0] + M[0] * (mc[:, 1] + M[1] * mc[:, 2])
+    assert np.all(b[m] >= r8[idx, 0]) and np.all(b[m] <= r8[idx, 1])
+    # constant field: span 0, every sample is the value itself
+    c = scenes.Scene(scalars=np.full((17, 17, 17), 0.375, np.float32), tf=scenes.tf_ramp(16), cells_per_mc=8)
+    oc = oracle.Oracle(c, u8=True)
+    sc = oc.sample(rng.uniform(-0.45, 0.45, (500, 3)).astype(np.float32))
+    assert np.all(sc == np.float32(0.375))
+    with pytest.raises(ValueError):
+        o8.render(use_double=True)
