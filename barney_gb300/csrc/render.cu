@@ -335,7 +335,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
     p.H = heights[i];
     p.accum = reinterpret_cast<float4 *>(d_accums[i]);
     p.maskWords = 0;
-    p.cdfYOff = p.pivOff = -1;
+    p.cdfYOff = p.pivOff = p.rowOff = -1;
     p.pivPerRow = 0;
     starts[i + 1] = starts[i] + (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
   }
@@ -390,7 +390,7 @@ extern "C" gbv_status gbv_batch_render(gbv_batch *b, int accum_id_start, int spp
   L.skip = b->skip;
   L.threshold = b->threshold;
   L.maskWords = 0;
-  L.cdfYOff = L.pivOff = -1;
+  L.cdfYOff = L.pivOff = L.rowOff = -1;
   L.profile = 0;
   cudaStream_t cs = (cudaStream_t)stream;
   if (b->layout == GBV_LAYOUT_LINEAR) return batch_launch_linear(b, L, cs);

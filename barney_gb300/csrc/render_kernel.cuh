@@ -59,6 +59,7 @@ struct RenderParams {
   int cdfYOff;    // >=0: env cdf_y staged here
   int pivOff;     // >=0: per-row pivots of cdf_x staged here
   int pivPerRow;
+  int rowOff;     // >=0: per env-map row (pdf_y, pdf denominator) staged here
   int profile;    // accumulate per-phase cycle counts
   // voxel store of this scene (see make_store)
   const void *vox;
@@ -108,18 +109,32 @@ struct LightSample {
   float distance, pdf;
 };
 
+// fmod(x, y), whose result is exact by definition (x - n y for the integer n
+// that truncates x / y, carrying the sign of x).  The wrap addressing of an
+// env-map lookup only meets |x| < 2|y|: there the result is x itself, or
+// |x| - |y| with the sign of x, a subtraction that is exact because
+// |y| <= |x| < 2|y| (Sterbenz's lemma).  Other arguments (and NaN, inf, zero
+// y) go to fmodf.  Identical results, a few instructions instead of a
+// general remainder.
+__device__ __forceinline__ float fmod_wrap(float x, float y) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  if (ax < ay) return x;
+  if (ax < 2.f * ay) return copysignf(ax - ay, x);
+  return fmodf(x, y);
+}
+
 // rtcore/embree/Texture.cpp:25-93 (normalized coordinates)
 __device__ __forceinline__ void compute_address(int mode, float tc, int N, int &i0, int &i1, float &f) {
   i0 = 0; i1 = 0; f = 0.f;
   if (mode == GBV_ADDR_WRAP) {
     tc = tc * (float)N - .5f;
-    tc = fmodf(tc, (float)N);
+    tc = fmod_wrap(tc, (float)N);
     if (tc < 0.f) tc += (float)N;
     float fc = floorf(tc);
     int ic = (int)fc;
     f = tc - (float)ic;
     i0 = ic;
-    i1 = (int)fmodf(tc + 1.f, (float)N);
+    i1 = (int)fmod_wrap(tc + 1.f, (float)N);
   } else if (mode == GBV_ADDR_MIRROR) {
     tc = tc * (float)N + .5f;
     float fc = floorf(tc);
@@ -149,8 +164,9 @@ __device__ __forceinline__ float4 lerp4(float f, float4 a, float4 b) {
   return make_float4((1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
                      (1.f - f) * a.w + f * b.w);
 }
-// rtcore/embree/Texture.cpp:295-321
-__device__ __forceinline__ float4 tex2D(const EnvDev &e, float u, float v) {
+// rtcore/embree/Texture.cpp:295-321 (one out-of-line copy for the env-map
+// sample and the miss lookup)
+static __device__ __noinline__ float4 tex2D(const EnvDev &e, float u, float v) {
   int x0, x1, y0, y1;
   float fx, fy;
   compute_address(e.addr[0], u, e.W, x0, x1, fx);
@@ -252,7 +268,20 @@ __device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, floa
 // of line (__noinline__, one copy each instead of one per call site), and
 // the kernel has one call site each for trace_begin and the env lookup of a
 // miss.  Measured on the 512^3 frame: +7% samples/s.
-// EnvMap.h:136-180
+// The two factors of the env-map pdf that depend on the pixel row only
+// (EnvMap.h:160-179): the row's marginal pdf and the solid-angle
+// denominator 2 pi^2 sin(theta) at the row centre.
+__device__ __forceinline__ float2 env_row_terms(const EnvDev &e, int py) {
+  const float pdf_y = (float)e.H * (__ldg(e.cdf_y + py) - (py ? __ldg(e.cdf_y + py - 1) : 0.f));
+  const float rel_y = ((float)py + .5f) / (float)e.H;
+  const float theta2 = kPi * rel_y;
+  float sinTheta2, cosTheta2;
+  sincos_angle(theta2, sinTheta2, cosTheta2);
+  return make_float2(pdf_y, kTwoPi * kPi * sinTheta2);
+}
+// EnvMap.h:136-180.  With the row terms staged in shared memory (rowOff >= 0,
+// computed by the same expressions at kernel start) the pdf is one shared
+// and two global loads.
 static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   if (!p.hasEnv) return kOneOverFourPi;
   const EnvDev &e = p.env;
@@ -262,13 +291,9 @@ static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   float u = phi * kOneOverTwoPi, v = theta * kOneOverPi;
   int px = (int)clampv(u * (float)e.W, 0.f, (float)e.W - 1.f);
   int py = (int)clampv(v * (float)e.H, 0.f, (float)e.H - 1.f);
-  float pdf_y = (float)e.H * (cdf_y_at(p, py) - (py ? cdf_y_at(p, py - 1) : 0.f));
+  const float2 row = p.rowOff >= 0 ? reinterpret_cast<const float2 *>(g_smem + p.rowOff)[py] : env_row_terms(e, py);
   float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
-  float rel_y = ((float)py + .5f) / (float)e.H;
-  const float theta2 = kPi * rel_y;
-  float sinTheta2, cosTheta2;
-  sincos_angle(theta2, sinTheta2, cosTheta2);
-  return pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinTheta2);
+  return pdf_x * row.x * 1.f / row.y;
 }
 // EnvMap.h:198-250
 static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Random &r) {
@@ -792,6 +817,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         g_smem[p.pivOff + i] = __float_as_uint(__ldg(p.env.cdf_x + (size_t)row * p.env.W + last));
       }
     }
+    if (p.rowOff >= 0)
+      for (int i = threadIdx.x; i < p.env.H; i += blockDim.x)
+        reinterpret_cast<float2 *>(g_smem + p.rowOff)[i] = env_row_terms(p.env, i);
     __syncthreads();
   }
   const long long numTiles = Batch ? tileStart[numItems] : warp_tile_count(p0);
@@ -1000,6 +1028,15 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
 }
 
 
+// 32-bit words of dynamic shared memory the staged tables take
+inline size_t staged_words(const RenderParams &p) {
+  long long end = p.maskWords;
+  if (p.cdfYOff >= 0) end = end > p.cdfYOff + p.env.H ? end : p.cdfYOff + p.env.H;
+  if (p.pivOff >= 0) end = end > p.pivOff + (long long)p.env.H * p.pivPerRow ? end : p.pivOff + (long long)p.env.H * p.pivPerRow;
+  if (p.rowOff >= 0) end = end > p.rowOff + 2LL * p.env.H ? end : p.rowOff + 2LL * p.env.H;
+  return (size_t)end;
+}
+
 template <class Store, int MinBlocks>
 inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cudaStream_t stream) {
   // persistent grid: as many resident blocks as the device holds
@@ -1007,8 +1044,7 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st != GBV_OK) return st;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t smem = (size_t)(p.maskWords + (p.cdfYOff >= 0 ? p.env.H : 0) +
-                               (p.pivOff >= 0 ? p.env.H * p.pivPerRow : 0)) * sizeof(uint32_t);
+  const size_t smem = staged_words(p) * sizeof(uint32_t);
   if (smem > 48 * 1024)
   {
     cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1055,21 +1091,27 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   // (default): the bitmask of non-zero majorants, one bit per macrocell, when
   // it takes at most 8 KB per block (64 Ki macrocells; 4 KB for the 32^3
   // grid of the 512^3 frame): the empty-cell test of the traversal becomes a
-  // shared-memory load (measured +1.8%).  =2 also stages the env-map cdf_y
-  // and the per-row pivots of cdf_x (up to 64 KB per block; measured slower:
-  // the shared memory comes out of L1, which spills and CDF loads use).
-  // =0 stages nothing.
+  // shared-memory load (measured +1.8%); with an env map of at most 1024
+  // rows also the row terms of its pdf (8 bytes a row).  =2 also stages the
+  // env-map cdf_y and the per-row pivots of cdf_x (up to 64 KB per block;
+  // measured slower: the shared memory comes out of L1, which spills and CDF
+  // loads use).  =0 stages nothing.
   const char *ns = getenv("GBV_RENDER_STAGE");
   const int stage = ns ? atoi(ns) : 1;
   const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
   const int budget = (stage >= 2 ? 64 : 8) * 1024 / 4;
   int used = 0;
   p.maskWords = 0;
-  p.cdfYOff = p.pivOff = -1;
+  p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
   if (stage >= 1 && nmc > 0 && (nmc + 31) / 32 <= budget) {
     p.maskWords = (int)((nmc + 31) / 32);
     used = p.maskWords;
+  }
+  if (stage >= 1 && p.hasEnv && p.env.H >= 1 && p.env.H <= 1024) {
+    used = (used + 1) & ~1;  // float2 entries
+    p.rowOff = used;
+    used += 2 * p.env.H;
   }
   if (stage >= 2 && p.hasEnv && p.env.W >= 2) {
     if (used + p.env.H <= budget) {
@@ -1102,7 +1144,7 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   p.skip = kSkipDefault;
   p.threshold = 5;
   p.maskWords = 0;
-  p.cdfYOff = p.pivOff = -1;
+  p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
   p.profile = 0;
   int dev = 0, sms = 0, perSM = 0;
