@@ -295,21 +295,35 @@ static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
   float pdf_x = cdf_get_pdf(px, e.cdf_x + (size_t)py * e.W, e.W);
   return pdf_x * row.x * 1.f / row.y;
 }
-// EnvMap.h:198-250
-static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Random &r) {
+// EnvMap.h:198-250, in two parts.  The light selection of sampleLights
+// needs only the sample's radiance, so the direction and pdf (two
+// sine/cosine pairs, a transform and a division) are formed only when the
+// env light is the one selected; they use no random numbers, so the random
+// stream is consumed exactly as in one piece.
+struct EnvPick {
+  vec3 radiance;
+  float sx, sy;  // sampled texture coordinates
+  float pdfxy;   // pdf_x * pdf_y
+};
+static __device__ __noinline__ EnvPick env_pick(const RenderParams &p, Random &r) {
   const EnvDev &e = p.env;
-  LightSample s;
+  EnvPick k;
   float r_y = r();
   float r_x = r();
   float pdf_y, pdf_x;
   int iy = sample_cdf_y(p, r_y, pdf_y);
   int ix = sample_cdf_x(p, iy, r_x, pdf_x);
-  float sx = ((float)ix + r()) / (float)e.W;
-  float sy = ((float)iy + r()) / (float)e.H;
-  float4 t = tex2D(e, sx, sy);
-  s.radiance = e.scale * vec3(t.x, t.y, t.z);
-  const float phi = kTwoPi * sx;
-  const float theta = kPi * sy;
+  k.sx = ((float)ix + r()) / (float)e.W;
+  k.sy = ((float)iy + r()) / (float)e.H;
+  float4 t = tex2D(e, k.sx, k.sy);
+  k.radiance = e.scale * vec3(t.x, t.y, t.z);
+  k.pdfxy = pdf_x * pdf_y;
+  return k;
+}
+static __device__ __noinline__ void env_pick_direction(const RenderParams &p, const EnvPick &k, LightSample &s) {
+  const EnvDev &e = p.env;
+  const float phi = kTwoPi * k.sx;
+  const float theta = kPi * k.sy;
   float sinTheta, cosTheta, sinPhi, cosPhi;
   sincos_angle(theta, sinTheta, cosTheta);  // theta in [0, pi]
   sincos_angle(phi, sinPhi, cosPhi);        // phi in [0, 2 pi]
@@ -318,9 +332,7 @@ static __device__ __noinline__ LightSample env_sample(const RenderParams &p, Ran
   d.x = cosPhi * sinTheta;
   d.y = sinPhi * sinTheta;
   s.direction = xfm_vector(e.toWorld, d);
-  s.pdf = pdf_x * pdf_y * 1.f / (kTwoPi * kPi * sinTheta);
-  s.distance = __int_as_float(0x7f800000);
-  return s;
+  s.pdf = k.pdfxy * 1.f / (kTwoPi * kPi * sinTheta);
 }
 
 // DG.h:183-193
@@ -372,8 +384,11 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
                                               bool &needsMIS, bool &isDir) {
   needsMIS = false;
   LightSample els;
+  EnvPick pick;
   if (p.hasEnv) {
-    els = env_sample(p, random);
+    pick = env_pick(p, random);
+    els.radiance = pick.radiance;
+    els.distance = __int_as_float(0x7f800000);
   } else {
     els.direction = random_direction(random);
     els.distance = __int_as_float(0x7f800000);
@@ -394,6 +409,7 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
   if (r <= alsWeight) {
     return false;  // empty area-light sample (pdf 0)
   } else if (r <= alsWeight + elsWeight) {
+    if (p.hasEnv) env_pick_direction(p, pick, els);
     ls = els;
     ls.radiance = ls.radiance * (1.f / elsWeight);
     needsMIS = true;
@@ -432,6 +448,7 @@ __device__ __forceinline__ float hg_phase(float g, float cosTheta) {
 }
 __device__ __forceinline__ float phase_pdf(const RenderParams &p, float g, vec3 wo, vec3 wi) {
   if (!p.multi) return kOneOverFourPi;
+  if (fabsf(g) < 1e-3f) return kOneOverFourPi;  // isotropic: no directions needed
   vec3 wi_in = normalize(-wo);
   return hg_phase(g, dot(wi_in, normalize(wi)));
 }
