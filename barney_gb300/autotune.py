@@ -28,7 +28,7 @@ import json
 import os
 from pathlib import Path
 
-LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (2, 5, 15) for k in (4, 8, 16)]
+LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (2, 3, 5) for k in (2, 3, 4, 8)]
 BRICK_CANDIDATES = [(3, 3, 3), (2, 2, 2), (4, 4, 4), (4, 4, 2), (5, 3, 2)]
 
 

@@ -14,8 +14,10 @@
 
 #if defined(__CUDACC__)
 #define GBV_HD __host__ __device__ __forceinline__
+#define GBV_HD_COLD static __host__ __device__ __noinline__  // rarely taken: one out-of-line copy
 #else
 #define GBV_HD inline
+#define GBV_HD_COLD static inline
 #endif
 
 namespace gbv {
@@ -79,27 +81,9 @@ constexpr float kOneOverFourPi = 1.f / (4.f * 3.14159265358979323846f);
 // zero).  Path throughput lives in half precision (render/Ray.h:19), so the
 // rounding rule is part of the path's arithmetic.
 // ---------------------------------------------------------------------------
-//
-// On the device, values whose rounded magnitude is a normal half
-// (2^-14 <= |v| < 65520) take a short path with the same result: adding half
-// a unit of the 13 dropped bits to the float's bit pattern and clearing them
-// rounds to nearest with ties away from zero (a carry into the exponent is
-// the correct round-up), and the result is a half exactly, so the
-// hardware's round-toward-zero conversion only re-encodes it.  Subnormal
-// halves, overflow to infinity and NaN keep the general path.
-GBV_HD uint16_t f2h(float value) {
-#if defined(__CUDA_ARCH__)
-  {
-    const uint32_t b = float_bits(value);
-    const uint32_t a = b & 0x7fffffffu;
-    if (a >= 0x38800000u && a < 0x477ff000u) {
-      const float r = __uint_as_float((b + 0x1000u) & ~0x1fffu);
-      unsigned short h;
-      asm("cvt.rz.f16.f32 %0, %1;" : "=h"(h) : "f"(r));
-      return (uint16_t)h;
-    }
-  }
-#endif
+// The general conversion (every input; on the device only the values the
+// short path below leaves out reach it)
+GBV_HD_COLD uint16_t f2h_general(float value) {
   int i = (int)float_bits(value);
   int s = (i >> 16) & 0x00008000;
   int e = ((i >> 23) & 0x000000ff) - (127 - 15);
@@ -120,6 +104,26 @@ GBV_HD uint16_t f2h(float value) {
   }
   if (e > 30) return uint16_t(s | 0x7c00);
   return uint16_t(s | (e << 10) | (m >> 13));
+}
+// On the device, values whose rounded magnitude is a normal half
+// (2^-14 <= |v| < 65520) take a short path with the same result: adding half
+// a unit of the 13 dropped bits to the float's bit pattern and clearing them
+// rounds to nearest with ties away from zero (a carry into the exponent is
+// the correct round-up), and the result is a half exactly, so the
+// hardware's round-toward-zero conversion only re-encodes it.  Subnormal
+// halves, overflow to infinity and NaN take the general path.
+GBV_HD uint16_t f2h(float value) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t b = float_bits(value);
+  const uint32_t a = b & 0x7fffffffu;
+  if (a >= 0x38800000u && a < 0x477ff000u) {
+    const float r = __uint_as_float((b + 0x1000u) & ~0x1fffu);
+    unsigned short h;
+    asm("cvt.rz.f16.f32 %0, %1;" : "=h"(h) : "f"(r));
+    return (uint16_t)h;
+  }
+#endif
+  return f2h_general(value);
 }
 // exact widening (on the device the hardware conversion, which widens every
 // finite and infinite half exactly; a NaN stays a NaN, and a NaN throughput

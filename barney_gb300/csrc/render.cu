@@ -347,7 +347,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
   b->layout = scenes[0].layout;
   b->totalTiles = starts[count];
   b->occ = 5;
-  b->threshold = 5;
+  b->threshold = kThresholdDefault;
   b->skip = kSkipDefault;
   cudaGetDevice(&b->device);
   gbv_status st = check_cuda(cudaMalloc((void **)&b->d_items, sizeof(RenderParams) * count), "gbv_batch_create");

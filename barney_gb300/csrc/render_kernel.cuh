@@ -116,13 +116,30 @@ struct LightSample {
 // |y| <= |x| < 2|y| (Sterbenz's lemma).  Other arguments (and NaN, inf, zero
 // y) go to fmodf.  Identical results, a few instructions instead of a
 // general remainder.
+static __device__ __noinline__ float fmod_general(float x, float y) { return fmodf(x, y); }
 __device__ __forceinline__ float fmod_wrap(float x, float y) {
   const float ax = fabsf(x), ay = fabsf(y);
   if (ax < ay) return x;
   if (ax < 2.f * ay) return copysignf(ax - ay, x);
-  return fmodf(x, y);
+  return fmod_general(x, y);
 }
 
+// Texture.cpp:25-93, mirror mode (out of line: env maps here wrap or clamp)
+static __device__ __noinline__ void compute_address_mirror(float tc, int N, int &i0, int &i1, float &f) {
+  tc = tc * (float)N + .5f;
+  float fc = floorf(tc);
+  int ic = (int)fc;
+  f = tc - (float)ic;
+  int a = ic - 1, b = ic;
+  if (a < 0) a = -a;
+  if (b < 0) b = -b;
+  a = a % (2 * N);
+  b = b % (2 * N);
+  if (a >= N) a = 2 * N - 1 - a;
+  if (b >= N) b = 2 * N - 1 - b;
+  i0 = a;
+  i1 = b;
+}
 // rtcore/embree/Texture.cpp:25-93 (normalized coordinates)
 __device__ __forceinline__ void compute_address(int mode, float tc, int N, int &i0, int &i1, float &f) {
   i0 = 0; i1 = 0; f = 0.f;
@@ -136,19 +153,7 @@ __device__ __forceinline__ void compute_address(int mode, float tc, int N, int &
     i0 = ic;
     i1 = (int)fmod_wrap(tc + 1.f, (float)N);
   } else if (mode == GBV_ADDR_MIRROR) {
-    tc = tc * (float)N + .5f;
-    float fc = floorf(tc);
-    int ic = (int)fc;
-    f = tc - (float)ic;
-    int a = ic - 1, b = ic;
-    if (a < 0) a = -a;
-    if (b < 0) b = -b;
-    a = a % (2 * N);
-    b = b % (2 * N);
-    if (a >= N) a = 2 * N - 1 - a;
-    if (b >= N) b = 2 * N - 1 - b;
-    i0 = a;
-    i1 = b;
+    compute_address_mirror(tc, N, i0, i1, f);
   } else if (mode == GBV_ADDR_CLAMP) {
     tc = tc * (float)N;
     if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; }
@@ -228,10 +233,9 @@ __device__ __forceinline__ int sample_cdf_y(const RenderParams &p, float v, floa
 // pivots (the last counted entry of every 32-entry segment) the same count is
 // the number of segments whose pivot is <= v, times 32, plus a count inside
 // the next segment, whose 32 entries are fetched with independent loads.
-__device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, float v, float &pdf) {
+static __device__ __noinline__ int sample_cdf_x_pivots(const RenderParams &p, int row, float v, float &pdf) {
   const int N = p.env.W;
   const float *cdf = p.env.cdf_x + (size_t)row * N;
-  if (p.pivOff < 0) return sample_cdf(cdf, N, v, pdf);
   const float *piv = reinterpret_cast<const float *>(g_smem + p.pivOff) + (size_t)row * p.pivPerRow;
   const int nseg = p.pivPerRow;
   int lo = 0, hi = nseg;  // first segment whose pivot is > v
@@ -258,6 +262,10 @@ __device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, floa
   const float before = begin ? __ldg(cdf + begin - 1) : 0.f;
   pdf = (float)N * (at - before);
   return begin;
+}
+__device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, float v, float &pdf) {
+  if (p.pivOff >= 0) return sample_cdf_x_pivots(p, row, v, pdf);
+  return sample_cdf(p.env.cdf_x + (size_t)row * p.env.W, p.env.W, v, pdf);
 }
 
 // Code size.  The render kernel is limited as much by instruction fetch as
@@ -578,7 +586,10 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
 // loop: a run of at most `skip` (default kSkipDefault) empty cells, or one
 // Woodcock step.
 // -------------------------------------------------------------------------
-constexpr int kSkipDefault = 8;
+// Defaults of the launch shape (the best of a same-box sweep of skip 2..8
+// and threshold 3..8 on the 512^3 1080p frame; results never depend on them)
+constexpr int kSkipDefault = 3;
+constexpr int kThresholdDefault = 3;
 
 // Per-lane event counts; with On == false the counting and its registers
 // compile away (timed launches pass no counter buffer).
@@ -1096,9 +1107,9 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
 // GBV_RENDER_OCC=4, 5 or 6 selects the resident blocks per SM the registers
 // are capped for (default 5: 40 warps per SM at 51 registers; the kernel is
 // latency-bound and gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
-// macrocells crossed per traversal step (default 8); GBV_RENDER_THRESH the
+// macrocells crossed per traversal step (default 3); GBV_RENDER_THRESH the
 // percentage of a warp's busy lanes that must still be tracing for the warp
-// to keep traversing before it shades and refills (default 5).
+// to keep traversing before it shades and refills (default 3).
 template <class Store>
 inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
   const char *sk = getenv("GBV_RENDER_SKIP");
@@ -1145,7 +1156,7 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   const char *pf = getenv("GBV_RENDER_PROFILE");
   p.profile = (pf && atoi(pf) != 0 && p.counters) ? 1 : 0;
   const char *th = getenv("GBV_RENDER_THRESH");
-  p.threshold = th ? atoi(th) : 5;
+  p.threshold = th ? atoi(th) : kThresholdDefault;
   if (p.threshold < 1) p.threshold = 1;
   const char *oc = getenv("GBV_RENDER_OCC");
   const int occ = oc ? atoi(oc) : 5;
@@ -1157,9 +1168,9 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
 template <class Store>
 inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cudaStream_t stream, int *pool) {
   // fixed launch settings (results do not depend on them): 5 resident
-  // blocks per SM, 8 cells per traversal step, no shared-memory staging
+  // blocks per SM, the default traversal settings, no shared-memory staging
   p.skip = kSkipDefault;
-  p.threshold = 5;
+  p.threshold = kThresholdDefault;
   p.maskWords = 0;
   p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
