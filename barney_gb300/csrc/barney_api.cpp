@@ -32,23 +32,43 @@ static void fail(const std::string &msg) {
   std::fprintf(stderr, "#bn: %s\n", msg.c_str());
 }
 
+// Device memory of one context.  Buffers come from a stream-ordered pool
+// that keeps the blocks it is given back (release threshold: unlimited), so
+// a scene rebuilt on the same context (new texel data, new field, new frame
+// buffer) reuses the memory of the one it replaces instead of calling
+// cudaMalloc and cudaFree (about a millisecond per GB each on GB300, and
+// cudaFree waits for the device).  Every use of a buffer is on the
+// context's stream, which also orders each reuse after the last use.  The
+// pool's memory returns to the device when the context is destroyed.
+struct DevPool {
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // null: plain cudaMalloc / cudaFree
+};
+
 template <typename T> struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  const DevPool *owner = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (owner && owner->pool) cudaFreeAsync(p, owner->stream);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
   }
-  bool alloc(size_t count) {
+  bool alloc(size_t count, const DevPool &mem) {
     if (count == n && p) return true;
     release();
     if (count == 0) return true;
-    if (cudaMalloc((void **)&p, count * sizeof(T)) != cudaSuccess) {
+    owner = &mem;
+    const cudaError_t e = mem.pool ? cudaMallocFromPoolAsync((void **)&p, count * sizeof(T), mem.pool, mem.stream)
+                                   : cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
       p = nullptr;
       fail("device allocation of " + std::to_string(count * sizeof(T)) + " bytes failed");
       return false;
@@ -80,6 +100,7 @@ using SP = std::shared_ptr<Object>;
 struct Context {
   int device = 0;
   cudaStream_t stream = nullptr;
+  DevPool mem;  // device buffers of this context's objects
   std::map<Object *, SP> handles;  // the app's references
   std::set<std::string> warned;
   SP find(void *h) {
@@ -190,15 +211,15 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
     }
     if (gbv_mc_dims(dims, cellsPerMC, mcDims) != GBV_OK) { fail(gbv_last_error()); return false; }
     size_t nmc = (size_t)mcDims[0] * mcDims[1] * mcDims[2];
-    if (!ranges.alloc(2 * std::max<size_t>(nmc, 1))) return false;
+    if (!ranges.alloc(2 * std::max<size_t>(nmc, 1), ctx->mem)) return false;
     if (layout == GBV_LAYOUT_BRICK_CORNERS) {
       size_t vb = 0, sb = 0;
       if (gbv_brick_store_bytes_shaped(dims, voxelFormat, brickLog2, &vb, &sb) != GBV_OK) {
         fail(gbv_last_error());
         return false;
       }
-      if (!bricks.alloc(vb)) return false;
-      if (sb && !scaleOffset.alloc(sb / sizeof(float))) return false;
+      if (!bricks.alloc(vb, ctx->mem)) return false;
+      if (sb && !scaleOffset.alloc(sb / sizeof(float), ctx->mem)) return false;
       if (gbv_build_brick_store_shaped(td->scalars.p, dims, voxelFormat, brickLog2, bricks.p,
                                        sb ? scaleOffset.p : nullptr, s) != GBV_OK) {
         fail(gbv_last_error());
@@ -241,14 +262,14 @@ struct Volume : Object {  // volume/Volume.{h,cpp}, TransferFunction
     if (!sf || !sf->build(s)) return false;
     if (tfDirty || !majorants.p) {
       int n = (int)(tfHost.size() / 4);
-      if (!tf.alloc(tfHost.size())) return false;
+      if (!tf.alloc(tfHost.size(), ctx->mem)) return false;
       if (cudaMemcpyAsync(tf.p, tfHost.data(), tfHost.size() * sizeof(float), cudaMemcpyHostToDevice, s) !=
           cudaSuccess) {
         fail("transfer function upload failed");
         return false;
       }
       size_t nmc = (size_t)sf->mcDims[0] * sf->mcDims[1] * sf->mcDims[2];
-      if (!majorants.alloc(std::max<size_t>(nmc, 1))) return false;
+      if (!majorants.alloc(std::max<size_t>(nmc, 1), ctx->mem)) return false;
       if (gbv_map_majorants(sf->ranges.p, (int)nmc, tf.p, n, domain[0], domain[1], densityAt1, majorants.p, s) !=
           GBV_OK) {
         fail(gbv_last_error());
@@ -301,7 +322,7 @@ struct Light : Object {  // light/DirLight, light/EnvMap
   bool buildEnv(cudaStream_t s) {
     if (!texture || !texture->texels.p) { fail("envmap light without a texture"); return false; }
     if (!cdfDirty) return true;
-    if (!cdfY.alloc(texture->H) || !cdfX.alloc((size_t)texture->W * texture->H)) return false;
+    if (!cdfY.alloc(texture->H, ctx->mem) || !cdfX.alloc((size_t)texture->W * texture->H, ctx->mem)) return false;
     if (gbv_env_build_cdfs(texture->texels.p, texture->W, texture->H, texture->addr, cdfY.p, cdfX.p, s) != GBV_OK) {
       fail(gbv_last_error());
       return false;
@@ -446,6 +467,19 @@ BNContext bnContextCreate(const int *dataRanks, int numDataRanks, const int *gpu
     delete c;
     return nullptr;  // bnContextCreate returns 0 on failure (barney.cu:923-927)
   }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = c->device;
+  c->mem.stream = c->stream;
+  if (cudaMemPoolCreate(&c->mem.pool, &props) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(c->mem.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    c->mem.pool = nullptr;  // fall back to cudaMalloc / cudaFree
+    cudaGetLastError();
+  }
+  g_err.clear();  // a new context starts with no recorded failure
   std::lock_guard<std::mutex> lock(g_mutex);
   g_contexts.insert(c);
   return (BNContext)c;
@@ -459,7 +493,9 @@ void bnContextDestroy(BNContext context) {
   }
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  c->handles.clear();
+  c->handles.clear();  // the objects hand their buffers back to the pool
+  cudaStreamSynchronize(c->stream);
+  if (c->mem.pool) cudaMemPoolDestroy(c->mem.pool);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -526,8 +562,8 @@ BNTextureData bnTextureData3DCreate(BNContext context, int, BNDataType texelForm
   size_t n = (size_t)width * height * depth;
   auto td = std::make_shared<TextureData3D>();
   td->dims[0] = width; td->dims[1] = height; td->dims[2] = depth;
-  if (!td->scalars.alloc(n)) return nullptr;
   cudaSetDevice(c->device);
+  if (!td->scalars.alloc(n, c->mem)) return nullptr;
   if (texelFormat == BN_FLOAT32) {
     // texels are copied at create time (rtcore/cudaCommon/TextureData.cu:59-75)
     if (cudaMemcpyAsync(td->scalars.p, items, n * sizeof(float), cudaMemcpyDefault, c->stream) != cudaSuccess) {
@@ -540,7 +576,7 @@ BNTextureData bnTextureData3DCreate(BNContext context, int, BNDataType texelForm
     // normalised integer texels: upload the raw texels, normalise on the device
     const int bits = (texelFormat == BN_UFIXED8 || texelFormat == BN_UINT8) ? 8 : 16;
     DevBuf<unsigned char> raw;
-    if (!raw.alloc(n * (bits / 8))) return nullptr;
+    if (!raw.alloc(n * (bits / 8), c->mem)) return nullptr;
     if (cudaMemcpyAsync(raw.p, items, n * (bits / 8), cudaMemcpyDefault, c->stream) != cudaSuccess ||
         gbv_normalize_texels(raw.p, bits, (long long)n, td->scalars.p, c->stream) != GBV_OK ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
@@ -568,9 +604,10 @@ BNTexture2D bnTexture2DCreate(BNContext context, int, BNDataType texelFormat, ui
   t->H = (int)sy;
   t->addr[0] = (int)ax;
   t->addr[1] = (int)ay;
-  if (!t->texels.alloc((size_t)4 * sx * sy)) return nullptr;
   cudaSetDevice(c->device);
-  if (cudaMemcpy(t->texels.p, texels, (size_t)16 * sx * sy, cudaMemcpyDefault) != cudaSuccess) {
+  if (!t->texels.alloc((size_t)4 * sx * sy, c->mem)) return nullptr;
+  if (cudaMemcpyAsync(t->texels.p, texels, (size_t)16 * sx * sy, cudaMemcpyDefault, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess) {
     fail("texture upload failed");
     return nullptr;
   }
@@ -739,8 +776,9 @@ void bnFrameBufferResize(BNFrameBuffer fb, BNDataType colorFormat, int sx, int s
   f->H = sy;
   f->colorFormat = colorFormat;
   f->accumID = 0;
-  if (!f->accum.alloc((size_t)4 * sx * sy)) return;
-  f->color.alloc((size_t)16 * sx * sy);
+  cudaSetDevice(f->ctx->device);
+  if (!f->accum.alloc((size_t)4 * sx * sy, f->ctx->mem)) return;
+  f->color.alloc((size_t)16 * sx * sy, f->ctx->mem);
 }
 
 void bnFrameBufferGetSize(BNFrameBuffer fb, int *sx, int *sy) {
@@ -845,7 +883,7 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   // counters: [0..GBV_NUM_COUNTERS) event counts (renderer "frameStats" = 1),
   // else only a loop-cap flag, kept in the word after them (the counting
   // kernel is some 3% slower)
-  if (!f->counters.alloc(GBV_NUM_COUNTERS + 1)) return;
+  if (!f->counters.alloc(GBV_NUM_COUNTERS + 1, c->mem)) return;
   cudaMemsetAsync(f->counters.p, 0, (GBV_NUM_COUNTERS + 1) * sizeof(unsigned long long), c->stream);
   int *capFlag = reinterpret_cast<int *>(f->counters.p + GBV_NUM_COUNTERS);
   const gbv_status rs = rp.frameStats

@@ -178,7 +178,8 @@ BARNEY_API void bnFrameBufferGetSize(BNFrameBuffer fb, int *sizeX, int *sizeY);
 BARNEY_API void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer fb);
 
 /* Additions of this library (no counterpart in barney.h). */
-/* Message of the last failed bn* call on this thread ("" if none). */
+/* Message of the last failed bn* call on this thread ("" if none since the
+   thread's last successful bnContextCreate, which starts it afresh). */
 BARNEY_API const char *bnGetLastError(void);
 /* Statistics of the last bnRender on this frame buffer: density samples,
    macrocells entered, rays traced, loop-cap events. */

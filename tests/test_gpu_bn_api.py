@@ -67,6 +67,25 @@ def test_bn_errors_are_recorded(cuda):
         fb = L.bnFrameBufferCreate(ses.ctx, 0)
         L.bnFrameBufferResize(fb, 123, 8, 8, 1)
         assert "unsupported color format" in bn.last_error()
+    # a new context starts without a recorded failure
+    with bn.BarneySession():
+        assert bn.last_error() == ""
+
+
+def test_bn_scene_rebuilds_reuse_context_memory(cuda):
+    """Scenes built and released one after another on one context (as an app
+    that uploads a new volume every frame does) render the same frame each
+    time; their device buffers come from the context's memory pool."""
+    s = scenes.small_scene(dims=24, spp=2, width=40, height=24)
+    frames = []
+    with bn.BarneySession() as ses:
+        for _ in range(3):
+            assert ses.build_scene(s, s.scalars.ctypes.data) == ""
+            ses.render()
+            frames.append(ses.read().copy())
+            ses.release_scene()
+    for f in frames[1:]:
+        np.testing.assert_array_equal(f.view(np.uint32), frames[0].view(np.uint32))
 
 
 @pytest.mark.parametrize("bits", [8, 16])
