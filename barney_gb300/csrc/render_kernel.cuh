@@ -583,12 +583,13 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
 // with Woodcock::sampleRange (Volume.h:188-223) inside each cell of non-zero
 // majorant, as set up by MCVolumeAccel::isProg (MCAccelerator.h:569-708).
 // The state advances by bounded units so that a warp's lanes stay in one
-// loop: a run of at most `skip` (default kSkipDefault) empty cells, or one
-// Woodcock step.
+// loop: per warp iteration a lane makes at most `skip` (default
+// kSkipDefault) cell tests and distance draws to reach its next sample
+// position, then the warp's ready lanes take their density samples together.
 // -------------------------------------------------------------------------
 // Defaults of the launch shape (the best of a same-box sweep of skip 2..8
 // and threshold 3..8 on the 512^3 1080p frame; results never depend on them)
-constexpr int kSkipDefault = 3;
+constexpr int kSkipDefault = 4;
 constexpr int kThresholdDefault = 3;
 
 // Per-lane event counts; with On == false the counting and its registers
@@ -708,14 +709,23 @@ __device__ __forceinline__ bool trace_advance(Traversal &T, float tc, bool sx, b
   return true;
 }
 
-template <class Store, class Cnt>
-__device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store, const XF &xf, const MCGridDev &G,
-                                          Traversal &T, Hit &h, Cnt &cnt, int skip, bool staged,
+// The traversal is split so that the expensive part, the density sample,
+// runs for all of a warp's tracing lanes at once.  trace_seek advances a lane
+// to its next sample position: it crosses empty macrocells, enters the next
+// cell of non-zero majorant and draws Woodcock distances until one falls
+// inside the current cell (T.inCell = 2: a position is ready), at most
+// `units` cell tests and distance draws per call.  trace_sample then
+// samples there and makes the accept test.  Every lane performs exactly the
+// operations, in exactly the order, of the one-step-at-a-time loop
+// (dda::dda3 with Woodcock::sampleRange inside each cell); only the grouping
+// of a lane's steps into warp iterations differs.
+template <class Cnt>
+__device__ __forceinline__ int trace_seek(const MCGridDev &G, Traversal &T, Cnt &cnt, int units, bool staged,
                                           int *capFlag) {
   const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
   const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
-  if (!T.inCell) {
-    for (int k = 0; k < skip; k++) {
+  for (int k = 0; k < units; k++) {
+    if (!T.inCell) {
       GBV_COUNT(cnt, cells);
       if (++T.cells > maxCells) {
         GBV_COUNT(cnt, caps);
@@ -725,35 +735,44 @@ __device__ __forceinline__ int trace_step(const FieldGeom &F, const Store &store
       const float tc = reduce_min(T.t_next);
       const int ci = T.cx + G.M[0] * (T.cy + G.M[1] * T.cz);
       const bool nonzero = staged ? ((g_smem[ci >> 5] >> (ci & 31)) & 1u) != 0u : __ldg(G.maj + ci) != 0.f;
-      if (nonzero) {
-        const float maj = __ldg(G.maj + ci);
-        const float cell_t0 = T.ray_t0 + T.ncb;
-        const float cell_t1 = T.ray_t0 + mn(tc, T.tMax);
-        T.inCell = 1;
-        T.tc = tc;
-        T.maj = maj;
-        T.t = cell_t0;
-        T.segHi = mn(cell_t1, T.rayTMax);
-        T.steps = 0;
-        GBV_COUNT(cnt, mcs);
-        break;
+      if (!nonzero) {
+        if (!trace_advance(T, tc, sx, sy, sz)) return TR_MISS;
+        continue;
       }
-      if (!trace_advance(T, tc, sx, sy, sz)) return TR_MISS;
+      const float maj = __ldg(G.maj + ci);
+      const float cell_t0 = T.ray_t0 + T.ncb;
+      const float cell_t1 = T.ray_t0 + mn(tc, T.tMax);
+      T.inCell = 1;
+      T.tc = tc;
+      T.maj = maj;
+      T.t = cell_t0;
+      T.segHi = mn(cell_t1, T.rayTMax);
+      T.steps = 0;
+      GBV_COUNT(cnt, mcs);
     }
-    if (!T.inCell) return TR_CONTINUE;
-  }
-  // one Woodcock step
-  const float r = T.rng();
-  const float dt = -fastLog(1.f - r) / T.maj;
-  T.t += dt;
-  if (T.t >= T.segHi || ++T.steps > kWoodcockCap) {
-    if (T.steps > kWoodcockCap) {
-      GBV_COUNT(cnt, caps);
-      if (capFlag) *capFlag = 1;
+    // one Woodcock distance
+    const float r = T.rng();
+    const float dt = -fastLog(1.f - r) / T.maj;
+    T.t += dt;
+    if (T.t >= T.segHi || ++T.steps > kWoodcockCap) {
+      if (T.steps > kWoodcockCap) {
+        GBV_COUNT(cnt, caps);
+        if (capFlag) *capFlag = 1;
+      }
+      T.inCell = 0;
+      if (!trace_advance(T, T.tc, sx, sy, sz)) return TR_MISS;
+      continue;
     }
-    T.inCell = 0;
-    return trace_advance(T, T.tc, sx, sy, sz) ? TR_CONTINUE : TR_MISS;
+    T.inCell = 2;
+    return TR_CONTINUE;
   }
+  return TR_CONTINUE;
+}
+
+template <class Store, class Cnt>
+__device__ __forceinline__ int trace_sample(const FieldGeom &F, const Store &store, const XF &xf, Traversal &T,
+                                            Hit &h, Cnt &cnt) {
+  T.inCell = 1;
   const vec3 P = T.org + T.t * T.dir;
   const vec4 smp = sample_and_map(F, store, xf, P);
   GBV_COUNT(cnt, samples);
@@ -967,8 +986,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
           simt[0]++;
           simt[1] += (unsigned)tracing;
         }
-        if (tstate == TRACING && trace_step(p.F, make_store<Store>(p), p.xf, p.G, T, h, cnt, L.skip,
-                                            !Batch && L.maskWords > 0, L.capFlag) != TR_CONTINUE)
+        if (tstate == TRACING && T.inCell != 2 &&
+            trace_seek(p.G, T, cnt, L.skip, !Batch && L.maskWords > 0, L.capFlag) == TR_MISS)
+          tstate = DONE;
+        if (tstate == TRACING && T.inCell == 2 && trace_sample(p.F, make_store<Store>(p), p.xf, T, h, cnt) == TR_HIT)
           tstate = DONE;
       }
     }
