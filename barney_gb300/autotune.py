@@ -11,7 +11,8 @@ and tests/test_gpu_bricks.py check both bit for bit):
   is compiled for each register budget);
 * threshold     -- a warp keeps traversing while at least this percentage of
   its busy lanes still traces, then shades together;
-* skip          -- empty macrocells a lane may cross in one traversal unit.
+* skip          -- cell tests and distance draws a lane may make per traversal
+  iteration to reach its next sample position.
 
 tune_batch() times launch shapes of an existing batch; tuned_batch() also
 rebuilds the stores with each candidate brick shape (coordinate descent:
@@ -28,7 +29,7 @@ import json
 import os
 from pathlib import Path
 
-LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (2, 3, 5) for k in (2, 3, 4, 8)]
+LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (5, 12, 20) for k in (4, 6, 8)]
 BRICK_CANDIDATES = [(3, 3, 3), (2, 2, 2), (4, 4, 4), (4, 4, 2), (5, 3, 2)]
 
 

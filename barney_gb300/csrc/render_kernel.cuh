@@ -587,10 +587,12 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
 // kSkipDefault) cell tests and distance draws to reach its next sample
 // position, then the warp's ready lanes take their density samples together.
 // -------------------------------------------------------------------------
-// Defaults of the launch shape (the best of a same-box sweep of skip 2..8
-// and threshold 3..8 on the 512^3 1080p frame; results never depend on them)
-constexpr int kSkipDefault = 4;
-constexpr int kThresholdDefault = 3;
+// Defaults of the launch shape (the best of a same-box sweep of 3..64 units
+// per seek and thresholds 3..30% on the 512^3 1080p frame; units 5..8 with
+// thresholds 12..20 are within 1% of each other; results never depend on
+// them)
+constexpr int kSkipDefault = 6;
+constexpr int kThresholdDefault = 12;
 
 // Per-lane event counts; with On == false the counting and its registers
 // compile away (timed launches pass no counter buffer).
@@ -1127,10 +1129,11 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
 
 // GBV_RENDER_OCC=4, 5 or 6 selects the resident blocks per SM the registers
 // are capped for (default 5: 40 warps per SM at 51 registers; the kernel is
-// latency-bound and gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the empty
-// macrocells crossed per traversal step (default 3); GBV_RENDER_THRESH the
-// percentage of a warp's busy lanes that must still be tracing for the warp
-// to keep traversing before it shades and refills (default 3).
+// latency-bound and gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the cell
+// tests and distance draws a lane may make per traversal iteration (default
+// 6); GBV_RENDER_THRESH the percentage of a warp's busy lanes that must still
+// be tracing for the warp to keep traversing before it shades and refills
+// (default 12).
 template <class Store>
 inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
   const char *sk = getenv("GBV_RENDER_SKIP");
