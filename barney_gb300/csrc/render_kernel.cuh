@@ -309,11 +309,13 @@ static __device__ __noinline__ float env_pdf(const RenderParams &p, vec3 dir) {
 // env light is the one selected; they use no random numbers, so the random
 // stream is consumed exactly as in one piece.
 struct EnvPick {
-  vec3 radiance;
+  vec3 radiance; // scale * texel(sx, sy)
   float sx, sy;  // sampled texture coordinates
   float pdfxy;   // pdf_x * pdf_y
 };
-static __device__ __noinline__ EnvPick env_pick(const RenderParams &p, Random &r) {
+// The random draws and CDF searches of the sample; the texel at (sx, sy)
+// is fetched by the caller (see the shading phase of render_kernel).
+static __device__ __noinline__ EnvPick env_pick_coords(const RenderParams &p, Random &r) {
   const EnvDev &e = p.env;
   EnvPick k;
   float r_y = r();
@@ -323,8 +325,6 @@ static __device__ __noinline__ EnvPick env_pick(const RenderParams &p, Random &r
   int ix = sample_cdf_x(p, iy, r_x, pdf_x);
   k.sx = ((float)ix + r()) / (float)e.W;
   k.sy = ((float)iy + r()) / (float)e.H;
-  float4 t = tex2D(e, k.sx, k.sy);
-  k.radiance = e.scale * vec3(t.x, t.y, t.z);
   k.pdfxy = pdf_x * pdf_y;
   return k;
 }
@@ -388,13 +388,11 @@ __device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random 
 }
 
 // shadeRays.cu:268-404 (no area or point lights in this world)
-__device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &random, LightSample &ls,
-                                              bool &needsMIS, bool &isDir) {
+__device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &random, const EnvPick &pick,
+                                              LightSample &ls, bool &needsMIS, bool &isDir) {
   needsMIS = false;
   LightSample els;
-  EnvPick pick;
   if (p.hasEnv) {
-    pick = env_pick(p, random);
     els.radiance = pick.radiance;
     els.distance = __int_as_float(0x7f800000);
   } else {
@@ -432,19 +430,16 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
   return true;
 }
 
-// shadeRays.cu:437-456
-static __device__ __noinline__ vec3 radiance_from_env(const RenderParams &p, vec3 rayDir) {
-  if (p.hasEnv) {
-    vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
-    const float2 tp = spherical_theta_phi(d);
-    float theta = tp.x;
-    float phi = tp.y;
-    const float invPi = 1.f / (float)3.14159265358979323846;
-    const float inv2Pi = 1.f / (2.f * (float)3.14159265358979323846);
-    float4 c = tex2D(p.env, phi * inv2Pi, theta * invPi);
-    return p.env.scale * vec3(c.x, c.y, c.z);
-  }
-  return vec3(p.ambient);
+// radianceFromEnv (shadeRays.cu:437-456) up to the texture read: the
+// env-map coordinates of a ray direction
+static __device__ __noinline__ float2 env_miss_coords(const RenderParams &p, vec3 rayDir) {
+  vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
+  const float2 tp = spherical_theta_phi(d);
+  float theta = tp.x;
+  float phi = tp.y;
+  const float invPi = 1.f / (float)3.14159265358979323846;
+  const float inv2Pi = 1.f / (2.f * (float)3.14159265358979323846);
+  return make_float2(phi * inv2Pi, theta * invPi);
 }
 
 // Phase.h:49-57
@@ -501,19 +496,22 @@ struct ShadeOut {
 
 // bounce() for a volume hit (shadeRays.cu:605-878).  Updates `ray`; a dead
 // ray has tMax = -1.
+// `random` is the hit's stream, Random2(ray.rngSeed, tHit), already derived
+// (it advanced ray.seed); with an env map `pick` holds the light sample's
+// texel coordinates and radiance.
 static __device__ __noinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
-                                                  int pathDepth, ShadeOut &out) {
+                                                  int pathDepth, Random &random, const EnvPick &pick,
+                                                  ShadeOut &out) {
   out.shadowValid = false;
   const float tHit = h.t;
   const vec3 albedo = p.multi ? p.scatAlb * h.rgb : .7f * h.rgb;
   const float g = p.multi ? p.aniso : 0.f;
   const vec3 incomingThroughput = from_half(ray.tp);
-  Random random = Random::derive(ray.seed, (uint64_t)float_bits(tHit));
   const vec3 wo = -normalize(ray.dir);
   const float offsetEpsilon = mx(1e-4f, 1e-6f * reduce_max(vabs(P)));
   LightSample ls;
   bool needsMIS = false, isDir = false;
-  if (sample_lights(p, random, ls, needsMIS, isDir)) {
+  if (sample_lights(p, random, pick, ls, needsMIS, isDir)) {
     float density = p.multi ? phase_pdf(p, g, wo, ls.direction) : kOneOverFourPi;
     vec3 fr = density * albedo;
     if (!(density > 0.f) || reduce_max(fr) < 1e-4f) {
@@ -1010,6 +1008,32 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       }
     }
     if (tstate == DONE) {
+      // Env-map texels: a main ray's miss lookup (radianceFromEnv) and a
+      // volume hit's env light sample (EnvMap::sample) each form their
+      // texture coordinates first; then one call fetches the texels of all
+      // lanes that need one, instead of one call per kind of lane.
+      Random rnd;
+      EnvPick pick;
+      float2 uv = make_float2(0.f, 0.f);
+      bool needTex = false;
+      if (kind == K_MAIN) {
+        if (h.hit) {
+          rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.t));
+          if (p.hasEnv) {
+            pick = env_pick_coords(p, rnd);
+            uv = make_float2(pick.sx, pick.sy);
+            needTex = true;
+          }
+        } else if (p.hasEnv) {
+          uv = env_miss_coords(p, ray.dir);
+          needTex = true;
+        }
+      }
+      vec3 texel(0.f);
+      if (needTex) {
+        const float4 t = tex2D(p.env, uv.x, uv.y);
+        texel = p.env.scale * vec3(t.x, t.y, t.z);
+      }
       tstate = NEED;
       const int accumID = L.accumIdStart + s;
       const float clampMax = 10.f * (float)(1 + accumID);
@@ -1021,7 +1045,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         float alpha = 0.f;
         if (!h.hit) {
           const float4 miss = miss_color(p, iy);
-          const vec3 env = (gen != 0 || p.hasEnv) ? radiance_from_env(p, ray.dir) : vec3(0.f);
+          const vec3 env = p.hasEnv ? texel : (gen != 0 ? vec3(p.ambient) : vec3(0.f));
           if (gen == 0) {
             alpha = miss.w;
             frag = p.hasEnv ? env : vec3(miss.x, miss.y, miss.z);
@@ -1033,7 +1057,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
           if (gen == 0) alpha = 1.f;
           ShadeOut so;
           // setVolumeHit's P = obj_org + t * obj_dir (MCAccelerator.h:79)
-          bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, so);
+          pick.radiance = texel;
+          bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
           if (so.shadowValid && so.shadow.tMax > 0.f) {
             sray = so.shadow;
             shadowPending = true;
