@@ -164,12 +164,23 @@ GBV_HD vec3 from_half(vec3h v) { return vec3(h2f(v.x), h2f(v.y), h2f(v.z)); }
 // ---------------------------------------------------------------------------
 struct RNGSeed {
   uint64_t state;
+  // The output is the low word of (x ^ (x >> 22)) >> (22 + (x >> 61)).  The
+  // shift is always 22..29, so on the device both shifts are 32-bit funnel
+  // shifts of the state's halves (identical result, fewer instructions than
+  // a general 64-bit shift).
   GBV_HD uint32_t next() {
     uint64_t x = state;
-    unsigned count = (unsigned)(x >> 61);
     state = x * 6364136223846793005ull;
+#if defined(__CUDA_ARCH__)
+    const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+    const uint32_t ylo = lo ^ __funnelshift_r(lo, hi, 22);
+    const uint32_t yhi = hi ^ (hi >> 22);
+    return __funnelshift_r(ylo, yhi, 22u + (hi >> 29));
+#else
+    unsigned count = (unsigned)(x >> 61);
     x ^= x >> 22;
     return (uint32_t)(x >> (22 + count));
+#endif
   }
   GBV_HD uint32_t next_h(uint64_t hash) {
     state ^= (hash << 1);
