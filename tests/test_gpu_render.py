@@ -235,3 +235,32 @@ def test_shared_memory_staging_is_transparent(cuda, stage):
         del os.environ["GBV_RENDER_STAGE"]
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(a), bits(b))
+
+
+@pytest.mark.parametrize("settings", [{"GBV_RENDER_SKIP": "1"},
+                                      {"GBV_RENDER_SKIP": "64", "GBV_RENDER_THRESH": "100"},
+                                      {"GBV_RENDER_THRESH": "1", "GBV_RENDER_OCC": "4"},
+                                      {"GBV_RENDER_OCC": "6", "GBV_RENDER_SKIP": "2"}])
+def test_launch_settings_do_not_change_frames(cuda, settings):
+    """Units per seek (1: one cell test or one distance draw per traversal
+    iteration; 64: the whole way to the next sample), traversal thresholds
+    (1%: traverse until every lane is done; 100%: shade as soon as one lane
+    finishes) and resident blocks only regroup each lane's steps: the frame
+    (multiple scattering, env map) is bit-identical to the default launch's."""
+    import os
+    import torch
+    s = _ms_scene(4, w=64, h=48, dims=48)
+    g = GpuScene(s)
+    a = g.render(spp=4, accum_id_start=3).cpu().numpy()
+    saved = {k: os.environ.get(k) for k in settings}
+    os.environ.update(settings)
+    try:
+        b = g.render(spp=4, accum_id_start=3).cpu().numpy()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(a), bits(b))
