@@ -124,7 +124,8 @@ __device__ __forceinline__ float fmod_wrap(float x, float y) {
   return fmod_general(x, y);
 }
 
-// Texture.cpp:25-93, mirror mode (out of line: env maps here wrap or clamp)
+// rtcore/embree/Texture.cpp:25-93, mirror mode (out of line: env maps here
+// wrap or clamp)
 static __device__ __noinline__ void compute_address_mirror(float tc, int N, int &i0, int &i1, float &f) {
   tc = tc * (float)N + .5f;
   float fc = floorf(tc);
