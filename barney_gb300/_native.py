@@ -77,6 +77,7 @@ def lib() -> C.CDLL:
             "gbv_render_tiles": (st, [C.POINTER(GbvScene), vp, i, i, i, i, i, i, vp, vp]),
             "gbv_tile_partition": (st, [i, i, i, i, ip, ip]),
             "gbv_selftest_sincos": (st, [vp, C.c_longlong, vp, vp, i, vp]),
+            "gbv_selftest_angles": (st, [vp, vp, C.c_longlong, vp, vp, i, vp]),
             "gbv_normalize_texels": (st, [vp, i, C.c_longlong, vp, vp]),
             "gbv_compressed_tile_bytes": (C.c_size_t, []),
             "gbv_compress_tiles": (st, [vp, i, i, i, i, i, vp, vp]),

@@ -186,6 +186,30 @@ gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn, float *cs
   return check_launch("sincos_angle_kernel");
 }
 
+__global__ void angles_kernel(const float *__restrict__ y, const float *__restrict__ x, long long n,
+                              float *__restrict__ acos_x, float *__restrict__ atan2_yx) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  acos_x[i] = acos_angle(x[i]);
+  atan2_yx[i] = atan2_angle(y[i], x[i]);
+}
+
+gbv_status gbv_selftest_angles(const float *y, const float *x, long long n, float *acos_x, float *atan2_yx,
+                               int on_device, void *stream) {
+  if (!y || !x || !acos_x || !atan2_yx || n < 0)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_selftest_angles: bad argument");
+  if (n == 0) return GBV_OK;
+  if (!on_device) {
+    for (long long i = 0; i < n; i++) {
+      acos_x[i] = acos_angle(x[i]);
+      atan2_yx[i] = atan2_angle(y[i], x[i]);
+    }
+    return GBV_OK;
+  }
+  angles_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(y, x, n, acos_x, atan2_yx);
+  return check_launch("angles_kernel");
+}
+
 gbv_status gbv_normalize_texels(const void *d_texels, int bits, long long n, float *d_scalars, void *stream) {
   if (!d_texels || !d_scalars || n < 0 || (bits != 8 && bits != 16))
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_normalize_texels: bad argument (bits must be 8 or 16)");

@@ -276,6 +276,65 @@ GBV_HD void sincos_angle(float x, float &sn, float &cs) {
   }
 }
 
+// Arc cosine and two-argument arc tangent of the env-map angles (theta =
+// acos z and phi = atan2(y, x) of a direction), written from the series of
+// arcsin and arctan so that host and device compute the same bits:
+// * asin(s) = s + s t P(t), t = s^2, for s in [0, 1/2]; acos z = pi/2 -
+//   asin z for |z| <= 1/2, and acos z = 2 asin(sqrt((1 - z)/2)) (z > 1/2) or
+//   pi - 2 asin(sqrt((1 + z)/2)) (z < -1/2);
+// * atan(u) = u + u w Q(w), w = u^2, for |u| <= tan(pi/8); atan2 reduces the
+//   ratio of the smaller to the larger magnitude to that range with
+//   atan(t) = pi/4 + atan((t - 1)/(t + 1)), then pi/2 - a, pi - a and the
+//   sign of y place it in its octant.
+// P (degree 5) and Q (degree 6) are least-squares fits, reweighted toward the
+// largest relative error, of (asin s - s)/(s t) and (atan u - u)/(u w) on
+// those ranges (fitted for this library).  pi/2, pi and pi/4 enter as
+// two-float sums.  Against float64: acos within 1.2 ulp, atan2 within 2.2
+// ulp (tests); no contraction, the same on host and device.
+constexpr float kPio2Hi = 0x1.921fb6p+0f, kPio2Lo = -0x1.777a5cp-25f;
+constexpr float kPiHi = 0x1.921fb6p+1f, kPiLo = -0x1.777a5cp-24f;
+constexpr float kPio4Hi = 0x1.921fb6p-1f, kPio4Lo = -0x1.777a5cp-26f;
+constexpr float kTanPi8 = 0x1.a8279ap-2f;
+GBV_HD float asin_series(float s, float t) {  // asin(s), s in [0, 1/2], t = s^2
+  const float p =
+      ((((0x1.06a85p-5f * t + 0x1.28e096p-6f) * t + 0x1.fa3d84p-6f) * t + 0x1.6d7fd6p-5f) * t + 0x1.3333a6p-4f) * t +
+      0x1.555556p-3f;
+  return s + (s * t) * p;
+}
+// Both functions pick their operands with selects, so that a warp whose
+// lanes fall on both sides of a reduction evaluates one series and (atan2)
+// one division, not both branches.
+GBV_HD float acos_angle(float z) {  // z in [-1, 1]
+  const float a = fabsf(z);
+  const bool mid = a <= .5f;
+  const float tb = (1.f - a) * .5f;
+  const float t = mid ? a * a : tb;
+  const float s = mid ? a : sqrtf(tb);
+  const float w = asin_series(s, t);
+  const float wm = copysignf(w, z), w2 = 2.f * w;
+  if (mid) return (kPio2Lo - wm) + kPio2Hi;
+  return z > 0.f ? w2 : (kPiLo - w2) + kPiHi;
+}
+GBV_HD float atan_series(float u) {  // atan(u), |u| <= tan(pi/8)
+  const float w = u * u;
+  const float q =
+      (((((-0x1.4b32d6p-5f * w + 0x1.2441d2p-4f) * w - 0x1.71d376p-4f) * w + 0x1.c6f68p-4f) * w - 0x1.2491cp-3f) * w +
+       0x1.999998p-3f) * w -
+      0x1.555556p-2f;
+  return u + (u * w) * q;
+}
+GBV_HD float atan2_angle(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = ax < ay ? ay : ax, mn = ax < ay ? ax : ay;
+  const bool red = mn > kTanPi8 * mx;
+  const float c = atan_series((red ? mn - mx : mn) / (red ? mn + mx : mx));
+  float a = red ? (kPio4Lo + c) + kPio4Hi : c;
+  if (mx == 0.f) a = 0.f;
+  if (ay > ax) a = (kPio2Lo - a) + kPio2Hi;
+  if (signbit(x)) a = (kPiLo - a) + kPiHi;
+  return copysignf(a, y);
+}
+
 // rtcore/embree/Texture.cpp:324-336
 GBV_HD void lerp_coords(int N, float tc, int &i0, int &i1, float &f) {
   if (tc - .5f <= 0.f) { i0 = i1 = 0; f = 0.f; return; }

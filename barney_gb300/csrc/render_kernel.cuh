@@ -182,10 +182,10 @@ static __device__ __noinline__ float4 tex2D(const EnvDev &e, float u, float v) {
   return lerp4(fy, lerp4(fx, v00, v01), lerp4(fx, v10, v11));
 }
 
-// DG.h:97-106
-__device__ __forceinline__ float spherical_theta(vec3 v) { return acosf(clampv(v.z, -1.f, 1.f)); }
+// DG.h:97-106 (acos and atan2 by this library's series, gbv_math.cuh)
+__device__ __forceinline__ float spherical_theta(vec3 v) { return acos_angle(clampv(v.z, -1.f, 1.f)); }
 __device__ __forceinline__ float spherical_phi(vec3 v) {
-  float p = atan2f(v.y, v.x);
+  float p = atan2_angle(v.y, v.x);
   return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
 }
 // (theta, phi) of a direction in the env map's frame; one out-of-line copy

@@ -166,7 +166,9 @@ __global__ void env_lines_kernel(int W, int H, float *cdf_y, float *cdf_x) {
   line[W - 1] = 1.f;
   float rel_y = ((float)y + .5f) / (float)H;
   const float theta = kPi * rel_y;
-  cdf_y[y] = sum * sinf(theta);
+  float sinTheta, cosTheta;
+  sincos_angle(theta, sinTheta, cosTheta);  // theta in (0, pi): the renderer's bounded sine
+  cdf_y[y] = sum * sinTheta;
 }
 __global__ void env_normalize_kernel(int H, float *cdf_y) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;

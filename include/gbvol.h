@@ -377,6 +377,15 @@ gbv_status gbv_iso_intersect(const gbv_scene *scene, const float *d_ranges,
 gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn,
                                float *cs, int on_device, void *stream);
 
+/* The renderer's arc cosine and two-argument arc tangent of env-map angles:
+   acos_x[i] = acos(x[i]) (x in [-1, 1]) and atan2_yx[i] = atan2(y[i], x[i]),
+   on the host (on_device = 0; host pointers) or in a kernel on `stream`
+   (on_device = 1; device pointers).  Both give identical results; tests
+   check them against float64. */
+gbv_status gbv_selftest_angles(const float *y, const float *x, long long n,
+                               float *acos_x, float *atan2_yx, int on_device,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif

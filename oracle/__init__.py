@@ -34,7 +34,7 @@ class OrcScene(C.Structure):
         ("env_dir", _f3), ("env_up", _f3), ("env_scale", C.c_float),
         ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
-        ("width", C.c_int), ("height", C.c_int), ("u8_scaled", C.c_int),
+        ("width", C.c_int), ("height", C.c_int), ("u8_scaled", C.c_int), ("bounded_math", C.c_int),
     ]
 
 
@@ -82,6 +82,8 @@ def lib() -> C.CDLL:
             "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
             "orc_ea_render": (None, [sp, C.POINTER(OrcEAView), i, f, i, i, vp]),
             "orc_ea_backward": (None, [sp, C.POINTER(OrcEAView), i, f, vp, i, vp, vp]),
+            "orc_bounded_sincos": (None, [vp, C.c_longlong, vp, vp]),
+            "orc_bounded_angles": (None, [vp, vp, C.c_longlong, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -95,13 +97,34 @@ def _p(a: np.ndarray) -> C.c_void_p:
     return a.ctypes.data_as(C.c_void_p)
 
 
+def bounded_sincos(x: np.ndarray):
+    """Sine and cosine of angles in [-pi/4, 2 pi + pi/4] by the oracle's
+    bounded method (one of those orc_scene.bounded_math selects)."""
+    x = np.ascontiguousarray(x, np.float32)
+    sn, cs = np.empty_like(x), np.empty_like(x)
+    lib().orc_bounded_sincos(_p(x), x.size, _p(sn), _p(cs))
+    return sn, cs
+
+
+def bounded_angles(y: np.ndarray, x: np.ndarray):
+    """acos(x) and atan2(y, x) by the oracle's bounded methods."""
+    y = np.ascontiguousarray(y, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    ac, at = np.empty_like(x), np.empty_like(x)
+    lib().orc_bounded_angles(_p(y), _p(x), x.size, _p(ac), _p(at))
+    return ac, at
+
+
 class Oracle:
     """Oracle view of a barney_gb300.scenes.Scene (keeps its arrays alive)."""
 
-    def __init__(self, scene, scalars=None, majorants=None, u8=False):
+    def __init__(self, scene, scalars=None, majorants=None, u8=False, bounded_math=False):
         """u8=True samples the field as the library's U8 brick store holds it
         (8-bit per 8^3-cell scale brick) and bounds macrocells by the
-        dequantized corners -- float arithmetic only."""
+        dequantized corners -- float arithmetic only.  bounded_math=True
+        takes the path's sines, cosines, arc cosines and arc tangents
+        (scattering azimuth, env-map CDF rows, env sample and pdf angles,
+        env lookups) by the device code's bounded methods instead of libm's."""
         self.s = scene
         self.u8 = bool(u8)
         self.scalars = np.ascontiguousarray(scene.scalars if scalars is None else scalars, dtype=np.float32)
@@ -147,6 +170,7 @@ class Oracle:
         r.max_volume_bounces = scene.max_volume_bounces
         r.width, r.height = scene.width, scene.height
         r.u8_scaled = 1 if self.u8 else 0
+        r.bounded_math = 1 if bounded_math else 0
         self.rec = r
 
     # -- macrocells --

@@ -86,6 +86,84 @@ static const float ONE_OVER_PI = 1.f / 3.14159265358979323846f;
 static const float ONE_OVER_TWO_PI = 1.f / (2.f * 3.14159265358979323846f);
 static const float ONE_OVER_FOUR_PI = 1.f / (4.f * 3.14159265358979323846f);
 
+// Sine and cosine of an angle x in [-pi/4, 2 pi + pi/4], the bounded method
+// of the library's device code (orc_scene.bounded_math; the reference uses
+// libm): Cody-Waite reduction r = x - k pi/2, k = rint(x 2/pi), with pi/2
+// split into three floats (201/128, the next 21 bits, the rest rounded), so
+// r is exact near multiples of pi/2; then Taylor polynomials of sin (to r^9)
+// and cos (to r^10) on |r| <= pi/4 in Horner form, and the quadrant k mod 4
+// picks signs and roles.  Built without contraction, like the device code.
+static void bounded_sincos(float x, float &sn, float &cs) {
+  const float k = rintf(x * 0.636619772f);
+  const float r = ((x - k * 0x1.92p+0f) - k * 0x1.fb544p-12f) - k * 0x1.0b4612p-34f;
+  const float r2 = r * r;
+  const float ps = r + (r * r2) * (-1.f / 6.f + r2 * (1.f / 120.f + r2 * (-1.f / 5040.f + r2 * (1.f / 362880.f))));
+  const float pc =
+      1.f - .5f * r2 + (r2 * r2) * (1.f / 24.f + r2 * (-1.f / 720.f + r2 * (1.f / 40320.f + r2 * (-1.f / 3628800.f))));
+  const int q = (int)k & 3;
+  if (q == 0) { sn = ps; cs = pc; }
+  else if (q == 1) { sn = pc; cs = -ps; }
+  else if (q == 2) { sn = -ps; cs = -pc; }
+  else { sn = -pc; cs = ps; }
+}
+// the path's sine and cosine: libm (the reference) or the bounded method
+inline void path_sincos(bool bounded, float x, float &sn, float &cs) {
+  if (bounded) bounded_sincos(x, sn, cs);
+  else { sn = sinf(x); cs = cosf(x); }
+}
+// Arc cosine and two-argument arc tangent by the library's series
+// (orc_scene.bounded_math; the reference uses libm): asin s = s + s t P(t)
+// with t = s^2 on [0, 1/2], acos from it by pi/2 - asin z or
+// 2 asin(sqrt((1 -+ z)/2)) (pi minus that for z < -1/2); atan u = u + u w Q(w)
+// with w = u^2 on |u| <= tan(pi/8), atan2 by the pi/4 reduction of the
+// magnitude ratio, then pi/2 - a, pi - a and the sign of y.  P, Q are the
+// library's fitted coefficients; pi/2, pi, pi/4 as two-float sums.
+static const float PIO2_HI = 0x1.921fb6p+0f, PIO2_LO = -0x1.777a5cp-25f;
+static const float PI_HI = 0x1.921fb6p+1f, PI_LO = -0x1.777a5cp-24f;
+static const float PIO4_HI = 0x1.921fb6p-1f, PIO4_LO = -0x1.777a5cp-26f;
+static float series_asin(float s, float t) {
+  float p = 0x1.06a85p-5f;
+  p = p * t + 0x1.28e096p-6f;
+  p = p * t + 0x1.fa3d84p-6f;
+  p = p * t + 0x1.6d7fd6p-5f;
+  p = p * t + 0x1.3333a6p-4f;
+  p = p * t + 0x1.555556p-3f;
+  return s + (s * t) * p;
+}
+static float bounded_acos(float z) {
+  const float a = fabsf(z);
+  if (a <= 0.5f) {
+    const float s = copysignf(series_asin(a, a * a), z);
+    return (PIO2_LO - s) + PIO2_HI;
+  }
+  const float t = (1.f - a) * 0.5f;
+  const float w = 2.f * series_asin(sqrtf(t), t);
+  if (z > 0.f) return w;
+  return (PI_LO - w) + PI_HI;
+}
+static float series_atan(float u) {
+  const float w = u * u;
+  float q = -0x1.4b32d6p-5f;
+  q = q * w + 0x1.2441d2p-4f;
+  q = q * w - 0x1.71d376p-4f;
+  q = q * w + 0x1.c6f68p-4f;
+  q = q * w - 0x1.2491cp-3f;
+  q = q * w + 0x1.999998p-3f;
+  q = q * w - 0x1.555556p-2f;
+  return u + (u * w) * q;
+}
+static float bounded_atan2(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float big = ax < ay ? ay : ax, small = ax < ay ? ax : ay;
+  float a;
+  if (big == 0.f) a = 0.f;
+  else if (small > 0x1.a8279ap-2f * big) a = (PIO4_LO + series_atan((small - big) / (small + big))) + PIO4_HI;
+  else a = series_atan(small / big);
+  if (ay > ax) a = (PIO2_LO - a) + PIO2_HI;
+  if (std::signbit(x)) a = (PI_LO - a) + PI_HI;
+  return copysignf(a, y);
+}
+
 // ---------------------------------------------------------------------------
 // half precision with the embree backend's rounding (rtcore/embree/Float16.cpp
 // float32ToFloat16: round to nearest, ties away from zero; subnormals kept)
@@ -479,6 +557,7 @@ inline M3 inverse(const M3 &m) {
 
 struct Env {
   bool present = false;
+  bool boundedMath = false;  // orc_scene.bounded_math
   const float *tex = nullptr;
   int W = 0, H = 0;
   int addr[2] = {0, 0};
@@ -551,7 +630,8 @@ inline V4<float> tex2D(const float *tex, int W, int H, const int addr[2], float 
 }
 
 // EnvMap.cu:61-137 (ComputeWeights_xy, ComputeCDFs_doLine, Normalize_cdf_y)
-inline void env_cdfs(const float *tex, int W, int H, const int addr[2], float *cdf_y, float *cdf_x) {
+inline void env_cdfs(const float *tex, int W, int H, const int addr[2], float *cdf_y, float *cdf_x,
+                     bool boundedMath = false) {
   for (int iy = 0; iy < H; iy++)
     for (int ix = 0; ix < W; ix++) {
       float weight = 0.f;
@@ -575,7 +655,9 @@ inline void env_cdfs(const float *tex, int W, int H, const int addr[2], float *c
     line[W - 1] = 1.f;
     float rel_y = (y + .5f) / H;
     const float theta = ONE_PI * rel_y;
-    cdf_y[y] = sum * sinf(theta);
+    float sinTheta, cosTheta;
+    path_sincos(boundedMath, theta, sinTheta, cosTheta);
+    cdf_y[y] = sum * sinTheta;
   }
   float sum = 0.f;
   for (int i = 0; i < H; i++) sum += cdf_y[i];
@@ -671,6 +753,7 @@ inline void build_scene(const orc_scene *s, Scene &S) {
     S.dir[i].color = V3<float>(s->dir_light_color[i][0], s->dir_light_color[i][1], s->dir_light_color[i][2]);
     S.dir[i].radiance = s->dir_light_radiance[i];
   }
+  S.env.boundedMath = s->bounded_math != 0;
   if (s->env_texels) {
     Env &e = S.env;
     e.present = true;
@@ -689,7 +772,7 @@ inline void build_scene(const orc_scene *s, Scene &S) {
     e.toLocal = inverse(e.toWorld);
     e.cdf_y.resize(e.H);
     e.cdf_x.resize((size_t)e.W * e.H);
-    env_cdfs(e.tex, e.W, e.H, e.addr, e.cdf_y.data(), e.cdf_x.data());
+    env_cdfs(e.tex, e.W, e.H, e.addr, e.cdf_y.data(), e.cdf_x.data(), e.boundedMath);
   }
   S.bg = {s->bg_color[0], s->bg_color[1], s->bg_color[2], s->bg_color[3]};
   S.ambient = s->ambient_radiance;
@@ -701,9 +784,12 @@ inline void build_scene(const orc_scene *s, Scene &S) {
 }
 
 // DG.h:97-106
-inline float sphericalTheta(V3<float> v) { return acosf(clampv(v.z, -1.f, 1.f)); }
-inline float sphericalPhi(V3<float> v) {
-  float p = atan2f(v.y, v.x);
+inline float sphericalTheta(V3<float> v, bool boundedMath) {
+  const float z = clampv(v.z, -1.f, 1.f);
+  return boundedMath ? bounded_acos(z) : acosf(z);
+}
+inline float sphericalPhi(V3<float> v, bool boundedMath) {
+  float p = boundedMath ? bounded_atan2(v.y, v.x) : atan2f(v.y, v.x);
   return (p < 0.f) ? (p + float(2.f * M_PI)) : p;
 }
 // EnvMap.h:98-134
@@ -728,8 +814,8 @@ inline int sampleCDF(const float *cdf, int N, float v, float &pdf) {
 // EnvMap.h:165-180
 inline void env_worldToPixel(const Env &e, V3<float> worldDir, int &ix, int &iy) {
   V3<float> localDir = xfmVector(e.toLocal, worldDir);
-  float theta = sphericalTheta(localDir);
-  float phi = sphericalPhi(localDir);
+  float theta = sphericalTheta(localDir, e.boundedMath);
+  float phi = sphericalPhi(localDir, e.boundedMath);
   float u = phi * ONE_OVER_TWO_PI, v = theta * ONE_OVER_PI;
   ix = (int)clampv(u * (float)e.W, 0.f, e.W - 1.f);
   iy = (int)clampv(v * (float)e.H, 0.f, e.H - 1.f);
@@ -743,16 +829,21 @@ inline float env_pdf(const Env &e, V3<float> dir) {
   float pdf_x = cdfGetPDF(px, e.cdf_x.data() + (size_t)py * e.W, e.W);
   float rel_y = (py + .5f) / e.H;
   const float theta = ONE_PI * rel_y;
-  return pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinf(theta));
+  float sinTheta, cosTheta;
+  path_sincos(e.boundedMath, theta, sinTheta, cosTheta);
+  return pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinTheta);
 }
 // EnvMap.h:198-210
 inline V3<float> env_uvToWorld(const Env &e, float fx, float fy) {
   const float phi = TWO_PI * fx;
   const float theta = ONE_PI * fy;
+  float sinTheta, cosTheta, sinPhi, cosPhi;
+  path_sincos(e.boundedMath, theta, sinTheta, cosTheta);
+  path_sincos(e.boundedMath, phi, sinPhi, cosPhi);
   V3<float> d;
-  d.z = cosf(theta);
-  d.x = cosf(phi) * sinf(theta);
-  d.y = sinf(phi) * sinf(theta);
+  d.z = cosTheta;
+  d.x = cosPhi * sinTheta;
+  d.y = sinPhi * sinTheta;
   return xfmVector(e.toWorld, d);
 }
 
@@ -778,7 +869,9 @@ inline LightSample env_sample(const Env &e, Random2 &r) {
   sample.direction = env_uvToWorld(e, sx, sy);
   float rel_y = sy;
   const float theta = ONE_PI * rel_y;
-  sample.pdf = pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinf(theta));
+  float sinTheta, cosTheta;
+  path_sincos(e.boundedMath, theta, sinTheta, cosTheta);
+  sample.pdf = pdf_x * pdf_y * 1.f / (TWO_PI * ONE_PI * sinTheta);
   sample.distance = INF;
   return sample;
 }
@@ -1031,8 +1124,8 @@ inline V3<float> radianceFromEnv(const Scene &S, const Ray &ray) {
   const Env &env = S.env;
   if (env.present) {
     V3<float> d = xfmVector(env.toLocal, normalize(ray.dir));
-    float theta = sphericalTheta(d);
-    float phi = sphericalPhi(d);
+    float theta = sphericalTheta(d, S.env.boundedMath);
+    float phi = sphericalPhi(d, S.env.boundedMath);
     const float invPi = 1.f / (float)M_PI;
     const float inv2Pi = 1.f / (2.f * (float)M_PI);
     float u = phi * inv2Pi, v = theta * invPi;
@@ -1060,7 +1153,7 @@ inline float hgPhase(float g, float cosTheta) {
   return ONE_OVER_FOUR_PI * (1.f - g2) / (denom * sqrtf(denom));
 }
 // Phase.h:74-99
-inline V3<float> sampleHGDirection(V3<float> wi_in, float g, Random2 &random) {
+inline V3<float> sampleHGDirection(V3<float> wi_in, float g, Random2 &random, bool boundedMath) {
   float u0 = random();
   float u1 = random();
   float cosTheta;
@@ -1071,7 +1164,9 @@ inline V3<float> sampleHGDirection(V3<float> wi_in, float g, Random2 &random) {
   }
   float sinTheta = sqrtf(mx(0.f, 1.f - cosTheta * cosTheta));
   float phi = TWO_PI * u1;
-  V3<float> local(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
+  float sinPhi, cosPhi;
+  path_sincos(boundedMath, phi, sinPhi, cosPhi);
+  V3<float> local(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
   V3<float> w = normalize(wi_in);
   V3<float> u, v;
   if (fabsf(w.x) > 0.1f) u = normalize(cross(V3<float>(0.f, 1.f, 0.f), w));
@@ -1160,7 +1255,7 @@ inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowR
   V3<float> sf_r;
   if (S.multi) {
     V3<float> wi_in = normalize(-wo);
-    sdir = sampleHGDirection(wi_in, ray.g, random);
+    sdir = sampleHGDirection(wi_in, ray.g, random, S.env.boundedMath);
     float density = hgPhase(ray.g, dot(wi_in, sdir));
     spdf = density;
     sf_r = ray.albedo * density;
@@ -1357,6 +1452,16 @@ void orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba) {
     rgba[4 * i + 1] = r.y;
     rgba[4 * i + 2] = r.z;
     rgba[4 * i + 3] = r.w;
+  }
+}
+
+extern "C" void orc_bounded_sincos(const float *x, long long n, float *sn, float *cs) {
+  for (long long i = 0; i < n; i++) bounded_sincos(x[i], sn[i], cs[i]);
+}
+extern "C" void orc_bounded_angles(const float *y, const float *x, long long n, float *acos_x, float *atan2_yx) {
+  for (long long i = 0; i < n; i++) {
+    acos_x[i] = bounded_acos(x[i]);
+    atan2_yx[i] = bounded_atan2(y[i], x[i]);
   }
 }
 

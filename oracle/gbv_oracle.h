@@ -63,6 +63,14 @@ typedef struct orc_scene {
      and bound macrocells by the dequantized corners (the library's own
      storage form; the reference has none) */
   int   u8_scaled;
+  /* 0: the path's sines, cosines, arc cosines and arc tangents are libm's
+     (sinf, cosf, acosf, atan2f), as in the reference's CPU backend.  1: they
+     use the bounded methods of the library's device code
+     (orc_bounded_sincos, orc_bounded_angles): the scattering azimuth, the
+     env-map CDF rows, the env light sample's angles and pdf, and the env
+     lookups' theta and phi.  Then nothing else differs and frames with
+     multiple scattering and an env map are comparable bit for bit. */
+  int   bounded_math;
 } orc_scene;
 
 typedef struct orc_stats {
@@ -85,6 +93,12 @@ void  orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba);
 void  orc_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
 void  orc_mc_ranges(const float *scalars, const int dims[3], int cells_per_mc,
                     float *ranges /* 2 per MC */);
+/* sine and cosine of each x[i] (x in [-pi/4, 2 pi + pi/4]), and arc cosine
+   of x[i] (x in [-1, 1]) with arc tangent of y[i]/x[i], by the bounded
+   methods of orc_scene.bounded_math */
+void orc_bounded_sincos(const float *x, long long n, float *sn, float *cs);
+void orc_bounded_angles(const float *y, const float *x, long long n, float *acos_x, float *atan2_yx);
+
 /* ranges of the scene's field in its storage form (orc_scene.u8_scaled) */
 void  orc_scene_mc_ranges(const orc_scene *s, float *ranges /* 2 per MC */);
 void  orc_majorants(const float *ranges, int num_mc, const float *tf, int tf_n,

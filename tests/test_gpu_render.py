@@ -21,14 +21,15 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
-def render_pair(s, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=N.GBV_VOXEL_F32, spp=None, start=0, oracle_vol=None):
+def render_pair(s, layout=N.GBV_LAYOUT_BRICK_CORNERS, fmt=N.GBV_VOXEL_F32, spp=None, start=0, oracle_vol=None,
+                **oracle_kw):
     import torch
     g = GpuScene(s, layout=layout, fmt=fmt)
     counters = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
     acc_g = g.new_accum()
     g.render(spp=spp, accum=acc_g, accum_id_start=start, counters=counters)
     torch.cuda.synchronize()
-    o = oracle.Oracle(s, scalars=oracle_vol)
+    o = oracle.Oracle(s, scalars=oracle_vol, **oracle_kw)
     acc_o = np.zeros((s.height, s.width, 4), np.float32)
     o.render(spp=spp, accum=acc_o, accum_id_start=start)
     return acc_g.cpu().numpy(), acc_o, counters.cpu().numpy(), o.stats
@@ -98,6 +99,21 @@ def test_full_size_multi_scatter_frame_paths_part_rarely(cuda):
     same = float(np.mean(np.all(bits(a) == bits(b), axis=-1)))
     print("pixels bit-identical to the oracle: %.5f" % same)
     assert same > 0.99, same
+    torch.cuda.empty_cache()
+
+
+def test_full_size_multi_scatter_frame_bit_exact_with_bounded_math(cuda):
+    """The same multiple-scattering frame against the oracle in its
+    bounded-sine/cosine mode (the device's method, restated in the oracle,
+    instead of libm): then nothing else on the path differs, and every
+    accumulation-buffer word and event count equals the oracle's -- light
+    sampling, MIS weights, half-precision throughput and up to 4 volume
+    bounces included."""
+    import torch
+    s = scenes.frame_scene(spp=1, with_env=False)
+    a, b, c, st = render_pair(s, spp=1, start=1, bounded_math=True)
+    assert c[0] == st["density_samples"] and c[1] == st["mc_visits"] and c[2] == st["rays"], (c[:3], st)
+    np.testing.assert_array_equal(bits(a), bits(b))
     torch.cuda.empty_cache()
 
 
@@ -299,3 +315,19 @@ def test_launch_settings_do_not_change_frames(cuda, settings):
                 os.environ[k] = v
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(a), bits(b))
+
+
+def test_bench_frame_bit_exact_with_bounded_math(cuda):
+    """The bench's frame itself at full size: 512^3 volume, 1920x1080, one
+    pass, multiple scattering up to 4 volume bounces, directional light and
+    the 512x256 sky env map (importance-sampled light, MIS, env lookups of
+    escaping paths).  Against the oracle in its bounded_math mode (the
+    device's sine/cosine, arc cosine and arc tangent restated instead of
+    libm's) every accumulation-buffer word and every event count is equal."""
+    import torch
+    s = scenes.frame_scene(spp=1)
+    assert s.env is not None and s.multi_scatter == 1
+    a, b, c, st = render_pair(s, spp=1, start=1, bounded_math=True)
+    assert c[0] == st["density_samples"] and c[1] == st["mc_visits"] and c[2] == st["rays"], (c[:3], st)
+    np.testing.assert_array_equal(bits(a), bits(b))
+    torch.cuda.empty_cache()

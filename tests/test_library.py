@@ -156,3 +156,34 @@ def test_bounded_sincos_within_two_ulp():
         ulp[r32 == 0] = np.float64(np.finfo(np.float32).smallest_subnormal)
         err = np.abs(got.astype(np.float64) - ref) / ulp
         assert err.max() <= 2.0, (err.max(), x[err.argmax()])
+
+
+def test_bounded_acos_atan2_accuracy():
+    """The renderer's arc cosine within 1.5 ulp and two-argument arc tangent
+    within 2.5 ulp of float64, over [-1, 1] and directions of the sphere;
+    atan2 keeps the sign conventions of signed zeros."""
+    rng = np.random.default_rng(5)
+    z = np.concatenate([rng.uniform(-1, 1, 400_000), np.linspace(-1, 1, 200_001)]).astype(np.float32)
+    v = rng.normal(size=(z.size, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    y, x = v[:, 1].astype(np.float32), v[:, 0].astype(np.float32)
+    ac, at = np.empty_like(z), np.empty_like(z)
+    assert N.lib().gbv_selftest_angles(y.ctypes.data, z.ctypes.data, z.size, ac.ctypes.data, at.ctypes.data, 0,
+                                       None) == N.GBV_OK
+    ref = np.arccos(z.astype(np.float64))
+    err = np.abs(ac.astype(np.float64) - ref) / np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    assert err.max() <= 1.5, (err.max(), z[err.argmax()])
+    assert N.lib().gbv_selftest_angles(y.ctypes.data, x.ctypes.data, x.size, ac.ctypes.data, at.ctypes.data, 0,
+                                       None) == N.GBV_OK
+    ref = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    r32 = np.abs(ref).astype(np.float32)
+    ulp = np.spacing(r32).astype(np.float64)
+    err = np.abs(at.astype(np.float64) - ref) / ulp
+    assert err.max() <= 2.5, (err.max(), y[err.argmax()], x[err.argmax()])
+    yy = np.array([0.0, -0.0, 0.0, -0.0], np.float32)
+    xx = np.array([0.0, 0.0, -0.0, -0.0], np.float32)
+    a2, t2 = np.empty_like(xx), np.empty_like(xx)
+    assert N.lib().gbv_selftest_angles(yy.ctypes.data, xx.ctypes.data, 4, a2.ctypes.data, t2.ctypes.data, 0,
+                                       None) == N.GBV_OK
+    np.testing.assert_array_equal(t2, np.arctan2(yy, xx))
+    np.testing.assert_array_equal(np.signbit(t2), np.signbit(np.arctan2(yy, xx)))

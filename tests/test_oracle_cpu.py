@@ -167,3 +167,35 @@ def test_u8_storage_form_of_the_oracle():
     assert np.all(sc == np.float32(0.375))
     with pytest.raises(ValueError):
         o8.render(use_double=True)
+
+
+def test_oracle_bounded_sincos_equals_library_host_routine():
+    """The oracle's restatement of the bounded sine/cosine (part of its
+    bounded_math mode) gives the library's host results bit for bit over
+    the whole angle range the renderer forms."""
+    from barney_gb300 import _native as N
+    x = np.concatenate([np.linspace(-np.pi / 4, 2 * np.pi + np.pi / 4, 400_001, dtype=np.float32),
+                        (np.random.default_rng(7).random(200_000) * 2 * np.pi).astype(np.float32)])
+    so, co = oracle.bounded_sincos(x)
+    sl, cl = np.empty_like(x), np.empty_like(x)
+    assert N.lib().gbv_selftest_sincos(x.ctypes.data, x.size, sl.ctypes.data, cl.ctypes.data, 0, None) == N.GBV_OK
+    np.testing.assert_array_equal(so.view(np.uint32), sl.view(np.uint32))
+    np.testing.assert_array_equal(co.view(np.uint32), cl.view(np.uint32))
+
+
+def test_oracle_bounded_angles_equal_library_host_routine():
+    """The oracle's restatement of the library's arc cosine and arc tangent
+    (bounded_math mode) gives its host results bit for bit, on directions
+    of the sphere, the axes, signed zeros and the ends of [-1, 1]."""
+    from barney_gb300 import _native as N
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=(300_000, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    y = np.concatenate([v[:, 1], [0.0, -0.0, 0.0, -0.0, 1.0, -1.0, 0.5, -0.5]]).astype(np.float32)
+    x = np.concatenate([v[:, 2], [0.0, 0.0, -0.0, -0.0, 0.0, 0.0, 1.0, -1.0]]).astype(np.float32)
+    ao, to = oracle.bounded_angles(y, x)
+    al, tl = np.empty_like(x), np.empty_like(x)
+    assert N.lib().gbv_selftest_angles(y.ctypes.data, x.ctypes.data, x.size, al.ctypes.data, tl.ctypes.data, 0,
+                                       None) == N.GBV_OK
+    np.testing.assert_array_equal(ao.view(np.uint32), al.view(np.uint32))
+    np.testing.assert_array_equal(to.view(np.uint32), tl.view(np.uint32))
