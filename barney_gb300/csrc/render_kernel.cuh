@@ -189,7 +189,7 @@ __device__ __forceinline__ float spherical_phi(vec3 v) {
   return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
 }
 // (theta, phi) of a direction in the env map's frame; one out-of-line copy
-// of acosf and atan2f for the env-map pdf and the env lookup
+// of the arc cosine and arc tangent for the env-map pdf and the env lookup
 static __device__ __noinline__ float2 spherical_theta_phi(vec3 v) {
   return make_float2(spherical_theta(v), spherical_phi(v));
 }

@@ -2,9 +2,12 @@
 
 * single scatter (the reference's default build): no transcendental function
   on the device path, so frames match the oracle bit for bit;
-* multiple scattering with an env map: sinf/cosf/acosf/atan2f of CUDA and of
-  the host libm differ in the last ulp, so paths can part; frames agree
-  statistically (per-pixel means within 3 sigma, RMSE falling as 1/sqrt(spp)).
+* multiple scattering with an env map: the device's sine/cosine, arc cosine
+  and arc tangent (this library's routines) and the host libm's differ in the
+  last ulp, so paths can part from the libm oracle's; frames agree
+  statistically (per-pixel means within 3 sigma, RMSE falling as 1/sqrt(spp)),
+  and bit for bit with the oracle in its bounded-math mode, which restates
+  the library's routines.
 """
 import numpy as np
 import pytest
