@@ -172,7 +172,7 @@ __device__ __forceinline__ float4 lerp4(float f, float4 a, float4 b) {
 }
 // rtcore/embree/Texture.cpp:295-321 (one out-of-line copy for the env-map
 // sample and the miss lookup)
-static __device__ __noinline__ float4 tex2D(const EnvDev &e, float u, float v) {
+__device__ __forceinline__ float4 tex2D(const EnvDev &e, float u, float v) {
   int x0, x1, y0, y1;
   float fx, fy;
   compute_address(e.addr[0], u, e.W, x0, x1, fx);
@@ -316,7 +316,7 @@ struct EnvPick {
 };
 // The random draws and CDF searches of the sample; the texel at (sx, sy)
 // is fetched by the caller (see the shading phase of render_kernel).
-static __device__ __noinline__ EnvPick env_pick_coords(const RenderParams &p, Random &r) {
+__device__ __forceinline__ EnvPick env_pick_coords(const RenderParams &p, Random &r) {
   const EnvDev &e = p.env;
   EnvPick k;
   float r_y = r();
@@ -329,7 +329,7 @@ static __device__ __noinline__ EnvPick env_pick_coords(const RenderParams &p, Ra
   k.pdfxy = pdf_x * pdf_y;
   return k;
 }
-static __device__ __noinline__ void env_pick_direction(const RenderParams &p, const EnvPick &k, LightSample &s) {
+__device__ __forceinline__ void env_pick_direction(const RenderParams &p, const EnvPick &k, LightSample &s) {
   const EnvDev &e = p.env;
   const float phi = kTwoPi * k.sx;
   const float theta = kPi * k.sy;
@@ -433,7 +433,7 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
 
 // radianceFromEnv (shadeRays.cu:437-456) up to the texture read: the
 // env-map coordinates of a ray direction
-static __device__ __noinline__ float2 env_miss_coords(const RenderParams &p, vec3 rayDir) {
+__device__ __forceinline__ float2 env_miss_coords(const RenderParams &p, vec3 rayDir) {
   vec3 d = xfm_vector(p.env.toLocal, normalize(rayDir));
   const float2 tp = spherical_theta_phi(d);
   float theta = tp.x;
@@ -457,7 +457,7 @@ __device__ __forceinline__ float phase_pdf(const RenderParams &p, float g, vec3 
   return hg_phase(g, dot(wi_in, normalize(wi)));
 }
 // Phase.h:74-99
-static __device__ __noinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
+__device__ __forceinline__ vec3 sample_hg_direction(vec3 wi_in, float g, Random &random) {
   float u0 = random();
   float u1 = random();
   float cosTheta;
@@ -500,7 +500,7 @@ struct ShadeOut {
 // `random` is the hit's stream, Random2(ray.rngSeed, tHit), already derived
 // (it advanced ray.seed); with an env map `pick` holds the light sample's
 // texel coordinates and radiance.
-static __device__ __noinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
+__device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
                                                   int pathDepth, Random &random, const EnvPick &pick,
                                                   ShadeOut &out) {
   out.shadowValid = false;
