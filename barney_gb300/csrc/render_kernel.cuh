@@ -273,11 +273,11 @@ __device__ __forceinline__ int sample_cdf_x(const RenderParams &p, int row, floa
 // as by memory: warps of one SM sit in different phases (start, traverse,
 // shade) at once, so the whole loop body is the instruction working set
 // (ncu: about 40% of the stall samples of a 1080p launch are "no
-// instruction").  Every shading helper has one call site (the trace set-up,
-// the texel fetch, the env coordinates, the bounce, and one pdf call per MIS
-// weight), so they are inlined: no code is duplicated, and no registers are
-// saved around calls (measured on the 512^3 frame: +9% against out-of-line
-// helpers).  Rarely taken branches (general fmod, mirror addressing, the
+// instruction").  The shading helpers are inlined: the trace set-up, the
+// texel fetch, the env coordinates and the bounce have one call site each,
+// only the env pdf (one call per MIS weight) is duplicated, and no registers
+// are saved around calls (measured on the 512^3 frame: +9% against
+// out-of-line helpers).  Rarely taken branches (general fmod, mirror addressing, the
 // pivot search, subnormal half rounding) stay out of line.
 // The two factors of the env-map pdf that depend on the pixel row only
 // (EnvMap.h:160-179): the row's marginal pdf and the solid-angle
