@@ -590,10 +590,10 @@ __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
 // -------------------------------------------------------------------------
 // Defaults of the launch shape (the best of a same-box sweep of 3..64 units
 // per seek and thresholds 3..30% on the 512^3 1080p frame; units 5..8 with
-// thresholds 12..20 are within 1% of each other; results never depend on
+// thresholds 16..25 are within 1% of each other; results never depend on
 // them)
 constexpr int kSkipDefault = 6;
-constexpr int kThresholdDefault = 12;
+constexpr int kThresholdDefault = 20;
 
 // Per-lane event counts; with On == false the counting and its registers
 // compile away (timed launches pass no counter buffer).
@@ -1161,7 +1161,7 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
 // tests and distance draws a lane may make per traversal iteration (default
 // 6); GBV_RENDER_THRESH the percentage of a warp's busy lanes that must still
 // be tracing for the warp to keep traversing before it shades and refills
-// (default 12).
+// (default 20).
 template <class Store>
 inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
   const char *sk = getenv("GBV_RENDER_SKIP");
