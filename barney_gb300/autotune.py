@@ -29,7 +29,7 @@ import json
 import os
 from pathlib import Path
 
-LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (12, 20, 30) for k in (4, 6, 8)]
+LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (5, 12, 20) for k in (4, 6, 8)]
 BRICK_CANDIDATES = [(3, 3, 3), (2, 2, 2), (4, 4, 4), (4, 4, 2), (5, 3, 2)]
 
 

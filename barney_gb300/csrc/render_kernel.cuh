@@ -573,6 +573,24 @@ __device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay
   }
 }
 
+// Out-of-line copies of the shading helpers for the batched kernel: its
+// lanes read their scenes' parameters from global memory (one record per
+// item), and inlined helpers keep more of them live than the registers hold
+// (measured on the 64-item workload: 13% slower inlined).  The one-scene
+// kernel inlines the helpers themselves.
+static __device__ __noinline__ void bounce_volume_hit_ool(const RenderParams &p, PathRay &ray, const Hit &h, vec3 P,
+                                                      int pathDepth, Random &random, const EnvPick &pick,
+                                                      ShadeOut &out) {
+  bounce_volume_hit(p, ray, h, P, pathDepth, random, pick, out);
+}
+static __device__ __noinline__ float4 tex2D_ool(const EnvDev &e, float u, float v) { return tex2D(e, u, v); }
+static __device__ __noinline__ float2 env_miss_coords_ool(const RenderParams &p, vec3 rayDir) {
+  return env_miss_coords(p, rayDir);
+}
+static __device__ __noinline__ EnvPick env_pick_coords_ool(const RenderParams &p, Random &r) {
+  return env_pick_coords(p, r);
+}
+
 __device__ __forceinline__ void accum_add(float4 &acc, vec3 frag) {
   if (frag.x > 0.f) acc.x += frag.x;
   if (frag.y > 0.f) acc.y += frag.y;
@@ -1023,18 +1041,18 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         if (h.hit) {
           rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.t));
           if (p.hasEnv) {
-            pick = env_pick_coords(p, rnd);
+            pick = Batch ? env_pick_coords_ool(p, rnd) : env_pick_coords(p, rnd);
             uv = make_float2(pick.sx, pick.sy);
             needTex = true;
           }
         } else if (p.hasEnv) {
-          uv = env_miss_coords(p, ray.dir);
+          uv = Batch ? env_miss_coords_ool(p, ray.dir) : env_miss_coords(p, ray.dir);
           needTex = true;
         }
       }
       vec3 texel(0.f);
       if (needTex) {
-        const float4 t = tex2D(p.env, uv.x, uv.y);
+        const float4 t = Batch ? tex2D_ool(p.env, uv.x, uv.y) : tex2D(p.env, uv.x, uv.y);
         texel = p.env.scale * vec3(t.x, t.y, t.z);
       }
       tstate = NEED;
@@ -1061,7 +1079,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
           ShadeOut so;
           // setVolumeHit's P = obj_org + t * obj_dir (MCAccelerator.h:79)
           pick.radiance = texel;
-          bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
+          if (Batch)
+            bounce_volume_hit_ool(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
+          else
+            bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
           if (so.shadowValid && so.shadow.tMax > 0.f) {
             sray = so.shadow;
             shadowPending = true;
