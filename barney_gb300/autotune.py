@@ -7,7 +7,7 @@ and tests/test_gpu_bricks.py check both bit for bit):
 
 * brick         -- log2 of the brick edge in cells per axis of the voxel
   stores (where neighbouring cells sit in HBM);
-* blocks_per_sm -- resident 256-thread blocks per SM (4, 5 or 6: the kernel
+* blocks_per_sm -- resident 288-thread blocks per SM (4, 5 or 6: the kernel
   is compiled for each register budget);
 * threshold     -- a warp keeps traversing while at least this percentage of
   its busy lanes still traces, then shades together;

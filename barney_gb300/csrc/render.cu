@@ -346,7 +346,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
   b->format = scenes[0].format;
   b->layout = scenes[0].layout;
   b->totalTiles = starts[count];
-  b->occ = 5;
+  b->occ = 4;
   b->threshold = kThresholdDefault;
   b->skip = kSkipDefault;
   cudaGetDevice(&b->device);

@@ -815,7 +815,10 @@ __device__ __forceinline__ int trace_sample(const FieldGeom &F, const Store &sto
 // lane by one bounded unit: a trace step, or a shade and the set-up of the
 // next trace.
 // -------------------------------------------------------------------------
-constexpr int kThreads = 256;
+// 9 warps per block: at 4 resident blocks per SM (36 warps) the register
+// budget is 56 per thread (measured fastest: 256 x 5 with 48 registers
+// -4.2%, 192 x 6 -2%)
+constexpr int kThreads = 288;
 enum { K_NONE = 0, K_MAIN = 1, K_SHADOW = 2 };
 
 __device__ __forceinline__ float4 miss_color(const RenderParams &p, int iy) {
@@ -1177,8 +1180,8 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
 }
 
 // GBV_RENDER_OCC=4, 5 or 6 selects the resident blocks per SM the registers
-// are capped for (default 5: 40 warps per SM at 51 registers; the kernel is
-// latency-bound and gains more from warps than it loses to spills).  GBV_RENDER_SKIP sets the cell
+// are capped for (default 4: 36 warps per SM at 56 registers; 5 blocks give
+// 45 warps at 40 registers and spill more).  GBV_RENDER_SKIP sets the cell
 // tests and distance draws a lane may make per traversal iteration (default
 // 6); GBV_RENDER_THRESH the percentage of a warp's busy lanes that must still
 // be tracing for the warp to keep traversing before it shades and refills
@@ -1232,7 +1235,7 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
   p.threshold = th ? atoi(th) : kThresholdDefault;
   if (p.threshold < 1) p.threshold = 1;
   const char *oc = getenv("GBV_RENDER_OCC");
-  const int occ = oc ? atoi(oc) : 5;
+  const int occ = oc ? atoi(oc) : 4;
   if (occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
   if (occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
   return launch_render_t<Store, 5>(p, store, stream);
@@ -1240,7 +1243,7 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
 
 template <class Store>
 inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cudaStream_t stream, int *pool) {
-  // fixed launch settings (results do not depend on them): 5 resident
+  // fixed launch settings (results do not depend on them): 4 resident
   // blocks per SM, the default traversal settings, no shared-memory staging
   p.skip = kSkipDefault;
   p.threshold = kThresholdDefault;
@@ -1252,7 +1255,7 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st != GBV_OK) return st;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 5, false, true>, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>, kThreads, 0);
   const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
@@ -1262,9 +1265,9 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "gbv_render_noalloc: clearing the tile pool");
   if (st != GBV_OK) return st;
   if (p.counters)
-    render_kernel<Store, 5, false, true><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
+    render_kernel<Store, 4, false, true><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
   else
-    render_kernel<Store, 5, false, false><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
+    render_kernel<Store, 4, false, false><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
   return check_launch("render_kernel (noalloc)");
 }
 

@@ -283,8 +283,8 @@ gbv_status gbv_render_noalloc(const gbv_scene *scene, float *d_accum, int width,
    gbv_batch_create uploads the items' parameters (allocates and copies; call
    it outside stream capture); gbv_batch_render is one memset and one kernel
    launch on `stream`, so a capture of it replays as a CUDA graph;
-   gbv_batch_set_launch sets the launch shape (resident 256-thread blocks per
-   SM, 4 to 6, default 5; traversal threshold %, default 20; cell tests and
+   gbv_batch_set_launch sets the launch shape (resident 288-thread blocks per
+   SM, 4 to 6, default 4; traversal threshold %, default 20; cell tests and
    Woodcock distance draws per lane and traversal iteration, default 6),
    which changes speed, never results.  Items must share the voxel format and
    layout; each item's frame accumulates exactly as gbv_render would. */

@@ -293,7 +293,7 @@ def test_shared_memory_staging_is_transparent(cuda, stage):
 
 @pytest.mark.parametrize("settings", [{"GBV_RENDER_SKIP": "1"},
                                       {"GBV_RENDER_SKIP": "64", "GBV_RENDER_THRESH": "100"},
-                                      {"GBV_RENDER_THRESH": "1", "GBV_RENDER_OCC": "4"},
+                                      {"GBV_RENDER_THRESH": "1", "GBV_RENDER_OCC": "5"},
                                       {"GBV_RENDER_OCC": "6", "GBV_RENDER_SKIP": "2"}])
 def test_launch_settings_do_not_change_frames(cuda, settings):
     """Units per seek (1: one cell test or one distance draw per traversal
