@@ -199,3 +199,20 @@ def test_oracle_bounded_angles_equal_library_host_routine():
                                        None) == N.GBV_OK
     np.testing.assert_array_equal(ao.view(np.uint32), al.view(np.uint32))
     np.testing.assert_array_equal(to.view(np.uint32), tl.view(np.uint32))
+
+
+def test_bounded_math_mode_only_replaces_the_transcendentals():
+    """Paths without a sine, cosine, arc cosine or arc tangent (single
+    scattering, no env map) render identically in both oracle modes; with
+    multiple scattering and the env map the modes differ only where a
+    last-ulp difference reaches the pixel, so most pixels stay identical."""
+    s = scenes.small_scene(dims=32, spp=2, width=48, height=32)
+    a = oracle.Oracle(s).render()
+    b = oracle.Oracle(s, bounded_math=True).render()
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    s = scenes.frame_scene(dims=32, width=48, height=32, spp=2)
+    assert s.env is not None and s.multi_scatter == 1
+    a = oracle.Oracle(s).render()
+    b = oracle.Oracle(s, bounded_math=True).render()
+    same = float(np.mean(np.all(a.view(np.uint32) == b.view(np.uint32), axis=-1)))
+    assert same > 0.5, same
