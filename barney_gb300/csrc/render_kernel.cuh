@@ -170,8 +170,8 @@ __device__ __forceinline__ float4 lerp4(float f, float4 a, float4 b) {
   return make_float4((1.f - f) * a.x + f * b.x, (1.f - f) * a.y + f * b.y, (1.f - f) * a.z + f * b.z,
                      (1.f - f) * a.w + f * b.w);
 }
-// rtcore/embree/Texture.cpp:295-321 (one out-of-line copy for the env-map
-// sample and the miss lookup)
+// rtcore/embree/Texture.cpp:295-321 (one call site: the shading phase
+// fetches the texels of the env-map samples and the miss lookups together)
 __device__ __forceinline__ float4 tex2D(const EnvDev &e, float u, float v) {
   int x0, x1, y0, y1;
   float fx, fy;
@@ -188,8 +188,8 @@ __device__ __forceinline__ float spherical_phi(vec3 v) {
   float p = atan2_angle(v.y, v.x);
   return (p < 0.f) ? (p + float(2.f * 3.14159265358979323846)) : p;
 }
-// (theta, phi) of a direction in the env map's frame; one out-of-line copy
-// of the arc cosine and arc tangent for the env-map pdf and the env lookup
+// (theta, phi) of a direction in the env map's frame, for the env-map pdf
+// and the env lookup
 __device__ __forceinline__ float2 spherical_theta_phi(vec3 v) {
   return make_float2(spherical_theta(v), spherical_phi(v));
 }
@@ -858,8 +858,9 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
 // always come from p0.  Count: whether to count events (see Ctr) and, with
 // GBV_RENDER_PROFILE, cycles and lanes per phase (the timed kernel, Count =
 // false, carries no profiling code).
-// p0 is __grid_constant__ so that out-of-line helpers can take it by
-// reference without a copy to local memory.
+// p0 is __grid_constant__ so that helpers (inlined, or the batched kernel's
+// out-of-line copies) can take it by reference without a copy to local
+// memory.
 template <class Store, int MinBlocks, bool Batch, bool Count>
 __global__ void __launch_bounds__(kThreads, MinBlocks)
     render_kernel(const __grid_constant__ RenderParams p0, const RenderParams *__restrict__ items,
