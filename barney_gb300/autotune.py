@@ -30,6 +30,10 @@ import os
 from pathlib import Path
 
 LAUNCH_CANDIDATES = [(b, t, k) for b in (4, 5, 6) for t in (5, 12, 20) for k in (4, 6, 8)]
+# What a launch shape means to the kernel (block size, traversal units); part
+# of every cache key, so choices cached by a build where the same numbers
+# meant another launch are not reused.
+LAUNCH_SHAPE_REVISION = "288-thread blocks, seek units"
 BRICK_CANDIDATES = [(3, 3, 3), (2, 2, 2), (4, 4, 4), (4, 4, 2), (5, 3, 2)]
 
 
@@ -41,12 +45,13 @@ def cache_path() -> Path:
 
 
 def workload_key(scenes, spp: int, fmt: int, what: str) -> str:
-    """GPU name and SM count, plus the items' frame sizes, field sizes,
-    macrocell sizes, scattering mode, voxel format and passes."""
+    """Launch-shape revision, GPU name and SM count, plus the items' frame
+    sizes, field sizes, macrocell sizes, scattering mode, voxel format and
+    passes."""
     import torch
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
     items = [(s.width, s.height, list(s.scalars.shape), s.cells_per_mc, s.multi_scatter) for s in scenes]
-    blob = json.dumps([what, props.name, props.multi_processor_count, spp, fmt, items])
+    blob = json.dumps([LAUNCH_SHAPE_REVISION, what, props.name, props.multi_processor_count, spp, fmt, items])
     return what + ":" + hashlib.sha1(blob.encode()).hexdigest()[:20]
 
 
