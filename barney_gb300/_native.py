@@ -42,6 +42,22 @@ class GbvScene(C.Structure):
     ]
 
 
+GBV_STAGE_DEFAULT, GBV_STAGE_NONE, GBV_STAGE_ALL = 0, 1, 2
+
+
+class GbvRenderConfig(C.Structure):
+    """gbv_render_config: launch settings (zero fields take the defaults)."""
+    _fields_ = [("blocks_per_sm", C.c_int), ("threshold_pct", C.c_int), ("skip_cells", C.c_int),
+                ("stage", C.c_int), ("profile", C.c_int), ("reserved", C.c_int * 3)]
+
+
+def render_config(**kw) -> GbvRenderConfig:
+    c = GbvRenderConfig()
+    for k, v in kw.items():
+        setattr(c, k, int(v))
+    return c
+
+
 class GbvEAView(C.Structure):
     _fields_ = [("pos", _f3), ("dir", _f3), ("up", _f3), ("fovy", C.c_float),
                 ("width", C.c_int), ("height", C.c_int)]
@@ -73,6 +89,7 @@ def lib() -> C.CDLL:
             "gbv_build_mc_ranges_from_store_shaped": (st, [vp, vp, i, ip, ip, i, vp, vp]),
             "gbv_env_build_cdfs": (st, [vp, i, i, ip, vp, vp, vp]),
             "gbv_render": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
+            "gbv_render_ex": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, C.POINTER(GbvRenderConfig), vp]),
             "gbv_render_noalloc": (st, [C.POINTER(GbvScene), vp, i, i, i, i, vp, vp]),
             "gbv_render_tiles": (st, [C.POINTER(GbvScene), vp, i, i, i, i, i, i, vp, vp]),
             "gbv_tile_partition": (st, [i, i, i, i, ip, ip]),
@@ -91,7 +108,7 @@ def lib() -> C.CDLL:
             "gbv_ea_render": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),
             "gbv_ea_render_f64": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp]),
             "gbv_ea_backward": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp, vp, vp, vp]),
-            "gbv_gen_blob_volume": (st, [ip, i, C.c_uint64, f, i, f, i, vp]),
+            "gbv_ea_backward_ex": (st, [C.POINTER(GbvScene), C.POINTER(GbvEAView), i, f, vp, vp, vp, vp, i, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -1,4 +1,6 @@
-"""Builds the native library in-tree: barney_gb300/_lib/libbarney_gb300.so.
+"""Builds the native library in-tree: barney_gb300/_lib/libbarney_gb300.so,
+and the synthetic-input generator beside it (barney_gb300/_lib/libgbv_scenegen.so,
+host code only, kept out of the renderer's library).
 
 Every CUDA translation unit is compiled for sm_103a only, in parallel, with
 ``-fmad=false`` so no multiply-add is fused (the path reproduces the
@@ -19,6 +21,8 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 OBJDIR = LIBDIR / "obj"
 LIBNAME = "libbarney_gb300.so"
+SCENEGEN = PKG / "scenegen"
+SCENEGEN_LIB = "libgbv_scenegen.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -51,6 +55,21 @@ def lib_path() -> Path:
     return LIBDIR / LIBNAME
 
 
+def scenegen_path() -> Path:
+    return LIBDIR / SCENEGEN_LIB
+
+
+def build_scenegen(force: bool = False) -> Path:
+    """The input generator: one g++ step, no CUDA."""
+    LIBDIR.mkdir(parents=True, exist_ok=True)
+    out = scenegen_path()
+    deps = sorted(SCENEGEN.glob("*.cpp")) + sorted(SCENEGEN.glob("*.h"))
+    if force or _stale(out, deps):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", "-Wall",
+              *[str(d) for d in deps if d.suffix == ".cpp"], "-o", str(out)])
+    return out
+
+
 def build(verbose: bool = False, force: bool = False) -> Path:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
@@ -78,6 +97,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     out = lib_path()
     if force or not out.exists() or any(Path(o).stat().st_mtime > out.stat().st_mtime for o in objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(out), *objs, "-lpthread"])
+    build_scenegen(force)
     return out
 
 

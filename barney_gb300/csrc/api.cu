@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include "gbv_volume.cuh"
 #include "gbv_internal.h"
+#include "../../include/gbvol_diag.h"
 
 namespace gbv {
 

@@ -12,7 +12,6 @@
 //   C = sum T_i alpha_i rgb_i, A = -expm1(-tau_n).
 // Adjoint (no stored per-step state): dC/dx_j = rgb_j T_{j+1} - (C - C_{<=j}),
 // dA/dx_j = T_n, dC/drgb_j = T_j alpha_j.
-#include <cstdlib>
 #include <cuda_runtime.h>
 #include "gbv_volume.cuh"
 #include "gbv_internal.h"
@@ -24,6 +23,15 @@ void commit_camera(const float pos[3], const float dir[3], const float up[3], fl
 bool make_field_geom(const gbv_scene *s, FieldGeom &F);
 
 constexpr int kMaxViewsPerLaunch = 32;
+// Steps per ray are bounded: the host rejects a step for which the field's
+// box diagonal would take more than kEAMaxSteps - 16 steps, and the device
+// clamps every ray's step count to kEAMaxSteps (never binding for an
+// accepted step, whose chord is at most the diagonal).
+constexpr int kEAMaxSteps = 1 << 24;
+__device__ __forceinline__ int ea_step_count(float chord, float dt) {
+  const float q = ceilf(chord / dt);
+  return q < (float)kEAMaxSteps ? (int)q : kEAMaxSteps;
+}
 
 struct EAViewDev {
   vec3 lens00, dir00, du, dv;
@@ -57,7 +65,7 @@ __device__ __forceinline__ bool ea_ray(const EAParams &p, const EAViewDev &v, in
   t1 = 1e30f;
   if (!box_test(org, dir, t0, t1, p.F.boundsLo, p.F.boundsHi)) return false;
   if (!(t1 > t0)) return false;
-  n = (int)ceilf((t1 - t0) / p.dt);
+  n = ea_step_count(t1 - t0, p.dt);
   return true;
 }
 
@@ -169,7 +177,8 @@ __global__ void __launch_bounds__(128) ea_forward_f64_kernel(const EAParams p, d
     t1 = mn(t1, tfar);
     if (t0 <= t1 && t1 > t0) {
       const double dt = (double)p.dt;
-      const int n = (int)ceil((t1 - t0) / dt);
+      const double q = ceil((t1 - t0) / dt);
+      const int n = q < (double)kEAMaxSteps ? (int)q : kEAMaxSteps;
       double tau = 0., comp = 0., C0 = 0., C1 = 0., C2 = 0.;
       for (int i = 0; i < n; i++) {
         const double t = t0 + ((double)i + .5) * dt;
@@ -421,6 +430,14 @@ static gbv_status ea_prepare(const gbv_scene *s, float step, EAParams &p, bool f
   if (s->dims[0] < 2 || s->dims[1] < 2 || s->dims[2] < 2)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "ea: a field needs at least 2 voxels per axis");
   make_field_geom(s, p.F);
+  {
+    const double dx = (double)p.F.boundsHi.x - p.F.boundsLo.x, dy = (double)p.F.boundsHi.y - p.F.boundsLo.y,
+                 dz = (double)p.F.boundsHi.z - p.F.boundsLo.z;
+    const double diag = sqrt(dx * dx + dy * dy + dz * dz);
+    if (!(diag / (double)step <= (double)(kEAMaxSteps - 16)))
+      return set_error(GBV_ERROR_INVALID_ARGUMENT,
+                       "ea: step too small for the field (a ray could take more than 2^24 steps)");
+  }
   p.store = StoreLinearF32{reinterpret_cast<const float *>(s->d_voxels), s->dims[0], s->dims[1]};
   p.vox = s->d_voxels;
   p.so = reinterpret_cast<const float2 *>(s->d_scale_offset);
@@ -505,36 +522,38 @@ gbv_status gbv_ea_render_f64(const gbv_scene *s, const gbv_ea_view *views, int n
   });
 }
 
-gbv_status gbv_ea_backward(const gbv_scene *s, const gbv_ea_view *views, int num_views, float step,
-                           const float *d_images, const float *d_grad_images, float *d_grad_scalars,
-                           float *d_grad_tf, void *stream) {
+gbv_status gbv_ea_backward_ex(const gbv_scene *s, const gbv_ea_view *views, int num_views, float step,
+                              const float *d_images, const float *d_grad_images, float *d_grad_scalars,
+                              float *d_grad_tf, int blocks_per_sm, void *stream) {
   EAParams p;
   gbv_status st = ea_prepare(s, step, p);
   if (st != GBV_OK) return st;
   if (!views || num_views <= 0 || !d_images || !d_grad_images || !d_grad_scalars || !d_grad_tf)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_ea_backward: null pointer");
+  if (blocks_per_sm != 0 && blocks_per_sm != 4 && blocks_per_sm != 6 && blocks_per_sm != 8)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_ea_backward_ex: blocks_per_sm is 4, 6 or 8 (0: 6)");
   size_t smem = (size_t)4 * s->tf_n * sizeof(float);
   if (smem > 48 * 1024) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_ea_backward: transfer function above 3072 entries");
+  // resident 128-thread blocks per SM the adjoint's registers are capped
+  // for (default 6: 80 registers, no spills)
+  const int occ = blocks_per_sm ? blocks_per_sm : 6;
   return for_view_chunks(p, views, num_views, [&](EAParams &q, int cnt, int maxW, int maxH) {
     dim3 grid((maxW + 15) / 16, (maxH + 7) / 8, cnt);
-    // GBV_EA_OCC: resident 128-thread blocks per SM the adjoint's registers
-    // are capped for (4, 6 or 8; default 6: 80 registers, no spills)
-    const char *oc = getenv("GBV_EA_OCC");
-    const int occ = oc ? atoi(oc) : 6;
-    if (occ >= 8)
-      ea_backward_kernel<8><<<grid, 128, smem, (cudaStream_t)stream>>>(
-          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
-          d_grad_scalars, d_grad_tf);
-    else if (occ >= 6)
-      ea_backward_kernel<6><<<grid, 128, smem, (cudaStream_t)stream>>>(
-          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
-          d_grad_scalars, d_grad_tf);
-    else
-      ea_backward_kernel<4><<<grid, 128, smem, (cudaStream_t)stream>>>(
-          q, reinterpret_cast<const float4 *>(d_images), reinterpret_cast<const float4 *>(d_grad_images),
-          d_grad_scalars, d_grad_tf);
+    const float4 *img = reinterpret_cast<const float4 *>(d_images);
+    const float4 *gimg = reinterpret_cast<const float4 *>(d_grad_images);
+    cudaStream_t cs = (cudaStream_t)stream;
+    if (occ == 8) ea_backward_kernel<8><<<grid, 128, smem, cs>>>(q, img, gimg, d_grad_scalars, d_grad_tf);
+    else if (occ == 6) ea_backward_kernel<6><<<grid, 128, smem, cs>>>(q, img, gimg, d_grad_scalars, d_grad_tf);
+    else ea_backward_kernel<4><<<grid, 128, smem, cs>>>(q, img, gimg, d_grad_scalars, d_grad_tf);
     return check_launch("ea_backward_kernel");
   });
+}
+
+gbv_status gbv_ea_backward(const gbv_scene *s, const gbv_ea_view *views, int num_views, float step,
+                           const float *d_images, const float *d_grad_images, float *d_grad_scalars,
+                           float *d_grad_tf, void *stream) {
+  return gbv_ea_backward_ex(s, views, num_views, step, d_images, d_grad_images, d_grad_scalars, d_grad_tf, 0,
+                            stream);
 }
 
 }  // extern "C"

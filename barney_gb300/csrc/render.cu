@@ -114,9 +114,31 @@ using namespace gbv;
 
 namespace gbv {
 
+// Launch settings of a gbv_render_config (zero fields: defaults); false if
+// a field is out of range.
+static bool resolve_config(const gbv_render_config *c, RenderParams &p, LaunchChoice &lc) {
+  p.skip = kSkipDefault;
+  p.threshold = kThresholdDefault;
+  p.profile = 0;
+  lc = LaunchChoice();
+  if (!c) return true;
+  if (c->blocks_per_sm != 0 && (c->blocks_per_sm < 4 || c->blocks_per_sm > 6)) return false;
+  if (c->threshold_pct < 0 || c->threshold_pct > 100) return false;
+  if (c->skip_cells < 0 || c->skip_cells > 1024) return false;
+  if (c->stage < GBV_STAGE_DEFAULT || c->stage > GBV_STAGE_ALL) return false;
+  if (c->profile != 0 && c->profile != 1) return false;
+  if (c->reserved[0] || c->reserved[1] || c->reserved[2]) return false;
+  if (c->blocks_per_sm) lc.occ = c->blocks_per_sm;
+  lc.stage = c->stage;
+  if (c->threshold_pct) p.threshold = c->threshold_pct;
+  if (c->skip_cells) p.skip = c->skip_cells;
+  p.profile = c->profile;
+  return true;
+}
+
 static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accum, int width, int height,
                                int accum_id_start, int spp, int rank, int num_ranks, unsigned long long *d_counters,
-                               void *stream, int *d_cap_flag = nullptr) {
+                               void *stream, int *d_cap_flag = nullptr, const gbv_render_config *config = nullptr) {
   char msg[160];
   if (!s || !d_accum || width <= 0 || height <= 0 || spp < 0 || accum_id_start < 0) {
     snprintf(msg, sizeof msg, "%s: null pointer or non-positive size", fn);
@@ -138,8 +160,14 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
     snprintf(msg, sizeof msg, "%s: U8 voxels need the brick scale/offset table", fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
-  if (spp == 0) return GBV_OK;
   RenderParams p;
+  LaunchChoice lc;
+  if (!resolve_config(config, p, lc)) {
+    snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..2)",
+             fn);
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
+  if (spp == 0) return GBV_OK;
   gbv_status st = fill_params(s, p);
   if (st != GBV_OK) return st;
   p.W = width;
@@ -157,16 +185,16 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
   cudaStream_t cs = (cudaStream_t)stream;
-  if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_linear(p, cs);
+  if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_linear(p, cs, lc);
   if (s->layout != GBV_LAYOUT_BRICK_CORNERS) {
     snprintf(msg, sizeof msg, "%s: unknown layout", fn);
     return set_error(GBV_ERROR_UNSUPPORTED, msg);
   }
   switch (s->format) {
-    case GBV_VOXEL_F32: return render_launch_f32(p, cs);
-    case GBV_VOXEL_F16: return render_launch_f16(p, cs);
-    case GBV_VOXEL_BF16: return render_launch_bf16(p, cs);
-    case GBV_VOXEL_U8_SCALED: return render_launch_u8(p, cs);
+    case GBV_VOXEL_F32: return render_launch_f32(p, cs, lc);
+    case GBV_VOXEL_F16: return render_launch_f16(p, cs, lc);
+    case GBV_VOXEL_BF16: return render_launch_bf16(p, cs, lc);
+    case GBV_VOXEL_U8_SCALED: return render_launch_u8(p, cs, lc);
   }
   snprintf(msg, sizeof msg, "%s: unknown voxel format", fn);
   return set_error(GBV_ERROR_UNSUPPORTED, msg);
@@ -187,6 +215,13 @@ extern "C" gbv_status gbv_render(const gbv_scene *s, float *d_accum, int width, 
   return render_frame("gbv_render", s, d_accum, width, height, accum_id_start, spp, 0, 1, d_counters, stream);
 }
 
+extern "C" gbv_status gbv_render_ex(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,
+                                    int spp, unsigned long long *d_counters, const gbv_render_config *config,
+                                    void *stream) {
+  return render_frame("gbv_render_ex", s, d_accum, width, height, accum_id_start, spp, 0, 1, d_counters, stream,
+                      nullptr, config);
+}
+
 extern "C" gbv_status gbv_render_tiles(const gbv_scene *s, float *d_accum, int width, int height,
                                        int accum_id_start, int spp, int rank, int num_ranks,
                                        unsigned long long *d_counters, void *stream) {
@@ -202,7 +237,7 @@ extern "C" gbv_status gbv_tile_partition(int width, int height, int rank, int nu
   if (n > (1ll << 31) - 1) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_tile_partition: too many tiles");
   *num_tiles = (int)n;
   if (tile_lower) {
-    const int tilesX = (width + kRefTile - 1) / kRefTile;
+    const long long tilesX = ((long long)width + kRefTile - 1) / kRefTile;
     for (long long k = 0; k < n; k++) {
       const long long id = (long long)rank + k * num_ranks;
       tile_lower[2 * k] = (int)(id % tilesX) * kRefTile;
@@ -234,26 +269,18 @@ namespace gbv {
 static __device__ __align__(256) int g_noalloc_tile_pool[1];
 constexpr long long kNoAllocMaxTiles = 1ll << 30;
 
-constexpr int kNoAllocMaxDevices = 64;
-static std::mutex g_noalloc_mutex;
-static int *g_noalloc_addr[kNoAllocMaxDevices];
-
-// Device address of the scratch on the current device, looked up once per
-// device (host code may not use the array's name as a device address).
+// Device address of the scratch on the current device.  Host code may not
+// use the array's name as a device address, so every call looks the address
+// up (cudaGetSymbolAddress allocates nothing); a device reset between calls,
+// which reloads this library's device code at possibly new addresses, is
+// therefore harmless.  The first lookup on a device (or after a reset) may
+// load the device code there, which is why the first call on a device
+// belongs before any stream capture.
 static gbv_status noalloc_scratch(int **out) {
-  int dev = 0;
-  gbv_status st = check_cuda(cudaGetDevice(&dev), "gbv_render_noalloc: cudaGetDevice");
+  void *ptr = nullptr;
+  gbv_status st = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_tile_pool), "gbv_render_noalloc: cudaGetSymbolAddress");
   if (st != GBV_OK) return st;
-  if (dev < 0 || dev >= kNoAllocMaxDevices)
-    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: device ordinal above 63");
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
-    void *ptr = nullptr;
-    st = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_tile_pool), "gbv_render_noalloc: cudaGetSymbolAddress");
-    if (st != GBV_OK) return st;
-    g_noalloc_addr[dev] = static_cast<int *>(ptr);
-  }
-  *out = g_noalloc_addr[dev];
+  *out = static_cast<int *>(ptr);
   return GBV_OK;
 }
 
@@ -267,7 +294,7 @@ extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_render_noalloc: null pointer or non-positive size");
   // the scratch is one 32-bit counter of 8x4-pixel tiles; every warp may take
   // one tile past the end, so the frame's tiles must leave room for them
-  const long long tiles = (long long)((width + 7) / 8) * ((height + 3) / 4);
+  const long long tiles = (((long long)width + 7) / 8) * (((long long)height + 3) / 4);
   if (tiles > kNoAllocMaxTiles)
     return set_error(GBV_ERROR_INVALID_ARGUMENT,
                      "gbv_render_noalloc: frame exceeds the 2^30 tiles of 8x4 pixels its 32-bit tile counter holds");
@@ -337,7 +364,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
     p.maskWords = 0;
     p.cdfYOff = p.pivOff = p.rowOff = -1;
     p.pivPerRow = 0;
-    starts[i + 1] = starts[i] + (long long)((p.W + 7) / 8) * ((p.H + 3) / 4);
+    starts[i + 1] = starts[i] + (((long long)p.W + 7) / 8) * (((long long)p.H + 3) / 4);
   }
   if (starts[count] >= (1ll << 31) - (1ll << 20))
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: more tiles than the 32-bit tile counter holds");
@@ -349,8 +376,8 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
   b->occ = 4;
   b->threshold = kThresholdDefault;
   b->skip = kSkipDefault;
-  cudaGetDevice(&b->device);
-  gbv_status st = check_cuda(cudaMalloc((void **)&b->d_items, sizeof(RenderParams) * count), "gbv_batch_create");
+  gbv_status st = check_cuda(cudaGetDevice(&b->device), "gbv_batch_create: cudaGetDevice");
+  if (st == GBV_OK) st = check_cuda(cudaMalloc((void **)&b->d_items, sizeof(RenderParams) * count), "gbv_batch_create");
   if (st == GBV_OK)
     st = check_cuda(cudaMalloc((void **)&b->d_tileStart, sizeof(long long) * (count + 1)), "gbv_batch_create");
   if (st == GBV_OK) st = check_cuda(cudaMalloc((void **)&b->d_pool, sizeof(int)), "gbv_batch_create");

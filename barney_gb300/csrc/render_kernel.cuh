@@ -10,7 +10,6 @@
 // generation the trace (MCVolumeAccel::isProg) and _shadeRays/bounce
 // (barney/kernels/shadeRays.cu:477-1041) of the pixel's queued rays.
 #pragma once
-#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -77,13 +76,13 @@ struct RenderParams {
 // setTileCoordsKernel, barney/fb/TiledFB.cu:226-255).
 constexpr int kRefTile = 32;
 __host__ __device__ inline long long owned_ref_tiles(int W, int H, int rank, int numRanks) {
-  const long long total = (long long)((W + kRefTile - 1) / kRefTile) * ((H + kRefTile - 1) / kRefTile);
+  const long long total = (((long long)W + kRefTile - 1) / kRefTile) * (((long long)H + kRefTile - 1) / kRefTile);
   return total > rank ? (total - rank + numRanks - 1) / numRanks : 0;
 }
 // 8x4-pixel warp tiles one (non-batched) launch hands out
 __host__ __device__ inline long long warp_tile_count(const RenderParams &p) {
   if (p.numRanks > 1) return owned_ref_tiles(p.W, p.H, p.rank, p.numRanks) * 32;
-  return (long long)((p.W + 7) >> 3) * ((p.H + 3) >> 2);
+  return (((long long)p.W + 7) >> 3) * (((long long)p.H + 3) >> 2);
 }
 
 template <class Store> __device__ __forceinline__ Store make_store(const RenderParams &p);
@@ -856,7 +855,8 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
 // lane reads the scene of the pixel it owns.  Otherwise the launch renders
 // the one scene `p0`.  Launch-wide settings (passes, thresholds, counters)
 // always come from p0.  Count: whether to count events (see Ctr) and, with
-// GBV_RENDER_PROFILE, cycles and lanes per phase (the timed kernel, Count =
+// a profile requested in the launch config (gbv_render_config.profile),
+// cycles and lanes per phase (the timed kernel, Count =
 // false, carries no profiling code).
 // p0 is __grid_constant__ so that helpers (inlined, or the batched kernel's
 // out-of-line copies) can take it by reference without a copy to local
@@ -947,11 +947,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         int tx, ty;
         if (!Batch && L.numRanks > 1) {  // the k-th 32x32 tile this rank owns, 4x8 warp tiles in it
           const long long big = (long long)L.rank + (long long)(tile >> 5) * L.numRanks;
-          const int bigX = (tp.W + kRefTile - 1) / kRefTile;
+          const int bigX = (int)(((long long)tp.W + kRefTile - 1) / kRefTile);
           tx = (int)(big % bigX) * kRefTile + (tile & 3) * 8;
           ty = (int)(big / bigX) * kRefTile + ((tile >> 2) & 7) * 4;
         } else {
-          const int tilesX = (tp.W + 7) >> 3;
+          const int tilesX = (int)(((long long)tp.W + 7) >> 3);
           tx = (tile % tilesX) * 8;
           ty = (tile / tilesX) * 4;
         }
@@ -1146,18 +1146,23 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   // persistent grid: as many resident blocks as the device holds
   int dev = 0, sms = 0, perSM = 0;
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st == GBV_OK) st = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   if (st != GBV_OK) return st;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = staged_words(p) * sizeof(uint32_t);
-  if (smem > 48 * 1024)
-  {
-    cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+  if (smem > 48 * 1024) {
+    st = check_cuda(cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "render_kernel: shared-memory size");
+    if (st == GBV_OK)
+      st = check_cuda(cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, false>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "render_kernel: shared-memory size");
+    if (st != GBV_OK) return st;
   }
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks, false, true>, kThreads,
-                                                smem);
+  st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks, false, true>,
+                                                                kThreads, smem),
+                  "render_kernel: occupancy");
+  if (st != GBV_OK) return st;
   const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
@@ -1168,57 +1173,58 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   int *pool = nullptr;
   st = check_cuda(cudaMallocAsync((void **)&pool, sizeof(int), stream), "cudaMallocAsync(tile pool)");
   if (st != GBV_OK) return st;
-  cudaMemsetAsync(pool, 0, sizeof(int), stream);
-  if (p.counters)
-    render_kernel<Store, MinBlocks, false, true><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr, 0,
-                                                                                               pool);
-  else
-    render_kernel<Store, MinBlocks, false, false><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr,
-                                                                                                0, pool);
-  st = check_launch("render_kernel");
-  cudaFreeAsync(pool, stream);
-  return st;
+  st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "render_kernel: clearing the tile pool");
+  if (st == GBV_OK) {
+    if (p.counters)
+      render_kernel<Store, MinBlocks, false, true><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr,
+                                                                                                 0, pool);
+    else
+      render_kernel<Store, MinBlocks, false, false><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr,
+                                                                                                  0, pool);
+    st = check_launch("render_kernel");
+  }
+  const gbv_status fst = check_cuda(cudaFreeAsync(pool, stream), "cudaFreeAsync(tile pool)");
+  return st != GBV_OK ? st : fst;
 }
 
-// GBV_RENDER_OCC=4, 5 or 6 selects the resident blocks per SM the registers
-// are capped for (default 4: 36 warps per SM at 56 registers; 5 blocks give
-// 45 warps at 40 registers and spill more).  GBV_RENDER_SKIP sets the cell
-// tests and distance draws a lane may make per traversal iteration (default
-// 6); GBV_RENDER_THRESH the percentage of a warp's busy lanes that must still
-// be tracing for the warp to keep traversing before it shades and refills
-// (default 20).
+// Launch settings resolved from a gbv_render_config (gbv_render_ex): the
+// resident 288-thread blocks per SM the registers are capped for (4: 36
+// warps per SM at 56 registers; 5 blocks give 45 warps at 40 registers and
+// spill more), and the shared-memory staging mode.  The traversal settings
+// (skip, threshold) and the profile switch travel in RenderParams.
+struct LaunchChoice {
+  int occ = 4;
+  int stage = GBV_STAGE_DEFAULT;
+};
+
+// Shared-memory staging (same results either way).  GBV_STAGE_DEFAULT: the
+// bitmask of non-zero majorants, one bit per macrocell, when it takes at
+// most 8 KB per block (64 Ki macrocells; 4 KB for the 32^3 grid of the 512^3
+// frame): the empty-cell test of the traversal becomes a shared-memory load
+// (measured +1.8%); with an env map of at most 1024 rows also the row terms
+// of its pdf (8 bytes a row).  GBV_STAGE_ALL also stages the env-map cdf_y
+// and the per-row pivots of cdf_x (up to 64 KB per block; measured slower:
+// the shared memory comes out of L1, which spills and CDF loads use).
+// GBV_STAGE_NONE stages nothing.
 template <class Store>
-inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream) {
-  const char *sk = getenv("GBV_RENDER_SKIP");
-  p.skip = sk ? atoi(sk) : kSkipDefault;
-  if (p.skip < 1) p.skip = 1;
-  // Shared-memory staging (same results either way).  GBV_RENDER_STAGE=1
-  // (default): the bitmask of non-zero majorants, one bit per macrocell, when
-  // it takes at most 8 KB per block (64 Ki macrocells; 4 KB for the 32^3
-  // grid of the 512^3 frame): the empty-cell test of the traversal becomes a
-  // shared-memory load (measured +1.8%); with an env map of at most 1024
-  // rows also the row terms of its pdf (8 bytes a row).  =2 also stages the
-  // env-map cdf_y and the per-row pivots of cdf_x (up to 64 KB per block;
-  // measured slower: the shared memory comes out of L1, which spills and CDF
-  // loads use).  =0 stages nothing.
-  const char *ns = getenv("GBV_RENDER_STAGE");
-  const int stage = ns ? atoi(ns) : 1;
+inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream, const LaunchChoice &lc) {
   const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
-  const int budget = (stage >= 2 ? 64 : 8) * 1024 / 4;
+  const bool any = lc.stage != GBV_STAGE_NONE, all = lc.stage == GBV_STAGE_ALL;
+  const int budget = (all ? 64 : 8) * 1024 / 4;
   int used = 0;
   p.maskWords = 0;
   p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
-  if (stage >= 1 && nmc > 0 && (nmc + 31) / 32 <= budget) {
+  if (any && nmc > 0 && (nmc + 31) / 32 <= budget) {
     p.maskWords = (int)((nmc + 31) / 32);
     used = p.maskWords;
   }
-  if (stage >= 1 && p.hasEnv && p.env.H >= 1 && p.env.H <= 1024) {
+  if (any && p.hasEnv && p.env.H >= 1 && p.env.H <= 1024) {
     used = (used + 1) & ~1;  // float2 entries
     p.rowOff = used;
     used += 2 * p.env.H;
   }
-  if (stage >= 2 && p.hasEnv && p.env.W >= 2) {
+  if (all && p.hasEnv && p.env.W >= 2) {
     if (used + p.env.H <= budget) {
       p.cdfYOff = used;
       used += p.env.H;
@@ -1230,15 +1236,9 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
       used += p.env.H * per;
     }
   }
-  const char *pf = getenv("GBV_RENDER_PROFILE");
-  p.profile = (pf && atoi(pf) != 0 && p.counters) ? 1 : 0;
-  const char *th = getenv("GBV_RENDER_THRESH");
-  p.threshold = th ? atoi(th) : kThresholdDefault;
-  if (p.threshold < 1) p.threshold = 1;
-  const char *oc = getenv("GBV_RENDER_OCC");
-  const int occ = oc ? atoi(oc) : 4;
-  if (occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
-  if (occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
+  if (!p.counters) p.profile = 0;
+  if (lc.occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
+  if (lc.occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
   return launch_render_t<Store, 5>(p, store, stream);
 }
 
@@ -1254,9 +1254,12 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   p.profile = 0;
   int dev = 0, sms = 0, perSM = 0;
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (st == GBV_OK) st = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (st == GBV_OK)
+    st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>,
+                                                                  kThreads, 0),
+                    "render_kernel: occupancy");
   if (st != GBV_OK) return st;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>, kThreads, 0);
   const long long tiles = warp_tile_count(p);
   const long long warpsPerBlock = kThreads / 32;
   long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);
@@ -1290,13 +1293,17 @@ namespace gbv {
 template <class Store>
 inline gbv_status batch_launch(const gbv_batch *b, RenderParams L, cudaStream_t stream) {
   int sms = 0, perSM = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  gbv_status st = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device), "SM count");
+  if (st != GBV_OK) return st;
   const long long warpsPerBlock = kThreads / 32;
-  gbv_status st = check_cuda(cudaMemsetAsync(b->d_pool, 0, sizeof(int), stream), "gbv_batch_render: pool");
+  st = check_cuda(cudaMemsetAsync(b->d_pool, 0, sizeof(int), stream), "gbv_batch_render: pool");
   if (st != GBV_OK) return st;
 #define GBV_BATCH_LAUNCH(OCC)                                                                              \
   {                                                                                                        \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, OCC, true, true>, kThreads, 0); \
+    st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, OCC, true, true>, \
+                                                                  kThreads, 0),                            \
+                    "render_kernel (batch): occupancy");                                                   \
+    if (st != GBV_OK) return st;                                                                           \
     long long blocks = (long long)sms * (perSM > 0 ? perSM : 1);                                           \
     const long long needed = (b->totalTiles + warpsPerBlock - 1) / warpsPerBlock;                         \
     if (blocks > needed) blocks = needed;                                                                  \
@@ -1319,8 +1326,8 @@ inline gbv_status batch_launch(const gbv_batch *b, RenderParams L, cudaStream_t 
 
 // The launchers of one voxel store, defined in render_store_*.cu
 #define GBV_STORE_LAUNCHERS(NAME, STORE)                                                        \
-  gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s) {                      \
-    return launch_render(p, STORE{}, s);                                                        \
+  gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s, const LaunchChoice &lc) { \
+    return launch_render(p, STORE{}, s, lc);                                                    \
   }                                                                                             \
   gbv_status render_launch_noalloc_##NAME(const RenderParams &p, cudaStream_t s, int *pool) {   \
     return launch_render_noalloc(p, STORE{}, s, pool);                                          \
@@ -1330,7 +1337,7 @@ inline gbv_status batch_launch(const gbv_batch *b, RenderParams L, cudaStream_t 
   }
 
 #define GBV_DECLARE_STORE_LAUNCHERS(NAME)                                                        \
-  gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s);                       \
+  gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s, const LaunchChoice &lc); \
   gbv_status render_launch_noalloc_##NAME(const RenderParams &p, cudaStream_t s, int *pool);    \
   gbv_status batch_launch_##NAME(const gbv_batch *b, const RenderParams &L, cudaStream_t s);
 

@@ -158,14 +158,22 @@ class GpuScene:
                            device="cuda")
 
     def render(self, spp: Optional[int] = None, accum=None, accum_id_start: int = 0, counters=None,
-               width: Optional[int] = None, height: Optional[int] = None):
-        """Accumulates `spp` passes into accum (H, W, 4); returns accum."""
+               width: Optional[int] = None, height: Optional[int] = None, config: Optional[dict] = None):
+        """Accumulates `spp` passes into accum (H, W, 4); returns accum.
+        config: launch settings of gbv_render_ex (blocks_per_sm,
+        threshold_pct, skip_cells, stage, profile); None = defaults."""
         w, h = width or self.s.width, height or self.s.height
         if accum is None:
             accum = self.new_accum(w, h)
         rec = self.record()
-        N.check(N.lib().gbv_render(C.byref(rec), _ptr(accum), w, h, accum_id_start,
-                                   self.s.spp if spp is None else spp, _ptr(counters), _stream()), "gbv_render")
+        n = self.s.spp if spp is None else spp
+        if config is None:
+            N.check(N.lib().gbv_render(C.byref(rec), _ptr(accum), w, h, accum_id_start, n, _ptr(counters),
+                                       _stream()), "gbv_render")
+        else:
+            cfg = N.render_config(**config)
+            N.check(N.lib().gbv_render_ex(C.byref(rec), _ptr(accum), w, h, accum_id_start, n, _ptr(counters),
+                                          C.byref(cfg), _stream()), "gbv_render_ex")
         return accum
 
     def render_tiles(self, rank: int, world: int, spp: Optional[int] = None, accum=None, accum_id_start: int = 0,

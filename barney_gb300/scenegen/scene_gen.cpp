@@ -9,13 +9,17 @@
 // one multiply-add per voxel.  The fBm is value noise: octave k has
 // 8*2^k lattice cells per axis, amplitude fbm_amplitude*2^-k, lattice values
 // U[-1,1], smoothstep-weighted trilinear interpolation.
+//
+// Built into its own library (libgbv_scenegen.so), apart from the renderer:
+// inputs are made by the same code for the GPU path, the CPU oracle and the
+// timed CPU baseline, and loading them maps no renderer code.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <thread>
 #include <vector>
-#include "../../include/gbvol.h"
+#include "scene_gen.h"
 
 namespace {
 
@@ -33,10 +37,10 @@ inline uint64_t hash64(uint64_t a, uint64_t b) {
 
 }  // namespace
 
-extern "C" gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed, float noise_amplitude,
-                                          int fbm_octaves, float fbm_amplitude, int nthreads, float *out) {
+extern "C" int sg_blob_volume(const int dims[3], int num_blobs, uint64_t seed, float noise_amplitude, int fbm_octaves,
+                              float fbm_amplitude, int nthreads, float *out) {
   if (!dims || !out || dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || num_blobs < 0 || fbm_octaves < 0)
-    return GBV_ERROR_INVALID_ARGUMENT;
+    return 1;
   const int nx = dims[0], ny = dims[1], nz = dims[2];
   uint64_t s = seed;
   struct Blob { double c[3], sig, amp; };
@@ -120,5 +124,5 @@ extern "C" gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint
   std::vector<std::thread> pool;
   for (int t = 0; t < nt; t++) pool.emplace_back(work);
   for (auto &th : pool) th.join();
-  return GBV_OK;
+  return 0;
 }

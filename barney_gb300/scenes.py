@@ -76,14 +76,35 @@ class Scene:
         return origin, spacing
 
 
+_SCENEGEN = None
+
+
+def _scenegen() -> C.CDLL:
+    """The input generator library (barney_gb300/_lib/libgbv_scenegen.so,
+    host code apart from the renderer); raises if it has not been built."""
+    global _SCENEGEN
+    if _SCENEGEN is None:
+        from pathlib import Path
+        path = Path(__file__).resolve().parent / "_lib" / "libgbv_scenegen.so"
+        if not path.exists():
+            raise RuntimeError(f"input generator missing: {path} (run __graft_entry__.build())")
+        L = C.CDLL(str(path))
+        L.sg_blob_volume.restype = C.c_int
+        L.sg_blob_volume.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_uint64, C.c_float, C.c_int, C.c_float,
+                                     C.c_int, C.c_void_p]
+        _SCENEGEN = L
+    return _SCENEGEN
+
+
 def blob_volume(dims, num_blobs: int, seed: int, noise: float = 0.05, fbm_octaves: int = 0,
                 fbm_amplitude: float = 0.0, nthreads: int = 0) -> np.ndarray:
-    """FP32 (nz, ny, nx) blob+noise volume from the native generator."""
+    """FP32 (nz, ny, nx) blob+noise volume from the seeded generator."""
     nx, ny, nz = dims
     out = np.empty((nz, ny, nx), dtype=np.float32)
-    N.check(N.lib().gbv_gen_blob_volume(N.ivec(nx, ny, nz), num_blobs, seed, noise, fbm_octaves,
-                                        fbm_amplitude, nthreads, out.ctypes.data_as(C.c_void_p)),
-            "gbv_gen_blob_volume")
+    dv = (C.c_int * 3)(int(nx), int(ny), int(nz))
+    if _scenegen().sg_blob_volume(dv, num_blobs, seed, noise, fbm_octaves, fbm_amplitude, nthreads,
+                                  out.ctypes.data_as(C.c_void_p)) != 0:
+        raise ValueError(f"sg_blob_volume: bad arguments {dims}, {num_blobs}, {fbm_octaves}")
     return out
 
 

@@ -39,6 +39,13 @@ WORKLOAD = ("512^3 blob+fBm volume, 256-entry two-peak TF, 16^3 macrocells, 1920
             "<=4 isotropic volume bounces, dir light + 512x256 env map")
 
 
+def bench_config(world: int, fmt: str = "f32") -> dict:
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD, "voxel_format": fmt,
+            "l2": "inputs larger than L2 (512^3 FP32 volume: 0.5 GB; its brick store on the GPU: 4.3 GB)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -161,7 +168,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": sample},
+            "data": "synthetic", "config": bench_config(world, args.format), "sample": sample,
             "frame_ms_extrapolated": 1e3 * sum(times) / len(times) * scene.spp,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -455,10 +462,8 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "voxel_format": args.format, "voxel_layout": "8^3-cell brick corners",
-                       "l2": "inputs larger than L2 (brick store %.1f GB)" % (g.voxels.numel() / 1e9),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(world, args.format),
+            "voxel_store": "8^3-cell brick corners, %.2f GB" % (g.voxels.numel() / 1e9),
             "frame_ms": frame_ms, "density_samples_per_frame": samples, "macrocells_per_frame": mcs,
             "rays_per_frame": rays, "loop_caps": caps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -518,6 +523,60 @@ def run_ours(args):
         dist.barrier()
 
 
+def profile_render_case(args):
+    """Small, self-contained render launches for ncu captures: the frame
+    scene (--dims, --width, --height, --spp, --format, --layout), --warmup
+    untimed launches, then --launches launches as timed runs make them (no
+    event counting), then one counted launch whose counters go to --out, so
+    that ncu's DRAM bytes of the uncounted launches can be related to
+    density samples (the frame is deterministic).  Capture the uncounted
+    launches with
+      ncu --clock-control none -k regex:render_kernel -s <warmup> -c <launches> ..."""
+    import torch
+    from barney_gb300 import _native as N, scenes
+    from barney_gb300.device import GpuScene
+    s = scenes.frame_scene(dims=args.dims, width=args.width, height=args.height, spp=args.spp)
+    fmt = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}[args.format]
+    layout = N.GBV_LAYOUT_BRICK_CORNERS if args.layout == "brick" else N.GBV_LAYOUT_LINEAR
+    g = GpuScene(s, layout=layout, fmt=fmt)
+    acc = g.new_accum()
+    for _ in range(args.warmup + args.launches):
+        g.render(accum=acc)
+    cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    g.render(accum=acc, counters=cnt)
+    torch.cuda.synchronize()
+    c = [int(x) for x in cnt.cpu().tolist()]
+    rec = dict(dims=args.dims, width=args.width, height=args.height, spp=args.spp, format=args.format,
+               layout=args.layout, samples_per_launch=c[0], mc_visits_per_launch=c[1], rays_per_launch=c[2])
+    if args.out:
+        Path(args.out).parent.mkdir(parents=True, exist_ok=True)
+        Path(args.out).write_text(json.dumps(rec, indent=1))
+    print(json.dumps(rec))
+
+
+def profile_ea_case(args):
+    """EA launches for ncu captures: the differentiable emission-absorption
+    workload (--dims^3 density grid, 256-entry TF, --views views of --size^2
+    on a sphere of radius 2.5, step 0.5 voxel): --warmup forward+adjoint
+    passes, then --launches more.  Capture the forward with
+    -k regex:ea_forward and the adjoint with -k regex:ea_backward, skipping
+    the warm-up launches (-s <warmup>), with --clock-control none."""
+    import torch
+    from barney_gb300 import scenes
+    from barney_gb300.ea import EAProblem
+    gt = scenes.ea_scene(args.dims)
+    views = scenes.fibonacci_views(args.views, 2.5, args.size)
+    step = 0.5 / (args.dims - 1)
+    tgt = EAProblem(gt, views, step).render()
+    start = scenes.Scene(scalars=np.full_like(gt.scalars, 0.1), tf=gt.tf, base_density=gt.base_density)
+    p = EAProblem(start, views, step)
+    for _ in range(args.warmup + args.launches):
+        img = p.render()
+        p.backward(img, 2 * (img - tgt))
+    torch.cuda.synchronize()
+    print("ok")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -525,11 +584,31 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--format", default="f32", choices=["f32", "f16", "bf16", "u8"])
-    ap.add_argument("--dims", type=int, default=512)
+    ap.add_argument("--dims", type=int, default=None, help="volume edge (default 512; 128 for --profile-case ea)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--quick", action="store_true", help="skip the FP16 and adjoint extras")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile-case", choices=["render", "ea"],
+                    help="small launches for an ncu capture instead of the benchmark")
+    ap.add_argument("--width", type=int, default=480, help="--profile-case render: frame width")
+    ap.add_argument("--height", type=int, default=270, help="--profile-case render: frame height")
+    ap.add_argument("--spp", type=int, default=1, help="--profile-case render: passes per launch")
+    ap.add_argument("--layout", default="brick", choices=["brick", "linear"], help="--profile-case render")
+    ap.add_argument("--launches", type=int, default=1, help="--profile-case: launches after the warm-up")
+    ap.add_argument("--views", type=int, default=32, help="--profile-case ea: views")
+    ap.add_argument("--size", type=int, default=256, help="--profile-case ea: view edge in pixels")
+    ap.add_argument("--out", default="", help="--profile-case render: counters JSON")
     args = ap.parse_args()
+    if args.dims is None:
+        args.dims = 128 if args.profile_case == "ea" else 512
+    if args.profile_case:
+        import torch
+        torch.cuda.set_device(0)
+        if args.profile_case == "render":
+            profile_render_case(args)
+        else:
+            profile_ea_case(args)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":

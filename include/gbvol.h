@@ -188,8 +188,8 @@ typedef struct gbv_scene {
    [5..7] SM cycles spent starting traces, traversing and shading, summed
    over warps, [8] traversal iterations of warps and [9] tracing lanes
    summed over them, [10] shading passes of warps and [11] shaded lanes
-   summed over them ([5..11] only with GBV_RENDER_PROFILE=1 in the
-   environment, else 0). */
+   summed over them ([5..11] only when gbv_render_ex's config asks for a
+   profile, else 0). */
 enum { GBV_COUNTER_SAMPLES = 0, GBV_COUNTER_MC_VISITS = 1, GBV_COUNTER_RAYS = 2,
        GBV_COUNTER_CAPS = 3, GBV_COUNTER_CELLS = 4, GBV_COUNTER_CYCLES_START = 5,
        GBV_COUNTER_CYCLES_TRAVERSE = 6, GBV_COUNTER_CYCLES_SHADE = 7,
@@ -216,6 +216,39 @@ gbv_status gbv_env_build_cdfs(const float *d_texels, int width, int height,
 gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
                       int height, int accum_id_start, int spp,
                       unsigned long long *d_counters, void *stream);
+
+/* Launch settings of the render kernel.  They change speed, never results:
+   every setting renders the identical frame.  A zero field takes its
+   default, so a zero-initialised struct (or a null pointer) is the default
+   launch.
+   blocks_per_sm: resident 288-thread blocks per SM the registers are capped
+     for: 4 (default; 56 registers), 5 or 6.
+   threshold_pct: a warp keeps traversing while at least this percentage of
+     its busy lanes is still tracing (1..100, default 20).
+   skip_cells: cell tests and Woodcock distance draws a lane makes per
+     traversal iteration before the warp samples (1..1024, default 6).
+   stage: shared-memory staging, GBV_STAGE_DEFAULT (the bitmask of non-zero
+     majorants, at most 8 KB, and the env map's per-row pdf terms),
+     GBV_STAGE_NONE, or GBV_STAGE_ALL (also the env map's CDF tables, up to
+     64 KB per block).
+   profile: 1 = per-phase cycle and lane counts into d_counters[5..11]
+     (needs d_counters). */
+enum { GBV_STAGE_DEFAULT = 0, GBV_STAGE_NONE = 1, GBV_STAGE_ALL = 2 };
+typedef struct gbv_render_config {
+  int blocks_per_sm;
+  int threshold_pct;
+  int skip_cells;
+  int stage;
+  int profile;
+  int reserved[3]; /* zero */
+} gbv_render_config;
+
+/* gbv_render with explicit launch settings (config may be null).  No
+   counterpart in the reference (whose launches are fixed). */
+gbv_status gbv_render_ex(const gbv_scene *scene, float *d_accum, int width,
+                         int height, int accum_id_start, int spp,
+                         unsigned long long *d_counters,
+                         const gbv_render_config *config, void *stream);
 
 /* Frame partition across ranks (one GPU each), as the reference's tiled
    frame buffer does it: the frame is cut into 32x32-pixel tiles, row-major,
@@ -266,9 +299,11 @@ gbv_status gbv_unpack_tiles(const void *d_tiles, int width, int height,
    Same arguments and results as gbv_render.  Its one word of scratch (the
    persistent kernel's tile-pool counter) lives in a file-scope device array
    of 4 bytes that every GPU loading this library keeps until exit, instead
-   of a cudaMallocAsync/cudaFreeAsync pair.  The first call on a device looks
-   up that array's device address once (cudaGetSymbolAddress); make that
-   first call before any stream capture.  All calls share the word and each
+   of a cudaMallocAsync/cudaFreeAsync pair.  Every call looks up that
+   array's device address on the current device (cudaGetSymbolAddress, which
+   allocates nothing), so a device reset between calls is harmless; the first
+   call on a device (or after a reset) may load the library's device code
+   there, so make it before any stream capture.  All calls share the word and each
    call clears it before its launch, so calls that overlap on the GPU (for
    example on two streams) race.  Frames above 2^30 tiles of 8x4 pixels are
    rejected with GBV_ERROR_INVALID_ARGUMENT. */
@@ -335,15 +370,17 @@ gbv_status gbv_ea_backward(const gbv_scene *scene, const gbv_ea_view *views,
                            int num_views, float step, const float *d_images,
                            const float *d_grad_images, float *d_grad_scalars,
                            float *d_grad_tf, void *stream);
+/* gbv_ea_backward with the adjoint kernel's resident 128-thread blocks per
+   SM chosen: 4, 6 (the default, also for 0) or 8.  Speed only; the
+   gradients are the same up to the order of floating-point atomics. */
+gbv_status gbv_ea_backward_ex(const gbv_scene *scene, const gbv_ea_view *views,
+                              int num_views, float step, const float *d_images,
+                              const float *d_grad_images, float *d_grad_scalars,
+                              float *d_grad_tf, int blocks_per_sm, void *stream);
 
-/* ------------------------------------------------------------------------
- * Synthetic inputs (host memory; no GPU needed).
- * ------------------------------------------------------------------------ */
-/* Blob-plus-noise volume: clamp(sum_i a_i exp(-|x-c_i|^2/(2 s_i^2))
-   + U[0,noise] + fBm, 0, 1) on the unit cube, x-fastest, FP32. */
-gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
-                               float noise_amplitude, int fbm_octaves,
-                               float fbm_amplitude, int nthreads, float *out);
+/* Every EA entry point rejects (GBV_ERROR_INVALID_ARGUMENT, before any
+   launch) a step for which a ray along the field's box diagonal would take
+   more than 2^24 steps. */
 
 /* ------------------------------------------------------------------------
  * Iso-surface ray queries.
@@ -365,26 +402,6 @@ gbv_status gbv_gen_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
 gbv_status gbv_iso_intersect(const gbv_scene *scene, const float *d_ranges,
                              float iso_value, const float *d_rays,
                              long long num_rays, float *d_hits, void *stream);
-
-/* ------------------------------------------------------------------------
- * Self-test (no counterpart in the reference).
- * ------------------------------------------------------------------------ */
-
-/* The renderer's bounded sine/cosine (angles in [-pi/4, 2pi + pi/4]) for n
-   arguments: on the host (on_device = 0; host pointers) or in a kernel on
-   `stream` (on_device = 1; device pointers).  Both give identical results;
-   tests check them against float64 sine and cosine. */
-gbv_status gbv_selftest_sincos(const float *x, long long n, float *sn,
-                               float *cs, int on_device, void *stream);
-
-/* The renderer's arc cosine and two-argument arc tangent of env-map angles:
-   acos_x[i] = acos(x[i]) (x in [-1, 1]) and atan2_yx[i] = atan2(y[i], x[i]),
-   on the host (on_device = 0; host pointers) or in a kernel on `stream`
-   (on_device = 1; device pointers).  Both give identical results; tests
-   check them against float64. */
-gbv_status gbv_selftest_angles(const float *y, const float *x, long long n,
-                               float *acos_x, float *atan2_yx, int on_device,
-                               void *stream);
 
 #ifdef __cplusplus
 }

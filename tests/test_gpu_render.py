@@ -269,55 +269,58 @@ def test_rmse_falls_as_inverse_sqrt_spp(cuda):
     assert ro < 1.5 * rmse[16], (ro, rmse)
 
 
-@pytest.mark.parametrize("stage", ["1", "2"])
+@pytest.mark.parametrize("stage", [N.GBV_STAGE_DEFAULT, N.GBV_STAGE_ALL])
 def test_shared_memory_staging_is_transparent(cuda, stage):
-    """Staging the majorant bitmask (GBV_RENDER_STAGE=1, the default) and
-    also the env-map CDF pivots (=2) in shared memory gives the same frame,
-    bit for bit, as reading them from global memory (=0; the pivot search
-    returns the reference binary search's index)."""
-    import os
+    """Staging the majorant bitmask (GBV_STAGE_DEFAULT) and also the env-map
+    CDF pivots (GBV_STAGE_ALL) in shared memory gives the same frame, bit
+    for bit, as reading them from global memory (GBV_STAGE_NONE; the pivot
+    search returns the reference binary search's index)."""
     import torch
     s = _ms_scene(8, w=64, h=48, dims=48)
     s.env = scenes.env_sky(200, 100)  # W not a multiple of 32
     g = GpuScene(s)
-    os.environ["GBV_RENDER_STAGE"] = "0"
-    try:
-        a = g.render(spp=8, accum_id_start=3).cpu().numpy()
-        os.environ["GBV_RENDER_STAGE"] = stage
-        b = g.render(spp=8, accum_id_start=3).cpu().numpy()
-    finally:
-        del os.environ["GBV_RENDER_STAGE"]
+    a = g.render(spp=8, accum_id_start=3, config={"stage": N.GBV_STAGE_NONE}).cpu().numpy()
+    b = g.render(spp=8, accum_id_start=3, config={"stage": stage}).cpu().numpy()
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(a), bits(b))
 
 
-@pytest.mark.parametrize("settings", [{"GBV_RENDER_SKIP": "1"},
-                                      {"GBV_RENDER_SKIP": "64", "GBV_RENDER_THRESH": "100"},
-                                      {"GBV_RENDER_THRESH": "1", "GBV_RENDER_OCC": "5"},
-                                      {"GBV_RENDER_OCC": "6", "GBV_RENDER_SKIP": "2"}])
+@pytest.mark.parametrize("settings", [{"skip_cells": 1},
+                                      {"skip_cells": 64, "threshold_pct": 100},
+                                      {"threshold_pct": 1, "blocks_per_sm": 5},
+                                      {"blocks_per_sm": 6, "skip_cells": 2},
+                                      {"blocks_per_sm": 4, "skip_cells": 1024, "stage": N.GBV_STAGE_NONE}])
 def test_launch_settings_do_not_change_frames(cuda, settings):
     """Units per seek (1: one cell test or one distance draw per traversal
-    iteration; 64: the whole way to the next sample), traversal thresholds
-    (1%: traverse until every lane is done; 100%: shade as soon as one lane
-    finishes) and resident blocks only regroup each lane's steps: the frame
-    (multiple scattering, env map) is bit-identical to the default launch's."""
-    import os
+    iteration; 64 or 1024: the whole way to the next sample), traversal
+    thresholds (1%: traverse until every lane is done; 100%: shade as soon
+    as one lane finishes) and resident blocks only regroup each lane's
+    steps: the frame (multiple scattering, env map) is bit-identical to the
+    default launch's.  The settings travel in gbv_render_ex's config."""
     import torch
     s = _ms_scene(4, w=64, h=48, dims=48)
     g = GpuScene(s)
     a = g.render(spp=4, accum_id_start=3).cpu().numpy()
-    saved = {k: os.environ.get(k) for k in settings}
-    os.environ.update(settings)
-    try:
-        b = g.render(spp=4, accum_id_start=3).cpu().numpy()
-    finally:
-        for k, v in saved.items():
-            if v is None:
-                del os.environ[k]
-            else:
-                os.environ[k] = v
+    b = g.render(spp=4, accum_id_start=3, config=settings).cpu().numpy()
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(a), bits(b))
+
+
+def test_profile_counts_through_config(cuda):
+    """config.profile = 1 fills the per-phase counters [5..11]; without it
+    they stay zero; the frame and the event counts are the same."""
+    import torch
+    s = _ms_scene(2, w=48, h=32, dims=32)
+    g = GpuScene(s)
+    c0 = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    c1 = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    a = g.render(spp=2, counters=c0).cpu().numpy()
+    b = g.render(spp=2, counters=c1, config={"profile": 1}).cpu().numpy()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(a), bits(b))
+    assert c0[:5].tolist() == c1[:5].tolist()
+    assert all(v == 0 for v in c0[5:].tolist())
+    assert all(v > 0 for v in c1[5:].tolist())
 
 
 def test_bench_frame_bit_exact_with_bounded_math(cuda):

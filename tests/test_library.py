@@ -80,7 +80,8 @@ def test_generator_deterministic_and_in_range():
     assert np.array_equal(a, b)
     assert not np.array_equal(a, c)
     assert a.min() >= 0.0 and a.max() <= 1.0 and a.std() > 0.01
-    assert N.lib().gbv_gen_blob_volume(N.ivec(1, 4, 4), 1, 0, 0.0, 0, 0.0, 1, C.c_void_p(16)) == 1
+    with pytest.raises(ValueError):
+        scenes.blob_volume((1, 4, 4), 1, seed=0)
 
 
 def test_bn_context_rejects_cpu_backend_and_multi_gpu():
@@ -187,3 +188,70 @@ def test_bounded_acos_atan2_accuracy():
                                        None) == N.GBV_OK
     np.testing.assert_array_equal(t2, np.arctan2(yy, xx))
     np.testing.assert_array_equal(np.signbit(t2), np.signbit(np.arctan2(yy, xx)))
+
+
+def test_ea_step_cap_rejected_before_the_device():
+    """A step so small that one ray could take more than 2^24 steps is an
+    error returned before any launch (the march's loop is bounded)."""
+    L = N.lib()
+    rec = N.GbvScene()
+    rec.d_voxels = 16
+    rec.d_tf = 16
+    rec.tf_n = 4
+    rec.format, rec.layout = N.GBV_VOXEL_F32, N.GBV_LAYOUT_LINEAR
+    rec.dims[:] = (8, 8, 8)
+    rec.origin[:] = (-.5, -.5, -.5)
+    rec.spacing[:] = (1 / 7, 1 / 7, 1 / 7)
+    rec.domain[:] = (0.0, 1.0)
+    view = N.GbvEAView()
+    view.width = view.height = 4
+    img = C.c_void_p(16)
+    for step in (1e-30, 1e-8, float("nan"), 0.0, -1.0):
+        assert L.gbv_ea_render(C.byref(rec), C.byref(view), 1, step, img, None) == N.GBV_ERROR_INVALID_ARGUMENT
+        assert L.gbv_ea_render_f64(C.byref(rec), C.byref(view), 1, step, img, None) == N.GBV_ERROR_INVALID_ARGUMENT
+        assert L.gbv_ea_backward(C.byref(rec), C.byref(view), 1, step, img, img, img, img,
+                                 None) == N.GBV_ERROR_INVALID_ARGUMENT
+    L.gbv_ea_render(C.byref(rec), C.byref(view), 1, 1e-30, img, None)
+    assert "2^24" in L.gbv_last_error().decode()
+
+
+def test_tile_counts_of_very_wide_frames():
+    """Tile counts are formed in 64-bit arithmetic: a frame 2^31-1 pixels wide
+    has ceil((2^31-1)/32) = 2^26 tiles of 32x32 per row (no int overflow)."""
+    L = N.lib()
+    n = C.c_int()
+    assert L.gbv_tile_partition(2 ** 31 - 1, 1, 0, 1, C.byref(n), None) == N.GBV_OK
+    assert n.value == 2 ** 26
+    assert L.gbv_tile_partition(2 ** 31 - 1, 1, 3, 4, C.byref(n), None) == N.GBV_OK
+    assert n.value == 2 ** 24
+    assert L.gbv_tile_partition(2 ** 31 - 1, 33, 0, 2 ** 26 + 1, C.byref(n), None) == N.GBV_OK
+    assert n.value == 2
+    buf = (C.c_int * (2 * n.value))()
+    assert L.gbv_tile_partition(2 ** 31 - 1, 33, 0, 2 ** 26 + 1, C.byref(n), buf) == N.GBV_OK
+    # rank 0 of 2^26+1 owns tiles 0 and 2^26+1: (0, 0) and the second tile of
+    # the second row of a 2^26-tile-wide grid
+    assert list(buf) == [0, 0, 32, 32]
+
+
+def test_render_config_checked_before_the_device():
+    """gbv_render_ex rejects out-of-range launch settings before any CUDA
+    call; a zero config is the default launch (spp = 0: nothing to do)."""
+    L = N.lib()
+    rec = N.GbvScene()
+    rec.d_voxels = rec.d_majorants = rec.d_tf = 16
+    rec.tf_n, rec.cells_per_mc = 4, 8
+    rec.dims[:] = (8, 8, 8)
+    acc = C.c_void_p(16)
+    bad = [dict(blocks_per_sm=3), dict(blocks_per_sm=7), dict(threshold_pct=101), dict(threshold_pct=-1),
+           dict(skip_cells=1025), dict(stage=3), dict(profile=2)]
+    for kw in bad:
+        cfg = N.render_config(**kw)
+        assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(cfg), None) == 1, kw
+        assert "launch config" in L.gbv_last_error().decode()
+    cfg = N.render_config()
+    cfg.reserved[1] = 1
+    assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(cfg), None) == 1
+    assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(N.render_config()), None) == 0
+    assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, None, None) == 0
+    good = N.render_config(blocks_per_sm=6, threshold_pct=100, skip_cells=1024, stage=N.GBV_STAGE_ALL, profile=1)
+    assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(good), None) == 0
