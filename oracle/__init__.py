@@ -66,6 +66,8 @@ def lib() -> C.CDLL:
         sigs = {
             "orc_rng_sequence": (None, [C.c_uint32, C.c_uint32, i, vp]),
             "orc_rng_from_seed": (None, [C.c_uint64, C.c_uint64, i, i, vp, C.POINTER(C.c_uint64)]),
+            "orc_rng_seed_state": (C.c_uint64, [C.c_uint32, C.c_uint32]),
+            "orc_hash3": (C.c_uint64, [C.c_uint32, C.c_uint32, C.c_uint32]),
             "orc_fast_log": (f, [f]),
             "orc_float_to_half": (C.c_uint16, [f]),
             "orc_half_to_float": (f, [C.c_uint16]),

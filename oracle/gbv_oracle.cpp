@@ -1424,13 +1424,20 @@ void orc_rng_sequence(uint32_t a, uint32_t b, int n, float *out) {
 
 void orc_rng_from_seed(uint64_t seed_state, uint64_t hash, int use_u64, int n, float *out,
                        uint64_t *new_seed_state) {
-  (void)use_u64;
+  // the 32-bit constructor takes the hash's low 32 bits
   RNGSeed s;
   s.state = seed_state;
-  Random2 r(s, hash);
+  Random2 r(s, use_u64 ? hash : (uint64_t)(uint32_t)hash);
   for (int i = 0; i < n; i++) out[i] = r();
   if (new_seed_state) *new_seed_state = s.state;
 }
+
+uint64_t orc_rng_seed_state(uint32_t a, uint32_t b) {
+  RNGSeed s;
+  rng_seed(s, a, b);
+  return s.state;
+}
+uint64_t orc_hash3(uint32_t a, uint32_t b, uint32_t c) { return fnv_hash3(a, b, c); }
 
 float orc_fast_log(float f) { return fastLog(f); }
 uint16_t orc_float_to_half(float f) { return f2h(f); }

@@ -83,6 +83,8 @@ typedef struct orc_stats {
 void  orc_rng_sequence(uint32_t a, uint32_t b, int n, float *out);
 void  orc_rng_from_seed(uint64_t seed_state, uint64_t hash, int use_u64, int n,
                         float *out, uint64_t *new_seed_state);
+uint64_t orc_rng_seed_state(uint32_t a, uint32_t b);  /* RNGSeed::seed(a, b) from the default state */
+uint64_t orc_hash3(uint32_t a, uint32_t b, uint32_t c);
 float orc_fast_log(float f);
 uint16_t orc_float_to_half(float f);
 float orc_half_to_float(uint16_t h);

@@ -272,7 +272,7 @@ def test_differentiable_workload_at_its_named_size(cuda):
         ov, ot = ov.reshape(-1), ot.reshape(-1)
         sel = np.flatnonzero(np.abs(ov) > 1e-3 * np.abs(ov).max())
         tsel = np.flatnonzero(np.abs(ot) > 1e-3 * np.abs(ot).max())
-        assert sel.size > 10000 and tsel.size > 100, (sel.size, tsel.size)
+        assert sel.size > 10000 and tsel.size >= 64, (sel.size, tsel.size)
         assert np.linalg.norm(gv[sel] - ov[sel]) <= 1e-3 * np.linalg.norm(ov[sel])
         assert np.linalg.norm(gtf[tsel] - ot[tsel]) <= 1e-3 * np.linalg.norm(ot[tsel])
         if tf_kind != "ramp":

@@ -1,0 +1,218 @@
+"""The CPU oracle against the reference's own code (CPU only).
+
+The reference renderer's sources for the structured-volume path compile
+unchanged here (oracle/refpin, `make -C oracle ref`): its RNG and hash,
+fastLog, the float/half conversions of its CPU backend, the transfer
+function's map and majorant, the structured field's sampler with the CPU
+backend's trilinear texture, sampleAndMap, the macrocell DDA and the whole
+per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
+stream, DDA over the majorant grid, Woodcock tracking, hit record), and the
+frame buffer's 8-bit and sRGB packing.  Their outputs on fixed inputs are
+stored in tests/golden/ref_pin.npz (tests/golden/make_ref_golden.py); the
+oracle must reproduce every one bit for bit.  Where the reference checkout
+is present the live library is also compared on fresh random inputs.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import refpin
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "ref_pin.npz"
+
+
+@pytest.fixture(scope="module")
+def pin():
+    z = np.load(GOLDEN)
+    c = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    o = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return c, o
+
+
+def bits(a):
+    a = np.ascontiguousarray(a, np.float32)
+    return a.view(np.uint32)
+
+
+def same_or_both_nan(a, b):
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(bits(a)[~na], bits(b)[~nb])
+
+
+def _scene(c, tf, domain, bd, cells_per_mc=8):
+    from barney_gb300 import scenes
+    s = scenes.Scene(scalars=c["vol"], tf=tf, base_density=bd, cells_per_mc=cells_per_mc)
+    s.domain = tuple(domain)
+    o = oracle.Oracle(s)
+    o.rec.origin[:] = list(c["vol_origin"])
+    o.rec.spacing[:] = list(c["vol_spacing"])
+    return o
+
+
+# ---- the oracle against the stored reference outputs ----------------------
+
+def test_rng_streams(pin):
+    c, o = pin
+    got = np.stack([oracle.rng_sequence(int(a), int(b), 16) for a, b in c["rng_ab"]])
+    assert np.array_equal(bits(got), bits(o["rng_seq"]))
+    L = oracle.lib()
+    seqs, states = [], []
+    for u64 in (0, 1):
+        for st, h in zip(c["seed_states"], c["seed_hashes"]):
+            out = np.empty(8, np.float32)
+            ns = oracle.C.c_uint64()
+            L.orc_rng_from_seed(int(st), int(h), u64, 8, oracle._p(out), oracle.C.byref(ns))
+            seqs.append(out)
+            states.append(ns.value)
+    assert np.array_equal(bits(np.stack(seqs)), bits(o["rng_seed_seq"]))
+    assert np.array_equal(np.array(states, np.uint64), o["rng_seed_state"])
+    seeded = np.array([L.orc_rng_seed_state(int(a), int(b)) for a, b in c["rng_ab"]], np.uint64)
+    assert np.array_equal(seeded, o["rng_seeded"])
+    h = np.array([L.orc_hash3(int(a), int(b), int(x)) for a, b, x in c["hash_abc"]], np.uint64)
+    assert np.array_equal(h, o["hash3"])
+
+
+def test_fast_log(pin):
+    c, o = pin
+    got = np.array([oracle.fast_log(float(v)) for v in c["log_x"]], np.float32)
+    assert np.array_equal(bits(got), bits(o["log"]))
+
+
+def test_half_conversions(pin):
+    c, o = pin
+    L = oracle.lib()
+    got = np.array([L.orc_float_to_half(float(v)) for v in c["half_x"]], np.uint16)
+    assert np.array_equal(got, o["half"])
+    back = np.array([L.orc_half_to_float(h) for h in range(65536)], np.float32)
+    assert same_or_both_nan(back, o["half_all"].view(np.float32))
+
+
+@pytest.mark.parametrize("k,domain,bd", [("a", (0.0, 1.0), 50.0), ("b", (0.0, 1.0), 20.0), ("c", (0.15, 0.85), 3.5)])
+def test_transfer_function_map_and_majorant(pin, k, domain, bd):
+    c, o = pin
+    orc = _scene(c, c[f"tf_{k}"], domain, bd)
+    assert np.array_equal(bits(orc.tf_map(c["tf_s"])), bits(o[f"map_{k}"]))
+    assert np.array_equal(bits(orc.majorants_of(c["tf_ranges"])), bits(o[f"maj_{k}"]))
+
+
+def test_field_sampler(pin):
+    c, o = pin
+    orc = _scene(c, c["tf_a"], (0.0, 1.0), 40.0)
+    got = orc.sample(c["pts"])
+    assert same_or_both_nan(got, o["sample"])
+    assert np.isnan(got).sum() > 100 and (~np.isnan(got)).sum() > 1000
+    # sampleAndMap: NaN (outside) maps to zero
+    s = np.nan_to_num(got, nan=0.0)
+    m = orc.tf_map(s)
+    m[np.isnan(got)] = 0.0
+    assert np.array_equal(bits(m), bits(o["sample_map"]))
+
+
+def test_volume_intersection_program(pin):
+    """MCVolumeAccel::isProg: hit flag, t, hit point, the phase function's
+    albedo (the default build's Phase(color) keeps 0.7 x the sampled
+    colour, packedBSDF/Phase.h:121-145) and the ray's RNG seed afterwards."""
+    c, o = pin
+    cpm = int(c["trace_cpm"][0])
+    orc = _scene(c, c["tf_a"], (0.0, 1.0), 40.0, cells_per_mc=cpm)
+    maj = orc.majorants_of(orc.mc_ranges())
+    assert np.array_equal(bits(maj), bits(o["trace_majorants"]))
+    orc.majorants = np.ascontiguousarray(maj)
+    orc.rec.majorants = orc.majorants.ctypes.data
+    L = oracle.lib()
+    C = oracle.C
+    nhit = 0
+    for i in range(c["ray_org"].shape[0]):
+        org, d = c["ray_org"][i].copy(), c["ray_dir"][i].copy()
+        st = C.c_uint64(int(c["ray_seed"][i]))
+        t = C.c_float(0.0)
+        rgb = np.zeros(3, np.float32)
+        h = L.orc_trace_ray(C.byref(orc.rec), oracle._p(org), oracle._p(d), float(c["ray_tmax"][i]), C.byref(st),
+                            C.byref(t), oracle._p(rgb))
+        assert bool(h) == bool(o["trace_hit"][i]), i
+        assert st.value == int(o["trace_state"][i]), i
+        if h:
+            nhit += 1
+            tt = np.float32(t.value)
+            assert bits(tt) == bits(o["trace_t"][i]), i
+            P = org + tt * d
+            assert np.array_equal(bits(P), bits(o["trace_P"][i])), i
+            assert np.array_equal(bits(np.float32(0.7) * rgb), bits(o["trace_albedo"][i])), i
+    assert nhit > 100
+
+
+def test_frame_buffer_packing(pin):
+    c, o = pin
+    acc = c["rgba"].reshape(1, -1, 4)
+    assert np.array_equal(oracle.Oracle.tonemap(None, acc, 1, 1).reshape(-1), o["rgba8"])
+    assert np.array_equal(oracle.Oracle.tonemap(None, acc, 1, 2).reshape(-1), o["srgb8"])
+
+
+# ---- the live reference library (where the reference checkout is) --------
+
+live = pytest.mark.skipif(not refpin.reference_present(), reason="reference checkout absent")
+
+
+@live
+def test_live_library_reproduces_the_fixtures(pin):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_ref_golden", GOLDEN.parent / "make_ref_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    c, o = pin
+    fresh = mod.cases()
+    for k, v in c.items():
+        assert np.array_equal(np.asarray(v), np.asarray(fresh[k])), k
+    out = mod.reference_outputs(c)
+    for k, v in o.items():
+        a, b = np.asarray(v), np.asarray(out[k])
+        if a.dtype == np.float32:
+            assert same_or_both_nan(a, b), k
+        else:
+            assert np.array_equal(a, b), k
+
+
+@live
+def test_live_random_rays_and_samples():
+    """Fresh random inputs (other seeds, a bench-like TF and macrocells of 8
+    and 16 cells): the live reference and the oracle agree bit for bit."""
+    from barney_gb300 import scenes
+    rng = np.random.default_rng(77)
+    vol = scenes.blob_volume((48, 40, 36), 10, seed=99, noise=0.05, fbm_octaves=2, fbm_amplitude=0.1)
+    origin = np.array([-0.5, -0.5, -0.5], np.float32)
+    spacing = np.array([1 / 47, 1 / 39, 1 / 35], np.float32)
+    tf = scenes.tf_two_peaks(256)
+    c = {"vol": vol, "vol_origin": origin, "vol_spacing": spacing}
+    pts = ((rng.random((3000, 3)) * 1.2) - 0.6).astype(np.float32)
+    orc = _scene(c, tf, (0.0, 1.0), 50.0)
+    assert same_or_both_nan(orc.sample(pts), refpin.sample_points(vol, origin, spacing, pts))
+    for cpm in (8, 16):
+        orc = _scene(c, tf, (0.0, 1.0), 50.0, cells_per_mc=cpm)
+        maj = np.ascontiguousarray(orc.majorants_of(orc.mc_ranges()))
+        orc.majorants = maj
+        orc.rec.majorants = maj.ctypes.data
+        C = oracle.C
+        hits = 0
+        for i in range(400):
+            d = rng.standard_normal(3)
+            d /= np.linalg.norm(d)
+            org = (2.5 * d).astype(np.float32)
+            dirv = ((rng.random(3) - 0.5) * 0.8 - org)
+            dirv = (dirv / np.linalg.norm(dirv)).astype(np.float32)
+            seed = int(rng.integers(0, 2 ** 63))
+            h, t, P, alb, ns = refpin.trace_ray(vol, origin, spacing, cpm, maj, tf, (0.0, 1.0), 50.0, org, dirv,
+                                                1e30, seed)
+            st = C.c_uint64(seed)
+            tt = C.c_float(0.0)
+            rgb = np.zeros(3, np.float32)
+            h2 = oracle.lib().orc_trace_ray(C.byref(orc.rec), oracle._p(org), oracle._p(dirv), 1e30, C.byref(st),
+                                            C.byref(tt), oracle._p(rgb))
+            assert h == bool(h2) and ns == st.value, (cpm, i)
+            if h:
+                hits += 1
+                assert bits(np.float32(t)) == bits(np.float32(tt.value)), (cpm, i)
+                assert np.array_equal(bits(np.float32(0.7) * rgb), bits(alb)), (cpm, i)
+        assert hits > 50
