@@ -43,12 +43,14 @@ class GbvScene(C.Structure):
 
 
 GBV_STAGE_DEFAULT, GBV_STAGE_NONE, GBV_STAGE_ALL = 0, 1, 2
+GBV_RENDER_PERSISTENT, GBV_RENDER_WAVEFRONT = 0, 1
 
 
 class GbvRenderConfig(C.Structure):
     """gbv_render_config: launch settings (zero fields take the defaults)."""
     _fields_ = [("blocks_per_sm", C.c_int), ("threshold_pct", C.c_int), ("skip_cells", C.c_int),
-                ("stage", C.c_int), ("profile", C.c_int), ("reserved", C.c_int * 3)]
+                ("stage", C.c_int), ("profile", C.c_int), ("mode", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 def render_config(**kw) -> GbvRenderConfig:

@@ -127,10 +127,13 @@ static bool resolve_config(const gbv_render_config *c, RenderParams &p, LaunchCh
   if (c->skip_cells < 0 || c->skip_cells > 1024) return false;
   if (c->stage < GBV_STAGE_DEFAULT || c->stage > GBV_STAGE_ALL) return false;
   if (c->profile != 0 && c->profile != 1) return false;
-  if (c->reserved[0] || c->reserved[1] || c->reserved[2]) return false;
+  if (c->mode != GBV_RENDER_PERSISTENT && c->mode != GBV_RENDER_WAVEFRONT) return false;
+  if (c->reserved[0] || c->reserved[1]) return false;
+  lc.mode = c->mode;
   if (c->blocks_per_sm) lc.occ = c->blocks_per_sm;
   lc.stage = c->stage;
   if (c->threshold_pct) p.threshold = c->threshold_pct;
+  else if (c->mode == GBV_RENDER_WAVEFRONT) p.threshold = 25;
   if (c->skip_cells) p.skip = c->skip_cells;
   p.profile = c->profile;
   return true;
@@ -163,7 +166,7 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   RenderParams p;
   LaunchChoice lc;
   if (!resolve_config(config, p, lc)) {
-    snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..2)",
+    snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..2, mode 0..1)",
              fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }

@@ -1195,6 +1195,7 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
 struct LaunchChoice {
   int occ = 4;
   int stage = GBV_STAGE_DEFAULT;
+  int mode = GBV_RENDER_PERSISTENT;
 };
 
 // Shared-memory staging (same results either way).  GBV_STAGE_DEFAULT: the
@@ -1206,10 +1207,9 @@ struct LaunchChoice {
 // and the per-row pivots of cdf_x (up to 64 KB per block; measured slower:
 // the shared memory comes out of L1, which spills and CDF loads use).
 // GBV_STAGE_NONE stages nothing.
-template <class Store>
-inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream, const LaunchChoice &lc) {
+inline void plan_staging(RenderParams &p, int stage) {
   const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
-  const bool any = lc.stage != GBV_STAGE_NONE, all = lc.stage == GBV_STAGE_ALL;
+  const bool any = stage != GBV_STAGE_NONE, all = stage == GBV_STAGE_ALL;
   const int budget = (all ? 64 : 8) * 1024 / 4;
   int used = 0;
   p.maskWords = 0;
@@ -1236,6 +1236,11 @@ inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t
       used += p.env.H * per;
     }
   }
+}
+
+template <class Store>
+inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream, const LaunchChoice &lc) {
+  plan_staging(p, lc.stage);
   if (!p.counters) p.profile = 0;
   if (lc.occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
   if (lc.occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
@@ -1323,18 +1328,6 @@ inline gbv_status batch_launch(const gbv_batch *b, RenderParams L, cudaStream_t 
 #undef GBV_BATCH_LAUNCH
   return check_launch("render_kernel (batch)");
 }
-
-// The launchers of one voxel store, defined in render_store_*.cu
-#define GBV_STORE_LAUNCHERS(NAME, STORE)                                                        \
-  gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s, const LaunchChoice &lc) { \
-    return launch_render(p, STORE{}, s, lc);                                                    \
-  }                                                                                             \
-  gbv_status render_launch_noalloc_##NAME(const RenderParams &p, cudaStream_t s, int *pool) {   \
-    return launch_render_noalloc(p, STORE{}, s, pool);                                          \
-  }                                                                                             \
-  gbv_status batch_launch_##NAME(const gbv_batch *b, const RenderParams &L, cudaStream_t s) {   \
-    return batch_launch<STORE>(b, L, s);                                                        \
-  }
 
 #define GBV_DECLARE_STORE_LAUNCHERS(NAME)                                                        \
   gbv_status render_launch_##NAME(const RenderParams &p, cudaStream_t s, const LaunchChoice &lc); \

@@ -232,15 +232,24 @@ gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
      GBV_STAGE_NONE, or GBV_STAGE_ALL (also the env map's CDF tables, up to
      64 KB per block).
    profile: 1 = per-phase cycle and lane counts into d_counters[5..11]
-     (needs d_counters). */
+     (needs d_counters; persistent mode only).
+   mode: GBV_RENDER_PERSISTENT (one persistent kernel renders every pass)
+     or GBV_RENDER_WAVEFRONT (per step, a trace kernel over a queue of rays
+     and a shade kernel over the active pixels, with the path state in HBM;
+     scratch of about 200 bytes per pixel from the stream's memory pool).
+     In wavefront mode threshold_pct is the share of a trace warp's lanes
+     that must be idle before it takes new rays (default 25) and
+     blocks_per_sm is ignored. */
 enum { GBV_STAGE_DEFAULT = 0, GBV_STAGE_NONE = 1, GBV_STAGE_ALL = 2 };
+enum { GBV_RENDER_PERSISTENT = 0, GBV_RENDER_WAVEFRONT = 1 };
 typedef struct gbv_render_config {
   int blocks_per_sm;
   int threshold_pct;
   int skip_cells;
   int stage;
   int profile;
-  int reserved[3]; /* zero */
+  int mode;
+  int reserved[2]; /* zero */
 } gbv_render_config;
 
 /* gbv_render with explicit launch settings (config may be null).  No
