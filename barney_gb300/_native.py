@@ -42,7 +42,7 @@ class GbvScene(C.Structure):
     ]
 
 
-GBV_STAGE_DEFAULT, GBV_STAGE_NONE, GBV_STAGE_ALL = 0, 1, 2
+GBV_STAGE_DEFAULT, GBV_STAGE_NONE, GBV_STAGE_ALL, GBV_STAGE_BALLOT = 0, 1, 2, 3
 GBV_RENDER_PERSISTENT, GBV_RENDER_WAVEFRONT = 0, 1
 
 

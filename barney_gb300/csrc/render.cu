@@ -125,7 +125,7 @@ static bool resolve_config(const gbv_render_config *c, RenderParams &p, LaunchCh
   if (c->blocks_per_sm != 0 && (c->blocks_per_sm < 4 || c->blocks_per_sm > 6)) return false;
   if (c->threshold_pct < 0 || c->threshold_pct > 100) return false;
   if (c->skip_cells < 0 || c->skip_cells > 1024) return false;
-  if (c->stage < GBV_STAGE_DEFAULT || c->stage > GBV_STAGE_ALL) return false;
+  if (c->stage < GBV_STAGE_DEFAULT || c->stage > GBV_STAGE_BALLOT) return false;
   if (c->profile != 0 && c->profile != 1) return false;
   if (c->mode != GBV_RENDER_PERSISTENT && c->mode != GBV_RENDER_WAVEFRONT) return false;
   if (c->reserved[0] || c->reserved[1]) return false;
@@ -166,7 +166,7 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   RenderParams p;
   LaunchChoice lc;
   if (!resolve_config(config, p, lc)) {
-    snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..2, mode 0..1)",
+    snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..3, mode 0..1)",
              fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }

@@ -54,12 +54,14 @@ struct RenderParams {
   int skip;       // empty macrocells crossed per traversal step
   int threshold;  // keep traversing while at least this % of busy lanes trace
   // shared-memory staging (offsets in 32-bit words of the dynamic smem)
-  int maskWords;  // >0: bitmask of non-zero majorants staged at offset 0
+  int maskWords;  // >0: bitmask of non-zero majorants staged at offset 0 (a multiple of 4 words)
+  const uint32_t *maskSrc;  // the bitmask in HBM (16-byte aligned), staged by one bulk copy; null: by ballots
   int cdfYOff;    // >=0: env cdf_y staged here
   int pivOff;     // >=0: per-row pivots of cdf_x staged here
   int pivPerRow;
   int rowOff;     // >=0: per env-map row (pdf_y, pdf denominator) staged here
   int profile;    // accumulate per-phase cycle counts
+  int maskMode;   // 0: the staged bitmask arrives by one bulk copy of a precomputed mask; 1: by ballots
   // voxel store of this scene (see make_store)
   const void *vox;
   const float2 *so;
@@ -102,6 +104,70 @@ GBV_BRICK_STORE(GBV_VOXEL_U8_SCALED)
 
 // Dynamic shared memory of the render kernel (layout in RenderParams).
 extern __shared__ uint32_t g_smem[];
+
+// One warp per 32 macrocells: bit k of word w is set when macrocell
+// 32 w + k has a non-zero majorant (words up to `words`, zero-padded).
+static __global__ void __launch_bounds__(256) majorant_mask_kernel(const float *__restrict__ maj, int nmc, int words,
+                                                            uint32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < words;
+       w += (int)((gridDim.x * blockDim.x) >> 5)) {
+    const int i = w * 32 + lane;
+    const float m = i < nmc ? __ldg(maj + i) : 0.f;
+    const unsigned b = __ballot_sync(0xffffffffu, m != 0.f);
+    if (lane == 0) out[w] = b;
+  }
+}
+
+// Stages the bitmask of non-zero majorants in shared-memory words
+// [0, p.maskWords).  With the precomputed mask in HBM (p.maskSrc) one thread
+// issues one bulk copy (cp.async.bulk global -> shared, completion counted
+// in bytes on an mbarrier) and every thread waits on the barrier; the wait
+// is bounded, and a copy that has not completed in time (which no working
+// GPU produces) sets *capFlag and the block builds the mask from the
+// majorants with warp ballots instead (the same bits).  Without a
+// precomputed mask the warps build it that way directly.  Every thread of
+// the block calls this.
+__device__ __forceinline__ void stage_majorant_mask(const RenderParams &p) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  bool staged = false;
+  if (p.maskSrc) {
+    __shared__ __align__(8) unsigned long long mbar;
+    const unsigned mb = (unsigned)__cvta_generic_to_shared(&mbar);
+    const unsigned bytes = (unsigned)p.maskWords * 4u;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              (unsigned)__cvta_generic_to_shared(g_smem)),
+          "l"(p.maskSrc), "r"(bytes), "r"(mb)
+          : "memory");
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    unsigned done = 0;
+    for (int it = 0; it < (1 << 20) && !done; it++)
+      asm volatile(
+          "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], 0;\n selp.u32 %0, 1, 0, P;\n}"
+          : "=r"(done)
+          : "r"(mb)
+          : "memory");
+    staged = __syncthreads_and(done != 0) != 0;
+    if (!staged && threadIdx.x == 0 && p.capFlag) *p.capFlag = 1;
+  }
+  if (!staged) {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
+    for (int w = warp; w < p.maskWords; w += nwarps) {
+      const int i = w * 32 + lane;
+      const float m = i < nmc ? __ldg(p.G.maj + i) : 0.f;
+      const unsigned b = __ballot_sync(FULL, m != 0.f);
+      if (lane == 0) g_smem[w] = b;
+    }
+  }
+}
 
 struct LightSample {
   vec3 radiance, direction;
@@ -871,14 +937,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
   // ---- stage the majorant bitmask and env-map tables in shared memory ----
   if (!Batch) {
     const RenderParams &p = p0;
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
-    for (int w = warp; w < p.maskWords; w += nwarps) {
-      const int i = w * 32 + lane;
-      const float m = i < nmc ? __ldg(p.G.maj + i) : 0.f;
-      const unsigned b = __ballot_sync(FULL, m != 0.f);
-      if (lane == 0) g_smem[w] = b;
-    }
+    if (p.maskWords > 0) stage_majorant_mask(p);
     if (p.cdfYOff >= 0)
       for (int i = threadIdx.x; i < p.env.H; i += blockDim.x) g_smem[p.cdfYOff + i] = __float_as_uint(__ldg(p.env.cdf_y + i));
     if (p.pivOff >= 0) {
@@ -1169,17 +1228,28 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   const long long needed = (tiles + warpsPerBlock - 1) / warpsPerBlock;
   if (blocks > needed) blocks = needed;
   if (blocks < 1) blocks = 1;
-  // the tile pool counter lives in stream-ordered scratch memory
+  // the tile pool counter and the majorant bitmask live in stream-ordered
+  // scratch memory (the mask at a 256-byte offset: 16-byte aligned for the
+  // bulk copy)
   int *pool = nullptr;
-  st = check_cuda(cudaMallocAsync((void **)&pool, sizeof(int), stream), "cudaMallocAsync(tile pool)");
+  const size_t maskBytes = (size_t)p.maskWords * 4;
+  st = check_cuda(cudaMallocAsync((void **)&pool, 256 + maskBytes, stream), "cudaMallocAsync(tile pool)");
   if (st != GBV_OK) return st;
   st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "render_kernel: clearing the tile pool");
+  RenderParams q = p;
+  if (st == GBV_OK && p.maskWords > 0 && p.maskSrc == nullptr && p.maskMode == 0) {
+    uint32_t *mask = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(pool) + 256);
+    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
+    majorant_mask_kernel<<<(unsigned)((p.maskWords + 7) / 8), 256, 0, stream>>>(p.G.maj, nmc, p.maskWords, mask);
+    st = check_launch("majorant_mask_kernel");
+    q.maskSrc = mask;
+  }
   if (st == GBV_OK) {
     if (p.counters)
-      render_kernel<Store, MinBlocks, false, true><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr,
+      render_kernel<Store, MinBlocks, false, true><<<(unsigned)blocks, kThreads, smem, stream>>>(q, nullptr, nullptr,
                                                                                                  0, pool);
     else
-      render_kernel<Store, MinBlocks, false, false><<<(unsigned)blocks, kThreads, smem, stream>>>(p, nullptr, nullptr,
+      render_kernel<Store, MinBlocks, false, false><<<(unsigned)blocks, kThreads, smem, stream>>>(q, nullptr, nullptr,
                                                                                                   0, pool);
     st = check_launch("render_kernel");
   }
@@ -1210,13 +1280,15 @@ struct LaunchChoice {
 inline void plan_staging(RenderParams &p, int stage) {
   const long long nmc = (long long)p.G.M[0] * p.G.M[1] * p.G.M[2];
   const bool any = stage != GBV_STAGE_NONE, all = stage == GBV_STAGE_ALL;
+  p.maskMode = stage == GBV_STAGE_BALLOT ? 1 : 0;
   const int budget = (all ? 64 : 8) * 1024 / 4;
   int used = 0;
   p.maskWords = 0;
   p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
-  if (any && nmc > 0 && (nmc + 31) / 32 <= budget) {
-    p.maskWords = (int)((nmc + 31) / 32);
+  p.maskSrc = nullptr;
+  if (any && nmc > 0 && (((nmc + 31) / 32 + 3) & ~3ll) <= budget) {
+    p.maskWords = (int)(((nmc + 31) / 32 + 3) & ~3ll);  // whole 16-byte units (one bulk copy)
     used = p.maskWords;
   }
   if (any && p.hasEnv && p.env.H >= 1 && p.env.H <= 1024) {

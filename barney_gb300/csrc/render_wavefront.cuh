@@ -146,14 +146,7 @@ __global__ void __launch_bounds__(256, 4) wf_trace_kernel(const __grid_constant_
   if (p.maskWords > 0) {
     // the bitmask of non-zero majorants in shared memory (as the persistent
     // kernel stages it)
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
-    for (int w = warp; w < p.maskWords; w += nwarps) {
-      const int i = w * 32 + lane;
-      const float m = i < nmc ? __ldg(p.G.maj + i) : 0.f;
-      const unsigned b = __ballot_sync(FULL, m != 0.f);
-      if (lane == 0) g_smem[w] = b;
-    }
+    stage_majorant_mask(p);
     __syncthreads();
   }
   const Store store = make_store<Store>(p);
@@ -371,7 +364,7 @@ inline gbv_status launch_wavefront(RenderParams p, const Store &, cudaStream_t s
   const size_t n = (size_t)nslots;
   const size_t bytes = n * (2 * sizeof(WfRay) + sizeof(WfMeta) + 2 * sizeof(float4) + 4 * 2 * sizeof(int) +
                             2 * sizeof(int)) +
-                       (size_t)(maxSteps + 1) * sizeof(WfStep) + 1024;
+                       (size_t)(maxSteps + 1) * sizeof(WfStep) + (size_t)p.maskWords * 4 + 4096;
   char *mem = nullptr;
   st = check_cuda(cudaMallocAsync((void **)&mem, bytes, stream), "cudaMallocAsync(wavefront state)");
   if (st != GBV_OK) return st;
@@ -391,12 +384,19 @@ inline gbv_status launch_wavefront(RenderParams p, const Store &, cudaStream_t s
   B.active[0] = reinterpret_cast<int *>(take(n * sizeof(int)));
   B.active[1] = reinterpret_cast<int *>(take(n * sizeof(int)));
   B.steps = reinterpret_cast<WfStep *>(take((size_t)(maxSteps + 1) * sizeof(WfStep)));
+  uint32_t *mask = reinterpret_cast<uint32_t *>(take((size_t)p.maskWords * 4 + 16));
   if (off > bytes) st = set_error(GBV_ERROR_INVALID_ARGUMENT, "wavefront render: scratch layout");
   if (st == GBV_OK)
     st = check_cuda(cudaMemsetAsync(B.steps, 0, (size_t)(maxSteps + 1) * sizeof(WfStep), stream),
                     "wavefront render: clearing the step counters");
   const unsigned gridTrace = (unsigned)(sms * (perSmTrace > 0 ? perSmTrace : 1));
   const unsigned gridShade = (unsigned)(sms * (perSmShade > 0 ? perSmShade : 1));
+  if (st == GBV_OK && p.maskWords > 0 && p.maskMode == 0) {
+    const int nmc = p.G.M[0] * p.G.M[1] * p.G.M[2];
+    majorant_mask_kernel<<<(unsigned)((p.maskWords + 7) / 8), 256, 0, stream>>>(p.G.maj, nmc, p.maskWords, mask);
+    st = check_launch("majorant_mask_kernel");
+    p.maskSrc = mask;
+  }
   if (st == GBV_OK) {
     wf_init_kernel<<<gridShade, 256, 0, stream>>>(p, B);
     st = check_launch("wf_init_kernel");

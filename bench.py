@@ -236,6 +236,15 @@ def ea_steps(scene, view, step):
     return int(n.sum())
 
 
+def _bias(d):
+    """Mean signed error over the crop and its standard error from the
+    per-row means (rows as independent batches): a storage format that
+    shifts the image shows a bias several sigma from zero, while path
+    divergence (a flipped decision changes the rest of a path) averages out."""
+    per_row = d.reshape(d.shape[0], -1).mean(axis=1)
+    return {"bias_vs_fp64": float(d.mean()), "bias_sigma": float(per_row.std(ddof=1) / math.sqrt(per_row.size))}
+
+
 def precision_study(scene, g32, rows=(523, 557), reps=2):
     """Voxel storage precision, two ways.
 
@@ -251,7 +260,10 @@ def precision_study(scene, g32, rows=(523, 557), reps=2):
     grid, so every pixel draws the same random numbers; still, a decision
     that flips between precisions changes the rest of that path, so these
     errors are dominated by path divergence: `oracle_fp32_vs_fp64` is that
-    floor for the FP32 arithmetic itself."""
+    floor for the FP32 arithmetic itself.  Two figures separate the storage
+    from that floor: `rmse_vs_f32` (the same store layout and streams, FP32
+    voxels against the format's) and `bias_vs_fp64` with `bias_sigma` (the
+    mean signed error over the crop and its standard error)."""
     import torch
     import oracle
     from barney_gb300 import _native as N
@@ -306,8 +318,8 @@ def precision_study(scene, g32, rows=(523, 557), reps=2):
     dt = out["delta_tracking"]
     dt.update({"crop": f"rows {rows[0]}-{rows[1]} x {W} columns ({(rows[1] - rows[0]) * W} pixels), {spp} spp",
                "majorants": "FP32 source majorant grid for every format", "oracle_fp64_s": t64,
-               "oracle_fp32_vs_fp64": {"rmse": float(np.sqrt(np.mean((ref32 - ref64) ** 2))),
-                                       "max_err": float(np.abs(ref32 - ref64).max())},
+               "oracle_fp32_vs_fp64": dict({"rmse": float(np.sqrt(np.mean((ref32 - ref64) ** 2))),
+                                            "max_err": float(np.abs(ref32 - ref64).max())}, **_bias(ref32 - ref64)),
                "formats": {}})
     cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
     img32 = None
@@ -332,10 +344,13 @@ def precision_study(scene, g32, rows=(523, 557), reps=2):
         d = img - ref64
         rec = {"Msamples_s": samples / (ms / 1e3) / 1e6, "frame_ms": ms, "store_GB": g.voxels.numel() / 1e9,
                "rmse_vs_fp64": float(np.sqrt(np.mean(d ** 2))), "max_err_vs_fp64": float(np.abs(d).max())}
+        rec.update(_bias(d))
         if img32 is None:
             img32 = full
         else:
             rec["pixels_identical_to_f32"] = float(np.mean(np.all(full == img32, axis=-1)))
+            d32 = img - img32[rows[0]:rows[1], :, :3] / spp
+            rec["rmse_vs_f32"] = float(np.sqrt(np.mean(d32 ** 2)))
         dt["formats"][name] = rec
         if fmt != 0:
             del g

@@ -228,9 +228,11 @@ gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
    skip_cells: cell tests and Woodcock distance draws a lane makes per
      traversal iteration before the warp samples (1..1024, default 6).
    stage: shared-memory staging, GBV_STAGE_DEFAULT (the bitmask of non-zero
-     majorants, at most 8 KB, and the env map's per-row pdf terms),
-     GBV_STAGE_NONE, or GBV_STAGE_ALL (also the env map's CDF tables, up to
-     64 KB per block).
+     majorants, at most 8 KB, computed once per launch in HBM and copied to
+     each block by one bulk copy, and the env map's per-row pdf terms),
+     GBV_STAGE_NONE, GBV_STAGE_ALL (also the env map's CDF tables, up to
+     64 KB per block) or GBV_STAGE_BALLOT (the default staging, with each
+     block building the bitmask from the majorants by warp ballots).
    profile: 1 = per-phase cycle and lane counts into d_counters[5..11]
      (needs d_counters; persistent mode only).
    mode: GBV_RENDER_PERSISTENT (one persistent kernel renders every pass)
@@ -240,7 +242,7 @@ gbv_status gbv_render(const gbv_scene *scene, float *d_accum, int width,
      In wavefront mode threshold_pct is the share of a trace warp's lanes
      that must be idle before it takes new rays (default 25) and
      blocks_per_sm is ignored. */
-enum { GBV_STAGE_DEFAULT = 0, GBV_STAGE_NONE = 1, GBV_STAGE_ALL = 2 };
+enum { GBV_STAGE_DEFAULT = 0, GBV_STAGE_NONE = 1, GBV_STAGE_ALL = 2, GBV_STAGE_BALLOT = 3 };
 enum { GBV_RENDER_PERSISTENT = 0, GBV_RENDER_WAVEFRONT = 1 };
 typedef struct gbv_render_config {
   int blocks_per_sm;

@@ -269,10 +269,11 @@ def test_rmse_falls_as_inverse_sqrt_spp(cuda):
     assert ro < 1.5 * rmse[16], (ro, rmse)
 
 
-@pytest.mark.parametrize("stage", [N.GBV_STAGE_DEFAULT, N.GBV_STAGE_ALL])
+@pytest.mark.parametrize("stage", [N.GBV_STAGE_DEFAULT, N.GBV_STAGE_ALL, N.GBV_STAGE_BALLOT])
 def test_shared_memory_staging_is_transparent(cuda, stage):
-    """Staging the majorant bitmask (GBV_STAGE_DEFAULT) and also the env-map
-    CDF pivots (GBV_STAGE_ALL) in shared memory gives the same frame, bit
+    """Staging the majorant bitmask (GBV_STAGE_DEFAULT: one bulk copy of the
+    mask per block; GBV_STAGE_BALLOT: built by each block's warps) and also
+    the env-map CDF pivots (GBV_STAGE_ALL) in shared memory gives the same frame, bit
     for bit, as reading them from global memory (GBV_STAGE_NONE; the pivot
     search returns the reference binary search's index)."""
     import torch

@@ -243,7 +243,7 @@ def test_render_config_checked_before_the_device():
     rec.dims[:] = (8, 8, 8)
     acc = C.c_void_p(16)
     bad = [dict(blocks_per_sm=3), dict(blocks_per_sm=7), dict(threshold_pct=101), dict(threshold_pct=-1),
-           dict(skip_cells=1025), dict(stage=3), dict(profile=2), dict(mode=2)]
+           dict(skip_cells=1025), dict(stage=4), dict(profile=2), dict(mode=2)]
     for kw in bad:
         cfg = N.render_config(**kw)
         assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(cfg), None) == 1, kw
