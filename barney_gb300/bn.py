@@ -8,6 +8,7 @@ camera, a renderer and a frame buffer, then bnRender and bnFrameBufferRead.
 from __future__ import annotations
 
 import ctypes as C
+from typing import Optional
 
 import numpy as np
 
@@ -131,17 +132,35 @@ class BarneySession:
 
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
                     layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None,
-                    texel_format: int = BN_FLOAT32, frame_stats: bool = False):
+                    texel_format: int = BN_FLOAT32, frame_stats: bool = False, anari: Optional[str] = None):
+        """anari: None (bn* calls as an app makes them), "vec4" or
+        "vec3+opacity": the field and the transfer function made through the
+        ANARI parameter translation (include/gbv_anari.h) from the
+        structuredRegular data and a transferFunction1D whose colors are the
+        scene TF's RGBA (or RGB with its alpha as the opacity array) and whose
+        unitDistance is 1 / base density."""
         L, ctx, s = self.L, self.ctx, scene
         nx, ny, nz = s.dims
-        td = _ok(L.bnTextureData3DCreate(ctx, 0, texel_format, nx, ny, nz, C.c_void_p(scalars_ptr)),
-                 "bnTextureData3DCreate")
-        sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"structured"), "bnScalarFieldCreate")
-        L.bnSetObject(sf, b"textureData", td)
-        L.bnSet3i(sf, b"dims", nx, ny, nz)
         origin, spacing = s.geometry()
-        L.bnSet3f(sf, b"gridOrigin", *origin)
-        L.bnSet3f(sf, b"gridSpacing", *spacing)
+        td = None
+        if anari is None:
+            td = _ok(L.bnTextureData3DCreate(ctx, 0, texel_format, nx, ny, nz, C.c_void_p(scalars_ptr)),
+                     "bnTextureData3DCreate")
+            sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"structured"), "bnScalarFieldCreate")
+            L.bnSetObject(sf, b"textureData", td)
+            L.bnSet3i(sf, b"dims", nx, ny, nz)
+            L.bnSet3f(sf, b"gridOrigin", *origin)
+            L.bnSet3f(sf, b"gridSpacing", *spacing)
+        else:
+            from . import anari as A
+            A.lib()
+            h = C.c_void_p(0)
+            et = {BN_FLOAT32: A.GBV_ANARI_FLOAT32, BN_UFIXED8: A.GBV_ANARI_UFIXED8}[texel_format]
+            N.check(L.gbv_anari_structured_regular(ctx, 0, et, C.c_void_p(scalars_ptr),
+                                                   N.ivec(nx, ny, nz), (C.c_float * 3)(*origin),
+                                                   (C.c_float * 3)(*spacing), C.byref(h)),
+                    "gbv_anari_structured_regular")
+            sf = h.value
         L.bnSet1i(sf, b"cellsPerMacrocell", s.cells_per_mc)
         L.bnSet1i(sf, b"voxelFormat", voxel_format)
         L.bnSet1i(sf, b"voxelLayout", layout)
@@ -151,7 +170,20 @@ class BarneySession:
         vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
         tf = np.ascontiguousarray(s.tf, np.float32)
         self.keep.append(tf)
-        L.bnVolumeSetXF(vol, BnFloat2(*s.domain), tf.ctypes.data_as(C.c_void_p), tf.shape[0], s.base_density)
+        if anari is None:
+            L.bnVolumeSetXF(vol, BnFloat2(*s.domain), tf.ctypes.data_as(C.c_void_p), tf.shape[0], s.base_density)
+        else:
+            from . import anari as A
+            rng = np.asarray(s.domain, np.float32)
+            if anari == "vec4":
+                col, ch, op = tf, 4, None
+            else:
+                col, ch, op = np.ascontiguousarray(tf[:, :3]), 3, np.ascontiguousarray(tf[:, 3])
+            self.keep += [col, op, rng]
+            N.check(L.gbv_anari_transfer_function_1d(vol, A._p(col), ch, col.shape[0], A._p(op),
+                                                     0 if op is None else op.shape[0], None, 1.0, A._p(rng),
+                                                     float(np.float32(1.0) / np.float32(s.base_density)), 7),
+                    "gbv_anari_transfer_function_1d")
         L.bnSet1f(vol, b"anisotropy", s.anisotropy)
         L.bnSet1f(vol, b"scatteringAlbedo", s.scattering_albedo)
         L.bnCommit(vol)
@@ -206,6 +238,8 @@ class BarneySession:
         fb = _ok(L.bnFrameBufferCreate(ctx, 0), "bnFrameBufferCreate")
         L.bnFrameBufferResize(fb, color_format, s.width, s.height, BN_FB_COLOR)
         self.handles = dict(td=td, sf=sf, vol=vol, grp=grp, model=model, cam=cam, renderer=r, fb=fb)
+        if td is None:
+            del self.handles["td"]
         self.scene, self.color_format = s, color_format
         err = last_error()
         return err
@@ -230,5 +264,6 @@ class BarneySession:
 
     def release_scene(self):
         for k in ("fb", "renderer", "cam", "model", "grp", "vol", "sf", "td"):
-            self.L.bnRelease(self.handles[k])
+            if k in self.handles:
+                self.L.bnRelease(self.handles[k])
         self.handles = {}

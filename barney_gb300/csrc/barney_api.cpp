@@ -253,9 +253,14 @@ struct Volume : Object {  // volume/Volume.{h,cpp}, TransferFunction
   bool tfDirty = true;
   DevBuf<float> tf;
   DevBuf<float> majorants;
+  int userID = 0;  // Volume::set1i("userID"); used by hit-ID channels, which this path has none of
   bool set1f(const std::string &m, float v) override {
     if (m == "anisotropy") { anisotropy = v; return true; }
     if (m == "scatteringAlbedo") { scatteringAlbedo = v; return true; }
+    return false;
+  }
+  bool set1i(const std::string &m, int v) override {
+    if (m == "userID") { userID = v; return true; }
     return false;
   }
   bool build(cudaStream_t s) {
