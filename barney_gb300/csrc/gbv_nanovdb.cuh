@@ -1,0 +1,139 @@
+// gbv_nanovdb.cuh -- NanoVDB float grids on the structured-volume path:
+// value lookup in a grid buffer, the reference's NanoVDB sampler and its
+// macrocell footprint.
+//
+// The grid buffer is one NanoVDB grid of value type Float in the NanoVDB
+// memory layout of format version 32 (the layout nanovdb::GridHandle holds
+// and nanovdb::io writes): a 672-byte grid header, a 64-byte tree header,
+// then the nodes -- a root of 32-byte tiles keyed by the coordinates of
+// their 4096^3 region, upper internal nodes of 32^3 entries, lower internal
+// nodes of 16^3 entries and 8^3-voxel leaves.  An internal entry whose
+// child-mask bit is set holds the signed byte offset of its child node,
+// otherwise a tile value; child offsets are relative to the parent node (to
+// the root node for the root's tiles).  The byte offsets below are those of
+// that layout for float values; the pin tests check them against the NanoVDB
+// headers the reference vendors (3rdParty/nanovdb, version 32.7).
+#pragma once
+#include <stdint.h>
+#include "gbv_math.cuh"
+
+namespace gbv {
+
+constexpr uint64_t kNvdbMagic0 = 0x304244566f6e614eull;  // "NanoVDB0"
+constexpr uint64_t kNvdbMagic1 = 0x314244566f6e614eull;  // "NanoVDB1"
+constexpr uint32_t kNvdbGridTypeFloat = 1;
+// grid header
+constexpr size_t kNvdbGridVersion = 16, kNvdbGridSize = 32, kNvdbGridInvMatF = 332, kNvdbGridVecF = 368;
+constexpr size_t kNvdbGridWorldBBox = 560, kNvdbGridVoxelSize = 608, kNvdbGridType = 636;
+constexpr size_t kNvdbGridHeader = 672;
+// tree header (after the grid header): byte offset of the root node
+constexpr size_t kNvdbTreeRootOffset = 24;
+// root node: index bbox, table size, background; tiles after 64 bytes
+constexpr size_t kNvdbRootTableSize = 24, kNvdbRootBackground = 28, kNvdbRootTiles = 64, kNvdbRootTile = 32;
+constexpr size_t kNvdbTileChild = 8, kNvdbTileValue = 20;
+// internal nodes: child mask and the table of values / child offsets
+constexpr size_t kNvdbUpperChildMask = 32 + 4096, kNvdbUpperTable = 8256;
+constexpr size_t kNvdbLowerChildMask = 32 + 512, kNvdbLowerTable = 1088;
+// leaves: the 512 values
+constexpr size_t kNvdbLeafValues = 96;
+
+// A parsed grid (host-side header fields, device pointer to the buffer).
+struct NvdbGrid {
+  const unsigned char *base;  // the grid buffer (device memory for kernels)
+  long long root;             // byte offset of the root node from base
+  uint32_t tiles;             // root table size
+  float background;
+  float invMatF[9], vecF[3];  // world -> index map, single precision
+  int lo[3], hi[3];           // index bbox of the active values
+};
+
+template <typename T> GBV_HD T nvdb_ld(const unsigned char *p) {
+#if defined(__CUDA_ARCH__)
+  return *reinterpret_cast<const T *>(p);
+#else
+  T v;
+  __builtin_memcpy(&v, p, sizeof(T));
+  return v;
+#endif
+}
+
+// ReadAccessor::getValue: the value at index coordinates (x, y, z) --
+// an active or inactive voxel, a tile value, or the background.
+GBV_HD float nvdb_value(const NvdbGrid &g, int x, int y, int z) {
+  const unsigned char *root = g.base + g.root;
+  const uint64_t key = (uint64_t)((uint32_t)z >> 12) | ((uint64_t)((uint32_t)y >> 12) << 21) |
+                       ((uint64_t)((uint32_t)x >> 12) << 42);
+  const unsigned char *tile = nullptr;
+  for (uint32_t i = 0; i < g.tiles; i++) {
+    const unsigned char *t = root + kNvdbRootTiles + (size_t)kNvdbRootTile * i;
+    if (nvdb_ld<uint64_t>(t) == key) {
+      tile = t;
+      break;
+    }
+  }
+  if (!tile) return g.background;
+  const long long child = nvdb_ld<long long>(tile + kNvdbTileChild);
+  if (child == 0) return nvdb_ld<float>(tile + kNvdbTileValue);
+  const unsigned char *up = root + child;
+  uint32_t n = (((uint32_t)x & 4095u) >> 7 << 10) | (((uint32_t)y & 4095u) >> 7 << 5) | (((uint32_t)z & 4095u) >> 7);
+  if (!((nvdb_ld<uint64_t>(up + kNvdbUpperChildMask + 8 * (n >> 6)) >> (n & 63)) & 1ull))
+    return nvdb_ld<float>(up + kNvdbUpperTable + 8 * (size_t)n);
+  const unsigned char *lw = up + nvdb_ld<long long>(up + kNvdbUpperTable + 8 * (size_t)n);
+  n = (((uint32_t)x & 127u) >> 3 << 8) | (((uint32_t)y & 127u) >> 3 << 4) | (((uint32_t)z & 127u) >> 3);
+  if (!((nvdb_ld<uint64_t>(lw + kNvdbLowerChildMask + 8 * (n >> 6)) >> (n & 63)) & 1ull))
+    return nvdb_ld<float>(lw + kNvdbLowerTable + 8 * (size_t)n);
+  const unsigned char *lf = lw + nvdb_ld<long long>(lw + kNvdbLowerTable + 8 * (size_t)n);
+  n = (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
+  return nvdb_ld<float>(lf + kNvdbLeafValues + 4 * (size_t)n);
+}
+
+// NanoVDBDataSampler::DD::sample (barney/volume/NanoVDB.h:100-129): world ->
+// index with the grid's single-precision inverse map (worldToIndexF: the
+// translation subtracted in double, the 3x3 product in float with fused
+// multiply-adds), shifted by -0.5 to voxel centres and clamped to the index
+// bbox, then the trilinear sampler (SampleFromVoxels<acc, 1>): the 8 values
+// at floor(x) + {0,1}^3 and lerp(a, b, w) = a + float(w) * (b - a) along z,
+// then y, then x.  Never NaN: points outside take the border values.
+GBV_HD float nvdb_sample(const NvdbGrid &g, float px, float py, float pz) {
+  const double dx = (double)px - (double)g.vecF[0], dy = (double)py - (double)g.vecF[1],
+               dz = (double)pz - (double)g.vecF[2];
+  const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+  const float *m = g.invMatF;
+  double ix = (double)fmaf(fx, m[0], fmaf(fy, m[1], fz * m[2]));
+  double iy = (double)fmaf(fx, m[3], fmaf(fy, m[4], fz * m[5]));
+  double iz = (double)fmaf(fx, m[6], fmaf(fy, m[7], fz * m[8]));
+  ix -= 0.5;
+  iy -= 0.5;
+  iz -= 0.5;
+  // nanovdb::math::Clamp(x, a, b) = fmax(fmin(x, b), a)
+  auto clampd = [](double x, double a, double b) { return fmax(fmin(x, b), a); };
+  ix = clampd(ix, (double)g.lo[0], (double)g.hi[0]);
+  iy = clampd(iy, (double)g.lo[1], (double)g.hi[1]);
+  iz = clampd(iz, (double)g.lo[2], (double)g.hi[2]);
+  const int i = (int)floor(ix), j = (int)floor(iy), k = (int)floor(iz);
+  const double u = ix - (double)i, v = iy - (double)j, w = iz - (double)k;
+  float s[2][2][2];
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int c = 0; c < 2; c++) s[a][b][c] = nvdb_value(g, i + a, j + b, k + c);
+  const float fu = (float)u, fv = (float)v, fw = (float)w;
+  auto lerp = [](float p, float q, float t) { return p + t * (q - p); };
+  return lerp(lerp(lerp(s[0][0][0], s[0][0][1], fw), lerp(s[0][1][0], s[0][1][1], fw), fv),
+              lerp(lerp(s[1][0][0], s[1][0][1], fw), lerp(s[1][1][0], s[1][1][1], fw), fv), fu);
+}
+
+// The index footprint of macrocell (mx, my, mz) of a grid of mc[3]
+// macrocells over an index bbox of size[3] voxels starting at lo[3]
+// (NanoVDBData_computeMCs, barney/volume/NanoVDB.cu:28-60): from
+// lo + (m * size) / mc to lo + ((m + 1) * size) / mc + 1, both inclusive.
+GBV_HD void nvdb_mc_footprint(const int lo[3], const int size[3], const int mc[3], int m[3], int a[3], int b[3]) {
+  for (int t = 0; t < 3; t++) {
+    a[t] = lo[t] + (m[t] * size[t]) / mc[t];
+    b[t] = lo[t] + ((m[t] + 1) * size[t]) / mc[t] + 1;
+  }
+}
+
+}  // namespace gbv

@@ -1,0 +1,134 @@
+// nanovdb.cu -- NanoVDB float grids: header parsing (host), the macrocell
+// range build and a sampling entry point (device).
+#include <cmath>
+#include <cstring>
+#include <cuda_runtime.h>
+#include "gbv_nanovdb.cuh"
+#include "gbv_internal.h"
+
+namespace gbv {
+
+NvdbGrid make_nvdb_grid(const void *d_grid, const gbv_nanovdb_info &info) {
+  NvdbGrid g;
+  g.base = reinterpret_cast<const unsigned char *>(d_grid);
+  g.root = info.root_offset;
+  g.tiles = info.root_tiles;
+  g.background = info.background;
+  for (int i = 0; i < 9; i++) g.invMatF[i] = info.inv_map[i];
+  for (int i = 0; i < 3; i++) {
+    g.vecF[i] = info.map_offset[i];
+    g.lo[i] = info.index_lo[i];
+    g.hi[i] = info.index_hi[i];
+  }
+  return g;
+}
+
+// One thread per macrocell (NanoVDBData_computeMCs, NanoVDB.cu:28-60).
+__global__ void __launch_bounds__(128) nvdb_mc_ranges_kernel(NvdbGrid g, int mx, int my, int mz,
+                                                             float2 *__restrict__ ranges) {
+  const long long n = (long long)mx * my * mz;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= n) return;
+  int m[3] = {(int)(tid % mx), (int)((tid / mx) % my), (int)(tid / ((long long)mx * my))};
+  const int mc[3] = {mx, my, mz};
+  const int size[3] = {g.hi[0] - g.lo[0] + 1, g.hi[1] - g.lo[1] + 1, g.hi[2] - g.lo[2] + 1};
+  int a[3], b[3];
+  nvdb_mc_footprint(g.lo, size, mc, m, a, b);
+  // range1f starts empty (+inf, -inf) and extends by min/max
+  float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+  for (int x = a[0]; x <= b[0]; x++)
+    for (int y = a[1]; y <= b[1]; y++)
+      for (int z = a[2]; z <= b[2]; z++) {
+        const float v = nvdb_value(g, x, y, z);
+        lo = mn(lo, v);
+        hi = mx(hi, v);
+      }
+  ranges[tid] = make_float2(lo, hi);
+}
+
+__global__ void __launch_bounds__(128) nvdb_sample_kernel(NvdbGrid g, const float *__restrict__ P, long long n,
+                                                          float *__restrict__ out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = nvdb_sample(g, P[3 * i], P[3 * i + 1], P[3 * i + 2]);
+}
+
+static bool nvdb_info_ok(const gbv_nanovdb_info *info) {
+  if (!info) return false;
+  for (int i = 0; i < 3; i++)
+    if (info->index_hi[i] < info->index_lo[i] || info->mc_dims[i] <= 0) return false;
+  return info->root_offset > 0 && (unsigned long long)info->root_offset < info->bytes;
+}
+
+}  // namespace gbv
+
+using namespace gbv;
+
+extern "C" gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_nanovdb_info *info) {
+  if (!h_grid || !info) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: null pointer");
+  const unsigned char *b = reinterpret_cast<const unsigned char *>(h_grid);
+  if (bytes < kNvdbGridHeader + 64 + kNvdbRootTiles)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: buffer smaller than a grid header");
+  const uint64_t magic = nvdb_ld<uint64_t>(b);
+  if (magic != kNvdbMagic0 && magic != kNvdbMagic1)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: not a NanoVDB grid (magic number)");
+  const uint32_t version = nvdb_ld<uint32_t>(b + kNvdbGridVersion);
+  if ((version >> 21) != 32)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: NanoVDB format version other than 32");
+  if (nvdb_ld<uint32_t>(b + kNvdbGridType) != kNvdbGridTypeFloat)
+    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: only grids of value type Float are supported");
+  const uint64_t gridSize = nvdb_ld<uint64_t>(b + kNvdbGridSize);
+  if (gridSize > bytes) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: buffer shorter than the grid");
+  const long long rootRel = nvdb_ld<long long>(b + kNvdbGridHeader + kNvdbTreeRootOffset);
+  const long long root = (long long)kNvdbGridHeader + rootRel;
+  if (rootRel <= 0 || (unsigned long long)root + kNvdbRootTiles > gridSize)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: root node outside the grid");
+  gbv_nanovdb_info r;
+  std::memset(&r, 0, sizeof r);
+  r.bytes = gridSize;
+  r.root_offset = root;
+  r.root_tiles = nvdb_ld<uint32_t>(b + root + kNvdbRootTableSize);
+  if ((unsigned long long)root + kNvdbRootTiles + (unsigned long long)kNvdbRootTile * r.root_tiles > gridSize)
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: root table outside the grid");
+  r.background = nvdb_ld<float>(b + root + kNvdbRootBackground);
+  for (int i = 0; i < 9; i++) r.inv_map[i] = nvdb_ld<float>(b + kNvdbGridInvMatF + 4 * i);
+  for (int i = 0; i < 3; i++) {
+    r.map_offset[i] = nvdb_ld<float>(b + kNvdbGridVecF + 4 * i);
+    r.index_lo[i] = nvdb_ld<int>(b + root + 4 * i);
+    r.index_hi[i] = nvdb_ld<int>(b + root + 12 + 4 * i);
+    // NanoVDBData::commit: world bounds as floats
+    r.world_lo[i] = (float)nvdb_ld<double>(b + kNvdbGridWorldBBox + 8 * i);
+    r.world_hi[i] = (float)nvdb_ld<double>(b + kNvdbGridWorldBBox + 24 + 8 * i);
+    r.voxel_size[i] = nvdb_ld<double>(b + kNvdbGridVoxelSize + 8 * i);
+    if (r.index_hi[i] < r.index_lo[i])
+      return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: grid without active values");
+    // NanoVDBData::buildMCs: divRoundUp(gridSize, 16)
+    const long long size = (long long)r.index_hi[i] - r.index_lo[i] + 1;
+    if (size > (1ll << 24)) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: index bbox too large");
+    r.mc_dims[i] = (int)((size + 15) / 16);
+  }
+  *info = r;
+  return GBV_OK;
+}
+
+extern "C" gbv_status gbv_nanovdb_mc_ranges(const void *d_grid, const gbv_nanovdb_info *info, float *d_ranges,
+                                            void *stream) {
+  if (!d_grid || !d_ranges || !nvdb_info_ok(info))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_mc_ranges: null pointer or bad grid info");
+  const NvdbGrid g = make_nvdb_grid(d_grid, *info);
+  const long long n = (long long)info->mc_dims[0] * info->mc_dims[1] * info->mc_dims[2];
+  if (n > (1ll << 31) - 1) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_mc_ranges: too many macrocells");
+  nvdb_mc_ranges_kernel<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      g, info->mc_dims[0], info->mc_dims[1], info->mc_dims[2], reinterpret_cast<float2 *>(d_ranges));
+  return check_launch("nvdb_mc_ranges_kernel");
+}
+
+extern "C" gbv_status gbv_nanovdb_sample(const void *d_grid, const gbv_nanovdb_info *info, const float *d_points,
+                                         long long n, float *d_values, void *stream) {
+  if (!d_grid || !d_points || !d_values || n < 0 || !nvdb_info_ok(info))
+    return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_sample: null pointer or bad grid info");
+  if (n == 0) return GBV_OK;
+  const NvdbGrid g = make_nvdb_grid(d_grid, *info);
+  nvdb_sample_kernel<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(g, d_points, n, d_values);
+  return check_launch("nvdb_sample_kernel");
+}

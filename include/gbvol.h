@@ -38,8 +38,9 @@ enum {
 };
 /* voxel layouts */
 enum {
-  GBV_LAYOUT_LINEAR = 0,       /* x-fastest scalars, FP32 only (the reference's texel array) */
-  GBV_LAYOUT_BRICK_CORNERS = 1 /* bricks of cells (8^3 unless shaped); each cell stores its 8 corner voxels */
+  GBV_LAYOUT_LINEAR = 0,        /* x-fastest scalars, FP32 only (the reference's texel array) */
+  GBV_LAYOUT_BRICK_CORNERS = 1, /* bricks of cells (8^3 unless shaped); each cell stores its 8 corner voxels */
+  GBV_LAYOUT_NANOVDB = 2        /* a NanoVDB float grid buffer (gbv_nanovdb_parse) */
 };
 /* frame-buffer read formats (BNDataType subset) */
 enum { GBV_FB_FLOAT4 = 0, GBV_FB_RGBA8 = 1, GBV_FB_RGBA8_SRGB = 2 };
@@ -137,6 +138,45 @@ gbv_status gbv_normalize_texels(const void *d_texels, int bits, long long n,
                                 float *d_scalars, void *stream);
 
 /* ------------------------------------------------------------------------
+ * NanoVDB fields: one NanoVDB grid of value type Float (format version 32,
+ * the buffer nanovdb::GridHandle holds), resident on the device as is.
+ * ------------------------------------------------------------------------ */
+typedef struct gbv_nanovdb_info {
+  /* from the grid buffer */
+  unsigned long long bytes;      /* the grid's size in bytes */
+  long long root_offset;         /* byte offset of the root node */
+  unsigned int root_tiles;       /* root table size */
+  float background;              /* value of unset voxels */
+  float inv_map[9], map_offset[3]; /* world -> index: inv_map x (P - map_offset), single precision */
+  int index_lo[3], index_hi[3];  /* index bbox of the active values (inclusive) */
+  float world_lo[3], world_hi[3];/* world bbox (single precision) */
+  double voxel_size[3];
+  /* macrocells: ceil(index bbox size / 16) per axis (NanoVDBData::buildMCs) */
+  int mc_dims[3];
+} gbv_nanovdb_info;
+
+/* Parses and checks a NanoVDB float grid held in HOST memory (h_grid,
+   `bytes` long): magic number, format version 32, value type Float, the
+   size the header states, the root within the buffer.  Replaces
+   NanoVDBData::commit (barney/volume/NanoVDB.cu:193-232). */
+gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_nanovdb_info *info);
+
+/* Per-macrocell scalar range (min, max) of a NanoVDB grid on the device:
+   macrocell m covers the index box lo + (m*size)/mc .. lo + ((m+1)*size)/mc
+   + 1, both ends inclusive, and takes every value the grid returns there
+   (active, inactive, tile or background).  d_ranges: 2 floats per
+   macrocell, x-fastest, info->mc_dims macrocells.  Replaces
+   NanoVDBData_computeMCs (barney/volume/NanoVDB.cu:28-60). */
+gbv_status gbv_nanovdb_mc_ranges(const void *d_grid, const gbv_nanovdb_info *info, float *d_ranges,
+                                 void *stream);
+
+/* The field's sampler at n world points (d_points: 3 floats each) into
+   d_values: NanoVDBDataSampler::DD::sample (barney/volume/NanoVDB.h:100-129),
+   the same function the renderer samples with. */
+gbv_status gbv_nanovdb_sample(const void *d_grid, const gbv_nanovdb_info *info, const float *d_points,
+                              long long n, float *d_values, void *stream);
+
+/* ------------------------------------------------------------------------
  * Scene description for rendering (device pointers where marked d_).
  * ------------------------------------------------------------------------ */
 typedef struct gbv_scene {
@@ -180,6 +220,11 @@ typedef struct gbv_scene {
   /* brick shape of a GBV_LAYOUT_BRICK_CORNERS store (as passed to
      gbv_build_brick_store_shaped; {0,0,0} = 8^3 cells) */
   int brick_log2[3];
+  /* GBV_LAYOUT_NANOVDB: the parsed grid (host memory); d_voxels is the grid
+     buffer on the device, d_majorants has nanovdb->mc_dims macrocells, and
+     dims, origin, spacing and cells_per_mc are not used (the grid's own
+     index bbox, world bbox and macrocells are) */
+  const gbv_nanovdb_info *nanovdb;
 } gbv_scene;
 
 /* Counters written by gbv_render when d_counters != 0 (uint64 each):
