@@ -13,7 +13,7 @@ _LIB = Path(__file__).resolve().parent / "_lib" / "libbarney_gb300.so"
 GBV_OK = 0
 GBV_ERROR_INVALID_ARGUMENT, GBV_ERROR_CUDA, GBV_ERROR_OUT_OF_MEMORY, GBV_ERROR_LIMIT, GBV_ERROR_UNSUPPORTED = 1, 2, 3, 4, 5
 GBV_VOXEL_F32, GBV_VOXEL_F16, GBV_VOXEL_BF16, GBV_VOXEL_U8_SCALED = 0, 1, 2, 3
-GBV_LAYOUT_LINEAR, GBV_LAYOUT_BRICK_CORNERS = 0, 1
+GBV_LAYOUT_LINEAR, GBV_LAYOUT_BRICK_CORNERS, GBV_LAYOUT_NANOVDB = 0, 1, 2
 GBV_FB_FLOAT4, GBV_FB_RGBA8, GBV_FB_RGBA8_SRGB = 0, 1, 2
 GBV_ADDR_WRAP, GBV_ADDR_CLAMP, GBV_ADDR_BORDER, GBV_ADDR_MIRROR = 0, 1, 2, 3
 GBV_NUM_COUNTERS = 12
@@ -39,6 +39,7 @@ class GbvScene(C.Structure):
         ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
         ("brick_log2", _i3),
+        ("nanovdb", C.c_void_p),
     ]
 
 

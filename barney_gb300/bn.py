@@ -132,7 +132,8 @@ class BarneySession:
 
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
                     layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None,
-                    texel_format: int = BN_FLOAT32, frame_stats: bool = False, anari: Optional[str] = None):
+                    texel_format: int = BN_FLOAT32, frame_stats: bool = False, anari: Optional[str] = None,
+                    nanovdb: Optional[bytes] = None):
         """anari: None (bn* calls as an app makes them), "vec4" or
         "vec3+opacity": the field and the transfer function made through the
         ANARI parameter translation (include/gbv_anari.h) from the
@@ -143,7 +144,15 @@ class BarneySession:
         nx, ny, nz = s.dims
         origin, spacing = s.geometry()
         td = None
-        if anari is None:
+        if nanovdb is not None:
+            # a "NanoVDB" field from a BN_UINT8 data array (anari/SpatialField.cpp:220-233)
+            grid = np.frombuffer(bytes(nanovdb), np.uint8).copy()
+            self.keep.append(grid)
+            sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"NanoVDB"), "bnScalarFieldCreate")
+            bd = _ok(L.bnDataCreate(ctx, 0, BN_UINT8, grid.size, grid.ctypes.data_as(C.c_void_p)), "bnDataCreate")
+            L.bnSetData(sf, b"data", bd)
+            L.bnRelease(bd)
+        elif anari is None:
             td = _ok(L.bnTextureData3DCreate(ctx, 0, texel_format, nx, ny, nz, C.c_void_p(scalars_ptr)),
                      "bnTextureData3DCreate")
             sf = _ok(L.bnScalarFieldCreate(ctx, 0, b"structured"), "bnScalarFieldCreate")
@@ -161,11 +170,12 @@ class BarneySession:
                                                    (C.c_float * 3)(*spacing), C.byref(h)),
                     "gbv_anari_structured_regular")
             sf = h.value
-        L.bnSet1i(sf, b"cellsPerMacrocell", s.cells_per_mc)
-        L.bnSet1i(sf, b"voxelFormat", voxel_format)
-        L.bnSet1i(sf, b"voxelLayout", layout)
-        if brick is not None:
-            L.bnSet3i(sf, b"brickLog2", *brick)
+        if nanovdb is None:
+            L.bnSet1i(sf, b"cellsPerMacrocell", s.cells_per_mc)
+            L.bnSet1i(sf, b"voxelFormat", voxel_format)
+            L.bnSet1i(sf, b"voxelLayout", layout)
+            if brick is not None:
+                L.bnSet3i(sf, b"brickLog2", *brick)
         L.bnCommit(sf)
         vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
         tf = np.ascontiguousarray(s.tf, np.float32)

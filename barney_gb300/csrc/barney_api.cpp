@@ -139,8 +139,9 @@ template <typename T> static T *track(Context *ctx, std::shared_ptr<T> obj, cons
 
 // ---------------------------------------------------------------- objects --
 
-struct Data : Object {  // bnDataCreate(BN_OBJECT, ...) -> ObjectRefsData
+struct Data : Object {  // bnDataCreate: ObjectRefsData (BN_OBJECT) or PODData (BN_UINT8)
   std::vector<SP> objects;
+  std::vector<unsigned char> bytes;
 };
 
 struct TextureData3D : Object {  // common/Texture.cpp, cudaCommon/TextureData.cu
@@ -154,7 +155,17 @@ struct Texture2D : Object {  // bnTexture2DCreate
   DevBuf<float> texels;  // RGBA float
 };
 
-struct StructuredField : Object {  // volume/StructuredData.{h,cu}
+// A scalar field as the volume and the renderer see it (ScalarField,
+// barney/volume/ScalarField.h): a macrocell range grid and the scene-record
+// fields of its voxels.
+struct Field : Object {
+  int mcDims[3] = {0, 0, 0};
+  DevBuf<float> ranges;
+  virtual bool build(cudaStream_t s) = 0;
+  virtual void fill(gbv_scene &s) const = 0;
+};
+
+struct StructuredField : Field {  // volume/StructuredData.{h,cu}
   std::shared_ptr<TextureData3D> td;
   int dims[3] = {0, 0, 0};
   float origin[3] = {0, 0, 0};
@@ -165,8 +176,6 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
   int brickLog2[3] = {3, 3, 3};
   // built state
   bool built = false;
-  int mcDims[3] = {0, 0, 0};
-  DevBuf<float> ranges;
   DevBuf<unsigned char> bricks;
   DevBuf<float> scaleOffset;
   bool set3i(const std::string &m, int x, int y, int z) override {
@@ -202,7 +211,20 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
     }
     return false;
   }
-  bool build(cudaStream_t s) {
+  void fill(gbv_scene &s) const override {
+    s.layout = layout;
+    s.format = voxelFormat;
+    s.d_voxels = layout == GBV_LAYOUT_BRICK_CORNERS ? (const void *)bricks.p : (const void *)td->scalars.p;
+    s.d_scale_offset = scaleOffset.p;
+    s.cells_per_mc = cellsPerMC;
+    for (int a = 0; a < 3; a++) {
+      s.brick_log2[a] = brickLog2[a];
+      s.dims[a] = dims[a];
+      s.origin[a] = origin[a];
+      s.spacing[a] = spacing[a];
+    }
+  }
+  bool build(cudaStream_t s) override {
     if (built) return true;
     if (!td || !td->scalars.p) { fail("structured field has no textureData"); return false; }
     if (td->dims[0] != dims[0] || td->dims[1] != dims[1] || td->dims[2] != dims[2]) {
@@ -243,8 +265,60 @@ struct StructuredField : Object {  // volume/StructuredData.{h,cu}
   }
 };
 
+// volume/NanoVDB.{h,cu}: a NanoVDB float grid given as a BN_UINT8 data
+// array ("data"), parsed and checked on commit, uploaded as is
+struct NanoVDBField : Field {
+  std::shared_ptr<Data> data;
+  gbv_nanovdb_info info;
+  DevBuf<unsigned char> grid;
+  bool built = false, parsed = false;
+  bool setData(const std::string &m, const SP &v) override {
+    if (m == "data") {
+      data = as<Data>(v);
+      built = parsed = false;
+      return data != nullptr;
+    }
+    return false;
+  }
+  void commit() override {
+    parsed = false;
+    if (!data || data->bytes.empty()) { fail("NanoVDB field has no data"); return; }
+    if (gbv_nanovdb_parse(data->bytes.data(), data->bytes.size(), &info) != GBV_OK) {
+      fail(gbv_last_error());
+      return;
+    }
+    parsed = true;
+  }
+  void fill(gbv_scene &s) const override {
+    s.layout = GBV_LAYOUT_NANOVDB;
+    s.format = GBV_VOXEL_F32;
+    s.d_voxels = grid.p;
+    s.nanovdb = &info;
+  }
+  bool build(cudaStream_t s) override {
+    if (built) return true;
+    if (!parsed) { fail("NanoVDB field: no valid grid committed"); return false; }
+    if (!grid.alloc(info.bytes, ctx->mem)) return false;
+    if (cudaMemcpyAsync(grid.p, data->bytes.data(), info.bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      fail("NanoVDB grid upload failed");
+      return false;
+    }
+    for (int a = 0; a < 3; a++) mcDims[a] = info.mc_dims[a];
+    const size_t nmc = (size_t)mcDims[0] * mcDims[1] * mcDims[2];
+    if (!ranges.alloc(2 * nmc, ctx->mem)) return false;
+    if (gbv_nanovdb_mc_ranges(grid.p, &info, ranges.p, s) != GBV_OK) {
+      fail(gbv_last_error());
+      return false;
+    }
+    // the host copy must live until the upload has run
+    if (cudaStreamSynchronize(s) != cudaSuccess) { fail("NanoVDB grid upload failed"); return false; }
+    built = true;
+    return true;
+  }
+};
+
 struct Volume : Object {  // volume/Volume.{h,cpp}, TransferFunction
-  std::shared_ptr<StructuredField> sf;
+  std::shared_ptr<Field> sf;
   std::vector<float> tfHost{1, 1, 1, 1, 1, 1, 1, 1};  // TransferFunction ctor default
   float domain[2] = {0.f, 1.f};
   float densityAt1 = 1.f;
@@ -540,8 +614,18 @@ BNRenderer bnRendererCreate(BNContext ctx, const char *) {
 
 BNData bnDataCreate(BNContext context, int, BNDataType dataType, size_t numItems, const void *items) {
   Context *c = (Context *)context;
+  if (dataType == BN_UINT8) {  // a byte array (PODData), e.g. a NanoVDB grid
+    auto d = std::make_shared<Data>();
+    if (numItems && !items) {
+      fail("bnDataCreate: null data");
+      return nullptr;
+    }
+    const unsigned char *b = (const unsigned char *)items;
+    d->bytes.assign(b, b + numItems);
+    return (BNData)track(c, d, "data");
+  }
   if (dataType != BN_OBJECT) {
-    fail("only BN_OBJECT data arrays are used by this path");
+    fail("only BN_OBJECT and BN_UINT8 data arrays are used by this path");
     return nullptr;
   }
   auto d = std::make_shared<Data>();
@@ -657,6 +741,8 @@ void bnGroupBuild(BNGroup group) {
 
 BNScalarField bnScalarFieldCreate(BNContext context, int, const char *type) {
   std::string t = type ? type : "";
+  if (t == "NanoVDB")  // ScalarFieldRegistry "NanoVDB" (barney/volume/ScalarField.cpp:56)
+    return (BNScalarField)track((Context *)context, std::make_shared<NanoVDBField>(), "NanoVDB");
   if (t != "structured") {
     fail("scalar field type '" + t + "' is not supported");
     return nullptr;
@@ -666,7 +752,7 @@ BNScalarField bnScalarFieldCreate(BNContext context, int, const char *type) {
 
 BNVolume bnVolumeCreate(BNContext context, int, BNScalarField sf) {
   Context *c = (Context *)context;
-  auto f = as<StructuredField>(c->find(sf));
+  auto f = as<Field>(c->find(sf));
   if (!f) {
     fail("bnVolumeCreate: unknown scalar field");
     return nullptr;
@@ -830,24 +916,15 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   if (!vol->build(c->stream)) return;
   if (env && !env->buildEnv(c->stream)) return;
   if (dirs.size() > 4) return fail("at most 4 directional lights are supported");
-  StructuredField &sf = *vol->sf;
   gbv_scene s;
   std::memset(&s, 0, sizeof(s));
-  s.layout = sf.layout;
-  s.format = sf.voxelFormat;
-  s.d_voxels = sf.layout == GBV_LAYOUT_BRICK_CORNERS ? (const void *)sf.bricks.p : (const void *)sf.td->scalars.p;
-  s.d_scale_offset = sf.scaleOffset.p;
+  vol->sf->fill(s);
   for (int a = 0; a < 3; a++) {
-    s.brick_log2[a] = sf.brickLog2[a];
-    s.dims[a] = sf.dims[a];
-    s.origin[a] = sf.origin[a];
-    s.spacing[a] = sf.spacing[a];
     s.cam_pos[a] = cam->position[a];
     s.cam_dir[a] = cam->direction[a];
     s.cam_up[a] = cam->up[a];
   }
   s.d_majorants = vol->majorants.p;
-  s.cells_per_mc = sf.cellsPerMC;
   s.d_tf = vol->tf.p;
   s.tf_n = (int)(vol->tfHost.size() / 4);
   s.domain[0] = vol->domain[0];

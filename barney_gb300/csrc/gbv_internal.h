@@ -11,6 +11,11 @@ gbv_status set_error(gbv_status st, const char *msg);
 gbv_status check_launch(const char *what);
 gbv_status check_cuda(cudaError_t e, const char *what);
 
+// The device view of a parsed NanoVDB grid whose buffer is at d_grid
+// (nanovdb.cu).
+struct NvdbGrid;
+NvdbGrid make_nvdb_grid(const void *d_grid, const gbv_nanovdb_info &info);
+
 // gbv_render without event counting whose loop-cap events store 1 in
 // *d_cap_flag (render.cu; the bn* frame path).
 gbv_status render_cap_flagged(const gbv_scene *s, float *d_accum, int width, int height, int accum_id_start,

@@ -4,6 +4,7 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 #include "gbv_math.cuh"
+#include "gbv_nanovdb.cuh"
 #include "../../include/gbvol.h"
 
 namespace gbv {
@@ -217,6 +218,22 @@ __host__ __device__ __forceinline__ float xf_majorant(const float4 *v, int n, fl
 template <class Store>
 __device__ __forceinline__ vec4 sample_and_map(const FieldGeom &F, const Store &S, const XF &xf, vec3 P) {
   float f = sample_field(F, S, P);
+  if (isnan(f)) return vec4{0.f, 0.f, 0.f, 0.f};
+  return xf_map(xf, f);
+}
+
+// A NanoVDB float grid as a voxel store: its own sampler (world -> index
+// map, clamp to the index bbox, trilinear over the tree), never NaN.
+struct StoreNanoVDB {
+  NvdbGrid g;
+  static constexpr bool kCellStore = false;
+};
+__device__ __forceinline__ float sample_field(const FieldGeom &, const StoreNanoVDB &S, vec3 P) {
+  return nvdb_sample(S.g, P.x, P.y, P.z);
+}
+// Volume::DD::sampleAndMap with NanoVDBDataSampler (NanoVDB.h:100-129)
+__device__ __forceinline__ vec4 sample_and_map(const FieldGeom &F, const StoreNanoVDB &S, const XF &xf, vec3 P) {
+  const float f = sample_field(F, S, P);
   if (isnan(f)) return vec4{0.f, 0.f, 0.f, 0.f};
   return xf_map(xf, f);
 }

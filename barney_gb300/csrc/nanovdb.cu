@@ -24,13 +24,13 @@ NvdbGrid make_nvdb_grid(const void *d_grid, const gbv_nanovdb_info &info) {
 }
 
 // One thread per macrocell (NanoVDBData_computeMCs, NanoVDB.cu:28-60).
-__global__ void __launch_bounds__(128) nvdb_mc_ranges_kernel(NvdbGrid g, int mx, int my, int mz,
+__global__ void __launch_bounds__(128) nvdb_mc_ranges_kernel(NvdbGrid g, int ncx, int ncy, int ncz,
                                                              float2 *__restrict__ ranges) {
-  const long long n = (long long)mx * my * mz;
+  const long long n = (long long)ncx * ncy * ncz;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (tid >= n) return;
-  int m[3] = {(int)(tid % mx), (int)((tid / mx) % my), (int)(tid / ((long long)mx * my))};
-  const int mc[3] = {mx, my, mz};
+  int m[3] = {(int)(tid % ncx), (int)((tid / ncx) % ncy), (int)(tid / ((long long)ncx * ncy))};
+  const int mc[3] = {ncx, ncy, ncz};
   const int size[3] = {g.hi[0] - g.lo[0] + 1, g.hi[1] - g.lo[1] + 1, g.hi[2] - g.lo[2] + 1};
   int a[3], b[3];
   nvdb_mc_footprint(g.lo, size, mc, m, a, b);
@@ -106,6 +106,31 @@ extern "C" gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_na
     const long long size = (long long)r.index_hi[i] - r.index_lo[i] + 1;
     if (size > (1ll << 24)) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: index bbox too large");
     r.mc_dims[i] = (int)((size + 15) / 16);
+  }
+  // Every child offset must land a whole node inside the grid: the device
+  // follows them without checks.
+  constexpr long long kUpperBytes = (long long)kNvdbUpperTable + 8ll * 32768;
+  constexpr long long kLowerBytes = (long long)kNvdbLowerTable + 8ll * 4096;
+  constexpr long long kLeafBytes = (long long)kNvdbLeafValues + 4ll * 512;
+  const long long end = (long long)gridSize;
+  auto inside = [&](long long off, long long size) { return off > 0 && off + size <= end; };
+  for (uint32_t t = 0; t < r.root_tiles; t++) {
+    const long long tile = root + (long long)kNvdbRootTiles + (long long)kNvdbRootTile * t;
+    const long long c = nvdb_ld<long long>(b + tile + kNvdbTileChild);
+    if (c == 0) continue;
+    const long long up = root + c;
+    if (!inside(up, kUpperBytes)) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad upper node");
+    for (uint32_t n = 0; n < 32768; n++) {
+      if (!((nvdb_ld<uint64_t>(b + up + kNvdbUpperChildMask + 8 * (n >> 6)) >> (n & 63)) & 1ull)) continue;
+      const long long lw = up + nvdb_ld<long long>(b + up + kNvdbUpperTable + 8ll * n);
+      if (!inside(lw, kLowerBytes))
+        return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad lower node");
+      for (uint32_t k = 0; k < 4096; k++) {
+        if (!((nvdb_ld<uint64_t>(b + lw + kNvdbLowerChildMask + 8 * (k >> 6)) >> (k & 63)) & 1ull)) continue;
+        const long long lf = lw + nvdb_ld<long long>(b + lw + kNvdbLowerTable + 8ll * k);
+        if (!inside(lf, kLeafBytes)) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad leaf");
+      }
+    }
   }
   *info = r;
   return GBV_OK;

@@ -45,19 +45,35 @@ void commit_camera(const float pos[3], const float dir[3], const float up[3], fl
 }
 
 static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
-  make_field_geom(s, p.F);
   p.xf.v = reinterpret_cast<const float4 *>(s->d_tf);
   p.xf.n = s->tf_n;
   p.xf.lo = s->domain[0];
   p.xf.span = s->domain[1] - s->domain[0];
   p.xf.baseDensity = s->base_density;
-  int M[3];
-  gbv_status st = gbv_mc_dims(s->dims, s->cells_per_mc, M);
-  if (st != GBV_OK) return st;
   p.G.maj = s->d_majorants;
-  for (int i = 0; i < 3; i++) p.G.M[i] = M[i];
-  p.G.origin = p.F.boundsLo;
-  p.G.spacing = vec3((float)s->cells_per_mc) * vec3(s->spacing[0], s->spacing[1], s->spacing[2]);
+  if (s->layout == GBV_LAYOUT_NANOVDB) {
+    // NanoVDBData::commit and ::buildMCs (barney/volume/NanoVDB.cu:70-92,
+    // 193-232): world bounds from the grid, macrocells over them
+    if (!s->nanovdb) return set_error(GBV_ERROR_INVALID_ARGUMENT, "NanoVDB scene without its parsed grid");
+    const gbv_nanovdb_info &nv = *s->nanovdb;
+    memset(&p.F, 0, sizeof(p.F));
+    p.F.boundsLo = vec3(nv.world_lo[0], nv.world_lo[1], nv.world_lo[2]);
+    p.F.boundsHi = vec3(nv.world_hi[0], nv.world_hi[1], nv.world_hi[2]);
+    p.F.origin = p.F.boundsLo;
+    for (int i = 0; i < 3; i++) p.G.M[i] = nv.mc_dims[i];
+    p.G.origin = p.F.boundsLo;
+    p.G.spacing = (p.F.boundsHi - p.F.boundsLo) * rcp(vec3((float)nv.mc_dims[0], (float)nv.mc_dims[1],
+                                                           (float)nv.mc_dims[2]));
+    p.nvdb = make_nvdb_grid(s->d_voxels, nv);
+  } else {
+    make_field_geom(s, p.F);
+    int M[3];
+    gbv_status st = gbv_mc_dims(s->dims, s->cells_per_mc, M);
+    if (st != GBV_OK) return st;
+    for (int i = 0; i < 3; i++) p.G.M[i] = M[i];
+    p.G.origin = p.F.boundsLo;
+    p.G.spacing = vec3((float)s->cells_per_mc) * vec3(s->spacing[0], s->spacing[1], s->spacing[2]);
+  }
   p.rcpMc = rcp(p.G.spacing);
   p.vox = s->d_voxels;
   p.so = reinterpret_cast<const float2 *>(s->d_scale_offset);
@@ -151,7 +167,8 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
     snprintf(msg, sizeof msg, "%s: rank must be in [0, num_ranks) and num_ranks >= 1", fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
-  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0) {
+  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 ||
+      (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0)) {
     snprintf(msg, sizeof msg, "%s: scene lacks voxels, majorants or a transfer function", fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
@@ -189,6 +206,7 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   }
   cudaStream_t cs = (cudaStream_t)stream;
   if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_linear(p, cs, lc);
+  if (s->layout == GBV_LAYOUT_NANOVDB) return render_launch_nvdb(p, cs, lc);
   if (s->layout != GBV_LAYOUT_BRICK_CORNERS) {
     snprintf(msg, sizeof msg, "%s: unknown layout", fn);
     return set_error(GBV_ERROR_UNSUPPORTED, msg);
@@ -301,7 +319,8 @@ extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int
   if (tiles > kNoAllocMaxTiles)
     return set_error(GBV_ERROR_INVALID_ARGUMENT,
                      "gbv_render_noalloc: frame exceeds the 2^30 tiles of 8x4 pixels its 32-bit tile counter holds");
-  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0)
+  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 ||
+      (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0))
     return set_error(GBV_ERROR_INVALID_ARGUMENT,
                      "gbv_render_noalloc: scene lacks voxels, majorants or a transfer function");
   if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
@@ -323,6 +342,7 @@ extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int
   p.counters = d_counters;
   cudaStream_t cs = (cudaStream_t)stream;
   if (s->layout == GBV_LAYOUT_LINEAR) return render_launch_noalloc_linear(p, cs, pool);
+  if (s->layout == GBV_LAYOUT_NANOVDB) return render_launch_noalloc_nvdb(p, cs, pool);
   if (s->layout != GBV_LAYOUT_BRICK_CORNERS)
     return set_error(GBV_ERROR_UNSUPPORTED, "gbv_render_noalloc: unknown layout");
   switch (s->format) {
@@ -349,7 +369,8 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
   std::vector<long long> starts(count + 1, 0);
   for (int i = 0; i < count; i++) {
     const gbv_scene *s = scenes + i;
-    if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 || s->cells_per_mc <= 0 || !d_accums[i] ||
+    if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 ||
+        (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0) || !d_accums[i] ||
         widths[i] <= 0 || heights[i] <= 0)
       return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: an item lacks data or has an empty frame");
     if (s->format != scenes[0].format || s->layout != scenes[0].layout)
@@ -424,6 +445,7 @@ extern "C" gbv_status gbv_batch_render(gbv_batch *b, int accum_id_start, int spp
   L.profile = 0;
   cudaStream_t cs = (cudaStream_t)stream;
   if (b->layout == GBV_LAYOUT_LINEAR) return batch_launch_linear(b, L, cs);
+  if (b->layout == GBV_LAYOUT_NANOVDB) return batch_launch_nvdb(b, L, cs);
   switch (b->format) {
     case GBV_VOXEL_F32: return batch_launch_f32(b, L, cs);
     case GBV_VOXEL_F16: return batch_launch_f16(b, L, cs);

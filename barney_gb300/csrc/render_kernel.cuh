@@ -66,6 +66,7 @@ struct RenderParams {
   const void *vox;
   const float2 *so;
   BrickGeom brick;
+  NvdbGrid nvdb;  // GBV_LAYOUT_NANOVDB: the grid (vox is its buffer)
   vec3 rcpMc;     // 1 / macrocell spacing
   // frame partition across ranks (TiledFB.cu:226-255): with numRanks > 1
   // this launch renders only the 32x32-pixel tiles rank, rank + numRanks, ...
@@ -90,6 +91,9 @@ __host__ __device__ inline long long warp_tile_count(const RenderParams &p) {
 template <class Store> __device__ __forceinline__ Store make_store(const RenderParams &p);
 template <> __device__ __forceinline__ StoreLinearF32 make_store<StoreLinearF32>(const RenderParams &p) {
   return StoreLinearF32{reinterpret_cast<const float *>(p.vox), p.F.N[0], p.F.N[1]};
+}
+template <> __device__ __forceinline__ StoreNanoVDB make_store<StoreNanoVDB>(const RenderParams &p) {
+  return StoreNanoVDB{p.nvdb};
 }
 #define GBV_BRICK_STORE(FMT)                                                                         \
   template <> __device__ __forceinline__ StoreBrickCorners<FMT> make_store<StoreBrickCorners<FMT>>(  \
@@ -1411,5 +1415,6 @@ GBV_DECLARE_STORE_LAUNCHERS(f32)
 GBV_DECLARE_STORE_LAUNCHERS(f16)
 GBV_DECLARE_STORE_LAUNCHERS(bf16)
 GBV_DECLARE_STORE_LAUNCHERS(u8)
+GBV_DECLARE_STORE_LAUNCHERS(nvdb)
 
 }  // namespace gbv

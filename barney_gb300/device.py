@@ -60,6 +60,12 @@ class GpuScene:
         elif fmt != N.GBV_VOXEL_F32:
             raise ValueError("the linear layout holds FP32 voxels only")
         self.build_macrocells()
+        self._init_env()
+
+    def _init_env(self) -> None:
+        import torch
+        scene = self.s
+        dev = torch.device("cuda")
         self.env_tex = self.cdf_y = self.cdf_x = None
         if scene.env is not None:
             e = scene.env

@@ -157,7 +157,9 @@ typedef struct gbv_nanovdb_info {
 
 /* Parses and checks a NanoVDB float grid held in HOST memory (h_grid,
    `bytes` long): magic number, format version 32, value type Float, the
-   size the header states, the root within the buffer.  Replaces
+   size the header states, and every node of the tree inside the buffer (the
+   device follows the child offsets unchecked, so a grid is parsed before it
+   is used on the device).  Replaces
    NanoVDBData::commit (barney/volume/NanoVDB.cu:193-232). */
 gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_nanovdb_info *info);
 

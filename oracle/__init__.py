@@ -35,6 +35,7 @@ class OrcScene(C.Structure):
         ("bg_color", C.c_float * 4), ("ambient_radiance", C.c_float),
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
         ("width", C.c_int), ("height", C.c_int), ("u8_scaled", C.c_int), ("bounded_math", C.c_int),
+        ("nanovdb", C.c_void_p), ("nanovdb_bytes", C.c_ulonglong),
     ]
 
 
@@ -76,6 +77,7 @@ def lib() -> C.CDLL:
             "orc_mc_dims": (None, [vp, i, vp]),
             "orc_mc_ranges": (None, [vp, vp, i, vp]),
             "orc_scene_mc_ranges": (None, [sp, vp]),
+            "orc_scene_mc_grid": (None, [sp, vp, vp]),
             "orc_majorants": (None, [vp, i, vp, i, f, f, f, vp]),
             "orc_trace_ray": (i, [sp, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float), vp]),
             "orc_iso_intersect": (i, [sp, vp, f, vp, vp, f, vp]),
@@ -120,7 +122,7 @@ def bounded_angles(y: np.ndarray, x: np.ndarray):
 class Oracle:
     """Oracle view of a barney_gb300.scenes.Scene (keeps its arrays alive)."""
 
-    def __init__(self, scene, scalars=None, majorants=None, u8=False, bounded_math=False):
+    def __init__(self, scene, scalars=None, majorants=None, u8=False, bounded_math=False, nanovdb=None):
         """u8=True samples the field as the library's U8 brick store holds it
         (8-bit per 8^3-cell scale brick) and bounds macrocells by the
         dequantized corners -- float arithmetic only.  bounded_math=True
@@ -173,6 +175,11 @@ class Oracle:
         r.width, r.height = scene.width, scene.height
         r.u8_scaled = 1 if self.u8 else 0
         r.bounded_math = 1 if bounded_math else 0
+        # nanovdb: the bytes of a NanoVDB float grid (the field instead of scalars)
+        self.nanovdb = None if nanovdb is None else np.frombuffer(bytes(nanovdb), dtype=np.uint8).copy()
+        if self.nanovdb is not None:
+            r.nanovdb = self.nanovdb.ctypes.data
+            r.nanovdb_bytes = self.nanovdb.size
         self.rec = r
 
     # -- macrocells --
@@ -181,8 +188,15 @@ class Oracle:
         lib().orc_mc_dims((C.c_int * 3)(*self.rec.dims), self.s.cells_per_mc, out)
         return tuple(out)
 
+    def mc_grid(self):
+        """(macrocell dims, world bounds lower+upper) of the scene's field."""
+        m = (C.c_int * 3)()
+        w = (C.c_float * 6)()
+        lib().orc_scene_mc_grid(C.byref(self.rec), m, w)
+        return tuple(m), tuple(w)
+
     def mc_ranges(self) -> np.ndarray:
-        M = self.mc_dims()
+        M = self.mc_grid()[0]
         out = np.empty((M[0] * M[1] * M[2], 2), dtype=np.float32)
         lib().orc_scene_mc_ranges(C.byref(self.rec), _p(out))
         return out

@@ -287,7 +287,130 @@ inline double fastLog(double f) {
 // ---------------------------------------------------------------------------
 // Field and transfer function
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// NanoVDB float grids (orc_scene.nanovdb): the reference's NanoVDB field
+// (barney/volume/NanoVDB.{h,cu}) over the NanoVDB 32 buffer layout -- grid
+// header (672 B), tree header (64 B), root (64 B + 32-byte tiles keyed by
+// the 4096^3 region), upper nodes (32^3 entries, child mask at 4128, table
+// at 8256), lower nodes (16^3, 544, 1088), leaves (8^3 floats at 96); child
+// offsets are signed and relative to the parent (the root for root tiles).
+// ---------------------------------------------------------------------------
+struct Nvdb {
+  const unsigned char *b = nullptr;
+  int64_t root = 0;
+  uint32_t tiles = 0;
+  float background = 0.f;
+  float inv[9] = {0}, vec[3] = {0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  V3<float> wlo, whi;  // world bounds as floats (NanoVDBData::commit)
+  int M[3] = {0, 0, 0};  // macrocells: divRoundUp(index size, 16) (NanoVDBData::buildMCs)
+};
+template <typename T> inline T nv_get(const unsigned char *p) {
+  T v;
+  std::memcpy(&v, p, sizeof(T));
+  return v;
+}
+inline Nvdb nv_parse(const unsigned char *b) {
+  Nvdb g;
+  g.b = b;
+  g.root = 672 + nv_get<int64_t>(b + 672 + 24);
+  g.tiles = nv_get<uint32_t>(b + g.root + 24);
+  g.background = nv_get<float>(b + g.root + 28);
+  for (int i = 0; i < 9; i++) g.inv[i] = nv_get<float>(b + 296 + 36 + 4 * i);
+  for (int i = 0; i < 3; i++) {
+    g.vec[i] = nv_get<float>(b + 296 + 72 + 4 * i);
+    g.lo[i] = nv_get<int32_t>(b + g.root + 4 * i);
+    g.hi[i] = nv_get<int32_t>(b + g.root + 12 + 4 * i);
+    g.wlo[i] = (float)nv_get<double>(b + 560 + 8 * i);
+    g.whi[i] = (float)nv_get<double>(b + 560 + 24 + 8 * i);
+    g.M[i] = (g.hi[i] - g.lo[i] + 1 + 15) / 16;
+  }
+  return g;
+}
+// ReadAccessor::getValue
+inline float nv_value(const Nvdb &g, int x, int y, int z) {
+  const unsigned char *root = g.b + g.root;
+  const uint64_t key = uint64_t(uint32_t(z) >> 12) | (uint64_t(uint32_t(y) >> 12) << 21) |
+                       (uint64_t(uint32_t(x) >> 12) << 42);
+  for (uint32_t t = 0; t < g.tiles; t++) {
+    const unsigned char *tile = root + 64 + 32 * (size_t)t;
+    if (nv_get<uint64_t>(tile) != key) continue;
+    const int64_t child = nv_get<int64_t>(tile + 8);
+    if (!child) return nv_get<float>(tile + 20);
+    const unsigned char *up = root + child;
+    const uint32_t n2 = ((uint32_t(x) & 4095u) >> 7) * 1024u + ((uint32_t(y) & 4095u) >> 7) * 32u +
+                        ((uint32_t(z) & 4095u) >> 7);
+    if (!(nv_get<uint64_t>(up + 4128 + 8 * (n2 / 64)) & (1ull << (n2 % 64))))
+      return nv_get<float>(up + 8256 + 8 * (size_t)n2);
+    const unsigned char *lw = up + nv_get<int64_t>(up + 8256 + 8 * (size_t)n2);
+    const uint32_t n1 = ((uint32_t(x) & 127u) >> 3) * 256u + ((uint32_t(y) & 127u) >> 3) * 16u +
+                        ((uint32_t(z) & 127u) >> 3);
+    if (!(nv_get<uint64_t>(lw + 544 + 8 * (n1 / 64)) & (1ull << (n1 % 64))))
+      return nv_get<float>(lw + 1088 + 8 * (size_t)n1);
+    const unsigned char *lf = lw + nv_get<int64_t>(lw + 1088 + 8 * (size_t)n1);
+    const uint32_t n0 = (uint32_t(x) & 7u) * 64u + (uint32_t(y) & 7u) * 8u + (uint32_t(z) & 7u);
+    return nv_get<float>(lf + 96 + 4 * (size_t)n0);
+  }
+  return g.background;
+}
+// NanoVDBDataSampler::DD::sample (NanoVDB.h:100-129): worldToIndexF (the
+// translation in double, the 3x3 product in float with fmaf), -0.5,
+// Clamp = fmax(fmin(x, hi), lo) to the index bbox, then the trilinear
+// SampleFromVoxels<acc, 1>: floor, fractions, 8 values, lerp a + float(w) (b - a)
+// along z, y, x.
+inline float nv_sample(const Nvdb &g, V3<float> P) {
+  const double d[3] = {(double)P.x - (double)g.vec[0], (double)P.y - (double)g.vec[1], (double)P.z - (double)g.vec[2]};
+  const float f[3] = {(float)d[0], (float)d[1], (float)d[2]};
+  double ip[3];
+  for (int r = 0; r < 3; r++) {
+    ip[r] = (double)std::fmaf(f[0], g.inv[3 * r], std::fmaf(f[1], g.inv[3 * r + 1], f[2] * g.inv[3 * r + 2]));
+    ip[r] -= 0.5;
+    ip[r] = std::fmax(std::fmin(ip[r], (double)g.hi[r]), (double)g.lo[r]);
+  }
+  int c[3];
+  float w[3];
+  for (int r = 0; r < 3; r++) {
+    const double fl = std::floor(ip[r]);
+    c[r] = (int32_t)fl;
+    w[r] = (float)(ip[r] - fl);
+  }
+  auto L = [](float a, float b, float t) { return a + t * (b - a); };
+  float v[2][2][2];
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 2; k++) v[i][j][k] = nv_value(g, c[0] + i, c[1] + j, c[2] + k);
+  return L(L(L(v[0][0][0], v[0][0][1], w[2]), L(v[0][1][0], v[0][1][1], w[2]), w[1]),
+           L(L(v[1][0][0], v[1][0][1], w[2]), L(v[1][1][0], v[1][1][1], w[2]), w[1]), w[0]);
+}
+// NanoVDBData_computeMCs (NanoVDB.cu:28-60): macrocell m spans index
+// coordinates lo + (m*size)/M .. lo + ((m+1)*size)/M + 1, inclusive
+inline void nv_mc_ranges(const Nvdb &g, float *out) {
+  const int64_t n = (int64_t)g.M[0] * g.M[1] * g.M[2];
+  int size[3];
+  for (int r = 0; r < 3; r++) size[r] = g.hi[r] - g.lo[r] + 1;
+  for (int64_t t = 0; t < n; t++) {
+    const int m[3] = {int(t % g.M[0]), int((t / g.M[0]) % g.M[1]), int(t / ((int64_t)g.M[0] * g.M[1]))};
+    int a[3], e[3];
+    for (int r = 0; r < 3; r++) {
+      a[r] = g.lo[r] + (m[r] * size[r]) / g.M[r];
+      e[r] = g.lo[r] + ((m[r] + 1) * size[r]) / g.M[r] + 1;
+    }
+    float lo = INFINITY, hi = -INFINITY;
+    for (int x = a[0]; x <= e[0]; x++)
+      for (int y = a[1]; y <= e[1]; y++)
+        for (int z = a[2]; z <= e[2]; z++) {
+          const float v = nv_value(g, x, y, z);
+          lo = mn(lo, v);
+          hi = mx(hi, v);
+        }
+    out[2 * t] = lo;
+    out[2 * t + 1] = hi;
+  }
+}
+
 struct Field {
+  bool isNvdb = false;
+  Nvdb nv;
   const float *data;
   int N[3];          // numScalars
   int C[3];          // numCells = dims-1 (StructuredData.cu:142-151)
@@ -321,6 +444,16 @@ inline void u8_cell_corners(const Field &F, int cx, int cy, int cz, float c[8]) 
 
 inline Field make_field(const orc_scene *s) {
   Field f;
+  if (s->nanovdb) {
+    f.isNvdb = true;
+    f.nv = nv_parse(s->nanovdb);
+    f.data = nullptr;
+    for (int i = 0; i < 3; i++) { f.N[i] = 0; f.C[i] = 0; }
+    f.boundsLo = f.nv.wlo;
+    f.boundsHi = f.nv.whi;
+    f.origin = f.boundsLo;
+    return f;
+  }
   f.data = s->scalars;
   for (int i = 0; i < 3; i++) { f.N[i] = s->dims[i]; f.C[i] = s->dims[i] - 1; }
   f.origin = {s->origin[0], s->origin[1], s->origin[2]};
@@ -374,6 +507,7 @@ inline float sample_field_u8(const Field &F, V3<float> P) {
 }
 
 template <typename R> inline R sample_field(const Field &F, V3<R> P, Tri *tri) {
+  if (F.isNvdb) return R(nv_sample(F.nv, V3<float>((float)P.x, (float)P.y, (float)P.z)));
   if constexpr (std::is_same<R, float>::value) {
     if (F.u8lohi) return sample_field_u8(F, P);
   }
@@ -726,18 +860,27 @@ inline void build_scene(const orc_scene *s, Scene &S) {
   S.F = make_field(s);
   S.xf = make_xf(s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density);
   int cpm = s->cells_per_mc;
-  mc_dims_of(S.F.N, cpm, S.M);
-  // StructuredData.cu:70-76: mc origin = worldBounds.lower, spacing = cpm*gridSpacing
-  S.mcOrigin = S.F.boundsLo;
-  S.mcSpacing = V3<float>((float)cpm) * S.F.spacing;
+  if (S.F.isNvdb) {
+    // NanoVDBData::buildMCs (NanoVDB.cu:70-92): origin = worldBounds.lower,
+    // spacing = worldBounds.size() * rcp(mcDims)
+    for (int i = 0; i < 3; i++) S.M[i] = S.F.nv.M[i];
+    S.mcOrigin = S.F.boundsLo;
+    S.mcSpacing = (S.F.boundsHi - S.F.boundsLo) * rcp(V3<float>((float)S.M[0], (float)S.M[1], (float)S.M[2]));
+  } else {
+    mc_dims_of(S.F.N, cpm, S.M);
+    // StructuredData.cu:70-76: mc origin = worldBounds.lower, spacing = cpm*gridSpacing
+    S.mcOrigin = S.F.boundsLo;
+    S.mcSpacing = V3<float>((float)cpm) * S.F.spacing;
+  }
   S.mcRcpSpacing = rcp(S.mcSpacing);
   size_t nmc = (size_t)S.M[0] * S.M[1] * S.M[2];
-  if (s->u8_scaled) u8_build(S.F, S.u8lohi);
+  if (s->u8_scaled && !S.F.isNvdb) u8_build(S.F, S.u8lohi);
   if (s->majorants) S.maj = s->majorants;
   else {
     S.majorants_own.resize(nmc);
     std::vector<float> r(2 * nmc);
-    if (s->u8_scaled) u8_mc_ranges(S.F, cpm, S.M, r.data());
+    if (S.F.isNvdb) nv_mc_ranges(S.F.nv, r.data());
+    else if (s->u8_scaled) u8_mc_ranges(S.F, cpm, S.M, r.data());
     else orc_mc_ranges(s->scalars, s->dims, cpm, r.data());
     orc_majorants(r.data(), (int)nmc, s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density,
                   S.majorants_own.data());
@@ -1487,8 +1630,29 @@ void orc_mc_ranges(const float *scalars, const int dims[3], int cpm, float *rang
   }, 64);
 }
 
+void orc_scene_mc_grid(const orc_scene *s, int mc_dims[3], float world[6]) {
+  Field F = make_field(s);
+  if (F.isNvdb) {
+    for (int i = 0; i < 3; i++) {
+      mc_dims[i] = F.nv.M[i];
+      world[i] = F.boundsLo[i];
+      world[3 + i] = F.boundsHi[i];
+    }
+    return;
+  }
+  mc_dims_of(F.N, s->cells_per_mc, mc_dims);
+  for (int i = 0; i < 3; i++) {
+    world[i] = F.boundsLo[i];
+    world[3 + i] = F.boundsHi[i];
+  }
+}
+
 void orc_scene_mc_ranges(const orc_scene *s, float *ranges) {
   Field F = make_field(s);
+  if (F.isNvdb) {
+    nv_mc_ranges(F.nv, ranges);
+    return;
+  }
   int M[3];
   mc_dims_of(F.N, s->cells_per_mc, M);
   if (!s->u8_scaled) {
@@ -1815,7 +1979,7 @@ inline void ea_backward_pixel(const Field &F, const XF &xf, const EAView &v, int
     double t = st.t0 + (double(i) + .5) * st.dt;
     if (t >= st.t1) break;
     V3<double> P = org + t * dir;
-    Tri tri;
+    Tri tri{};
     double s = sample_field<double>(F, P, &tri);
     if (std::isnan(s)) continue;  // sampleAndMap -> 0: no dependence
     int idx;

@@ -71,6 +71,11 @@ typedef struct orc_scene {
      lookups' theta and phi.  Then nothing else differs and frames with
      multiple scattering and an env map are comparable bit for bit. */
   int   bounded_math;
+  /* a NanoVDB float grid (format 32) in host memory; when set it is the
+     field (scalars, dims, origin, spacing and cells_per_mc are not used):
+     the reference's NanoVDB field (barney/volume/NanoVDB.{h,cu}) */
+  const unsigned char *nanovdb;
+  unsigned long long nanovdb_bytes;
 } orc_scene;
 
 typedef struct orc_stats {
@@ -92,6 +97,9 @@ void  orc_sample_points(const orc_scene *s, const float *P, int n, float *out);
 void  orc_tf_map(const orc_scene *s, const float *scalars, int n, float *rgba);
 
 /* --- macrocell build (StructuredData_computeMCs + mapMCs) --- */
+/* macrocell grid of the scene's field: dims, and for NanoVDB fields the
+   world bounds (lower xyz, upper xyz) the grid spans */
+void  orc_scene_mc_grid(const orc_scene *s, int mc_dims[3], float world[6]);
 void  orc_mc_dims(const int dims[3], int cells_per_mc, int mc_dims[3]);
 void  orc_mc_ranges(const float *scalars, const int dims[3], int cells_per_mc,
                     float *ranges /* 2 per MC */);

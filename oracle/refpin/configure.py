@@ -3,7 +3,8 @@
 The reference's public header barney/include/barney.h and its
 barney/common/barneyConfig.h.in are CMake templates (#cmakedefine01,
 @VAR@).  This step does what the reference build's configure_file does for
-an embree-only (CPU backend), single-process build without NanoVDB, MPI,
+an embree-only (CPU backend), single-process build with NanoVDB (its
+headers are vendored in the reference, 3rdParty/nanovdb) and without MPI,
 denoisers or the multi-scatter build option, and writes the configured
 headers to oracle/_ref/gen/barney/ (build output, never committed).
 
@@ -16,7 +17,7 @@ from pathlib import Path
 VALUES = {
     "BARNEY_VERSION_MAJOR": "1", "BARNEY_VERSION_MINOR": "1", "BARNEY_VERSION_PATCH": "8",
     "BARNEY_BACKEND_OPTIX": "0", "BARNEY_BACKEND_CUDA": "0", "BARNEY_BACKEND_EMBREE": "1",
-    "BARNEY_BACKEND_HIPRT": "0", "BARNEY_HAVE_MPI": "0", "BARNEY_HAVE_NANOVDB": "0",
+    "BARNEY_BACKEND_HIPRT": "0", "BARNEY_HAVE_MPI": "0", "BARNEY_HAVE_NANOVDB": "1",
     "BARNEY_HAVE_CUDA": "0", "BARNEY_OIDN_CPU": "0", "BARNEY_OIDN_GPU": "0",
     "BARNEY_DISABLE_DENOISING": "1", "BARNEY_USE_MULTI_SCATTERING": "0", "BARNEY_CUBQL_BVH_WIDTH": "4",
 }

@@ -89,6 +89,7 @@ struct Field {
 
 }  // namespace
 
+#pragma GCC visibility push(default)
 extern "C" {
 
 int ref_pin_version(void) { return 1; }
@@ -285,3 +286,4 @@ void ref_rgba8(const float *rgba, int n, int srgb, uint32_t *out) {
 }
 
 }  // extern "C"
+#pragma GCC visibility pop

@@ -23,6 +23,8 @@ template <typename T> struct vec_t<T, 3> {
   vec_t(T s) : x(s), y(s), z(s) {}
   vec_t(T a, T b, T c) : x(a), y(b), z(c) {}
   template <typename U> explicit vec_t(const vec_t<U, 3> &o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
+  // the xyz of a 4-vector
+  template <typename U> explicit vec_t(const vec_t<U, 4> &o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
   T &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
   T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
 };

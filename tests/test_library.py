@@ -255,3 +255,36 @@ def test_render_config_checked_before_the_device():
     assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, None, None) == 0
     good = N.render_config(blocks_per_sm=6, threshold_pct=100, skip_cells=1024, stage=N.GBV_STAGE_ALL, profile=1)
     assert L.gbv_render_ex(C.byref(rec), acc, 4, 4, 0, 0, None, C.byref(good), None) == 0
+
+
+def test_nanovdb_parse():
+    """gbv_nanovdb_parse on the pinned grid (tests/golden/nanovdb_pin.npz):
+    header fields, index and world bboxes, macrocell grid; and the checks
+    that keep malformed buffers off the device."""
+    from barney_gb300 import nanovdb
+    z = np.load(ROOT / "tests" / "golden" / "nanovdb_pin.npz")
+    grid = z["grid"].tobytes()
+    info = nanovdb.parse(grid)
+    assert info.bytes == len(grid)
+    assert list(info.mc_dims) == z["mc_dims"].tolist()
+    assert np.array_equal(np.array(list(info.world_lo) + list(info.world_hi), np.float32), z["world"])
+    assert all(info.index_hi[i] >= info.index_lo[i] for i in range(3))
+    assert info.background == 0.0 and info.root_tiles >= 1
+    L = nanovdb.lib()
+    out = nanovdb.GbvNanovdbInfo()
+
+    def parse(b):
+        a = np.frombuffer(b, np.uint8).copy()
+        return L.gbv_nanovdb_parse(a.ctypes.data_as(C.c_void_p), a.size, C.byref(out))
+
+    assert parse(grid) == N.GBV_OK
+    assert parse(b"X" + grid[1:]) == N.GBV_ERROR_INVALID_ARGUMENT        # magic number
+    assert parse(grid[:1000]) == N.GBV_ERROR_INVALID_ARGUMENT            # truncated
+    bad = bytearray(grid)
+    bad[636:640] = (2).to_bytes(4, "little")                             # value type Double
+    assert parse(bytes(bad)) == N.GBV_ERROR_UNSUPPORTED
+    # a root tile whose child offset points past the end of the buffer
+    root = 672 + int.from_bytes(grid[672 + 24:672 + 32], "little", signed=True)
+    bad = bytearray(grid)
+    bad[root + 64 + 8:root + 64 + 16] = (len(grid)).to_bytes(8, "little", signed=True)
+    assert parse(bytes(bad)) == N.GBV_ERROR_INVALID_ARGUMENT

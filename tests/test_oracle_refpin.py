@@ -216,3 +216,64 @@ def test_live_random_rays_and_samples():
                 assert bits(np.float32(t)) == bits(np.float32(tt.value)), (cpm, i)
                 assert np.array_equal(bits(np.float32(0.7) * rgb), bits(alb)), (cpm, i)
         assert hits > 50
+
+
+# ---- NanoVDB fields ---------------------------------------------------------
+
+NVDB = Path(__file__).resolve().parent / "golden" / "nanovdb_pin.npz"
+# the byte offsets of the NanoVDB float-grid layout the library and the
+# oracle read (grid header, map, bboxes, tree header, root, tiles, internal
+# nodes, leaves and their sizes)
+NVDB_LAYOUT = [672, 296, 560, 608, 636, 36, 72, 64, 24, 64, 32, 8, 20, 24, 28, 4128, 8256, 544, 1088, 96,
+               270400, 33856, 2144]
+
+
+@pytest.fixture(scope="module")
+def nvdb():
+    z = np.load(NVDB)
+    return {k: z[k] for k in z.files}
+
+
+def test_nanovdb_layout_is_the_vendored_library_layout(nvdb):
+    assert nvdb["layout"].tolist() == NVDB_LAYOUT
+
+
+def _nvdb_oracle(grid):
+    from barney_gb300 import scenes
+    s = scenes.Scene(scalars=np.zeros((2, 2, 2), np.float32), tf=scenes.tf_ramp(128), base_density=20.0)
+    return oracle.Oracle(s, nanovdb=grid)
+
+
+def test_oracle_nanovdb_field_against_the_reference(nvdb):
+    """NanoVDBDataSampler::DD::sample and NanoVDBData_computeMCs of the
+    reference (with the vendored NanoVDB library) against the oracle's
+    restatement: samples, macrocell grid and ranges bit for bit."""
+    o = _nvdb_oracle(nvdb["grid"].tobytes())
+    assert same_or_both_nan(o.sample(nvdb["points"]), nvdb["samples"])
+    assert (o.sample(nvdb["points"]) > 0).sum() > 500
+    mc, world = o.mc_grid()
+    assert list(mc) == nvdb["mc_dims"].tolist()
+    assert np.array_equal(np.array(world, np.float32).view(np.uint32), nvdb["world"].view(np.uint32))
+    assert np.array_equal(o.mc_ranges().view(np.uint32), nvdb["ranges"].view(np.uint32))
+
+
+@live
+def test_live_nanovdb_grids():
+    """Fresh grids (another volume, index origin, voxel size and
+    translation): the live reference and the oracle agree."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_nanovdb_golden", NVDB.parent / "make_nanovdb_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    from barney_gb300 import scenes
+    rng = np.random.default_rng(5)
+    for seed, origin, vs, tr in ((31, (0, 0, 0), 0.05, (-0.5, -0.5, -0.5)), (32, (-40, 17, -3), 0.021, (0.1, -0.3, 0.2))):
+        vol = scenes.blob_volume((45, 21, 33), 5, seed=seed, noise=0.02)
+        vol = np.where(vol < 0.03, np.float32(0.0), vol).astype(np.float32)
+        grid = mod.make_grid(vol, origin, vs, tr)
+        pts = (rng.random((2000, 3)) * 2.4 - 1.2).astype(np.float32)
+        o = _nvdb_oracle(grid)
+        assert same_or_both_nan(o.sample(pts), mod.reference_samples(grid, pts))
+        mc, world, ranges = mod.reference_mc(grid)
+        assert list(o.mc_grid()[0]) == mc.tolist()
+        assert np.array_equal(o.mc_ranges().view(np.uint32), ranges.view(np.uint32))
