@@ -362,6 +362,33 @@ def precision_study(scene, g32, rows=(523, 557), reps=2):
     return out
 
 
+def wavefront_timing(g, scene, persistent_ms, reps=3):
+    """The same frame in the wavefront mode (a trace kernel over a ray queue
+    and a shade kernel over the active pixels per step, path state in HBM)
+    against the persistent kernel's time: an A/B of the two structures; the
+    frames are identical."""
+    import torch
+    from barney_gb300 import _native as N
+    acc = g.new_accum()
+    cfg = {"mode": N.GBV_RENDER_WAVEFRONT}
+    g.render(spp=scene.spp, accum=acc, config=cfg)
+    ref = g.new_accum()
+    g.render(spp=scene.spp, accum=ref)
+    torch.cuda.synchronize()
+    identical = bool(torch.equal(acc, ref))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ts = []
+    for _ in range(reps):
+        e0.record()
+        g.render(spp=scene.spp, accum=acc, config=cfg)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ms = min(ts)
+    return {"frame_ms": ms, "persistent_frame_ms": persistent_ms, "vs_persistent": persistent_ms / ms,
+            "frames_identical": identical}
+
+
 def batch_timing(count=64, reps=3):
     """The batched uneven workload: `count` volumes (sides log-uniform in
     [32, 256] per axis), each with its own TF, camera and image size from
@@ -507,6 +534,10 @@ def run_ours(args):
             line["ea_adjoint"] = ea_timing()
         except Exception as e:
             line["ea_adjoint"] = {"error": str(e)}
+        try:
+            line["wavefront"] = wavefront_timing(g, scene, frame_ms)
+        except Exception as e:
+            line["wavefront"] = {"error": str(e)}
     # ---- e2e through the bn* C-ABI with host buffers ----
     from barney_gb300 import bn
     host_vol = torch.from_numpy(np.ascontiguousarray(scene.scalars)).pin_memory()
