@@ -205,8 +205,13 @@ __global__ void __launch_bounds__(256, 4) wf_trace_kernel(const __grid_constant_
 }
 
 // One shade step over the step's active slots.
+// Resident 256-thread blocks per SM the shade kernel's registers are capped
+// for (2: 128 registers, no spills).
+#ifndef GBV_WF_SHADE_BLOCKS
+#define GBV_WF_SHADE_BLOCKS 2
+#endif
 template <class Store>
-__global__ void __launch_bounds__(256) wf_shade_kernel(const __grid_constant__ RenderParams p, WfBuffers B, int step) {
+__global__ void __launch_bounds__(256, GBV_WF_SHADE_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p, WfBuffers B, int step) {
   if (p.rowOff >= 0) {
     for (int i = threadIdx.x; i < p.env.H; i += blockDim.x)
       reinterpret_cast<float2 *>(g_smem + p.rowOff)[i] = env_row_terms(p.env, i);

@@ -4,8 +4,8 @@ A restatement of the reference renderer's embree (CPU) backend for this path
 (gbv_oracle.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg may use it, and only as the checker.
 
-parity unpinned: the reference ships no golden vectors for this path and its
-sources cannot be built here; see gbv_oracle.cpp.
+Pinned by the reference's own code where that compiles here (oracle.refpin,
+tests/test_oracle_refpin.py); see gbv_oracle.cpp.
 """
 from __future__ import annotations
 

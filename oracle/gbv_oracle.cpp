@@ -6,11 +6,15 @@
 // measured as the product.  Only tests/, __graft_entry__.smoke() and the
 // CPU-baseline leg of bench.py may load it.
 //
-// parity unpinned: the reference holds no golden vectors or known-answer tests
+// Pinned by the reference's own code: the reference holds no golden vectors
 // for this path (its unitTests/ cover umesh iso-surfaces and an omni camera
-// only) and cannot be compiled here (submodules owl/embree/cuBQL/optix are
-// empty).  The oracle is pinned by hand-computed known-answer tests and by an
-// independent pure-Python restatement of its scalar kernels.
+// only) and cannot be built as a whole here (submodules owl/embree/cuBQL/
+// optix are empty), but its sources for the path compile unchanged against a
+// restated owl and a stubbed embree API (oracle/refpin); the scalar kernels,
+// the sampler, the per-ray isProg, the sRGB packing and the NanoVDB field
+// code agree with this file bit for bit (tests/test_oracle_refpin.py).  The
+// rest is pinned by known-answer tests and by an independent pure-Python
+// restatement of the scalar kernels.
 //
 // Every function names the reference file:line it follows.  The third-party
 // owl math library (owl::common, >= 1.2.9, submodule commit unrecorded) is

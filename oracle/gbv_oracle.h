@@ -5,10 +5,14 @@
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load
  * this library.  It is the checker, never the product.
  *
- * parity unpinned: the reference ships no golden vectors or known-answer tests
- * for this path, and its sources cannot be built here (the owl, embree, cuBQL
- * and optix submodules are empty).  The oracle is pinned only by hand-computed
- * known-answer tests and by a second, pure-Python restatement of its scalar
+ * Pinned by the reference's own code: the reference ships no golden vectors
+ * for this path and cannot be built as a whole here, but its sources for the
+ * path compile unchanged against a restated owl and a stubbed embree API
+ * (oracle/refpin, `make ref`); the RNG, fastLog, float/half, the transfer
+ * function, the field sampler, sampleAndMap, the per-ray isProg, the sRGB
+ * packing and the NanoVDB field code agree with this oracle bit for bit
+ * (tests/test_oracle_refpin.py).  Ray generation and shading are pinned by
+ * known-answer tests and a second, pure-Python restatement of the scalar
  * kernels (tests/golden/make_golden.py).
  */
 #pragma once

@@ -24,6 +24,13 @@ struct AffineSpace3f {
   LinearSpace3f l;
   vec3f p;
 };
+// rcp of a linear space: its inverse, the transposed adjoint (cross products
+// of the columns) times 1 / det
+inline LinearSpace3f rcp(const LinearSpace3f &m) {
+  const vec3f a = cross(m.vy, m.vz), b = cross(m.vz, m.vx), c = cross(m.vx, m.vy);
+  const float r = 1.f / dot(m.vx, a);
+  return LinearSpace3f(vec3f(a.x, b.x, c.x) * r, vec3f(a.y, b.y, c.y) * r, vec3f(a.z, b.z, c.z) * r);
+}
 typedef LinearSpace3f linear3f;
 typedef AffineSpace3f affine3f;
 inline vec3f xfmVector(const affine3f &a, const vec3f &v) { return xfmVector(a.l, v); }

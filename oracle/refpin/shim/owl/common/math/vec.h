@@ -135,8 +135,8 @@ template <typename T> inline T length(const vec_t<T, 3> &a) { return std::sqrt(d
 template <typename T> inline vec_t<T, 3> normalize(const vec_t<T, 3> &a) {
   return a * (T(1) / std::sqrt(dot(a, a)));
 }
-template <typename T> inline vec_t<T, 3> divRoundUp(const vec_t<T, 3> &a, const vec_t<T, 3> &b) {
-  return (a + b - vec_t<T, 3>(T(1))) / b;
+template <typename T, int N> inline vec_t<T, N> divRoundUp(const vec_t<T, N> &a, const vec_t<T, N> &b) {
+  return (a + b - vec_t<T, N>(T(1))) / b;
 }
 template <typename T, int N> inline vec_t<T, N> clamp(const vec_t<T, N> &v, const vec_t<T, N> &lo,
                                                       const vec_t<T, N> &hi) {
