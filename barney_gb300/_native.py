@@ -17,9 +17,17 @@ GBV_LAYOUT_LINEAR, GBV_LAYOUT_BRICK_CORNERS, GBV_LAYOUT_NANOVDB = 0, 1, 2
 GBV_FB_FLOAT4, GBV_FB_RGBA8, GBV_FB_RGBA8_SRGB = 0, 1, 2
 GBV_ADDR_WRAP, GBV_ADDR_CLAMP, GBV_ADDR_BORDER, GBV_ADDR_MIRROR = 0, 1, 2, 3
 GBV_NUM_COUNTERS = 12
+(GBV_COUNTER_SAMPLES, GBV_COUNTER_MC_VISITS, GBV_COUNTER_RAYS, GBV_COUNTER_CAPS,
+ GBV_COUNTER_CELLS) = 0, 1, 2, 3, 4
 
 _f3 = C.c_float * 3
 _i3 = C.c_int * 3
+
+
+class GbvIsoSurface(C.Structure):
+    """gbv_iso_surface: an iso-surface of the field with a matte material."""
+    _fields_ = [("iso_value", C.c_float), ("d_ranges", C.c_void_p), ("color", C.c_float * 4),
+                ("opacity", C.c_float), ("instance", C.c_int)]
 
 
 class GbvScene(C.Structure):
@@ -40,6 +48,7 @@ class GbvScene(C.Structure):
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
         ("brick_log2", _i3),
         ("nanovdb", C.c_void_p),
+        ("iso", C.c_void_p), ("volume_instance", C.c_int),
     ]
 
 

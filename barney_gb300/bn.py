@@ -34,7 +34,8 @@ BN_SYMBOLS = [
     "bnVolumeCreate", "bnVolumeSetXF", "bnCommit", "bnSetString", "bnSetData", "bnSetObject", "bnSetLight",
     "bnSet1i", "bnSet2i", "bnSet3i", "bnSet4i", "bnSet1f", "bnSet2f", "bnSet3f", "bnSet4f", "bnSet4x3fv",
     "bnSetInstances", "bnBuild", "bnAccumReset", "bnFrameBufferResize", "bnFrameBufferRead",
-    "bnFrameBufferGetSize", "bnRender", "bnGetLastError", "bnFrameBufferGetStats",
+    "bnFrameBufferGetSize", "bnRender", "bnGetLastError", "bnFrameBufferGetStats", "bnGeometryCreate",
+    "bnMaterialCreate",
 ]
 
 
@@ -85,6 +86,9 @@ def lib() -> C.CDLL:
             "bnRender": (None, [vp, vp, vp, vp]),
             "bnGetLastError": (cp, []),
             "bnFrameBufferGetStats": (None, [vp, C.POINTER(C.c_ulonglong)]),
+            "bnGeometryCreate": (vp, [vp, i, cp]),
+            "bnMaterialCreate": (vp, [vp, i, cp]),
+            "bnSetString": (None, [vp, cp, cp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -177,6 +181,18 @@ class BarneySession:
             if brick is not None:
                 L.bnSet3i(sf, b"brickLog2", *brick)
         L.bnCommit(sf)
+        geom = mat = None
+        if s.iso is not None:
+            # an iso_surface geometry with a matte material (IsoSurface, AnariMatte)
+            mat = _ok(L.bnMaterialCreate(ctx, 0, b"matte"), "bnMaterialCreate")
+            L.bnSet4f(mat, b"color", *[float(c) for c in s.iso.color])
+            L.bnSet1f(mat, b"opacity", float(s.iso.opacity))
+            L.bnCommit(mat)
+            geom = _ok(L.bnGeometryCreate(ctx, 0, b"iso_surface"), "bnGeometryCreate")
+            L.bnSetObject(geom, b"scalarField", sf)
+            L.bnSet1f(geom, b"isoValue", float(s.iso.value))
+            L.bnSetObject(geom, b"material", mat)
+            L.bnCommit(geom)
         vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
         tf = np.ascontiguousarray(s.tf, np.float32)
         self.keep.append(tf)
@@ -217,17 +233,34 @@ class BarneySession:
             L.bnSet1f(l, b"scale", e.scale)
             L.bnCommit(l)
             lights.append(l)
+        # groups in instance order: the iso-surface shares the volume's group
+        # when its instance index is the lower one (a group's user geometries
+        # come before its volumes), else it has a group of its own after
         vols = (C.c_void_p * 1)(vol)
-        grp = _ok(L.bnGroupCreate(ctx, 0, None, 0, vols, 1), "bnGroupCreate")
+        geoms = (C.c_void_p * 1)(geom)
+        grp2 = None
+        if geom is None:
+            grp = _ok(L.bnGroupCreate(ctx, 0, None, 0, vols, 1), "bnGroupCreate")
+        elif s.no_volume:
+            grp = _ok(L.bnGroupCreate(ctx, 0, geoms, 1, None, 0), "bnGroupCreate")
+        elif (s.iso.instance, s.volume_instance) == (0, 1):
+            grp = _ok(L.bnGroupCreate(ctx, 0, geoms, 1, vols, 1), "bnGroupCreate")
+        elif (s.iso.instance, s.volume_instance) == (1, 0):
+            grp = _ok(L.bnGroupCreate(ctx, 0, None, 0, vols, 1), "bnGroupCreate")
+            grp2 = _ok(L.bnGroupCreate(ctx, 0, geoms, 1, None, 0), "bnGroupCreate")
+        else:
+            raise ValueError("iso-surface and volume instances must be (0, 1) or (1, 0)")
         if lights:
             arr = (C.c_void_p * len(lights))(*lights)
             data = _ok(L.bnDataCreate(ctx, 0, BN_OBJECT, len(lights), arr), "bnDataCreate")
             L.bnSetData(grp, b"lights", data)
-        L.bnCommit(grp)
-        L.bnGroupBuild(grp)
+        gl = [grp] if grp2 is None else [grp, grp2]
+        for g in gl:
+            L.bnCommit(g)
+            L.bnGroupBuild(g)
         model = _ok(L.bnModelCreate(ctx), "bnModelCreate")
-        groups = (C.c_void_p * 1)(grp)
-        L.bnSetInstances(model, 0, groups, None, 1)
+        groups = (C.c_void_p * len(gl))(*gl)
+        L.bnSetInstances(model, 0, groups, None, len(gl))
         L.bnBuild(model, 0)
         cam = _ok(L.bnCameraCreate(ctx, b"perspective"), "bnCameraCreate")
         L.bnSet3f(cam, b"position", *s.cam_pos)
@@ -247,9 +280,9 @@ class BarneySession:
         L.bnCommit(r)
         fb = _ok(L.bnFrameBufferCreate(ctx, 0), "bnFrameBufferCreate")
         L.bnFrameBufferResize(fb, color_format, s.width, s.height, BN_FB_COLOR)
-        self.handles = dict(td=td, sf=sf, vol=vol, grp=grp, model=model, cam=cam, renderer=r, fb=fb)
-        if td is None:
-            del self.handles["td"]
+        self.handles = dict(td=td, sf=sf, vol=vol, grp=grp, grp2=grp2, geom=geom, mat=mat, model=model, cam=cam,
+                            renderer=r, fb=fb)
+        self.handles = {k: v for k, v in self.handles.items() if v is not None}
         self.scene, self.color_format = s, color_format
         err = last_error()
         return err
@@ -273,7 +306,7 @@ class BarneySession:
         return list(st)
 
     def release_scene(self):
-        for k in ("fb", "renderer", "cam", "model", "grp", "vol", "sf", "td"):
+        for k in ("fb", "renderer", "cam", "model", "grp2", "grp", "geom", "mat", "vol", "sf", "td"):
             if k in self.handles:
                 self.L.bnRelease(self.handles[k])
         self.handles = {}

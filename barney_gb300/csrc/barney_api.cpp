@@ -93,6 +93,7 @@ struct Object {
   virtual bool set4f(const std::string &, float, float, float, float) { return false; }
   virtual bool setObject(const std::string &, const std::shared_ptr<Object> &) { return false; }
   virtual bool setData(const std::string &, const std::shared_ptr<Object> &) { return false; }
+  virtual bool setString(const std::string &, const std::string &) { return false; }
   virtual void commit() {}
 };
 using SP = std::shared_ptr<Object>;
@@ -411,7 +412,84 @@ struct Light : Object {  // light/DirLight, light/EnvMap
   }
 };
 
+// render/AnariMatte (barney/material/AnariMatte.{h,cpp}): constant color
+// (default 0.8 grey, alpha 1) and opacity; parameters take effect on commit
+// (HostMaterial::commit writes the device material).
+struct Material : Object {
+  struct P {
+    float color[4] = {.8f, .8f, .8f, 1.f};
+    float opacity = 1.f;
+  } staged, live;
+  bool committed = false;
+  bool set1f(const std::string &m, float v) override {
+    if (m == "opacity") { staged.opacity = v; return true; }
+    return false;
+  }
+  bool set3f(const std::string &m, float x, float y, float z) override {
+    if (m == "color") { staged.color[0] = x; staged.color[1] = y; staged.color[2] = z; staged.color[3] = 1.f; return true; }
+    return false;
+  }
+  bool set4f(const std::string &m, float x, float y, float z, float w) override {
+    if (m == "color") { staged.color[0] = x; staged.color[1] = y; staged.color[2] = z; staged.color[3] = w; return true; }
+    return false;
+  }
+  bool setString(const std::string &m, const std::string &) override {
+    if (m == "color" || m == "opacity") {
+      fail("matte material: parameters mapped to geometry attributes are not supported (constant values only)");
+      return true;
+    }
+    return false;
+  }
+  bool setObject(const std::string &m, const SP &) override {
+    if (m == "color" || m == "opacity") {
+      fail("matte material: parameters mapped to samplers are not supported (constant values only)");
+      return true;
+    }
+    return false;
+  }
+  void commit() override {
+    live = staged;
+    committed = true;
+  }
+};
+
+// geometry/IsoSurface (barney/geometry/IsoSurface.{h,cpp}): an iso-surface of
+// a scalar field with a material
+struct IsoSurfaceGeom : Object {
+  std::shared_ptr<Field> sf;
+  std::shared_ptr<Material> material;
+  float isoValue = NAN;  // IsoSurface.h:79
+  int userID = 0;        // used by hit-ID channels, which this path has none of
+  bool set1f(const std::string &m, float v) override {
+    if (m == "isoValue") { isoValue = v; return true; }
+    return false;
+  }
+  bool set1i(const std::string &m, int v) override {
+    if (m == "userID") { userID = v; return true; }
+    return false;
+  }
+  bool setData(const std::string &m, const SP &) override {
+    // "isoValues": kept by the reference but not read by its intersection
+    // program, which tests isoValue alone (MCAccelerator.h:433-441)
+    return m == "isoValues";
+  }
+  bool setObject(const std::string &m, const SP &v) override {
+    if (m == "scalarField") {
+      sf = as<Field>(v);
+      if (!sf) fail("'scalarField' value set on 'iso_surface' is not a scalar field");
+      return true;
+    }
+    if (m == "material") {
+      material = as<Material>(v);
+      if (v && !material) fail("'material' value set on 'iso_surface' is not a material");
+      return true;
+    }
+    return false;
+  }
+};
+
 struct Group : Object {
+  std::vector<std::shared_ptr<IsoSurfaceGeom>> geoms;
   std::vector<std::shared_ptr<Volume>> volumes;
   std::shared_ptr<Data> lights;
   bool setData(const std::string &m, const SP &v) override {
@@ -712,13 +790,35 @@ BNLight bnLightCreate(BNContext context, int, const char *type) {
   return (BNLight)track((Context *)context, std::make_shared<Light>(), t == "envmap" ? "envmap" : "directional");
 }
 
-BNGroup bnGroupCreate(BNContext context, int, BNGeom *geoms, int numGeoms, BNVolume *volumes, int numVolumes) {
-  Context *c = (Context *)context;
-  if (numGeoms > 0 && geoms) {
-    fail("surface geometry is not part of this library");
+BNGeom bnGeometryCreate(BNContext context, int, const char *type) {
+  std::string t = type ? type : "";
+  if (t != "iso_surface") {  // Geometry::create (barney/geometry/Geometry.cpp:26-43)
+    fail("geometry type '" + t + "' is not supported (surface geometry other than iso_surface)");
     return nullptr;
   }
+  return (BNGeom)track((Context *)context, std::make_shared<IsoSurfaceGeom>(), "iso_surface");
+}
+
+BNMaterial bnMaterialCreate(BNContext context, int, const char *type) {
+  std::string t = type ? type : "";
+  if (t != "matte" && t != "AnariMatte") {  // HostMaterial::create (barney/material/Material.cpp:83-98)
+    fail("material type '" + t + "' is not supported (matte only)");
+    return nullptr;
+  }
+  return (BNMaterial)track((Context *)context, std::make_shared<Material>(), "matte");
+}
+
+BNGroup bnGroupCreate(BNContext context, int, BNGeom *geoms, int numGeoms, BNVolume *volumes, int numVolumes) {
+  Context *c = (Context *)context;
   auto g = std::make_shared<Group>();
+  for (int i = 0; geoms && i < numGeoms; i++) {
+    auto iso = as<IsoSurfaceGeom>(c->find(geoms[i]));
+    if (!iso) {
+      fail("bnGroupCreate: unknown geometry handle");
+      return nullptr;
+    }
+    g->geoms.push_back(iso);
+  }
   for (int i = 0; i < numVolumes; i++) {
     auto v = as<Volume>(c->find(volumes[i]));
     if (!v) {
@@ -735,6 +835,8 @@ void bnGroupBuild(BNGroup group) {
   auto g = as<Group>(lookup(group, &c));
   if (!g) return fail("bnGroupBuild: unknown group");
   cudaSetDevice(c->device);
+  for (auto &iso : g->geoms)
+    if (iso->sf && !iso->sf->build(c->stream)) return;
   for (auto &v : g->volumes)
     if (!v->build(c->stream)) return;
 }
@@ -784,10 +886,11 @@ void bnCommit(BNObject target) {
   if (!o) return fail(std::string("set '") + paramName + "' on an unknown object");           \
   if (!o->call) c->warnOnce(o->kind + " ignores parameter '" + paramName + "'");
 
-void bnSetString(BNObject target, const char *paramName, const char *) {
+void bnSetString(BNObject target, const char *paramName, const char *value) {
   Context *c = nullptr;
   SP o = lookup(target, &c);
-  if (o) c->warnOnce(o->kind + " ignores string parameter '" + paramName + "'");
+  if (o && !o->setString(paramName, value ? value : ""))
+    c->warnOnce(o->kind + " ignores string parameter '" + paramName + "'");
 }
 void bnSetData(BNObject target, const char *paramName, BNData value) {
   BN_SETTER(setData(paramName, c ? c->find(value) : SP()));
@@ -848,6 +951,8 @@ void bnBuild(BNModel model, int) {
   cudaSetDevice(c->device);
   for (size_t i = 0; i < m->groups.size(); i++) {
     if (!isIdentity(m->xfms[i])) return fail("instance transforms other than the identity are not supported");
+    for (auto &iso : m->groups[i]->geoms)
+      if (iso->sf && !iso->sf->build(c->stream)) return;
     for (auto &v : m->groups[i]->volumes)
       if (!v->build(c->stream)) return;
   }
@@ -893,16 +998,30 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   if (!r || !m || !cam || !f) return fail("bnRender: unknown handle");
   if (!f->accum.p) return fail("bnRender: frame buffer was never resized");
   cudaSetDevice(c->device);
-  // collect the world: one structured volume, directional lights, env map
+  // collect the world: one volume and/or one iso-surface, directional
+  // lights, env map.  RTC instance indices follow
+  // ModelSlot::flattenInstancesForDevice (barney/ModelSlot.cpp:129-155): per
+  // group, its user-geometry group (the iso-surface), then one instance per
+  // volume.
   std::shared_ptr<Volume> vol;
+  std::shared_ptr<IsoSurfaceGeom> iso;
+  int volInst = 0, isoInst = 0, nextInst = 0;
   std::vector<std::shared_ptr<Light>> dirs;
   std::shared_ptr<Light> env;
   for (size_t i = 0; i < m->groups.size(); i++) {
     if (!isIdentity(m->xfms[i])) return fail("instance transforms other than the identity are not supported");
     auto &g = m->groups[i];
+    if (!g->geoms.empty()) {
+      for (auto &gm : g->geoms) {
+        if (iso && iso != gm) return fail("more than one iso-surface per model is not supported");
+        iso = gm;
+      }
+      isoInst = nextInst++;
+    }
     for (auto &v : g->volumes) {
       if (vol && vol != v) return fail("more than one volume per model is not supported");
       vol = v;
+      volInst = nextInst++;
     }
     if (g->lights)
       for (auto &o : g->lights->objects) {
@@ -912,26 +1031,46 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
         else dirs.push_back(l);
       }
   }
-  if (!vol) return fail("bnRender: the model holds no volume");
-  if (!vol->build(c->stream)) return;
+  if (!vol && !iso) return fail("bnRender: the model holds no volume and no iso-surface");
+  if (vol && !vol->build(c->stream)) return;
+  gbv_iso_surface isoRec;
+  if (iso) {
+    // Geometry::getMaterial requires a committed material (Geometry.cpp:86-99)
+    if (!iso->sf) return fail("bnRender: the iso-surface has no scalar field");
+    if (!iso->material || !iso->material->committed)
+      return fail("bnRender: the iso-surface has no committed material");
+    if (vol && vol->sf != iso->sf)
+      return fail("bnRender: an iso-surface and a volume over different scalar fields are not supported");
+    if (!iso->sf->build(c->stream)) return;
+    std::memset(&isoRec, 0, sizeof(isoRec));
+    isoRec.iso_value = iso->isoValue;
+    isoRec.d_ranges = iso->sf->ranges.p;
+    for (int a = 0; a < 4; a++) isoRec.color[a] = iso->material->live.color[a];
+    isoRec.opacity = iso->material->live.opacity;
+    isoRec.instance = isoInst;
+  }
   if (env && !env->buildEnv(c->stream)) return;
   if (dirs.size() > 4) return fail("at most 4 directional lights are supported");
   gbv_scene s;
   std::memset(&s, 0, sizeof(s));
-  vol->sf->fill(s);
+  (vol ? vol->sf : iso->sf)->fill(s);
   for (int a = 0; a < 3; a++) {
     s.cam_pos[a] = cam->position[a];
     s.cam_dir[a] = cam->direction[a];
     s.cam_up[a] = cam->up[a];
   }
-  s.d_majorants = vol->majorants.p;
-  s.d_tf = vol->tf.p;
-  s.tf_n = (int)(vol->tfHost.size() / 4);
-  s.domain[0] = vol->domain[0];
-  s.domain[1] = vol->domain[1];
-  s.base_density = vol->densityAt1;
-  s.anisotropy = vol->anisotropy;
-  s.scattering_albedo = vol->scatteringAlbedo;
+  if (iso) s.iso = &isoRec;
+  s.volume_instance = vol ? volInst : 0;
+  if (vol) {
+    s.d_majorants = vol->majorants.p;
+    s.d_tf = vol->tf.p;
+    s.tf_n = (int)(vol->tfHost.size() / 4);
+    s.domain[0] = vol->domain[0];
+    s.domain[1] = vol->domain[1];
+    s.base_density = vol->densityAt1;
+    s.anisotropy = vol->anisotropy;
+    s.scattering_albedo = vol->scatteringAlbedo;
+  }
   s.fovy = cam->fovy;
   s.num_dir_lights = (int)dirs.size();
   for (size_t i = 0; i < dirs.size(); i++) {

@@ -217,6 +217,11 @@ struct Random {
 constexpr uint64_t kFnvOffset = 0xcbf29ce484222325ull;
 constexpr uint64_t kFnvPrime = 0x100000001b3ull;
 constexpr uint64_t kVolumeStreamHash = ((kFnvOffset ^ (kFnvPrime * 0ull)) * kFnvPrime ^ 0ull) * kFnvPrime ^ 0ull;
+// hash(a, b, c) (barney-common.h:132-146): the stream id of instance a,
+// geometry b, primitive c
+GBV_HD uint64_t fnv_hash3(uint32_t a, uint32_t b, uint32_t c) {
+  return (((kFnvOffset ^ (kFnvPrime * (uint64_t)a)) * kFnvPrime ^ (uint64_t)b) * kFnvPrime) ^ (uint64_t)c;
+}
 
 // Volume.h:174-184: three-term atanh series for log
 GBV_HD float fastLog(float f) {

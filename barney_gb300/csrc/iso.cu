@@ -6,9 +6,10 @@
 // and a cell whose range holds it is cut into 10 sub-steps; the first
 // sub-step whose end samples bracket the iso value gives the hit t by linear
 // interpolation.  The normal is the central difference of the field at
-// +-delta per axis, one-sided where a sample falls outside the field.
-// Materials, opacity and hit IDs of the reference's surface path are not on
-// this path: the query returns t, the hit point and the unit normal.
+// +-delta per axis, one-sided where a sample falls outside the field
+// (iso_search, shared with the frame render).  The query returns t, the hit
+// point and the unit normal; the frame render adds the material (opacity,
+// Lambertian) and the surface shading (gbv_scene.iso).
 #include "render_kernel.cuh"
 
 namespace gbv {
@@ -59,63 +60,11 @@ __global__ void __launch_bounds__(128) iso_kernel(const IsoParams p, const float
   Ctr<false> cnt;
   // box test, zero-direction guard and DDA set-up, as for a volume ray
   if (trace_begin(p.F, p.G, p.rcpMc, vec3(r0.x, r0.y, r0.z), vec3(r1.x, r1.y, r1.z), tmax, seed, T, cnt)) {
-    const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
-    const int maxCells = p.G.M[0] + p.G.M[1] + p.G.M[2] + 8;
-    float tHit = tmax;
-    bool stopped = false;
-    for (int it = 0; it < maxCells; it++) {
-      const float tc = reduce_min(T.t_next);
-      const float t0 = T.ray_t0 + T.ncb;
-      const float t1 = T.ray_t0 + mn(tc, T.tMax);
-      // the iso lambda (MCAccelerator.h:405-471)
-      if (!(t0 >= mn(t1, tmax))) {
-        const float2 vr = __ldg(p.ranges + (T.cx + p.G.M[0] * (T.cy + p.G.M[1] * T.cz)));
-        if (p.iso >= vr.x && p.iso <= vr.y) {
-          float tt1 = t0;
-          float ff1 = sample_field(p.F, store, T.org + tt1 * T.dir);
-#pragma unroll 1
-          for (int i = 1; i <= 10; i++) {
-            const float tt0 = tt1;
-            const float ff0 = ff1;
-            tt1 = lerp_l((float)i / 10.f, t0, t1);
-            ff1 = sample_field(p.F, store, T.org + tt1 * T.dir);
-            if (isnan(ff0) || isnan(ff1)) continue;
-            if (p.iso >= mn(ff0, ff1) && p.iso <= mx(ff0, ff1)) {
-              float t = (p.iso - ff0) / (ff1 - ff0);
-              t = lerp_l(t, tt0, tt1);
-              tHit = mn(tHit, t);
-              if (tHit < tmax) {
-                stopped = true;
-                break;
-              }
-            }
-          }
-        }
-      }
-      if (stopped || !trace_advance(T, tc, sx, sy, sz)) break;
-    }
-    if (tHit < tmax) {
-      const vec3 P = T.org + tHit * T.dir;
-      const float d = p.delta;
-      const float fP = sample_field(p.F, store, P);
-      float fx0 = sample_field(p.F, store, P + vec3(-d, 0.f, 0.f));
-      float fx1 = sample_field(p.F, store, P + vec3(+d, 0.f, 0.f));
-      float fy0 = sample_field(p.F, store, P + vec3(0.f, -d, 0.f));
-      float fy1 = sample_field(p.F, store, P + vec3(0.f, +d, 0.f));
-      float fz0 = sample_field(p.F, store, P + vec3(0.f, 0.f, -d));
-      float fz1 = sample_field(p.F, store, P + vec3(0.f, 0.f, +d));
-      float dx = 2.f, dy = 2.f, dz = 2.f;
-      if (isnan(fx0)) { dx -= 1.f; fx0 = fP; }
-      if (isnan(fx1)) { dx -= 1.f; fx1 = fP; }
-      if (isnan(fy0)) { dy -= 1.f; fy0 = fP; }
-      if (isnan(fy1)) { dy -= 1.f; fy1 = fP; }
-      if (isnan(fz0)) { dz -= 1.f; fz0 = fP; }
-      if (isnan(fz1)) { dz -= 1.f; fz1 = fP; }
-      vec3 N(dx == 0.f ? 0.f : (fx1 - fx0) / dx, dy == 0.f ? 0.f : (fy1 - fy0) / dy,
-             dz == 0.f ? 0.f : (fz1 - fz0) / dz);
-      if (is_zero(N)) N = -normalize(T.dir);
-      N = normalize(N);
-      h0 = make_float4(tHit, P.x, P.y, P.z);
+    float t;
+    vec3 N;
+    if (iso_search(p.F, store, p.G, p.ranges, p.iso, p.delta, T, tmax, t, N)) {
+      const vec3 P = T.org + t * T.dir;
+      h0 = make_float4(t, P.x, P.y, P.z);
       h1 = make_float4(N.x, N.y, N.z, 1.f);
     }
   }

@@ -121,7 +121,54 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   p.rank = 0;
   p.numRanks = 1;
   p.capFlag = nullptr;
+  // the world's instances (gbv_iso_surface): the volume's and the
+  // iso-surface's stream hashes and their order
+  p.hasVolume = s->d_majorants != nullptr;
+  if (!p.hasVolume) p.G.maj = nullptr;
+  if (s->volume_instance < 0) return set_error(GBV_ERROR_INVALID_ARGUMENT, "volume_instance must be >= 0");
+  p.volHash = fnv_hash3((uint32_t)s->volume_instance, 0, 0);
+  p.isoOn = s->iso != nullptr;
+  p.isoFirst = 0;
+  p.isoValue = p.isoDelta = 0.f;
+  p.isoAlpha = 1.f;
+  p.isoRanges = nullptr;
+  p.isoAlbedo = vec3(0.f);
+  p.isoHash = 0;
+  if (p.isoOn) {
+    const gbv_iso_surface &iso = *s->iso;
+    if (!iso.d_ranges) return set_error(GBV_ERROR_INVALID_ARGUMENT, "iso-surface without macrocell ranges");
+    if (iso.instance < 0 || (p.hasVolume && iso.instance == s->volume_instance))
+      return set_error(GBV_ERROR_INVALID_ARGUMENT,
+                       "iso-surface instance must be >= 0 and differ from the volume's");
+    p.isoFirst = !p.hasVolume || iso.instance < s->volume_instance;
+    p.isoHash = fnv_hash3((uint32_t)iso.instance, 0, 0);
+    p.isoValue = iso.iso_value;
+    p.isoRanges = reinterpret_cast<const float2 *>(iso.d_ranges);
+    // MCAccelerator.h:476-479: delta = |bounds size| * .1 / (Mx + My + Mz)
+    const vec3 size = p.F.boundsHi - p.F.boundsLo;
+    p.isoDelta = sqrtf(dot(size, size)) * .1f / (float)(p.G.M[0] + p.G.M[1] + p.G.M[2]);
+    // AnariMatte::DD::createBSDF (AnariMatte.h:50-62) with VALUE parameters
+    // (PossiblyMappedParameter::DD::eval, Material.h:101-106: a NaN value
+    // reads as (0, 0, 0, 1); opacity is (opacity, 0, 0, 1))
+    float c[4] = {iso.color[0], iso.color[1], iso.color[2], iso.color[3]};
+    if (c[0] != c[0]) {
+      c[0] = c[1] = c[2] = 0.f;
+      c[3] = 1.f;
+    }
+    const float opacity = iso.opacity != iso.opacity ? 0.f : iso.opacity;
+    const float reflectance = .85f;
+    p.isoAlbedo = reflectance * vec3(c[0], c[1], c[2]) * kOneOverPi;
+    p.isoAlpha = c[3] * opacity;
+  }
   return GBV_OK;
+}
+
+// A scene's field, and its volume unless an iso-surface stands alone
+// (gbv_scene.iso with d_majorants == 0).
+static bool scene_complete(const gbv_scene *s) {
+  if (!s->d_voxels || (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0)) return false;
+  const bool volume = s->d_majorants != nullptr || s->iso == nullptr;
+  return !volume || (s->d_majorants && s->d_tf && s->tf_n >= 2);
 }
 
 }  // namespace gbv
@@ -167,8 +214,7 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
     snprintf(msg, sizeof msg, "%s: rank must be in [0, num_ranks) and num_ranks >= 1", fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
-  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 ||
-      (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0)) {
+  if (!scene_complete(s)) {
     snprintf(msg, sizeof msg, "%s: scene lacks voxels, majorants or a transfer function", fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
   }
@@ -186,6 +232,10 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
     snprintf(msg, sizeof msg, "%s: launch config out of range (blocks 4..6, threshold 0..100, skip 0..1024, stage 0..3, mode 0..1)",
              fn);
     return set_error(GBV_ERROR_INVALID_ARGUMENT, msg);
+  }
+  if (s->iso && lc.mode == GBV_RENDER_WAVEFRONT) {
+    snprintf(msg, sizeof msg, "%s: the wavefront mode renders volume-only worlds", fn);
+    return set_error(GBV_ERROR_UNSUPPORTED, msg);
   }
   if (spp == 0) return GBV_OK;
   gbv_status st = fill_params(s, p);
@@ -319,8 +369,7 @@ extern "C" gbv_status gbv_render_noalloc(const gbv_scene *s, float *d_accum, int
   if (tiles > kNoAllocMaxTiles)
     return set_error(GBV_ERROR_INVALID_ARGUMENT,
                      "gbv_render_noalloc: frame exceeds the 2^30 tiles of 8x4 pixels its 32-bit tile counter holds");
-  if (!s->d_voxels || !s->d_majorants || !s->d_tf || s->tf_n < 2 ||
-      (s->layout != GBV_LAYOUT_NANOVDB && s->cells_per_mc <= 0))
+  if (!scene_complete(s))
     return set_error(GBV_ERROR_INVALID_ARGUMENT,
                      "gbv_render_noalloc: scene lacks voxels, majorants or a transfer function");
   if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
@@ -375,6 +424,7 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
       return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_batch_create: an item lacks data or has an empty frame");
     if (s->format != scenes[0].format || s->layout != scenes[0].layout)
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: items must share voxel format and layout");
+    if (s->iso) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: batches render volume-only worlds");
     if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: the linear layout holds FP32 voxels only");
     if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)

@@ -71,6 +71,16 @@ struct RenderParams {
   // frame partition across ranks (TiledFB.cu:226-255): with numRanks > 1
   // this launch renders only the 32x32-pixel tiles rank, rank + numRanks, ...
   int rank, numRanks;
+  // the world's instances: the volume's stream hash, and an iso-surface
+  // (gbv_iso_surface) with its matte material, intersected before the
+  // volume when its instance index is the lower one
+  uint64_t volHash;
+  int hasVolume;
+  int isoOn, isoFirst;
+  float isoValue, isoDelta, isoAlpha;
+  const float2 *isoRanges;
+  vec3 isoAlbedo;
+  uint64_t isoHash;
 };
 
 // The reference frame buffer's tiles (TiledFB tileSize) and their
@@ -428,8 +438,12 @@ __device__ __forceinline__ vec3 random_direction(Random &rng) {
   return vec3(0.f, 0.f, 1.f);
 }
 
-// shadeRays.cu:141-191 (the world's only normal here is the volume's N=0)
-__device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random &random, LightSample &ls) {
+// shadeRays.cu:141-191.  Surf = false: a volume hit, whose normal is zero
+// (weight 1); Surf = true: the light's weight is dot(lightDir, N) for the
+// front-facing surface normal N.
+template <bool Surf = false>
+__device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random &random, LightSample &ls,
+                                                  vec3 N = vec3()) {
   if (p.numDir == 0) return false;
   int lID[2];
   float weights[2];
@@ -441,6 +455,10 @@ __device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random 
     const DirLightDev &light = p.dir[lID[i]];
     vec3 lr = light.color * light.radiance;
     float weight = 1.f;  // N == 0
+    if (Surf) {
+      weight = is_zero(N) ? 1.f : dot(-light.direction, N);
+      if (weight <= 1e-3f) continue;
+    }
     weight *= reduce_max(lr);
     if (weight <= 1e-3f) continue;
     weights[i] = weight;
@@ -459,9 +477,12 @@ __device__ __forceinline__ bool sample_dir_lights(const RenderParams &p, Random 
   return weights[i] != 0.f;
 }
 
-// shadeRays.cu:268-404 (no area or point lights in this world)
+// shadeRays.cu:268-404 (no area or point lights in this world).  Surf:
+// sampling at a surface of front-facing normal N, where the ambient light's
+// direction turns into N's hemisphere (radiance 2 pi ambient, pdf 1/(2 pi)).
+template <bool Surf = false>
 __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &random, const EnvPick &pick,
-                                              LightSample &ls, bool &needsMIS, bool &isDir) {
+                                              LightSample &ls, bool &needsMIS, bool &isDir, vec3 N = vec3()) {
   needsMIS = false;
   LightSample els;
   if (p.hasEnv) {
@@ -470,13 +491,19 @@ __device__ __forceinline__ bool sample_lights(const RenderParams &p, Random &ran
   } else {
     els.direction = random_direction(random);
     els.distance = __int_as_float(0x7f800000);
-    els.radiance = vec3(kFourPi * p.ambient);
-    els.pdf = kOneOverFourPi;
+    if (Surf && !is_zero(N)) {
+      els.radiance = vec3(kTwoPi * p.ambient);
+      if (dot(els.direction, N) < 0.f) els.direction = -els.direction;
+      els.pdf = kOneOverTwoPi;
+    } else {
+      els.radiance = vec3(kFourPi * p.ambient);
+      els.pdf = kOneOverFourPi;
+    }
   }
   float elsWeight = reduce_max(els.radiance);
   LightSample dls;
   dls.pdf = 0.f;
-  float dlsWeight = sample_dir_lights(p, random, dls) ? reduce_max(dls.radiance) : 0.f;
+  float dlsWeight = sample_dir_lights<Surf>(p, random, dls, N) ? reduce_max(dls.radiance) : 0.f;
   float alsWeight = 0.f, plsWeight = 0.f;
   float sumWeights = alsWeight + dlsWeight + elsWeight + plsWeight;
   if (sumWeights == 0.f) return false;
@@ -558,6 +585,7 @@ struct PathRay {
   vec3h tp;
   float misWeight;
   int numVolumeBounces;
+  int numDiffuseBounces;  // surface bounces (iso-surface worlds only)
 };
 
 struct ShadeOut {
@@ -652,6 +680,105 @@ static __device__ __noinline__ void bounce_volume_hit_ool(const RenderParams &p,
                                                       ShadeOut &out) {
   bounce_volume_hit(p, ray, h, P, pathDepth, random, pick, out);
 }
+// owl::common::frame: the orthonormal frame about a unit normal N that
+// xfmVector(frame(N), v) uses -- dx the longer of (1,0,0) x N and
+// (0,1,0) x N, normalized, dy = normalize(N x dx)
+__device__ __forceinline__ void frame_of(vec3 N, vec3 &dx, vec3 &dy) {
+  const vec3 dx0 = cross(vec3(1.f, 0.f, 0.f), N), dx1 = cross(vec3(0.f, 1.f, 0.f), N);
+  dx = normalize(dot(dx0, dx0) > dot(dx1, dx1) ? dx0 : dx1);
+  dy = normalize(cross(N, dx));
+}
+// Lambertian::pdf (packedBSDF/Lambertian.h:46-55): the cosine-hemisphere
+// pdf about the normal turned toward wi
+__device__ __forceinline__ float lambert_pdf(vec3 Ng, vec3 wi) {
+  const vec3 N = dot(wi, Ng) < 0.f ? -Ng : Ng;
+  return mx(dot(wi, N), 0.f) * kOneOverPi;
+}
+
+// bounce() for an iso-surface hit (shadeRays.cu:541-878 with isVolumeHit
+// false), the matte material's Lambertian (AnariMatte.h:50-62,
+// packedBSDF/Lambertian.h:57-90): Ng = normalize(ray.N), offsets and light
+// sampling along the front-facing normal, the cosine factors of the surface
+// branches and a diffuse scatter, at most MAX_DIFFUSE_BOUNCES = 1 per path
+// (shadeRays.cu:18, 795-808).  Updates `ray` like bounce_volume_hit.
+static __device__ __noinline__ void bounce_surface_hit(const RenderParams &p, PathRay &ray, vec3h Nh, float tHit,
+                                                      vec3 P, int pathDepth, Random &random, const EnvPick &pick,
+                                                      ShadeOut &out) {
+  out.shadowValid = false;
+  const vec3 Ng = normalize(from_half(Nh));
+  const vec3 Ngff = dot(ray.dir, Ng) < 0.f ? Ng : -Ng;
+  const vec3 incomingThroughput = from_half(ray.tp);
+  const vec3 wo = -normalize(ray.dir);
+  const float offsetEpsilon = mx(1e-4f, 1e-6f * reduce_max(vabs(P)));
+  LightSample ls;
+  bool needsMIS = false, isDir = false;
+  if (sample_lights<true>(p, random, pick, ls, needsMIS, isDir, Ngff)) {
+    // Lambertian::eval: the cosine against the unflipped normal
+    const float cosThetaI = mx(dot(ls.direction, Ng), 0.f);
+    vec3 fr = p.isoAlbedo * kOneOverPi * cosThetaI;
+    if (!(cosThetaI * kOneOverPi > 0.f) || reduce_max(fr) < 1e-4f) {
+      out.shadowValid = false;
+    } else {
+      fr = vmin(fr, vec3(13.f));
+      vec3 tp_sr = incomingThroughput * (isinf(ls.pdf) ? 1.f : 1.f / ls.pdf) * fr * ls.radiance *
+                   (kOneOverPi * fabsf(dot(Ng, ls.direction)));
+      out.shadow.dir = ls.direction;
+      out.shadow.org = P + offsetEpsilon * Ngff;
+      out.shadow.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
+      out.shadow.tp = to_half(tp_sr);
+      out.shadow.seed = ray.seed;
+      ray.seed.next_h((uint64_t)float_bits(tHit));
+      out.shadow.misWeight = 1.f;
+      out.shadowValid = true;
+      if (!isDir && needsMIS) {
+        const float pdf_l = env_pdf(p, ls.direction);
+        const float pdf_s = lambert_pdf(Ng, ls.direction);
+        out.shadow.misWeight = pdf_l / (pdf_l + pdf_s + 1e-10f);
+        if (out.shadow.misWeight < 1e-5f) out.shadowValid = false;
+      }
+    }
+  }
+  if (pathDepth >= 10) {  // MAX_PATH_DEPTH
+    ray.tMax = -1.f;
+    return;
+  }
+  ray.tMax = __int_as_float(0x7f800000);
+  // Lambertian::scatter: cosineSampleHemisphere (DG.h:135-168) about the
+  // normal turned toward wo.  Its vec2f s(random(), random()) takes the
+  // second argument's draw first, as the reference's CPU backend (built
+  // with gcc, which evaluates arguments right to left) does.
+  const vec3 N = dot(wo, Ng) < 0.f ? -Ng : Ng;
+  const float r0 = random();
+  const float r1 = random();
+  const float phi = kTwoPi * r1;
+  const float cosTheta = sqrtf(r0);
+  const float sinTheta = sqrtf(1.0f - r0);
+  float sinPhi, cosPhi;
+  sincos_angle(phi, sinPhi, cosPhi);  // phi in [0, 2 pi)
+  vec3 dx, dy;
+  frame_of(N, dx, dy);
+  const vec3 sdir = dx * (cosPhi * sinTheta) + dy * (sinPhi * sinTheta) + N * cosTheta;
+  const float spdf = cosTheta * kOneOverPi;
+  if (!(spdf > 0.f) || spdf <= 1e-6f) return;  // the ray stays alive unchanged
+  if (ray.numDiffuseBounces >= 1) {
+    ray.tMax = -1.f;
+    return;
+  }
+  ray.numDiffuseBounces = ray.numDiffuseBounces + 1;
+  ray.org = P + (1.f * offsetEpsilon) * Ngff;
+  ray.dir = normalize(sdir);
+  vec3 scatterFactor = p.isoAlbedo * fabsf(dot(Ng, normalize(ray.dir))) / (isinf(spdf) ? 1.f : (spdf + 1e-10f));
+  scatterFactor = vmin(scatterFactor, vec3(2.5f));
+  ray.tp = to_half(from_half(ray.tp) * scatterFactor);
+  if (needsMIS && !isinf(spdf)) {
+    const float pdf_s = lambert_pdf(Ng, ray.dir);
+    const float pdf_l = env_pdf(p, ray.dir);
+    ray.misWeight = pdf_s / (pdf_s + pdf_l);
+  } else {
+    ray.misWeight = 1.f;
+  }
+}
+
 static __device__ __noinline__ float4 tex2D_ool(const EnvDev &e, float u, float v) { return tex2D(e, u, v); }
 static __device__ __noinline__ float2 env_miss_coords_ool(const RenderParams &p, vec3 rayDir) {
   return env_miss_coords(p, rayDir);
@@ -716,10 +843,12 @@ __device__ __forceinline__ float majorant_at(const MCGridDev &G, int cx, int cy,
 
 // Box test, RNG stream and DDA set-up.  Returns false when the ray reaches
 // no cell.  `seed` advances exactly when the reference advances ray.rngSeed
-// (once the box test passes).
+// (once the box test passes); the stream is Random2(seed, streamHash), the
+// hash of the geometry's instance (hash(0, 0, 0) for a lone volume).
 template <class Cnt>
 __device__ __forceinline__ bool trace_begin(const FieldGeom &F, const MCGridDev &G, const vec3 &rcpMc, vec3 org,
-                                            vec3 rayDir, float rayTMax, RNGSeed &seed, Traversal &T, Cnt &cnt) {
+                                            vec3 rayDir, float rayTMax, RNGSeed &seed, Traversal &T, Cnt &cnt,
+                                            uint64_t streamHash = kVolumeStreamHash) {
   GBV_COUNT(cnt, rays);
   vec3 dir = rayDir;
   if (dir.x == 0.f) dir.x = 1e-6f;
@@ -730,7 +859,7 @@ __device__ __forceinline__ bool trace_begin(const FieldGeom &F, const MCGridDev 
   if (!box_test(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return false;
   const vec3 dda_org = (org - G.origin) * rcpMc;
   const vec3 dda_dir = dir * rcpMc;
-  T.rng = Random::derive(seed, kVolumeStreamHash);
+  T.rng = Random::derive(seed, streamHash);
   const float tMax = tHi;
   const vec3 f_size((float)G.M[0], (float)G.M[1], (float)G.M[2]);
   const vec3 rcp_dir = rcp(dda_dir);
@@ -875,6 +1004,102 @@ __device__ __forceinline__ int trace_sample(const FieldGeom &F, const Store &sto
   return TR_CONTINUE;
 }
 
+// The hit search and normal of MCIsoSurfaceAccel::isProg
+// (MCAccelerator.h:393-503) along a DDA that trace_begin set up: per
+// macrocell whose scalar range holds the iso value, the cell's t range is
+// cut into 10 sub-steps; the first sub-step whose end values bracket the
+// value gives the hit t by linear interpolation.  The normal is the central
+// difference of the field at +-delta per axis, one-sided where a sample
+// falls outside the field, normalized.  Returns whether t < tmax.
+template <class Store>
+__device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &store, const MCGridDev &G,
+                                           const float2 *__restrict__ ranges, float iso, float delta, Traversal &T,
+                                           float tmax, float &tOut, vec3 &N) {
+  const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
+  const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
+  float tHit = tmax;
+  bool stopped = false;
+#pragma unroll 1
+  for (int it = 0; it < maxCells; it++) {
+    const float tc = reduce_min(T.t_next);
+    const float t0 = T.ray_t0 + T.ncb;
+    const float t1 = T.ray_t0 + mn(tc, T.tMax);
+    // the iso lambda (MCAccelerator.h:405-471)
+    if (!(t0 >= mn(t1, tmax))) {
+      const float2 vr = __ldg(ranges + (T.cx + G.M[0] * (T.cy + G.M[1] * T.cz)));
+      if (iso >= vr.x && iso <= vr.y) {
+        float tt1 = t0;
+        float ff1 = sample_field(F, store, T.org + tt1 * T.dir);
+#pragma unroll 1
+        for (int i = 1; i <= 10; i++) {
+          const float tt0 = tt1;
+          const float ff0 = ff1;
+          tt1 = lerp_l((float)i / 10.f, t0, t1);
+          ff1 = sample_field(F, store, T.org + tt1 * T.dir);
+          if (isnan(ff0) || isnan(ff1)) continue;
+          if (iso >= mn(ff0, ff1) && iso <= mx(ff0, ff1)) {
+            float t = (iso - ff0) / (ff1 - ff0);
+            t = lerp_l(t, tt0, tt1);
+            tHit = mn(tHit, t);
+            if (tHit < tmax) {
+              stopped = true;
+              break;
+            }
+          }
+        }
+      }
+    }
+    if (stopped || !trace_advance(T, tc, sx, sy, sz)) break;
+  }
+  if (!(tHit < tmax)) return false;
+  const vec3 P = T.org + tHit * T.dir;
+  const float d = delta;
+  const float fP = sample_field(F, store, P);
+  float fx0 = sample_field(F, store, P + vec3(-d, 0.f, 0.f));
+  float fx1 = sample_field(F, store, P + vec3(+d, 0.f, 0.f));
+  float fy0 = sample_field(F, store, P + vec3(0.f, -d, 0.f));
+  float fy1 = sample_field(F, store, P + vec3(0.f, +d, 0.f));
+  float fz0 = sample_field(F, store, P + vec3(0.f, 0.f, -d));
+  float fz1 = sample_field(F, store, P + vec3(0.f, 0.f, +d));
+  float dx = 2.f, dy = 2.f, dz = 2.f;
+  if (isnan(fx0)) { dx -= 1.f; fx0 = fP; }
+  if (isnan(fx1)) { dx -= 1.f; fx1 = fP; }
+  if (isnan(fy0)) { dy -= 1.f; fy0 = fP; }
+  if (isnan(fy1)) { dy -= 1.f; fy1 = fP; }
+  if (isnan(fz0)) { dz -= 1.f; fz0 = fP; }
+  if (isnan(fz1)) { dz -= 1.f; fz1 = fP; }
+  N = vec3(dx == 0.f ? 0.f : (fx1 - fx0) / dx, dy == 0.f ? 0.f : (fy1 - fy0) / dy,
+           dz == 0.f ? 0.f : (fz1 - fz0) / dz);
+  if (is_zero(N)) N = -normalize(T.dir);
+  N = normalize(N);
+  tOut = tHit;
+  return true;
+}
+
+// The iso-surface's intersection program for a render ray (org, rayDir,
+// [0, tmax]): the box test and the geometry's random stream
+// Random2(seed, hash(instance, 0, 0)), which advances `seed`; the hit
+// search; the material's opacity test (opacity < 1: the ray passes when
+// rng() > opacity, MCAccelerator.h:533-539); and Ray::setHit's record (the
+// hit point and the normal in half precision).  Returns whether the surface
+// records a hit.
+template <class Store>
+static __device__ __noinline__ bool iso_trace(const RenderParams &p, vec3 org, vec3 rayDir, float tmax, RNGSeed &seed,
+                                              float &tOut, vec3 &P, vec3h &Nh) {
+  Traversal T;
+  Ctr<false> none;
+  if (!trace_begin(p.F, p.G, p.rcpMc, org, rayDir, tmax, seed, T, none, p.isoHash)) return false;
+  float t;
+  vec3 N;
+  if (!iso_search(p.F, make_store<Store>(p), p.G, p.isoRanges, p.isoValue, p.isoDelta, T, tmax, t, N))
+    return false;
+  if (p.isoAlpha < 1.f && T.rng() > p.isoAlpha) return false;
+  tOut = t;
+  P = T.org + t * T.dir;
+  Nh = to_half(N);
+  return true;
+}
+
 // -------------------------------------------------------------------------
 // The persistent frame kernel.  Each lane owns one pixel for all of the
 // launch's passes, so fragments accumulate in the reference's order
@@ -918,6 +1143,7 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
   ray.tp = vec3h{0x3c00, 0x3c00, 0x3c00};  // 1.0 in half
   ray.misWeight = 0.f;
   ray.numVolumeBounces = 0;
+  ray.numDiffuseBounces = 0;
 }
 
 // Batch: the launch renders `numItems` scenes (items[]), whose 8x4-pixel
@@ -931,10 +1157,15 @@ __device__ __forceinline__ void generate_primary(const RenderParams &p, int ix, 
 // p0 is __grid_constant__ so that helpers (inlined, or the batched kernel's
 // out-of-line copies) can take it by reference without a copy to local
 // memory.
-template <class Store, int MinBlocks, bool Batch, bool Count>
+// Iso: the world holds an iso-surface (p0.isoOn; never batched): each trace
+// also runs its intersection program, before the volume's when its instance
+// index is the lower one (p0.isoFirst) and otherwise after it, each bounded
+// by the other's hit, and shading takes the surface branch on its hits.
+template <class Store, int MinBlocks, bool Batch, bool Count, bool Iso = false>
 __global__ void __launch_bounds__(kThreads, MinBlocks)
     render_kernel(const __grid_constant__ RenderParams p0, const RenderParams *__restrict__ items,
                   const long long *__restrict__ tileStart, int numItems, int *__restrict__ pool) {
+  static_assert(!(Iso && Batch), "batched launches render volume-only worlds");
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const RenderParams &L = p0;  // launch-wide settings
@@ -973,6 +1204,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
   Traversal T;
   Hit h;
   h.hit = false;
+  // the iso-surface's hit of the current trace (Iso only)
+  bool sHit = false;
+  float sT = 0.f;
+  vec3 sP;
+  vec3h sN{0, 0, 0};
   unsigned long long cyc[3] = {0ull, 0ull, 0ull};
   // profile: traversal iterations and tracing lanes summed over them, shading
   // passes and shaded lanes summed over them (lane 0 of each warp counts)
@@ -1051,9 +1287,21 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       h.hit = false;
       kind = shadowPending ? K_SHADOW : K_MAIN;
       RNGSeed seed = shadowPending ? sray.seed : ray.seed;
-      const bool active = trace_begin(p.F, p.G, p.rcpMc, shadowPending ? sray.org : ray.org,
-                                      shadowPending ? sray.dir : ray.dir, shadowPending ? sray.tMax : ray.tMax, seed,
-                                      T, cnt);
+      bool active;
+      if (Iso) {
+        const vec3 org = shadowPending ? sray.org : ray.org, dir = shadowPending ? sray.dir : ray.dir;
+        float tmax = shadowPending ? sray.tMax : ray.tMax;
+        sHit = false;
+        if (!p.hasVolume) GBV_COUNT(cnt, rays);
+        if (p.isoFirst) {
+          sHit = iso_trace<Store>(p, org, dir, tmax, seed, sT, sP, sN);
+          if (sHit) tmax = sT;
+        }
+        active = p.hasVolume && trace_begin(p.F, p.G, p.rcpMc, org, dir, tmax, seed, T, cnt, p.volHash);
+      } else {
+        active = trace_begin(p.F, p.G, p.rcpMc, shadowPending ? sray.org : ray.org, shadowPending ? sray.dir : ray.dir,
+                             shadowPending ? sray.tMax : ray.tMax, seed, T, cnt);
+      }
       if (shadowPending) sray.seed = seed;
       else ray.seed = seed;
       tstate = active ? TRACING : DONE;
@@ -1095,18 +1343,25 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         simt[3] += shading;
       }
     }
+    if (Iso && tstate == DONE && p.hasVolume && !p.isoFirst) {
+      // the iso-surface after the volume, up to the volume's hit
+      PathRay &r = kind == K_SHADOW ? sray : ray;
+      sHit = iso_trace<Store>(p, r.org, r.dir, h.hit ? h.t : r.tMax, r.seed, sT, sP, sN);
+      if (sHit) h.hit = false;
+    }
     if (tstate == DONE) {
       // Env-map texels: a main ray's miss lookup (radianceFromEnv) and a
-      // volume hit's env light sample (EnvMap::sample) each form their
-      // texture coordinates first; then one call fetches the texels of all
-      // lanes that need one, instead of one call per kind of lane.
+      // hit's env light sample (EnvMap::sample) each form their texture
+      // coordinates first; then one call fetches the texels of all lanes
+      // that need one, instead of one call per kind of lane.
       Random rnd;
       EnvPick pick;
       float2 uv = make_float2(0.f, 0.f);
       bool needTex = false;
+      const bool anyHit = h.hit || (Iso && sHit);
       if (kind == K_MAIN) {
-        if (h.hit) {
-          rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.t));
+        if (anyHit) {
+          rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.hit ? h.t : sT));
           if (p.hasEnv) {
             pick = Batch ? env_pick_coords_ool(p, rnd) : env_pick_coords(p, rnd);
             uv = make_float2(pick.sx, pick.sy);
@@ -1126,12 +1381,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       const int accumID = L.accumIdStart + s;
       const float clampMax = 10.f * (float)(1 + accumID);
       if (kind == K_SHADOW) {
-        if (!h.hit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
+        if (!anyHit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
         shadowPending = false;
       } else {
         vec3 frag(0.f);
         float alpha = 0.f;
-        if (!h.hit) {
+        if (!anyHit) {
           const float4 miss = miss_color(p, iy);
           const vec3 env = p.hasEnv ? texel : (gen != 0 ? vec3(p.ambient) : vec3(0.f));
           if (gen == 0) {
@@ -1146,7 +1401,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
           ShadeOut so;
           // setVolumeHit's P = obj_org + t * obj_dir (MCAccelerator.h:79)
           pick.radiance = texel;
-          if (Batch)
+          if (Iso && !h.hit)
+            bounce_surface_hit(p, ray, sN, sT, sP, gen, rnd, pick, so);
+          else if (Batch)
             bounce_volume_hit_ool(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
           else
             bounce_volume_hit(p, ray, h, T.org + h.t * T.dir, gen, rnd, pick, so);
@@ -1204,6 +1461,22 @@ inline size_t staged_words(const RenderParams &p) {
   return (size_t)end;
 }
 
+// The one-scene render kernels of a launch: with and without event
+// counting, for a volume-only world or (at 4 resident blocks per SM) one
+// with an iso-surface.
+using RenderKernelFn = void (*)(const RenderParams, const RenderParams *, const long long *, int, int *);
+template <class Store, int MinBlocks>
+inline void render_kernels(const RenderParams &p, RenderKernelFn &counting, RenderKernelFn &plain) {
+  counting = render_kernel<Store, MinBlocks, false, true>;
+  plain = render_kernel<Store, MinBlocks, false, false>;
+  if constexpr (MinBlocks == 4) {
+    if (p.isoOn) {
+      counting = render_kernel<Store, 4, false, true, true>;
+      plain = render_kernel<Store, 4, false, false, true>;
+    }
+  }
+}
+
 template <class Store, int MinBlocks>
 inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cudaStream_t stream) {
   // persistent grid: as many resident blocks as the device holds
@@ -1211,19 +1484,18 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st == GBV_OK) st = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   if (st != GBV_OK) return st;
+  RenderKernelFn kCount, kPlain;
+  render_kernels<Store, MinBlocks>(p, kCount, kPlain);
   const size_t smem = staged_words(p) * sizeof(uint32_t);
   if (smem > 48 * 1024) {
-    st = check_cuda(cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    st = check_cuda(cudaFuncSetAttribute(kCount, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "render_kernel: shared-memory size");
     if (st == GBV_OK)
-      st = check_cuda(cudaFuncSetAttribute(render_kernel<Store, MinBlocks, false, false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+      st = check_cuda(cudaFuncSetAttribute(kPlain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "render_kernel: shared-memory size");
     if (st != GBV_OK) return st;
   }
-  st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, MinBlocks, false, true>,
-                                                                kThreads, smem),
+  st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kCount, kThreads, smem),
                   "render_kernel: occupancy");
   if (st != GBV_OK) return st;
   const long long tiles = warp_tile_count(p);
@@ -1249,12 +1521,7 @@ inline gbv_status launch_render_t(const RenderParams &p, const Store &store, cud
     q.maskSrc = mask;
   }
   if (st == GBV_OK) {
-    if (p.counters)
-      render_kernel<Store, MinBlocks, false, true><<<(unsigned)blocks, kThreads, smem, stream>>>(q, nullptr, nullptr,
-                                                                                                 0, pool);
-    else
-      render_kernel<Store, MinBlocks, false, false><<<(unsigned)blocks, kThreads, smem, stream>>>(q, nullptr, nullptr,
-                                                                                                  0, pool);
+    (p.counters ? kCount : kPlain)<<<(unsigned)blocks, kThreads, smem, stream>>>(q, nullptr, nullptr, 0, pool);
     st = check_launch("render_kernel");
   }
   const gbv_status fst = check_cuda(cudaFreeAsync(pool, stream), "cudaFreeAsync(tile pool)");
@@ -1291,7 +1558,7 @@ inline void plan_staging(RenderParams &p, int stage) {
   p.cdfYOff = p.pivOff = p.rowOff = -1;
   p.pivPerRow = 0;
   p.maskSrc = nullptr;
-  if (any && nmc > 0 && (((nmc + 31) / 32 + 3) & ~3ll) <= budget) {
+  if (any && nmc > 0 && p.hasVolume && (((nmc + 31) / 32 + 3) & ~3ll) <= budget) {
     p.maskWords = (int)(((nmc + 31) / 32 + 3) & ~3ll);  // whole 16-byte units (one bulk copy)
     used = p.maskWords;
   }
@@ -1318,7 +1585,7 @@ template <class Store>
 inline gbv_status launch_render(RenderParams p, const Store &store, cudaStream_t stream, const LaunchChoice &lc) {
   plan_staging(p, lc.stage);
   if (!p.counters) p.profile = 0;
-  if (lc.occ <= 4) return launch_render_t<Store, 4>(p, store, stream);
+  if (lc.occ <= 4 || p.isoOn) return launch_render_t<Store, 4>(p, store, stream);
   if (lc.occ >= 6) return launch_render_t<Store, 6>(p, store, stream);
   return launch_render_t<Store, 5>(p, store, stream);
 }
@@ -1334,11 +1601,12 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   p.pivPerRow = 0;
   p.profile = 0;
   int dev = 0, sms = 0, perSM = 0;
+  RenderKernelFn kCount, kPlain;
+  render_kernels<Store, 4>(p, kCount, kPlain);
   gbv_status st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
   if (st == GBV_OK) st = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
   if (st == GBV_OK)
-    st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, render_kernel<Store, 4, false, true>,
-                                                                  kThreads, 0),
+    st = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kCount, kThreads, 0),
                     "render_kernel: occupancy");
   if (st != GBV_OK) return st;
   const long long tiles = warp_tile_count(p);
@@ -1349,10 +1617,7 @@ inline gbv_status launch_render_noalloc(RenderParams p, const Store &store, cuda
   if (blocks < 1) blocks = 1;
   st = check_cuda(cudaMemsetAsync(pool, 0, sizeof(int), stream), "gbv_render_noalloc: clearing the tile pool");
   if (st != GBV_OK) return st;
-  if (p.counters)
-    render_kernel<Store, 4, false, true><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
-  else
-    render_kernel<Store, 4, false, false><<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
+  (p.counters ? kCount : kPlain)<<<(unsigned)blocks, kThreads, 0, stream>>>(p, nullptr, nullptr, 0, pool);
   return check_launch("render_kernel (noalloc)");
 }
 

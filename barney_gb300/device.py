@@ -155,6 +155,18 @@ class GpuScene:
         r.multi_scatter = s.multi_scatter
         r.volume_multi_scatter = s.volume_multi_scatter
         r.max_volume_bounces = s.max_volume_bounces
+        r.volume_instance = s.volume_instance
+        if s.iso is not None:
+            iso = N.GbvIsoSurface()
+            iso.iso_value = s.iso.value
+            iso.d_ranges = self.ranges.data_ptr()
+            iso.color[:] = [float(c) for c in s.iso.color]
+            iso.opacity = s.iso.opacity
+            iso.instance = s.iso.instance
+            self._iso_record = iso  # kept alive with the scene record's pointer to it
+            r.iso = C.addressof(iso)
+            if s.no_volume:
+                r.d_majorants = None
         return r
 
     # -- rendering --------------------------------------------------------------

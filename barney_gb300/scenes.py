@@ -38,6 +38,19 @@ class EnvMap:
 
 
 @dataclass
+class IsoSurface:
+    """An iso-surface of the scene's field (IsoSurface geometry) with a matte
+    material (AnariMatte: constant color and opacity).  `instance` is the RTC
+    instance index of the geometry's group in the world's instance list
+    (0 when it shares a group with the volume: a group's user geometries
+    come before its volumes)."""
+    value: float
+    color: tuple = (0.8, 0.8, 0.8, 1.0)  # AnariMatte default color (AnariMatte.h:43), alpha 1
+    opacity: float = 1.0
+    instance: int = 0
+
+
+@dataclass
 class Scene:
     scalars: np.ndarray                # (nz, ny, nx) float32
     tf: np.ndarray                     # (n, 4) float32 RGBA
@@ -62,6 +75,12 @@ class Scene:
     spp: int = 16
     origin: Optional[tuple] = None
     spacing: Optional[tuple] = None
+    # an iso-surface over the same field; the volume's RTC instance index
+    # (1 when the iso-surface shares its group); no_volume: the world holds
+    # the iso-surface only
+    iso: Optional[IsoSurface] = None
+    volume_instance: int = 0
+    no_volume: bool = False
 
     @property
     def dims(self) -> tuple:

@@ -141,6 +141,13 @@ BARNEY_API BNTexture2D bnTexture2DCreate(BNContext context, int whichSlot, BNDat
                                          BNTextureAddressMode addressMode_y BN_IF_CPP(= BN_TEXTURE_WRAP),
                                          BNTextureColorSpace colorSpace BN_IF_CPP(= BN_COLOR_SPACE_LINEAR));
 BARNEY_API BNLight bnLightCreate(BNContext context, int whichSlot, const char *type);
+/* "iso_surface" (IsoSurface: "scalarField", "isoValue", "material"); other
+   geometry types are outside this path and return 0 (barney.h:498-500,
+   barney/geometry/Geometry.cpp:26-43) */
+BARNEY_API BNGeom bnGeometryCreate(BNContext context, int whichSlot, const char *type);
+/* "matte" / "AnariMatte" (constant "color" and "opacity"); other material
+   types return 0 (barney.h:513-516, barney/material/Material.cpp:83-98) */
+BARNEY_API BNMaterial bnMaterialCreate(BNContext context, int whichSlot, const char *type);
 BARNEY_API BNGroup bnGroupCreate(BNContext context, int whichSlot, BNGeom *geoms, int numGeoms,
                                  BNVolume *volumes, int numVolumes);
 BARNEY_API void bnGroupBuild(BNGroup group);

@@ -181,6 +181,29 @@ gbv_status gbv_nanovdb_sample(const void *d_grid, const gbv_nanovdb_info *info, 
 /* ------------------------------------------------------------------------
  * Scene description for rendering (device pointers where marked d_).
  * ------------------------------------------------------------------------ */
+/* An iso-surface of the scene's field with a matte material: the
+   "iso_surface" geometry (IsoSurface, barney/geometry/IsoSurface.{h,cpp}:
+   "isoValue") and the "matte" material (AnariMatte,
+   barney/material/AnariMatte.{h,cpp}: "color", "opacity"), rendered as the
+   reference's surface path does (MCIsoSurfaceAccel::isProg,
+   barney/volume/MCAccelerator.h:338-567; the surface branch of
+   barney/kernels/shadeRays.cu:541-878 with the material's Lambertian).  The
+   world's instances are intersected in ascending order of their RTC
+   instance index (ModelSlot::flattenInstancesForDevice,
+   barney/ModelSlot.cpp:129-155, lists a group's user geometries before its
+   volumes), each one's random stream seeded with hash(instance, 0, 0).
+   The persistent mode of gbv_render/gbv_render_ex/gbv_render_tiles and
+   gbv_render_noalloc render it; the wavefront mode and batches do not. */
+typedef struct gbv_iso_surface {
+  float iso_value;
+  /* the field's macrocell scalar ranges, (lower, upper) per macrocell, as
+     gbv_build_mc_ranges (or gbv_nanovdb_mc_ranges) writes them */
+  const float *d_ranges;
+  float color[4];         /* AnariMatte color, RGBA (a color set as 3 floats has alpha 1) */
+  float opacity;          /* AnariMatte opacity */
+  int instance;           /* RTC instance index of the geometry's group */
+} gbv_iso_surface;
+
 typedef struct gbv_scene {
   /* structured field */
   const void *d_voxels;          /* per layout/format */
@@ -227,6 +250,11 @@ typedef struct gbv_scene {
      dims, origin, spacing and cells_per_mc are not used (the grid's own
      index bbox, world bbox and macrocells are) */
   const gbv_nanovdb_info *nanovdb;
+  /* an iso-surface of the field (host memory), or 0.  With an iso-surface,
+     d_majorants == 0 means the world holds no volume (d_tf is then not
+     used either). */
+  const gbv_iso_surface *iso;
+  int volume_instance;   /* RTC instance index of the volume's group (0 without an iso-surface) */
 } gbv_scene;
 
 /* Counters written by gbv_render when d_counters != 0 (uint64 each):

@@ -36,6 +36,9 @@ class OrcScene(C.Structure):
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
         ("width", C.c_int), ("height", C.c_int), ("u8_scaled", C.c_int), ("bounded_math", C.c_int),
         ("nanovdb", C.c_void_p), ("nanovdb_bytes", C.c_ulonglong),
+        ("iso_enabled", C.c_int), ("iso_value", C.c_float), ("iso_color", C.c_float * 4),
+        ("iso_opacity", C.c_float), ("iso_instance", C.c_int), ("volume_instance", C.c_int),
+        ("no_volume", C.c_int),
     ]
 
 
@@ -81,6 +84,9 @@ def lib() -> C.CDLL:
             "orc_majorants": (None, [vp, i, vp, i, f, f, f, vp]),
             "orc_trace_ray": (i, [sp, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float), vp]),
             "orc_iso_intersect": (i, [sp, vp, f, vp, vp, f, vp]),
+            "orc_iso_hit": (i, [sp, vp, f, vp, f, i, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float),
+                                vp, vp, vp]),
+            "orc_lambertian": (None, [vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp]),
             "orc_render": (None, [sp, vp, i, i, i, i, i, i, C.POINTER(OrcStats)]),
             "orc_tonemap": (None, [vp, i, i, i, i, vp]),
             "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
@@ -180,6 +186,15 @@ class Oracle:
         if self.nanovdb is not None:
             r.nanovdb = self.nanovdb.ctypes.data
             r.nanovdb_bytes = self.nanovdb.size
+        iso = getattr(scene, "iso", None)
+        if iso is not None:
+            r.iso_enabled = 1
+            r.iso_value = iso.value
+            r.iso_color[:] = [float(c) for c in iso.color]
+            r.iso_opacity = iso.opacity
+            r.iso_instance = iso.instance
+            r.no_volume = 1 if scene.no_volume else 0
+        r.volume_instance = getattr(scene, "volume_instance", 0)
         self.rec = r
 
     # -- macrocells --
@@ -215,6 +230,23 @@ class Oracle:
                 out[k, :7] = o7
                 out[k, 7] = 1.0
         return out
+
+    def iso_hit(self, org, dir, tmax, seed_state, iso, color=(0.8, 0.8, 0.8, 1.0), opacity=1.0, inst=0,
+                ranges=None):
+        """One ray against the iso-surface with a matte material (orc_iso_hit).
+        Returns (hit, seed_state_out, t, P, N as 3 uint16 halfs, albedo+alpha)."""
+        if ranges is None:
+            ranges = self.mc_ranges()
+        rg = np.ascontiguousarray(ranges, np.float32)
+        seed = C.c_uint64(seed_state)
+        t = C.c_float(0.0)
+        P = np.zeros(3, np.float32)
+        Nh = np.zeros(3, np.uint16)
+        alb = np.zeros(4, np.float32)
+        h = lib().orc_iso_hit(C.byref(self.rec), _p(rg), iso, _p(np.asarray(color, np.float32)), opacity, inst,
+                              _p(np.asarray(org, np.float32)), _p(np.asarray(dir, np.float32)), tmax,
+                              C.byref(seed), C.byref(t), _p(P), _p(Nh), _p(alb))
+        return bool(h), seed.value, t.value, P, Nh, alb
 
     def majorants_of(self, ranges: np.ndarray) -> np.ndarray:
         out = np.empty(ranges.shape[0], dtype=np.float32)
@@ -292,6 +324,15 @@ class Oracle:
         lib().orc_ea_backward(C.byref(self.rec), self._views(views), len(views), step,
                               _p(np.ascontiguousarray(d_images, np.float32)), nthreads, _p(gv), _p(gt))
         return gv.reshape(self.scalars.shape), gt.reshape(self.tf.shape)
+
+
+def lambertian(color, Ng, wo, wi, a: int, b: int) -> np.ndarray:
+    """The AnariMatte Lambertian (orc_lambertian): eval value[3], eval pdf,
+    pdf(wi), scatter dir[3], scatter pdf, f_r[3]."""
+    out = np.zeros(12, np.float32)
+    f4 = lambda v: _p(np.ascontiguousarray(v, np.float32))
+    lib().orc_lambertian(f4(color), f4(Ng), f4(wo), f4(wi), a, b, _p(out))
+    return out
 
 
 def rng_sequence(a: int, b: int, n: int) -> np.ndarray:

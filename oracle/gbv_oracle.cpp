@@ -256,6 +256,9 @@ struct Random2 : RNGSeed {                       // :97-111
     seed.next();
     next_h(b ? b : 290374ull);
   }
+  // a stream resumed from a saved state
+  struct Resume {};
+  Random2(Resume, uint64_t st) { state = st; }
   float operator()() { return (next() & 0x00FFFFFF) * (1.f / (float)0x01000000); }
 };
 inline uint64_t fnv_hash1(uint32_t v) {          // :132-137
@@ -858,6 +861,14 @@ struct Scene {
   float ambient;
   int multi, volMS, maxVB;
   float aniso, scatAlb;
+  // RTC instance hashes of the volume and the iso-surface (hash(instance,
+  // 0, 0), MCAccelerator.h:389-392 and :614-615)
+  uint64_t volHash = 0, isoHash = 0;
+  // iso-surface geometry with its AnariMatte material
+  bool iso = false, noVolume = false, isoFirst = false;
+  float isoValue = 0.f, isoAlpha = 1.f, isoDelta = 0.f;
+  V3<float> isoAlbedo{0.f, 0.f, 0.f};
+  std::vector<float> isoRanges;  // the field's macrocell scalar ranges
 };
 
 inline void build_scene(const orc_scene *s, Scene &S) {
@@ -879,16 +890,41 @@ inline void build_scene(const orc_scene *s, Scene &S) {
   S.mcRcpSpacing = rcp(S.mcSpacing);
   size_t nmc = (size_t)S.M[0] * S.M[1] * S.M[2];
   if (s->u8_scaled && !S.F.isNvdb) u8_build(S.F, S.u8lohi);
-  if (s->majorants) S.maj = s->majorants;
-  else {
-    S.majorants_own.resize(nmc);
-    std::vector<float> r(2 * nmc);
+  std::vector<float> r;
+  if (!s->majorants || s->iso_enabled) {
+    r.resize(2 * nmc);
     if (S.F.isNvdb) nv_mc_ranges(S.F.nv, r.data());
     else if (s->u8_scaled) u8_mc_ranges(S.F, cpm, S.M, r.data());
     else orc_mc_ranges(s->scalars, s->dims, cpm, r.data());
-    orc_majorants(r.data(), (int)nmc, s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density,
-                  S.majorants_own.data());
+  }
+  if (s->majorants) S.maj = s->majorants;
+  else {
+    S.majorants_own.resize(nmc);
+    if (s->iso_enabled && s->no_volume) std::fill(S.majorants_own.begin(), S.majorants_own.end(), 0.f);
+    else
+      orc_majorants(r.data(), (int)nmc, s->tf, s->tf_n, s->domain[0], s->domain[1], s->base_density,
+                    S.majorants_own.data());
     S.maj = S.majorants_own.data();
+  }
+  S.volHash = fnv_hash3((uint32_t)s->volume_instance, 0, 0);
+  if (s->iso_enabled) {
+    S.iso = true;
+    S.noVolume = s->no_volume != 0;
+    S.isoFirst = S.noVolume || s->iso_instance < s->volume_instance;
+    S.isoHash = fnv_hash3((uint32_t)s->iso_instance, 0, 0);
+    S.isoValue = s->iso_value;
+    S.isoRanges = std::move(r);
+    // MCAccelerator.h:476-479
+    S.isoDelta = length(S.F.boundsHi - S.F.boundsLo) * .1f / float(S.M[0] + S.M[1] + S.M[2]);
+    // AnariMatte::DD::createBSDF (AnariMatte.h:50-62) with VALUE parameters
+    // (PossiblyMappedParameter::DD::eval, Material.h:101-106): a NaN value
+    // reads as (0, 0, 0, 1); opacity is (opacity, 0, 0, 1)
+    V4<float> base{s->iso_color[0], s->iso_color[1], s->iso_color[2], s->iso_color[3]};
+    if (std::isnan(base.x)) base = {0.f, 0.f, 0.f, 1.f};
+    const float opacity = std::isnan(s->iso_opacity) ? 0.f : s->iso_opacity;
+    const float reflectance = .85f;
+    S.isoAlbedo = reflectance * V3<float>(base.x, base.y, base.z) * ONE_OVER_PI;
+    S.isoAlpha = base.w * opacity;
   }
   S.cam = commit_camera(s->cam_pos, s->cam_dir, s->cam_up, s->fovy);
   S.W = s->width;
@@ -1043,9 +1079,11 @@ struct Ray {
   RNGSeed rngSeed;
   V3<float> P;
   bool hit;          // bsdfType != NONE
+  bool surf;         // the hit is on the iso-surface (Lambertian), else a volume hit (Phase)
   bool isShadowRay;
   V3<float> albedo;  // Phase data
   float g;
+  V3h N;             // Ray::N, the surface hit's normal in half precision (Ray.h:84)
   V4<float> missColor;
 };
 struct PathState {   // render/Ray.h:18-26
@@ -1092,7 +1130,8 @@ template <typename R> inline bool boxTest(V3<R> org, V3<R> dir, R &t0, R &t1, V3
 
 // MCVolumeAccel::isProg (MCAccelerator.h:569-708) + dda::dda3 (DDA.h:65-206)
 // as dispatched by the embree backend (tmin 0, tmax ray.tMax, identity
-// instance transform, one instance and one geometry: hash(0,0,0)).
+// instance transform, geometry 0 of the volume's instance: S.volHash =
+// hash(instance, 0, 0), instance 0 unless an iso-surface precedes it).
 // The trace direction has zero components replaced by 1e-6
 // (traceRays.dev.cu:41-44).  On a hit, fills t/rgb/P and returns true.
 template <typename R>
@@ -1109,7 +1148,7 @@ inline bool trace(const Scene &S, Ray &ray, Counters &cnt, R &t_hit, V3<R> &rgb_
 
   V3<R> dda_org = (org - cvt<R>(S.mcOrigin)) * rcp(cvt<R>(S.mcSpacing));
   V3<R> dda_dir = dir * rcp(cvt<R>(S.mcSpacing));
-  Random2 rng(ray.rngSeed, fnv_hash3(0, 0, 0));
+  Random2 rng(ray.rngSeed, S.volHash);
   const R tMaxRay = R(ray.tMax);
   const R tMax = tHi;
 
@@ -1172,6 +1211,129 @@ inline bool trace(const Scene &S, Ray &ray, Counters &cnt, R &t_hit, V3<R> &rgb_
   }
   return false;
 }
+
+// MCIsoSurfaceAccel::isProg (barney/volume/MCAccelerator.h:338-567) up to
+// the hit record: dda::dda3 (DDA.h:65-206) over the macrocell grid; per
+// macrocell whose scalar range holds the iso value, the cell's t range is
+// cut into 10 sub-steps, and the first sub-step whose end values bracket the
+// iso value gives t by linear interpolation.  The normal is the central
+// difference of the field at +-d per axis (one-sided where a sample falls
+// outside the field), normalized.  `dir` is the trace direction (zero
+// components already replaced by 1e-6, traceRays.dev.cu:41-44); the box test
+// runs on [0, tmax].  `onBox` runs once the box test passes, where the
+// reference constructs the geometry's random stream from ray.rngSeed.
+template <class OnBox>
+inline bool iso_isprog(const Field &F, const int M[3], V3<float> mcOrigin, V3<float> mcSpacing, const float *ranges,
+                       float iso, float d, V3<float> org, V3<float> dir, float tmax, float &tOut, V3<float> &P,
+                       V3<float> &N, OnBox onBox) {
+  if (M[0] <= 0 || M[1] <= 0 || M[2] <= 0) return false;
+  float tLo = 0.f, tHi = tmax;
+  if (!boxTest<float>(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return false;
+  onBox();
+  const V3<float> dda_org = (org - mcOrigin) * rcp(mcSpacing);
+  const V3<float> dda_dir = dir * rcp(mcSpacing);
+  const float tMax = tHi;
+  // ---- dda3 ----
+  const V3<float> f_size((float)M[0], (float)M[1], (float)M[2]);
+  const V3<float> rcp_dir = rcp(dda_dir);
+  V3<float> t_lo = (V3<float>(0.f) - dda_org) * rcp(dda_dir);
+  V3<float> t_hi = (f_size - dda_org) * rcp(dda_dir);
+  V3<float> t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
+  for (int a = 0; a < 3; a++) {
+    if (dda_dir[a] == 0.f) {
+      if (dda_org[a] < 0.f || dda_org[a] > f_size[a]) return false;
+      t_nr[a] = -INF;
+      t_fr[a] = +INF;
+    }
+  }
+  const float ray_t0 = mx(0.f, reduce_max(t_nr));
+  const float ray_t1 = mn(tMax, reduce_min(t_fr));
+  if (ray_t0 > ray_t1) return false;
+  const V3<float> oiv = dda_org + ray_t0 * dda_dir;
+  const V3<float> f_cell = vmax(V3<float>(0.f), vmin(f_size - V3<float>(1.f), vfloor(oiv)));
+  const V3<float> f_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
+                        dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
+  const V3<float> t_step = vabs(rcp_dir);
+  V3<float> t_next;
+  for (int a = 0; a < 3; a++)
+    t_next[a] = (dda_dir[a] == 0.f) ? INF : (std::fabs(f_end[a] - oiv[a]) * t_step[a]);
+  int stop[3], delta[3], cell[3];
+  for (int a = 0; a < 3; a++) {
+    stop[a] = dda_dir[a] > 0.f ? M[a] : -1;
+    delta[a] = dda_dir[a] > 0.f ? +1 : -1;
+    cell[a] = int(f_cell[a]);
+  }
+  float tHit = tmax;
+  float next_cell_begin = 0.f;
+  const int maxIter = M[0] + M[1] + M[2] + 8;
+  bool stopped = false;
+  for (int it = 0; it < maxIter && !stopped; it++) {
+    const float t_closest = reduce_min(t_next);
+    const float t0 = ray_t0 + next_cell_begin;
+    const float t1 = ray_t0 + mn(t_closest, tMax);
+    // ---- the iso lambda (MCAccelerator.h:405-471) ----
+    [&]() {
+      if (t0 >= mn(t1, tmax)) return;
+      const size_t ci = (size_t)cell[0] + (size_t)M[0] * ((size_t)cell[1] + (size_t)M[1] * cell[2]);
+      const float vlo = ranges[2 * ci], vhi = ranges[2 * ci + 1];
+      if (!(iso >= vlo && iso <= vhi)) return;
+      float tt1 = t0;
+      float ff1 = sample_field<float>(F, org + tt1 * dir);
+      for (int i = 1; i <= 10; i++) {
+        const float tt0 = tt1;
+        const float ff0 = ff1;
+        tt1 = lerp_l((float)i / 10.f, t0, t1);
+        ff1 = sample_field<float>(F, org + tt1 * dir);
+        if (std::isnan(ff0) || std::isnan(ff1)) continue;
+        const float lo = mn(ff0, ff1), hi = mx(ff0, ff1);
+        if (iso >= lo && iso <= hi) {
+          float t = (iso - ff0) / (ff1 - ff0);
+          t = lerp_l(t, tt0, tt1);
+          tHit = mn(tHit, t);
+          if (tHit < tmax) {
+            stopped = true;
+            return;
+          }
+        }
+      }
+    }();
+    if (stopped) break;
+    next_cell_begin = t_closest;
+    bool done = false;
+    for (int a = 0; a < 3 && !done; a++) {
+      if (t_next[a] == t_closest) {
+        t_next[a] += t_step[a];
+        cell[a] += delta[a];
+        if (cell[a] == stop[a]) done = true;
+      }
+    }
+    if (done) break;
+  }
+  if (!(tHit < tmax)) return false;
+  // ---- normal (MCAccelerator.h:476-503) ----
+  P = org + tHit * dir;
+  const float fP = sample_field<float>(F, P);
+  float fx0 = sample_field<float>(F, P + V3<float>(-d, 0.f, 0.f));
+  float fx1 = sample_field<float>(F, P + V3<float>(+d, 0.f, 0.f));
+  float fy0 = sample_field<float>(F, P + V3<float>(0.f, -d, 0.f));
+  float fy1 = sample_field<float>(F, P + V3<float>(0.f, +d, 0.f));
+  float fz0 = sample_field<float>(F, P + V3<float>(0.f, 0.f, -d));
+  float fz1 = sample_field<float>(F, P + V3<float>(0.f, 0.f, +d));
+  float dx = 2.f, dy = 2.f, dz = 2.f;
+  if (std::isnan(fx0)) { dx -= 1.f; fx0 = fP; }
+  if (std::isnan(fx1)) { dx -= 1.f; fx1 = fP; }
+  if (std::isnan(fy0)) { dy -= 1.f; fy0 = fP; }
+  if (std::isnan(fy1)) { dy -= 1.f; fy1 = fP; }
+  if (std::isnan(fz0)) { dz -= 1.f; fz0 = fP; }
+  if (std::isnan(fz1)) { dz -= 1.f; fz1 = fP; }
+  N = V3<float>(dx == 0.f ? 0.f : (fx1 - fx0) / dx, dy == 0.f ? 0.f : (fy1 - fy0) / dy,
+                dz == 0.f ? 0.f : (fz1 - fz0) / dz);
+  if (N == V3<float>(0.f)) N = -normalize(dir);
+  N = normalize(N);
+  tOut = tHit;
+  return true;
+}
+
 
 // ---------------------------------------------------------------------------
 // Shading (kernels/shadeRays.cu), volume-only world
@@ -1324,8 +1486,130 @@ inline V3<float> sampleHGDirection(V3<float> wi_in, float g, Random2 &random, bo
 
 struct Fragment { V3<float> rgb; };
 
-// bounce() (shadeRays.cu:477-878), volume-hit and miss branches only.
-// Returns the fragment; updates ray/state; fills the shadow ray.
+// owl::common::frame, the orthonormal frame around a unit normal N that
+// xfmVector(frame(N), v) uses: dx is the longer of (1,0,0) x N and
+// (0,1,0) x N, normalized, and dy = normalize(N x dx).  (owl's source is
+// absent from the reference checkout; this restates it.)
+inline void frame_of(V3<float> N, V3<float> &dx, V3<float> &dy) {
+  const V3<float> dx0 = cross(V3<float>(1.f, 0.f, 0.f), N), dx1 = cross(V3<float>(0.f, 1.f, 0.f), N);
+  dx = normalize(dot(dx0, dx0) > dot(dx1, dx1) ? dx0 : dx1);
+  dy = normalize(cross(N, dx));
+}
+
+// Lambertian::pdf (packedBSDF/Lambertian.h:46-55): cosine-hemisphere pdf
+// about the normal turned toward wi
+inline float lambert_pdf(V3<float> Ng, V3<float> wi) {
+  V3<float> N = Ng;
+  if (dot(wi, N) < 0.f) N = -N;
+  const float cosThetaI = mx(dot(wi, N), 0.f);
+  return cosThetaI * ONE_OVER_PI;  // cosineSampleHemispherePDF (DG.h:177-180)
+}
+
+// bounce() for an iso-surface hit (shadeRays.cu:541-878 with isVolumeHit
+// false): Ng = normalize(ray.N), offsets along the front-facing normal Ngff,
+// light sampling with Ngff (sampleDirLights weights by dot(lightDir, N), the
+// ambient sample turns into N's hemisphere), the Lambertian of the
+// AnariMatte material (Lambertian.h:57-90) with the cosine factors of the
+// surface branches, and a diffuse scatter, at most MAX_DIFFUSE_BOUNCES = 1
+// per path (shadeRays.cu:18, 795-808).  No fragment of its own.
+inline V3<float> bounce_surface(const Scene &S, Ray &ray, PathState &state, Ray &shadowRay, PathState &shadowState,
+                                bool &shadowValid, int pathDepth) {
+  const float EPS = 1e-4f;
+  const V3<float> fragment(0.f);
+  const V3<float> incomingThroughput = fromh(state.throughput);
+  const V3<float> Ng = normalize(fromh(ray.N));
+  const bool hitWasOnFront = dot(ray.dir, Ng) < 0.f;
+  const V3<float> Ngff = hitWasOnFront ? Ng : -Ng;
+  Random2 random(ray.rngSeed, (uint64_t)fbits(ray.tMax));
+  // DG (shadeRays.cu:625-629): Ng = Ns = the unflipped normal
+  const V3<float> P = ray.P;
+  const V3<float> wo = -normalize(ray.dir);
+  const float offsetEpsilon = mx(EPS, 1e-6f * reduce_max(vabs(P)));  // safe_eps :39-43
+  LightSample ls;
+  bool needsMIS = false, isDir = false;
+  if (sampleLights(S, Ngff, random, ls, needsMIS, isDir)) {
+    // Lambertian::eval: cosine against Ns, unflipped
+    const float cosThetaI = mx(dot(ls.direction, Ng), 0.f);
+    V3<float> fr_value = S.isoAlbedo * ONE_OVER_PI * cosThetaI;
+    const float fr_pdf = cosThetaI * ONE_OVER_PI;
+    if (!(fr_pdf > 0.f) || reduce_max(fr_value) < 1e-4f) {
+      shadowValid = false;
+    } else {
+      fr_value = vmin(fr_value, V3<float>(13.f));  // CLAMP_F_R
+      V3<float> tp_sr = incomingThroughput * (std::isinf(ls.pdf) ? 1.f : 1.f / ls.pdf) * fr_value * ls.radiance *
+                        (ONE_OVER_PI * std::fabs(dot(Ng, ls.direction)));
+      shadowRay.hit = false;
+      shadowRay.surf = false;
+      shadowRay.isShadowRay = true;
+      shadowRay.dir = ls.direction;
+      shadowRay.org = P + offsetEpsilon * Ngff;
+      shadowRay.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
+      shadowState.throughput = toh(tp_sr);
+      shadowRay.rngSeed = ray.rngSeed;
+      ray.rngSeed.next_h((uint64_t)fbits(ray.tMax));
+      shadowState.misWeight = 1.f;
+      shadowValid = true;
+      if (!isDir && needsMIS) {
+        const float pdf_l = env_pdf(S.env, ls.direction);
+        const float pdf_s = lambert_pdf(Ng, ls.direction);
+        shadowState.misWeight = pdf_l / (pdf_l + pdf_s + 1e-10f);
+        if (shadowState.misWeight < 1e-5f) shadowValid = false;
+      }
+    }
+  }
+  if (pathDepth >= 10) {  // MAX_PATH_DEPTH
+    ray.tMax = -1.f;
+    return fragment;
+  }
+  ray.hit = false;
+  ray.surf = false;
+  ray.tMax = INF;
+  // Lambertian::scatter: a cosine-weighted direction about the normal
+  // turned toward wo.  Its vec2f s(random(), random()) takes the second
+  // argument's draw first: the reference's CPU backend is built with gcc,
+  // which evaluates the arguments right to left.
+  V3<float> N = Ng;
+  if (dot(wo, N) < 0.f) N = -N;
+  const float r0 = random();
+  const float r1 = random();
+  const float sx = r1, sy = r0;
+  // cosineSampleHemisphere / cartesian (DG.h:135-168)
+  const float phi = TWO_PI * sx;
+  const float cosTheta = std::sqrt(sy);
+  const float sinTheta = std::sqrt(1.0f - sy);
+  float sinPhi, cosPhi;
+  path_sincos(S.env.boundedMath, phi, sinPhi, cosPhi);
+  const V3<float> local(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
+  V3<float> dx, dy;
+  frame_of(N, dx, dy);
+  const V3<float> sdir = dx * local.x + dy * local.y + N * local.z;
+  const float spdf = local.z * ONE_OVER_PI;
+  if (!(spdf > 0.f) || spdf <= 1e-6f) return fragment;  // ray stays alive unchanged
+  // DIFFUSE scatter
+  if (state.numDiffuseBounces >= 1) {
+    ray.tMax = -1.f;
+    return fragment;
+  }
+  state.numDiffuseBounces = state.numDiffuseBounces + 1;
+  ray.org = P + (1.f * offsetEpsilon) * Ngff;
+  ray.dir = normalize(sdir);
+  V3<float> scatterFactor =
+      S.isoAlbedo * std::fabs(dot(Ng, normalize(ray.dir))) / (std::isinf(spdf) ? 1.f : (spdf + 1e-10f));
+  scatterFactor = vmin(scatterFactor, V3<float>(2.5f));
+  state.throughput = toh(fromh(state.throughput) * scatterFactor);
+  if (needsMIS && !std::isinf(spdf)) {
+    const float pdf_s = lambert_pdf(Ng, ray.dir);
+    const float pdf_l = env_pdf(S.env, ray.dir);
+    state.misWeight = pdf_s / (pdf_s + pdf_l);
+  } else {
+    state.misWeight = 1.f;
+  }
+  return fragment;
+}
+
+// bounce() (shadeRays.cu:477-878): miss, volume-hit and (bounce_surface)
+// iso-surface branches.  Returns the fragment; updates ray/state; fills the
+// shadow ray.
 inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowRay, PathState &shadowState,
                         bool &shadowValid, int pathDepth) {
   const float EPS = 1e-4f;
@@ -1349,6 +1633,7 @@ inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowR
     ray.tMax = -1.f;
     return fragment;
   }
+  if (ray.surf) return bounce_surface(S, ray, state, shadowRay, shadowState, shadowValid, pathDepth);
   // volume hit: isVolumeHit, hitWasOnFront false, Ngff = -Ng = -0
   const V3<float> Ngff(-0.f, -0.f, -0.f);
   Random2 random(ray.rngSeed, (uint64_t)fbits(ray.tMax));
@@ -1373,6 +1658,7 @@ inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowR
                         ls.radiance * 1.f;
       // makeShadowRay (Ray.h:152-163)
       shadowRay.hit = false;
+      shadowRay.surf = false;
       shadowRay.isShadowRay = true;
       shadowRay.dir = ls.direction;
       shadowRay.org = P + offsetEpsilon * frontFacingSurfaceOffset;
@@ -1458,6 +1744,7 @@ inline void generate(const Scene &S, int ix, int iy, int accumID, Ray &ray, Path
   V3<float> ray_dir = S.cam.dir00 + (1.f * aspect * (image_u - .5f)) * S.cam.du + (1.f * (image_v - .5f)) * S.cam.dv;
   ray.dir = normalize(ray_dir);
   ray.hit = false;
+  ray.surf = false;
   ray.isShadowRay = false;
   ray.tMax = 1e30f;
   state.numDiffuseBounces = 0;
@@ -1474,9 +1761,64 @@ inline void generate(const Scene &S, int ix, int iy, int accumID, Ray &ray, Path
   state.throughput = toh(V3<float>(1.f));
 }
 
+// The iso-surface's isProg (MCAccelerator.h:338-567) from the box test on:
+// its random stream Random2(ray.rngSeed, hash(instance, 0, 0)) -- which
+// advances ray.rngSeed -- the hit search on [0, ray.tMax], the opacity test
+// (a material of opacity < 1 lets the ray through when rng() > opacity) and
+// DeviceMaterial::setHit (DeviceMaterial.h:70-78): Ray::setHit stores P, the
+// unit normal in half precision, t and the Lambertian.
+inline void iso_hit_record(const Field &F, const int M[3], V3<float> mcOrigin, V3<float> mcSpacing,
+                           const float *ranges, float iso, float delta, uint64_t isoHash, float alpha, Ray &ray) {
+  V3<float> dirf = ray.dir;
+  if (dirf.x == 0.f) dirf.x = 1e-6f;
+  if (dirf.y == 0.f) dirf.y = 1e-6f;
+  if (dirf.z == 0.f) dirf.z = 1e-6f;
+  uint64_t isoRng = 0;  // the geometry's Random2, made at the box test
+  float t;
+  V3<float> P, N;
+  if (!iso_isprog(F, M, mcOrigin, mcSpacing, ranges, iso, delta, ray.org, dirf, ray.tMax, t, P, N,
+                  [&]() { isoRng = Random2(ray.rngSeed, isoHash).state; }))
+    return;
+  if (alpha < 1.f) {
+    Random2 rng(Random2::Resume{}, isoRng);
+    if (rng() > alpha) return;
+  }
+  ray.hit = true;
+  ray.surf = true;
+  ray.tMax = t;
+  ray.P = P;
+  ray.N = toh(N);
+}
+inline void trace_iso(const Scene &S, Ray &ray) {
+  iso_hit_record(S.F, S.M, S.mcOrigin, S.mcSpacing, S.isoRanges.data(), S.isoValue, S.isoDelta, S.isoHash,
+                 S.isoAlpha, ray);
+}
+
 // trace + setVolumeHit (Ray.h:118-149): albedo = 0.7*rgb (default build) or
 // scatteringAlbedo*rgb with the volume's anisotropy (multi-scatter build).
+// With an iso-surface the world's two instances run in ascending instance
+// order, each bounded by the other's hit (ray.tMax), so the closest hit
+// stays; the order decides which one's random stream comes from the seed
+// first.  (The reference leaves the order of two instances with the same
+// bounds to embree's traversal.)
+template <typename R> inline void trace_volume(const Scene &S, Ray &ray, Counters &cnt);
 template <typename R> inline void trace_and_record(const Scene &S, Ray &ray, Counters &cnt) {
+  if (!S.iso) {
+    trace_volume<R>(S, ray, cnt);
+    return;
+  }
+  if (S.noVolume) {
+    cnt.rays++;
+    trace_iso(S, ray);
+  } else if (S.isoFirst) {
+    trace_iso(S, ray);
+    trace_volume<R>(S, ray, cnt);
+  } else {
+    trace_volume<R>(S, ray, cnt);
+    trace_iso(S, ray);
+  }
+}
+template <typename R> inline void trace_volume(const Scene &S, Ray &ray, Counters &cnt) {
   R t;
   V3<R> rgb;
   if (trace<R>(S, ray, cnt, t, rgb)) {
@@ -1489,6 +1831,7 @@ template <typename R> inline void trace_and_record(const Scene &S, Ray &ray, Cou
     ray.P = cvt<float>(cvt<R>(ray.org) + t * cvt<R>(dirf));
     ray.tMax = tf;
     ray.hit = true;
+    ray.surf = false;
     if (S.multi) {
       ray.albedo = S.scatAlb * rgbf;
       ray.g = S.aniso;
@@ -1713,128 +2056,97 @@ int orc_iso_intersect(const orc_scene *s, const float *ranges, float iso, const 
   if (s->u8_scaled) u8_build(F, lohi);
   int M[3];
   mc_dims_of(F.N, s->cells_per_mc, M);
-  if (M[0] <= 0 || M[1] <= 0 || M[2] <= 0) return 0;
   std::vector<float> own;
-  if (!ranges) {
+  if (!ranges && M[0] > 0 && M[1] > 0 && M[2] > 0) {
     own.resize((size_t)2 * M[0] * M[1] * M[2]);
     orc_scene_mc_ranges(s, own.data());
     ranges = own.data();
   }
-  const V3<float> org(org_[0], org_[1], org_[2]);
   V3<float> dir(dir_[0], dir_[1], dir_[2]);
   if (dir.x == 0.f) dir.x = 1e-6f;
   if (dir.y == 0.f) dir.y = 1e-6f;
   if (dir.z == 0.f) dir.z = 1e-6f;
-  float tLo = 0.f, tHi = tmax;
-  if (!boxTest<float>(org, dir, tLo, tHi, F.boundsLo, F.boundsHi)) return 0;
-  const V3<float> mcOrigin = F.boundsLo;
   const V3<float> mcSpacing = V3<float>((float)s->cells_per_mc) * F.spacing;
-  const V3<float> dda_org = (org - mcOrigin) * rcp(mcSpacing);
-  const V3<float> dda_dir = dir * rcp(mcSpacing);
-  const float tMax = tHi;
-  // ---- dda3 ----
-  const V3<float> f_size((float)M[0], (float)M[1], (float)M[2]);
-  const V3<float> rcp_dir = rcp(dda_dir);
-  V3<float> t_lo = (V3<float>(0.f) - dda_org) * rcp(dda_dir);
-  V3<float> t_hi = (f_size - dda_org) * rcp(dda_dir);
-  V3<float> t_nr = vmin(t_lo, t_hi), t_fr = vmax(t_lo, t_hi);
-  for (int a = 0; a < 3; a++) {
-    if (dda_dir[a] == 0.f) {
-      if (dda_org[a] < 0.f || dda_org[a] > f_size[a]) return 0;
-      t_nr[a] = -INF;
-      t_fr[a] = +INF;
-    }
-  }
-  const float ray_t0 = mx(0.f, reduce_max(t_nr));
-  const float ray_t1 = mn(tMax, reduce_min(t_fr));
-  if (ray_t0 > ray_t1) return 0;
-  const V3<float> oiv = dda_org + ray_t0 * dda_dir;
-  const V3<float> f_cell = vmax(V3<float>(0.f), vmin(f_size - V3<float>(1.f), vfloor(oiv)));
-  const V3<float> f_end(dda_dir.x > 0.f ? f_cell.x + 1.f : f_cell.x, dda_dir.y > 0.f ? f_cell.y + 1.f : f_cell.y,
-                        dda_dir.z > 0.f ? f_cell.z + 1.f : f_cell.z);
-  const V3<float> t_step = vabs(rcp_dir);
-  V3<float> t_next;
-  for (int a = 0; a < 3; a++)
-    t_next[a] = (dda_dir[a] == 0.f) ? INF : (std::fabs(f_end[a] - oiv[a]) * t_step[a]);
-  int stop[3], delta[3], cell[3];
-  for (int a = 0; a < 3; a++) {
-    stop[a] = dda_dir[a] > 0.f ? M[a] : -1;
-    delta[a] = dda_dir[a] > 0.f ? +1 : -1;
-    cell[a] = int(f_cell[a]);
-  }
-  float tHit = tmax;
-  float next_cell_begin = 0.f;
-  const int maxIter = M[0] + M[1] + M[2] + 8;
-  bool stopped = false;
-  for (int it = 0; it < maxIter && !stopped; it++) {
-    const float t_closest = reduce_min(t_next);
-    const float t0 = ray_t0 + next_cell_begin;
-    const float t1 = ray_t0 + mn(t_closest, tMax);
-    // ---- the iso lambda (MCAccelerator.h:405-471) ----
-    [&]() {
-      if (t0 >= mn(t1, tmax)) return;
-      const size_t ci = (size_t)cell[0] + (size_t)M[0] * ((size_t)cell[1] + (size_t)M[1] * cell[2]);
-      const float vlo = ranges[2 * ci], vhi = ranges[2 * ci + 1];
-      if (!(iso >= vlo && iso <= vhi)) return;
-      float tt1 = t0;
-      float ff1 = sample_field<float>(F, org + tt1 * dir);
-      for (int i = 1; i <= 10; i++) {
-        const float tt0 = tt1;
-        const float ff0 = ff1;
-        tt1 = lerp_l((float)i / 10.f, t0, t1);
-        ff1 = sample_field<float>(F, org + tt1 * dir);
-        if (std::isnan(ff0) || std::isnan(ff1)) continue;
-        const float lo = mn(ff0, ff1), hi = mx(ff0, ff1);
-        if (iso >= lo && iso <= hi) {
-          float t = (iso - ff0) / (ff1 - ff0);
-          t = lerp_l(t, tt0, tt1);
-          tHit = mn(tHit, t);
-          if (tHit < tmax) {
-            stopped = true;
-            return;
-          }
-        }
-      }
-    }();
-    if (stopped) break;
-    next_cell_begin = t_closest;
-    bool done = false;
-    for (int a = 0; a < 3 && !done; a++) {
-      if (t_next[a] == t_closest) {
-        t_next[a] += t_step[a];
-        cell[a] += delta[a];
-        if (cell[a] == stop[a]) done = true;
-      }
-    }
-    if (done) break;
-  }
-  if (!(tHit < tmax)) return 0;
-  // ---- normal (MCAccelerator.h:476-503) ----
-  const V3<float> P = org + tHit * dir;
-  const V3<float> size = F.boundsHi - F.boundsLo;
-  const float d = length(size) * .1f / float(M[0] + M[1] + M[2]);
-  const float fP = sample_field<float>(F, P);
-  float fx0 = sample_field<float>(F, P + V3<float>(-d, 0.f, 0.f));
-  float fx1 = sample_field<float>(F, P + V3<float>(+d, 0.f, 0.f));
-  float fy0 = sample_field<float>(F, P + V3<float>(0.f, -d, 0.f));
-  float fy1 = sample_field<float>(F, P + V3<float>(0.f, +d, 0.f));
-  float fz0 = sample_field<float>(F, P + V3<float>(0.f, 0.f, -d));
-  float fz1 = sample_field<float>(F, P + V3<float>(0.f, 0.f, +d));
-  float dx = 2.f, dy = 2.f, dz = 2.f;
-  if (std::isnan(fx0)) { dx -= 1.f; fx0 = fP; }
-  if (std::isnan(fx1)) { dx -= 1.f; fx1 = fP; }
-  if (std::isnan(fy0)) { dy -= 1.f; fy0 = fP; }
-  if (std::isnan(fy1)) { dy -= 1.f; fy1 = fP; }
-  if (std::isnan(fz0)) { dz -= 1.f; fz0 = fP; }
-  if (std::isnan(fz1)) { dz -= 1.f; fz1 = fP; }
-  V3<float> N(dx == 0.f ? 0.f : (fx1 - fx0) / dx, dy == 0.f ? 0.f : (fy1 - fy0) / dy,
-              dz == 0.f ? 0.f : (fz1 - fz0) / dz);
-  if (N == V3<float>(0.f)) N = -normalize(dir);
-  N = normalize(N);
-  out[0] = tHit;
+  const float delta = length(F.boundsHi - F.boundsLo) * .1f / float(M[0] + M[1] + M[2]);
+  float t;
+  V3<float> P, N;
+  if (!iso_isprog(F, M, F.boundsLo, mcSpacing, ranges, iso, delta, V3<float>(org_[0], org_[1], org_[2]), dir, tmax,
+                  t, P, N, []() {}))
+    return 0;
+  out[0] = t;
   out[1] = P.x; out[2] = P.y; out[3] = P.z;
   out[4] = N.x; out[5] = N.y; out[6] = N.z;
   return 1;
+}
+
+// The iso-surface isProg with an AnariMatte material of constant color and
+// opacity, as ref_iso_hit exposes the reference's: returns 1 on a hit with t,
+// P, the normal's three halfs and the Lambertian's albedo (xyz) and alpha
+// (w); *seed_state carries the ray's seed in and out.
+int orc_iso_hit(const orc_scene *s, const float *ranges, float iso, const float color[4], float opacity, int inst,
+                const float org[3], const float dir[3], float tmax, uint64_t *seed_state, float *t_hit, float P[3],
+                uint16_t N[3], float albedo[4]) {
+  Field F = make_field(s);
+  std::vector<float> lohi;
+  if (s->u8_scaled) u8_build(F, lohi);
+  int M[3];
+  mc_dims_of(F.N, s->cells_per_mc, M);
+  const V3<float> mcSpacing = V3<float>((float)s->cells_per_mc) * F.spacing;
+  const float delta = length(F.boundsHi - F.boundsLo) * .1f / float(M[0] + M[1] + M[2]);
+  V4<float> base{color[0], color[1], color[2], color[3]};
+  if (std::isnan(base.x)) base = {0.f, 0.f, 0.f, 1.f};
+  const float op = std::isnan(opacity) ? 0.f : opacity;
+  Ray ray;
+  ray.org = V3<float>(org[0], org[1], org[2]);
+  ray.dir = V3<float>(dir[0], dir[1], dir[2]);
+  ray.tMax = tmax;
+  ray.rngSeed.state = *seed_state;
+  ray.hit = ray.surf = false;
+  iso_hit_record(F, M, F.boundsLo, mcSpacing, ranges, iso, delta, fnv_hash3((uint32_t)inst, 0, 0), base.w * op, ray);
+  *seed_state = ray.rngSeed.state;
+  if (!ray.hit) return 0;
+  const V3<float> alb = .85f * V3<float>(base.x, base.y, base.z) * ONE_OVER_PI;
+  *t_hit = ray.tMax;
+  P[0] = ray.P.x; P[1] = ray.P.y; P[2] = ray.P.z;
+  N[0] = ray.N.x; N[1] = ray.N.y; N[2] = ray.N.z;
+  albedo[0] = alb.x; albedo[1] = alb.y; albedo[2] = alb.z;
+  albedo[3] = base.w * op;
+  return 1;
+}
+
+// The AnariMatte Lambertian at a surface of normal Ng seen from wo, as
+// ref_lambertian exposes the reference's: eval and pdf toward wi, then one
+// scatter drawing from Random2(a, b) (libm sine and cosine).  out: eval
+// value[3], eval pdf, pdf(wi), scatter dir[3], scatter pdf, f_r[3].
+void orc_lambertian(const float color[4], const float Ng_[3], const float wo_[3], const float wi_[3], uint32_t a,
+                    uint32_t b, float out[12]) {
+  V4<float> base{color[0], color[1], color[2], color[3]};
+  if (std::isnan(base.x)) base = {0.f, 0.f, 0.f, 1.f};
+  const V3<float> albedo = .85f * V3<float>(base.x, base.y, base.z) * ONE_OVER_PI;
+  const V3<float> Ng(Ng_[0], Ng_[1], Ng_[2]), wo(wo_[0], wo_[1], wo_[2]), wi(wi_[0], wi_[1], wi_[2]);
+  const float cosThetaI = mx(dot(wi, Ng), 0.f);
+  const V3<float> v = albedo * ONE_OVER_PI * cosThetaI;
+  out[0] = v.x; out[1] = v.y; out[2] = v.z;
+  out[3] = cosThetaI * ONE_OVER_PI;
+  out[4] = lambert_pdf(Ng, wi);
+  Random2 random(a, b);
+  V3<float> N = Ng;
+  if (dot(wo, N) < 0.f) N = -N;
+  const float r0 = random();
+  const float r1 = random();
+  const float sx = r1, sy = r0;
+  const float phi = TWO_PI * sx;
+  const float cosTheta = std::sqrt(sy);
+  const float sinTheta = std::sqrt(1.0f - sy);
+  float sinPhi, cosPhi;
+  path_sincos(false, phi, sinPhi, cosPhi);
+  const V3<float> local(cosPhi * sinTheta, sinPhi * sinTheta, cosTheta);
+  V3<float> dx, dy;
+  frame_of(N, dx, dy);
+  const V3<float> d = dx * local.x + dy * local.y + N * local.z;
+  out[5] = d.x; out[6] = d.y; out[7] = d.z;
+  out[8] = local.z * ONE_OVER_PI;
+  out[9] = albedo.x; out[10] = albedo.y; out[11] = albedo.z;
 }
 
 void orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp, int use_double, int nthreads,

@@ -80,6 +80,20 @@ typedef struct orc_scene {
      the reference's NanoVDB field (barney/volume/NanoVDB.{h,cu}) */
   const unsigned char *nanovdb;
   unsigned long long nanovdb_bytes;
+  /* an iso-surface geometry over the same field (IsoSurface,
+     barney/geometry/IsoSurface.{h,cpp}) with a matte material (AnariMatte,
+     barney/material/AnariMatte.h); iso_enabled = 0: none.  The world's
+     instances are intersected in ascending order of their RTC instance
+     index (ModelSlot::flattenInstancesForDevice appends a group's
+     user-geometry group before its volumes), and each one's hash(instance,
+     0, 0) seeds its random stream. */
+  int   iso_enabled;
+  float iso_value;
+  float iso_color[4];        /* AnariMatte "color" (set3f: alpha 1) */
+  float iso_opacity;         /* AnariMatte "opacity" */
+  int   iso_instance;
+  int   volume_instance;
+  int   no_volume;           /* 1: the world holds the iso-surface only */
 } orc_scene;
 
 typedef struct orc_stats {
@@ -127,6 +141,18 @@ int   orc_trace_ray(const orc_scene *s, const float org[3], const float dir[3],
 int   orc_iso_intersect(const orc_scene *s, const float *ranges, float iso,
                         const float org[3], const float dir[3], float tmax,
                         float out[7]);
+
+/* The iso-surface isProg with a constant-color AnariMatte material for one
+   ray (instance `inst`, geometry 0, primitive 0): 1 on a hit with t, P, the
+   normal's halfs and the Lambertian's albedo (xyz) and alpha (w); the ray's
+   RNG seed state in and out. */
+int   orc_iso_hit(const orc_scene *s, const float *ranges, float iso, const float color[4],
+                  float opacity, int inst, const float org[3], const float dir[3], float tmax,
+                  uint64_t *seed_state, float *t_hit, float P[3], uint16_t N[3], float albedo[4]);
+/* The AnariMatte Lambertian at normal Ng seen from wo: eval value[3], eval
+   pdf, pdf toward wi, then a scatter from Random2(a, b): dir[3], pdf, f_r[3]. */
+void  orc_lambertian(const float color[4], const float Ng[3], const float wo[3], const float wi[3],
+                     uint32_t a, uint32_t b, float out[12]);
 
 /* --- full render: bnRender's generate/trace/shade loop for `spp`
        consecutive accumulation passes starting at accum_id_start.

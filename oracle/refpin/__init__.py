@@ -67,6 +67,9 @@ def lib() -> C.CDLL:
             "ref_trace_ray": (i, [vp, vp, vp, vp, i, vp, vp, i, f, f, f, vp, vp, f, C.POINTER(u64), C.POINTER(f),
                                   vp, vp]),
             "ref_rgba8": (None, [vp, i, i, vp]),
+            "ref_iso_hit": (i, [vp, vp, vp, vp, i, vp, f, vp, f, i, vp, vp, f, C.POINTER(u64), C.POINTER(f), vp,
+                                vp, vp]),
+            "ref_lambertian": (None, [vp, vp, vp, vp, u32, u32, vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -168,6 +171,31 @@ def trace_ray(scalars, origin, spacing, cells_per_mc, majorants, tf, domain, bas
                             domain[0], domain[1], base_density, _p(_f32(org)), _p(_f32(direction)), tmax,
                             C.byref(st), C.byref(t), _p(P), _p(alb))
     return bool(h), t.value, P, alb, st.value
+
+
+def iso_hit(scalars, origin, spacing, cells_per_mc, ranges, iso, color, opacity, inst, org, direction, tmax,
+            seed_state):
+    """MCIsoSurfaceAccel::isProg with an AnariMatte material for one ray:
+    (hit, new seed state, t, P, N as 3 uint16 halfs, albedo + alpha)."""
+    scalars = _f32(scalars)
+    dims, o, sp = _geom(scalars, origin, spacing)
+    st = C.c_uint64(seed_state)
+    t = C.c_float(0.0)
+    P = np.zeros(3, np.float32)
+    Nh = np.zeros(3, np.uint16)
+    alb = np.zeros(4, np.float32)
+    h = lib().ref_iso_hit(_p(scalars), _p(dims), _p(o), _p(sp), cells_per_mc, _p(_f32(ranges)), iso,
+                          _p(_f32(color)), opacity, inst, _p(_f32(org)), _p(_f32(direction)), tmax, C.byref(st),
+                          C.byref(t), _p(P), _p(Nh), _p(alb))
+    return bool(h), st.value, t.value, P, Nh, alb
+
+
+def lambertian(color, Ng, wo, wi, a: int, b: int) -> np.ndarray:
+    """The reference's AnariMatte Lambertian: eval value[3], eval pdf,
+    pdf(wi), scatter dir[3], scatter pdf, f_r[3]."""
+    out = np.zeros(12, np.float32)
+    lib().ref_lambertian(_p(_f32(color)), _p(_f32(Ng)), _p(_f32(wo)), _p(_f32(wi)), a, b, _p(out))
+    return out
 
 
 def rgba8(rgba, srgb: bool) -> np.ndarray:

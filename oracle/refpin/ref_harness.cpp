@@ -22,16 +22,27 @@
 //   barney/common/math.h            linear_to_srgb, make_8bit, make_rgba
 //   rtcore/embree/Texture.cpp       TextureData, TextureSamplerT::tex3D
 //   rtcore/embree/Float16.cpp       float32ToFloat16, float16ToFloat32
+//   barney/volume/MCAccelerator.h   MCIsoSurfaceAccel::isProg
+//   barney/material/DeviceMaterial.h, AnariMatte.h  createBSDF, setHit
+//   barney/packedBSDF/Lambertian.h  eval, pdf, scatter
+//   barney/render/DG.h              cosineSampleHemisphere, EvalRes
 // Restated here (glue of the embree backend, no arithmetic of the path):
-//   TraceInterface::transformPointFromObjectToWorldSpace (embree
-//   Device.cpp:31-35: xfmPoint(*objectToWorldXfm, v)); the trace set-up that
-//   rtcore/embree/Group.cpp:34-78 does before calling isProg (tmin 0, tmax
-//   = ray.tMax, instance 0, geometry 0, identity instance transform).
+//   TraceInterface::transformNormal/PointFromObjectToWorldSpace (embree
+//   Device.cpp:26-35: xfmVector(objectToWorldXfm->l, v), xfmPoint(
+//   *objectToWorldXfm, v)); the trace set-up that rtcore/embree/Group.cpp:
+//   34-78 does before calling isProg (tmin 0, tmax = ray.tMax, the
+//   instance's index, geometry 0, primitive 0, identity instance transform).
+// The owl math the reference calls (vec, box, frame, xfmVector ...) is the
+// shim's restatement: the owl submodule is absent, so what depends on it --
+// the Lambertian scatter direction through frame() -- is pinned only by
+// restatement.
 #include "barney/common/barney-common.h"
 #include "barney/common/math.h"
 #include "barney/volume/DDA.h"
 #include "barney/volume/Volume.h"
 #include "barney/volume/StructuredData.h"
+#include "barney/geometry/IsoSurface.h"
+#include "barney/material/DeviceMaterial.h"
 #include "rtcore/embree/Texture.h"
 #include "rtcore/embree/ComputeInterface.h"
 #include "rtcore/embree/TraceInterface.h"
@@ -41,7 +52,8 @@ using namespace BARNEY_NS;
 
 namespace rtc {
 namespace embree {
-// embree Device.cpp:31-35
+// embree Device.cpp:26-35
+vec3f TraceInterface::transformNormalFromObjectToWorldSpace(vec3f v) const { return xfmVector(objectToWorldXfm->l, v); }
 vec3f TraceInterface::transformPointFromObjectToWorldSpace(vec3f v) const { return xfmPoint(*objectToWorldXfm, v); }
 }  // namespace embree
 }  // namespace rtc
@@ -268,6 +280,129 @@ int ref_trace_ray(const float *scalars, const int dims[3], const float origin[3]
   const render::packedBSDF::Phase &phase = (const render::packedBSDF::Phase &)ray.hitBSDF;
   albedo[0] = phase.albedo.x; albedo[1] = phase.albedo.y; albedo[2] = phase.albedo.z;
   return 1;
+}
+
+// One ray against an iso-surface of the structured field:
+// MCIsoSurfaceAccel<StructuredDataSampler>::isProg (MCAccelerator.h:338-567)
+// as the embree backend calls it for the iso-surface's user geometry (tmin
+// 0, tmax = ray.tMax, geometry 0, primitive 0, instance `inst`, identity
+// instance transform), with one AnariMatte material of constant color and
+// opacity (DeviceMaterial::setHit, AnariMatte::DD::createBSDF).  ranges: the
+// field's macrocell scalar ranges, (lower, upper) per macrocell.  On a hit
+// returns 1 with *t_hit, P[3], the normal as Ray::setHit stores it (three
+// halfs) and the Lambertian's albedo (xyz) and alpha (w); *seed_state carries
+// the ray's RNG seed in and out.
+int ref_iso_hit(const float *scalars, const int dims[3], const float origin[3], const float spacing[3],
+                int cells_per_mc, const float *ranges, float iso, const float color[4], float opacity, int inst,
+                const float org[3], const float dir[3], float tmax, uint64_t *seed_state, float *t_hit, float P[3],
+                uint16_t N[3], float albedo[4]) {
+  Field f(scalars, dims);
+  MCIsoSurfaceAccel<StructuredDataSampler>::DD dd;
+  std::memset((void *)&dd, 0, sizeof(dd));
+  const vec3f gridOrigin(origin[0], origin[1], origin[2]), gridSpacing(spacing[0], spacing[1], spacing[2]);
+  const vec3i numCells(dims[0] - 1, dims[1] - 1, dims[2] - 1);
+  dd.isoSurface.sfCommon.worldBounds.lower = gridOrigin;
+  dd.isoSurface.sfCommon.worldBounds.upper = gridOrigin + gridSpacing * vec3f(numCells);
+  dd.isoSurface.sfSampler = f.sampler(dims, origin, spacing);
+  dd.isoSurface.isoValue = iso;
+  dd.isoSurface.materialID = 0;
+  dd.isoSurface.userID = 0;
+  dd.mcGrid.scalarRanges = (range1f *)const_cast<float *>(ranges);
+  dd.mcGrid.dims = divRoundUp(numCells, vec3i(cells_per_mc));
+  dd.mcGrid.gridOrigin = dd.isoSurface.sfCommon.worldBounds.lower;
+  dd.mcGrid.gridSpacing = vec3f((float)cells_per_mc) * gridSpacing;
+
+  // AnariMatte::getDD with VALUE parameters (Material.h:19-47, Material.cpp:37-52)
+  render::DeviceMaterial mat;
+  std::memset((void *)&mat, 0, sizeof(mat));
+  mat.type = render::DeviceMaterial::TYPE_AnariMatte;
+  mat.anariMatte.color.type = render::PossiblyMappedParameter::VALUE;
+  mat.anariMatte.color.value = rtc::float4{color[0], color[1], color[2], color[3]};
+  mat.anariMatte.opacity.type = render::PossiblyMappedParameter::VALUE;
+  mat.anariMatte.opacity.value = rtc::float4{opacity, 0.f, 0.f, 1.f};
+
+  render::Ray ray;
+  std::memset((void *)&ray, 0, sizeof(ray));
+  ray.org = vec3f(org[0], org[1], org[2]);
+  ray.dir = vec3f(dir[0], dir[1], dir[2]);
+  ray.tMax = tmax;
+  ray.rngSeed.state = *seed_state;
+  ray.bsdfType = PackedBSDF::NONE;
+
+  render::OptixGlobals globals;
+  std::memset((void *)&globals, 0, sizeof(globals));
+  globals.hitIDs = nullptr;
+  globals.world.materials = &mat;
+  globals.world.samplers = nullptr;
+
+  embree_for_barney::RTCRay er;
+  er.org_x = ray.org.x; er.org_y = ray.org.y; er.org_z = ray.org.z; er.tnear = 0.f;
+  er.dir_x = ray.dir.x; er.dir_y = ray.dir.y; er.dir_z = ray.dir.z; er.time = 0.f;
+  er.tfar = ray.tMax;
+  er.mask = ~0u; er.id = 0; er.flags = 0;
+  const affine3f identity{LinearSpace3f(vec3f(1.f, 0.f, 0.f), vec3f(0.f, 1.f, 0.f), vec3f(0.f, 0.f, 1.f)),
+                          vec3f(0.f)};
+  std::vector<int> instIDs(inst + 1);
+  for (int i = 0; i <= inst; i++) instIDs[i] = i;
+  rtc::embree::TraceInterface ti;
+  std::memset((void *)&ti, 0, sizeof(ti));
+  ti.isec_t = INFINITY;
+  ti.instIdx = inst;
+  ti.geomID = 0;
+  ti.primID = 0;
+  ti.worldOrigin = ray.org;
+  ti.worldDirection = ray.dir;
+  ti.prd = &ray;
+  ti.instIDs = instIDs.data();
+  ti.geomData = &dd;
+  ti.lpData = &globals;
+  ti.objectToWorldXfm = &identity;
+  ti.worldToObjectXfm = &identity;
+  ti.embreeRay = &er;
+  MCIsoSurfaceAccel<StructuredDataSampler>::isProg(ti);
+  *seed_state = ray.rngSeed.state;
+  if (ray.bsdfType == PackedBSDF::NONE) return 0;
+  *t_hit = ray.tMax;
+  P[0] = ray.P.x; P[1] = ray.P.y; P[2] = ray.P.z;
+  const uint16_t *nh = (const uint16_t *)&ray.N;
+  N[0] = nh[0]; N[1] = nh[1]; N[2] = nh[2];
+  const render::packedBSDF::Lambertian &lam = (const render::packedBSDF::Lambertian &)ray.hitBSDF;
+  albedo[0] = lam.albedo.x; albedo[1] = lam.albedo.y; albedo[2] = lam.albedo.z;
+  albedo[3] = lam.alpha;
+  return 1;
+}
+
+// The Lambertian BSDF an AnariMatte material of constant color makes
+// (AnariMatte.h:50-62, packedBSDF/Lambertian.h), at a surface point with
+// normal Ng (dg.Ng = dg.Ns, as shadeRays.cu:625-629 sets them) seen from
+// wo: eval and pdf toward wi, then one scatter drawing from Random2(a, b).
+// out: eval value[3], eval pdf, pdf(wi), scatter dir[3], scatter pdf,
+// scatter f_r[3].
+void ref_lambertian(const float color[4], const float Ng[3], const float wo[3], const float wi[3], uint32_t a,
+                    uint32_t b, float out[12]) {
+  render::AnariMatte::DD m;
+  std::memset((void *)&m, 0, sizeof(m));
+  m.color.type = render::PossiblyMappedParameter::VALUE;
+  m.color.value = rtc::float4{color[0], color[1], color[2], color[3]};
+  m.opacity.type = render::PossiblyMappedParameter::VALUE;
+  m.opacity.value = rtc::float4{1.f, 0.f, 0.f, 1.f};
+  render::HitAttributes hit;
+  const PackedBSDF bsdf = m.createBSDF(hit, nullptr, false);
+  render::DG dg;
+  dg.Ng = vec3f(Ng[0], Ng[1], Ng[2]);
+  dg.Ns = dg.Ng;
+  dg.wo = vec3f(wo[0], wo[1], wo[2]);
+  dg.P = vec3f(0.f);
+  dg.insideMedium = false;
+  const vec3f w(wi[0], wi[1], wi[2]);
+  const render::EvalRes e = bsdf.eval(dg, w);
+  out[0] = e.value.x; out[1] = e.value.y; out[2] = e.value.z; out[3] = e.pdf;
+  out[4] = bsdf.pdf(dg, w);
+  Random2 r(a, b);
+  render::ScatterResult s;
+  bsdf.scatter(s, dg, r);
+  out[5] = s.dir.x; out[6] = s.dir.y; out[7] = s.dir.z; out[8] = s.pdf;
+  out[9] = s.f_r.x; out[10] = s.f_r.y; out[11] = s.f_r.z;
 }
 
 // linear_to_srgb and the 8-bit packing of the frame-buffer read

@@ -72,7 +72,43 @@ def cases(seed: int = 2024) -> dict:
     c["rgba"] = np.concatenate([rng.random((1000, 4)).astype(np.float32) * np.float32(1.3),
                                 np.array([[0.0031308, 0.0031309, 1.0, 0.0], [0.5, 0.999, 1.001, 1.0]],
                                          np.float32)])
+    c.update(surface_cases())
     return c
+
+
+def surface_cases(seed: int = 2025) -> dict:
+    """Inputs of the iso-surface intersection program (the trace rays above
+    against two iso values, three materials and instance indices) and of the
+    AnariMatte Lambertian (random normals, view and light directions)."""
+    rng = np.random.default_rng(seed)
+    c = {}
+    c["iso_cpm"] = np.array([4], np.int32)
+    c["iso_values"] = np.array([0.25, 0.45], np.float32)
+    c["iso_colors"] = np.array([[0.8, 0.8, 0.8, 1.0], [0.2, 0.7, 0.4, 1.0], [1.0, 0.5, 0.25, 0.9]], np.float32)
+    c["iso_opacity"] = np.array([1.0, 1.0, 0.7], np.float32)
+    c["iso_inst"] = np.array([0, 1, 3], np.int32)
+    n = 2000
+    unit = lambda v: (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    c["lam_Ng"] = unit(rng.standard_normal((n, 3)))
+    c["lam_wo"] = unit(rng.standard_normal((n, 3)))
+    c["lam_wi"] = unit(rng.standard_normal((n, 3)))
+    c["lam_ab"] = rng.integers(0, 2 ** 32, size=(n, 2), dtype=np.uint64).astype(np.uint32)
+    c["lam_color"] = rng.random((n, 4)).astype(np.float32)
+    c["lam_color"][:, 3] = 1.0
+    c["lam_Ng"][:3] = np.eye(3, dtype=np.float32)  # axis-aligned normals
+    return c
+
+
+def iso_ranges(c: dict) -> np.ndarray:
+    """Macrocell scalar ranges of the trace field at the iso macrocell size,
+    from the oracle's range build."""
+    import oracle
+    from barney_gb300 import scenes
+    s = scenes.Scene(scalars=c["vol"], tf=c["tf_a"], base_density=40.0, cells_per_mc=int(c["iso_cpm"][0]))
+    o = oracle.Oracle(s)
+    o.rec.origin[:] = list(c["vol_origin"])
+    o.rec.spacing[:] = list(c["vol_spacing"])
+    return o.mc_ranges()
 
 
 def trace_majorants(c: dict) -> np.ndarray:
@@ -128,6 +164,29 @@ def reference_outputs(c: dict) -> dict:
     out["trace_majorants"] = maj
     out["rgba8"] = R.rgba8(c["rgba"], False)
     out["srgb8"] = R.rgba8(c["rgba"], True)
+    rg = iso_ranges(c)
+    out["iso_ranges"] = rg
+    hit, st, t, P, Nh, alb = [], [], [], [], [], []
+    for iv in c["iso_values"]:
+        for m in range(c["iso_colors"].shape[0]):
+            for o, d, tm, sd in zip(c["ray_org"], c["ray_dir"], c["ray_tmax"], c["ray_seed"]):
+                h, ns, tt, PP, NN, aa = R.iso_hit(c["vol"], c["vol_origin"], c["vol_spacing"], int(c["iso_cpm"][0]),
+                                                  rg, float(iv), c["iso_colors"][m], float(c["iso_opacity"][m]),
+                                                  int(c["iso_inst"][m]), o, d, float(tm), int(sd))
+                hit.append(h)
+                st.append(ns)
+                t.append(tt if h else 0.0)
+                P.append(PP)
+                Nh.append(NN)
+                alb.append(aa)
+    out["iso_hit"] = np.array(hit, np.int32)
+    out["iso_state"] = np.array(st, np.uint64)
+    out["iso_t"] = np.array(t, np.float32)
+    out["iso_P"] = np.stack(P).astype(np.float32)
+    out["iso_N"] = np.stack(Nh).astype(np.uint16)
+    out["iso_albedo"] = np.stack(alb).astype(np.float32)
+    out["lambertian"] = np.stack([R.lambertian(col, ng, wo, wi, int(a), int(b)) for col, ng, wo, wi, (a, b) in
+                                  zip(c["lam_color"], c["lam_Ng"], c["lam_wo"], c["lam_wi"], c["lam_ab"])])
     return out
 
 
@@ -139,7 +198,7 @@ def main() -> None:
     out = reference_outputs(c)
     np.savez_compressed(OUT, **{f"in_{k}": v for k, v in c.items()}, **{f"out_{k}": v for k, v in out.items()})
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes): {int(out['trace_hit'].sum())} of {len(out['trace_hit'])} "
-          f"rays hit")
+          f"rays hit the volume, {int(out['iso_hit'].sum())} of {len(out['iso_hit'])} the iso-surfaces")
 
 
 if __name__ == "__main__":

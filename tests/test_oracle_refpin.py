@@ -6,8 +6,10 @@ fastLog, the float/half conversions of its CPU backend, the transfer
 function's map and majorant, the structured field's sampler with the CPU
 backend's trilinear texture, sampleAndMap, the macrocell DDA and the whole
 per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
-stream, DDA over the majorant grid, Woodcock tracking, hit record), and the
-frame buffer's 8-bit and sRGB packing.  Their outputs on fixed inputs are
+stream, DDA over the majorant grid, Woodcock tracking, hit record), the
+iso-surface intersection program MCIsoSurfaceAccel::isProg with an AnariMatte
+material (hit search, normal, opacity test, Ray::setHit), the material's
+Lambertian BSDF, and the frame buffer's 8-bit and sRGB packing.  Their outputs on fixed inputs are
 stored in tests/golden/ref_pin.npz (tests/golden/make_ref_golden.py); the
 oracle must reproduce every one bit for bit.  Where the reference checkout
 is present the live library is also compared on fresh random inputs.
@@ -142,6 +144,51 @@ def test_volume_intersection_program(pin):
             assert np.array_equal(bits(P), bits(o["trace_P"][i])), i
             assert np.array_equal(bits(np.float32(0.7) * rgb), bits(o["trace_albedo"][i])), i
     assert nhit > 100
+
+
+def test_iso_surface_intersection_program(pin):
+    """MCIsoSurfaceAccel::isProg with an AnariMatte material: hit flag, t,
+    hit point, the normal in half precision, the Lambertian's albedo
+    (0.85 color / pi) and alpha, the opacity test's stream (opacity 0.7)
+    and the ray's RNG seed afterwards, for instance indices 0, 1 and 3."""
+    c, o = pin
+    cpm = int(c["iso_cpm"][0])
+    orc = _scene(c, c["tf_a"], (0.0, 1.0), 40.0, cells_per_mc=cpm)
+    rg = orc.mc_ranges()
+    assert np.array_equal(bits(rg), bits(o["iso_ranges"]))
+    k = 0
+    hits = 0
+    for iv in c["iso_values"]:
+        for m in range(c["iso_colors"].shape[0]):
+            for org, d, tm, sd in zip(c["ray_org"], c["ray_dir"], c["ray_tmax"], c["ray_seed"]):
+                h, st, t, P, Nh, alb = orc.iso_hit(org, d, float(tm), int(sd), float(iv), c["iso_colors"][m],
+                                                   float(c["iso_opacity"][m]), int(c["iso_inst"][m]), ranges=rg)
+                assert h == bool(o["iso_hit"][k]), k
+                assert st == int(o["iso_state"][k]), k
+                if h:
+                    hits += 1
+                    assert bits(np.float32(t)) == bits(o["iso_t"][k]), k
+                    assert np.array_equal(bits(P), bits(o["iso_P"][k])), k
+                    assert np.array_equal(Nh, o["iso_N"][k]), k
+                    assert np.array_equal(bits(alb), bits(o["iso_albedo"][k])), k
+                k += 1
+    assert hits > 1000
+    # the opacity test let some rays through that the opaque material stops
+    per = len(c["ray_org"])
+    assert o["iso_hit"][2 * per:3 * per].sum() < o["iso_hit"][0:per].sum()
+
+
+def test_lambertian_bsdf(pin):
+    """The AnariMatte Lambertian: eval (value, pdf), pdf, and a scatter
+    (direction, pdf, f_r).  The scatter takes its two draws in the order the
+    reference's gcc build evaluates vec2f s(random(), random()): the second
+    argument first.  The direction goes through owl's frame(), which the
+    reference pin restates (the owl source is absent)."""
+    c, o = pin
+    got = np.stack([oracle.lambertian(col, ng, wo, wi, int(a), int(b)) for col, ng, wo, wi, (a, b) in
+                    zip(c["lam_color"], c["lam_Ng"], c["lam_wo"], c["lam_wi"], c["lam_ab"])])
+    assert np.array_equal(bits(got), bits(o["lambertian"]))
+    assert (o["lambertian"][:, 3] == 0).sum() > 500  # light below the surface: pdf 0
 
 
 def test_frame_buffer_packing(pin):
