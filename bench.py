@@ -577,7 +577,10 @@ def profile_render_case(args):
     that ncu's DRAM bytes of the uncounted launches can be related to
     density samples (the frame is deterministic).  Capture the uncounted
     launches with
-      ncu --clock-control none -k regex:render_kernel -s <warmup> -c <launches> ..."""
+      ncu --clock-control none -k regex:render_kernel -s <warmup> -c <launches> ...
+    With --mode wavefront a frame is a sequence of wf_trace_kernel and
+    wf_shade_kernel launches (one of each per step).  Count=0 in the trace
+    kernel's template arguments marks the uncounted frames."""
     import torch
     from barney_gb300 import _native as N, scenes
     from barney_gb300.device import GpuScene
@@ -586,14 +589,16 @@ def profile_render_case(args):
     layout = N.GBV_LAYOUT_BRICK_CORNERS if args.layout == "brick" else N.GBV_LAYOUT_LINEAR
     g = GpuScene(s, layout=layout, fmt=fmt)
     acc = g.new_accum()
+    cfg = {"mode": N.GBV_RENDER_WAVEFRONT} if args.mode == "wavefront" else None
     for _ in range(args.warmup + args.launches):
-        g.render(accum=acc)
+        g.render(accum=acc, config=cfg)
     cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
-    g.render(accum=acc, counters=cnt)
+    g.render(accum=acc, counters=cnt, config=cfg)
     torch.cuda.synchronize()
     c = [int(x) for x in cnt.cpu().tolist()]
     rec = dict(dims=args.dims, width=args.width, height=args.height, spp=args.spp, format=args.format,
-               layout=args.layout, samples_per_launch=c[0], mc_visits_per_launch=c[1], rays_per_launch=c[2])
+               layout=args.layout, mode=args.mode, samples_per_launch=c[0], mc_visits_per_launch=c[1],
+               rays_per_launch=c[2])
     if args.out:
         Path(args.out).parent.mkdir(parents=True, exist_ok=True)
         Path(args.out).write_text(json.dumps(rec, indent=1))
@@ -640,6 +645,9 @@ def main():
     ap.add_argument("--height", type=int, default=270, help="--profile-case render: frame height")
     ap.add_argument("--spp", type=int, default=1, help="--profile-case render: passes per launch")
     ap.add_argument("--layout", default="brick", choices=["brick", "linear"], help="--profile-case render")
+    ap.add_argument("--mode", default="persistent", choices=["persistent", "wavefront"],
+                    help="--profile-case render: the persistent kernel, or the trace/shade kernels per step "
+                         "(a frame is then many launches of each)")
     ap.add_argument("--launches", type=int, default=1, help="--profile-case: launches after the warm-up")
     ap.add_argument("--views", type=int, default=32, help="--profile-case ea: views")
     ap.add_argument("--size", type=int, default=256, help="--profile-case ea: view edge in pixels")

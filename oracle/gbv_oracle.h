@@ -9,7 +9,8 @@
  * for this path and cannot be built as a whole here, but its sources for the
  * path compile unchanged against a restated owl and a stubbed embree API
  * (oracle/refpin, `make ref`); the RNG, fastLog, float/half, the transfer
- * function, the field sampler, sampleAndMap, the per-ray isProg, the sRGB
+ * function, the field sampler, sampleAndMap, the per-ray volume isProg, the
+ * iso-surface isProg with a matte material, the Lambertian BSDF, the sRGB
  * packing and the NanoVDB field code agree with this oracle bit for bit
  * (tests/test_oracle_refpin.py).  Ray generation and shading are pinned by
  * known-answer tests and a second, pure-Python restatement of the scalar

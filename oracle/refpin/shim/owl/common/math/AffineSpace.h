@@ -11,8 +11,9 @@ struct LinearSpace3f {
   LinearSpace3f() = default;
   LinearSpace3f(const vec3f &x, const vec3f &y, const vec3f &z) : vx(x), vy(y), vz(z) {}
 };
-// Orthonormal frame around N (used by the reference's surface BSDFs, which
-// are not on the structured-volume path; present so their headers compile).
+// Orthonormal frame around a unit normal N, as the reference's surface BSDFs
+// call it (the Lambertian's scatter: xfmVector(frame(N), localDir)): dx the
+// longer of (1,0,0) x N and (0,1,0) x N, normalized; dy = normalize(N x dx).
 inline LinearSpace3f frame(const vec3f &N) {
   const vec3f dx0 = cross(vec3f(1.f, 0.f, 0.f), N), dx1 = cross(vec3f(0.f, 1.f, 0.f), N);
   const vec3f dx = normalize(dot(dx0, dx0) > dot(dx1, dx1) ? dx0 : dx1);
