@@ -217,6 +217,15 @@ struct Random {
 constexpr uint64_t kFnvOffset = 0xcbf29ce484222325ull;
 constexpr uint64_t kFnvPrime = 0x100000001b3ull;
 constexpr uint64_t kVolumeStreamHash = ((kFnvOffset ^ (kFnvPrime * 0ull)) * kFnvPrime ^ 0ull) * kFnvPrime ^ 0ull;
+// The hash a hit's distance gives the shading step's random streams
+// (shadeRays.cu:610, 722: Random(ray.rngSeed, (const uint32_t&)ray.tMax) and
+// ray.rngSeed.next((const uint32_t&)ray.tMax)).  A C-style cast to a const
+// reference of another type is a static_cast that converts the value into a
+// temporary, so the hash is the distance truncated to an integer (0 for
+// t < 1, where Random2 falls back to 290374), not its bit pattern.  Hit
+// distances are finite, positive and far below 2^32, where host and device
+// conversions agree.
+GBV_HD uint32_t hit_hash(float t) { return (uint32_t)t; }
 // hash(a, b, c) (barney-common.h:132-146): the stream id of instance a,
 // geometry b, primitive c
 GBV_HD uint64_t fnv_hash3(uint32_t a, uint32_t b, uint32_t c) {

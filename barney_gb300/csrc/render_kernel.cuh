@@ -624,7 +624,7 @@ __device__ __forceinline__ void bounce_volume_hit(const RenderParams &p, PathRay
       out.shadow.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
       out.shadow.tp = to_half(tp_sr);
       out.shadow.seed = ray.seed;
-      ray.seed.next_h((uint64_t)float_bits(tHit));
+      ray.seed.next_h((uint64_t)hit_hash(tHit));
       out.shadow.misWeight = 1.f;
       out.shadowValid = true;
       if (!isDir && needsMIS) {
@@ -727,7 +727,7 @@ static __device__ __noinline__ void bounce_surface_hit(const RenderParams &p, Pa
       out.shadow.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
       out.shadow.tp = to_half(tp_sr);
       out.shadow.seed = ray.seed;
-      ray.seed.next_h((uint64_t)float_bits(tHit));
+      ray.seed.next_h((uint64_t)hit_hash(tHit));
       out.shadow.misWeight = 1.f;
       out.shadowValid = true;
       if (!isDir && needsMIS) {
@@ -1361,7 +1361,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
       const bool anyHit = h.hit || (Iso && sHit);
       if (kind == K_MAIN) {
         if (anyHit) {
-          rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.hit ? h.t : sT));
+          rnd = Random::derive(ray.seed, (uint64_t)hit_hash(h.hit ? h.t : sT));
           if (p.hasEnv) {
             pick = Batch ? env_pick_coords_ool(p, rnd) : env_pick_coords(p, rnd);
             uv = make_float2(pick.sx, pick.sy);

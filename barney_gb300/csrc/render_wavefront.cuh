@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256, GBV_WF_SHADE_BLOCKS) wf_shade_kernel(cons
         float2 uv = make_float2(0.f, 0.f);
         bool needTex = false;
         if (h.hit) {
-          rnd = Random::derive(ray.seed, (uint64_t)float_bits(h.t));
+          rnd = Random::derive(ray.seed, (uint64_t)hit_hash(h.t));
           if (p.hasEnv) {
             pick = env_pick_coords(p, rnd);
             uv = make_float2(pick.sx, pick.sy);

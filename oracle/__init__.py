@@ -42,6 +42,29 @@ class OrcScene(C.Structure):
     ]
 
 
+class OrcShadeWorld(C.Structure):
+    """orc_shade_world: the world one shading step sees (DD-level values)."""
+    _fields_ = [
+        ("num_dir_lights", C.c_int), ("dir_light_dir", _f3 * 4), ("dir_light_color", _f3 * 4),
+        ("dir_light_radiance", C.c_float * 4),
+        ("env_texels", C.c_void_p), ("env_dims", C.c_int * 2), ("env_addr", C.c_int * 2),
+        ("env_to_world", C.c_float * 9), ("env_to_local", C.c_float * 9), ("env_scale", C.c_float),
+        ("env_cdf_y", C.c_void_p), ("env_cdf_x", C.c_void_p),
+        ("ambient_radiance", C.c_float), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
+    ]
+
+
+class OrcShadePath(C.Structure):
+    """orc_shade_path: a ray with its hit record and path state."""
+    _fields_ = [
+        ("org", _f3), ("dir", _f3), ("tmax", C.c_float), ("seed", C.c_uint64), ("hit", C.c_int),
+        ("P", _f3), ("rgb", _f3), ("g", C.c_float), ("scattering_albedo", C.c_float), ("N", _f3),
+        ("color", C.c_float * 4), ("opacity", C.c_float), ("shadow", C.c_int), ("tp", C.c_uint16 * 3),
+        ("pad", C.c_uint16), ("mis", C.c_float), ("diffuse_bounces", C.c_int), ("volume_bounces", C.c_int),
+        ("miss_color", C.c_float * 4),
+    ]
+
+
 class OrcStats(C.Structure):
     _fields_ = [("density_samples", C.c_uint64), ("mc_visits", C.c_uint64), ("rays", C.c_uint64)]
 
@@ -87,6 +110,8 @@ def lib() -> C.CDLL:
             "orc_iso_hit": (i, [sp, vp, f, vp, f, i, vp, vp, f, C.POINTER(C.c_uint64), C.POINTER(C.c_float),
                                 vp, vp, vp]),
             "orc_lambertian": (None, [vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp]),
+            "orc_bounce": (None, [C.POINTER(OrcShadeWorld), i, i, C.POINTER(OrcShadePath), C.POINTER(OrcShadePath),
+                                  vp]),
             "orc_render": (None, [sp, vp, i, i, i, i, i, i, C.POINTER(OrcStats)]),
             "orc_tonemap": (None, [vp, i, i, i, i, vp]),
             "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
@@ -333,6 +358,25 @@ def lambertian(color, Ng, wo, wi, a: int, b: int) -> np.ndarray:
     f4 = lambda v: _p(np.ascontiguousarray(v, np.float32))
     lib().orc_lambertian(f4(color), f4(Ng), f4(wo), f4(wi), a, b, _p(out))
     return out
+
+
+def bounce(world: OrcShadeWorld, multi: bool, depth: int, path: OrcShadePath):
+    """One shading step (orc_bounce) of the default or the multi-scatter
+    build: (path afterwards, shadow ray, fragment); the inputs are copied."""
+    io = OrcShadePath.from_buffer_copy(path)
+    sh = OrcShadePath()
+    frag = np.zeros(3, np.float32)
+    lib().orc_bounce(C.byref(world), 1 if multi else 0, depth, C.byref(io), C.byref(sh), _p(frag))
+    return io, sh, frag
+
+
+def env_cdfs(texels: np.ndarray, addr) -> tuple:
+    """The env map's importance tables (orc_env_cdfs): cdf_y (H), cdf_x (H*W)."""
+    texels = np.ascontiguousarray(texels, np.float32)
+    H, W, _ = texels.shape
+    cy, cx = np.empty(H, np.float32), np.empty(H * W, np.float32)
+    lib().orc_env_cdfs(_p(texels), _p(np.array([W, H], np.int32)), _p(np.asarray(addr, np.int32)), _p(cy), _p(cx))
+    return cy, cx
 
 
 def rng_sequence(a: int, b: int, n: int) -> np.ndarray:

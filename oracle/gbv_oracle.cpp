@@ -268,6 +268,11 @@ inline uint64_t fnv_hash1(uint32_t v) {          // :132-137
 inline uint64_t fnv_hash2(uint64_t h, uint32_t v) { return (h * 0x100000001b3ull) ^ (uint64_t)v; }
 inline uint64_t fnv_hash3(uint32_t a, uint32_t b, uint32_t c) { return fnv_hash2(fnv_hash2(fnv_hash1(a), b), c); }
 inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+// The shading step's `(const uint32_t&)ray.tMax` (shadeRays.cu:610, 722): a
+// C-style cast to a const reference of another type is a static_cast that
+// converts the value into a temporary -- the hit distance truncated to an
+// integer, not its bits.
+inline uint32_t hit_hash(float t) { return static_cast<uint32_t>(t); }
 
 // Volume.h:174-184
 inline float fastLog(float f) {
@@ -1520,7 +1525,7 @@ inline V3<float> bounce_surface(const Scene &S, Ray &ray, PathState &state, Ray 
   const V3<float> Ng = normalize(fromh(ray.N));
   const bool hitWasOnFront = dot(ray.dir, Ng) < 0.f;
   const V3<float> Ngff = hitWasOnFront ? Ng : -Ng;
-  Random2 random(ray.rngSeed, (uint64_t)fbits(ray.tMax));
+  Random2 random(ray.rngSeed, (uint64_t)hit_hash(ray.tMax));
   // DG (shadeRays.cu:625-629): Ng = Ns = the unflipped normal
   const V3<float> P = ray.P;
   const V3<float> wo = -normalize(ray.dir);
@@ -1546,7 +1551,7 @@ inline V3<float> bounce_surface(const Scene &S, Ray &ray, PathState &state, Ray 
       shadowRay.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
       shadowState.throughput = toh(tp_sr);
       shadowRay.rngSeed = ray.rngSeed;
-      ray.rngSeed.next_h((uint64_t)fbits(ray.tMax));
+      ray.rngSeed.next_h((uint64_t)hit_hash(ray.tMax));
       shadowState.misWeight = 1.f;
       shadowValid = true;
       if (!isDir && needsMIS) {
@@ -1636,7 +1641,7 @@ inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowR
   if (ray.surf) return bounce_surface(S, ray, state, shadowRay, shadowState, shadowValid, pathDepth);
   // volume hit: isVolumeHit, hitWasOnFront false, Ngff = -Ng = -0
   const V3<float> Ngff(-0.f, -0.f, -0.f);
-  Random2 random(ray.rngSeed, (uint64_t)fbits(ray.tMax));
+  Random2 random(ray.rngSeed, (uint64_t)hit_hash(ray.tMax));
   // DG (shadeRays.cu:625-639)
   const V3<float> P = ray.P;
   const V3<float> wo = -normalize(ray.dir);
@@ -1665,7 +1670,7 @@ inline V3<float> bounce(const Scene &S, Ray &ray, PathState &state, Ray &shadowR
       shadowRay.tMax = ls.distance * (1.f - 2.f * offsetEpsilon);
       shadowState.throughput = toh(tp_sr);
       shadowRay.rngSeed = ray.rngSeed;
-      ray.rngSeed.next_h((uint64_t)fbits(ray.tMax));
+      ray.rngSeed.next_h((uint64_t)hit_hash(ray.tMax));
       shadowState.misWeight = 1.f;
       shadowValid = true;
       if (!isDir && needsMIS) {
@@ -2147,6 +2152,99 @@ void orc_lambertian(const float color[4], const float Ng_[3], const float wo_[3]
   out[5] = d.x; out[6] = d.y; out[7] = d.z;
   out[8] = local.z * ONE_OVER_PI;
   out[9] = albedo.x; out[10] = albedo.y; out[11] = albedo.z;
+}
+
+// bounce() on a world and path given as DD-level records (the reference
+// pin's ref_bounce takes the same), for the shading pin tests.
+void orc_bounce(const orc_shade_world *w, int multi, int depth, orc_shade_path *io, orc_shade_path *sh,
+                float fragment[3]) {
+  Scene S;
+  S.numDir = std::min(4, std::max(0, w->num_dir_lights));
+  for (int i = 0; i < S.numDir; i++) {
+    S.dir[i].direction = V3<float>(w->dir_light_dir[i][0], w->dir_light_dir[i][1], w->dir_light_dir[i][2]);
+    S.dir[i].color = V3<float>(w->dir_light_color[i][0], w->dir_light_color[i][1], w->dir_light_color[i][2]);
+    S.dir[i].radiance = w->dir_light_radiance[i];
+  }
+  S.env.boundedMath = false;
+  if (w->env_texels) {
+    Env &e = S.env;
+    e.present = true;
+    e.tex = w->env_texels;
+    e.W = w->env_dims[0];
+    e.H = w->env_dims[1];
+    e.addr[0] = w->env_addr[0];
+    e.addr[1] = w->env_addr[1];
+    e.scale = w->env_scale;
+    const float *a = w->env_to_world, *b = w->env_to_local;
+    e.toWorld.vx = V3<float>(a[0], a[1], a[2]);
+    e.toWorld.vy = V3<float>(a[3], a[4], a[5]);
+    e.toWorld.vz = V3<float>(a[6], a[7], a[8]);
+    e.toLocal.vx = V3<float>(b[0], b[1], b[2]);
+    e.toLocal.vy = V3<float>(b[3], b[4], b[5]);
+    e.toLocal.vz = V3<float>(b[6], b[7], b[8]);
+    e.cdf_y.assign(w->env_cdf_y, w->env_cdf_y + e.H);
+    e.cdf_x.assign(w->env_cdf_x, w->env_cdf_x + (size_t)e.W * e.H);
+  }
+  S.ambient = w->ambient_radiance;
+  S.multi = multi;
+  S.volMS = w->volume_multi_scatter;
+  S.maxVB = w->max_volume_bounces;
+  Ray ray;
+  ray.org = V3<float>(io->org[0], io->org[1], io->org[2]);
+  ray.dir = V3<float>(io->dir[0], io->dir[1], io->dir[2]);
+  ray.tMax = io->tmax;
+  ray.rngSeed.state = io->seed;
+  ray.P = V3<float>(io->P[0], io->P[1], io->P[2]);
+  ray.hit = io->hit != 0;
+  ray.surf = io->hit == 2;
+  ray.isShadowRay = io->shadow != 0;
+  ray.missColor = {io->miss_color[0], io->miss_color[1], io->miss_color[2], io->miss_color[3]};
+  ray.g = 0.f;
+  const V3<float> rgb(io->rgb[0], io->rgb[1], io->rgb[2]);
+  if (io->hit == 1) {
+    ray.albedo = multi ? io->scattering_albedo * rgb : .7f * rgb;  // Phase(color) (Phase.h:40-46, 121-129)
+    ray.g = multi ? io->g : 0.f;
+  } else if (io->hit == 2) {
+    V4<float> base{io->color[0], io->color[1], io->color[2], io->color[3]};
+    if (std::isnan(base.x)) base = {0.f, 0.f, 0.f, 1.f};
+    S.isoAlbedo = .85f * V3<float>(base.x, base.y, base.z) * ONE_OVER_PI;
+    S.isoAlpha = base.w * (std::isnan(io->opacity) ? 0.f : io->opacity);
+    ray.N = toh(V3<float>(io->N[0], io->N[1], io->N[2]));
+  }
+  PathState st;
+  st.throughput = {io->tp[0], io->tp[1], io->tp[2]};
+  st.misWeight = io->mis;
+  st.numDiffuseBounces = io->diffuse_bounces;
+  st.numVolumeBounces = io->volume_bounces;
+  Ray sray;
+  PathState sst;
+  bool sValid = false;
+  const V3<float> f = bounce(S, ray, st, sray, sst, sValid, depth);
+  fragment[0] = f.x; fragment[1] = f.y; fragment[2] = f.z;
+  for (int a = 0; a < 3; a++) {
+    io->org[a] = ray.org[a];
+    io->dir[a] = ray.dir[a];
+  }
+  io->tmax = ray.tMax;
+  io->seed = ray.rngSeed.state;
+  io->hit = ray.hit ? (ray.surf ? 2 : 1) : 0;
+  io->tp[0] = st.throughput.x; io->tp[1] = st.throughput.y; io->tp[2] = st.throughput.z;
+  io->mis = st.misWeight;
+  io->diffuse_bounces = st.numDiffuseBounces;
+  io->volume_bounces = st.numVolumeBounces;
+  std::memset(sh, 0, sizeof(*sh));
+  sh->tmax = -1.f;
+  if (sValid) {
+    for (int a = 0; a < 3; a++) {
+      sh->org[a] = sray.org[a];
+      sh->dir[a] = sray.dir[a];
+    }
+    sh->tmax = sray.tMax;
+    sh->seed = sray.rngSeed.state;
+    sh->shadow = 1;
+    sh->tp[0] = sst.throughput.x; sh->tp[1] = sst.throughput.y; sh->tp[2] = sst.throughput.z;
+    sh->mis = sst.misWeight;
+  }
 }
 
 void orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp, int use_double, int nthreads,

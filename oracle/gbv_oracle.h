@@ -10,9 +10,10 @@
  * path compile unchanged against a restated owl and a stubbed embree API
  * (oracle/refpin, `make ref`); the RNG, fastLog, float/half, the transfer
  * function, the field sampler, sampleAndMap, the per-ray volume isProg, the
- * iso-surface isProg with a matte material, the Lambertian BSDF, the sRGB
- * packing and the NanoVDB field code agree with this oracle bit for bit
- * (tests/test_oracle_refpin.py).  Ray generation and shading are pinned by
+ * iso-surface isProg with a matte material, the Lambertian BSDF, the
+ * shading step bounce() of both scattering builds, the env-map importance
+ * tables, the sRGB packing and the NanoVDB field code agree with this oracle
+ * bit for bit (tests/test_oracle_refpin.py).  Ray generation is pinned by
  * known-answer tests and a second, pure-Python restatement of the scalar
  * kernels (tests/golden/make_golden.py).
  */
@@ -154,6 +155,46 @@ int   orc_iso_hit(const orc_scene *s, const float *ranges, float iso, const floa
    pdf, pdf toward wi, then a scatter from Random2(a, b): dir[3], pdf, f_r[3]. */
 void  orc_lambertian(const float color[4], const float Ng[3], const float wo[3], const float wi[3],
                      uint32_t a, uint32_t b, float out[12]);
+
+/* --- one shading step, bounce() (shadeRays.cu:477-878), on a given world
+       and path: the records the reference pin (ref_bounce) shares --- */
+typedef struct orc_shade_world {
+  int   num_dir_lights;            /* DirLight::DD: unit direction, colour, radiance */
+  float dir_light_dir[4][3];
+  float dir_light_color[4][3];
+  float dir_light_radiance[4];
+  const float *env_texels;         /* RGBA float env map, or 0: none */
+  int   env_dims[2];
+  int   env_addr[2];
+  float env_to_world[9], env_to_local[9];  /* EnvMapLight::DD toWorld/toLocal: columns vx, vy, vz */
+  float env_scale;
+  const float *env_cdf_y, *env_cdf_x;      /* its importance tables */
+  float ambient_radiance;
+  int   volume_multi_scatter, max_volume_bounces;  /* multi-scatter build */
+} orc_shade_world;
+
+typedef struct orc_shade_path {
+  float org[3], dir[3], tmax;      /* on a hit: tmax = the hit's t */
+  uint64_t seed;                   /* ray.rngSeed */
+  int   hit;                       /* 0 none; 1 volume (Phase of rgb); 2 surface (AnariMatte Lambertian) */
+  float P[3];
+  float rgb[3];                    /* volume hit: the sampled colour */
+  float g, scattering_albedo;      /* volume hit, multi-scatter build */
+  float N[3];                      /* surface hit: unit normal (stored in half precision) */
+  float color[4], opacity;         /* surface hit: the matte material */
+  int   shadow;                    /* isShadowRay */
+  uint16_t tp[3];                  /* PathState throughput (halfs) */
+  uint16_t pad;
+  float mis;
+  int   diffuse_bounces, volume_bounces;
+  float miss_color[4];
+} orc_shade_path;
+
+/* bounce() of the default (multi = 0) or the multi-scatter build (multi = 1)
+   at path depth `depth`: updates *ray (dead: tmax = -1), fills *shadow
+   (none: tmax = -1) and fragment[3]; libm sines and cosines. */
+void  orc_bounce(const orc_shade_world *w, int multi, int depth, orc_shade_path *ray,
+                 orc_shade_path *shadow, float fragment[3]);
 
 /* --- full render: bnRender's generate/trace/shade loop for `spp`
        consecutive accumulation passes starting at accum_id_start.

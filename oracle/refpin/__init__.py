@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
             "ref_iso_hit": (i, [vp, vp, vp, vp, i, vp, f, vp, f, i, vp, vp, f, C.POINTER(u64), C.POINTER(f), vp,
                                 vp, vp]),
             "ref_lambertian": (None, [vp, vp, vp, vp, u32, u32, vp]),
+            "ref_env_cdfs": (None, [vp, vp, vp, vp, vp]),
+            "ref_shade_multi_scatter": (i, []),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -196,6 +198,51 @@ def lambertian(color, Ng, wo, wi, a: int, b: int) -> np.ndarray:
     out = np.zeros(12, np.float32)
     lib().ref_lambertian(_p(_f32(color)), _p(_f32(Ng)), _p(_f32(wo)), _p(_f32(wi)), a, b, _p(out))
     return out
+
+
+_lib_ms = None
+
+
+def _shade_lib(multi: bool) -> C.CDLL:
+    """The default build's pin (lib()) or the multi-scatter build's
+    (_ref/libbarney_ref_ms.so: the shading step compiled with
+    BARNEY_USE_MULTI_SCATTERING=1)."""
+    global _lib_ms
+    from oracle import OrcShadePath, OrcShadeWorld
+    L = lib()
+    if multi:
+        if _lib_ms is None:
+            _lib_ms = C.CDLL(str(LIB.parent / "libbarney_ref_ms.so"))
+            _lib_ms.ref_shade_multi_scatter.restype = C.c_int
+        L = _lib_ms
+    fn = L.ref_bounce
+    fn.restype = None
+    fn.argtypes = [C.POINTER(OrcShadeWorld), C.c_int, C.POINTER(OrcShadePath), C.POINTER(OrcShadePath), C.c_void_p]
+    assert L.ref_shade_multi_scatter() == (1 if multi else 0)
+    return L
+
+
+def bounce(world, multi: bool, depth: int, path):
+    """The reference's bounce() of the default or the multi-scatter build on
+    oracle.OrcShadeWorld / OrcShadePath records: (path afterwards, shadow
+    ray, fragment); the inputs are copied."""
+    from oracle import OrcShadePath
+    L = _shade_lib(multi)
+    io = OrcShadePath.from_buffer_copy(path)
+    sh = OrcShadePath()
+    frag = np.zeros(3, np.float32)
+    L.ref_bounce(C.byref(world), depth, C.byref(io), C.byref(sh), _p(frag))
+    return io, sh, frag
+
+
+def env_cdfs(texels, addr) -> tuple:
+    """EnvMapLight::computeCDFs' tables: cdf_y (H), cdf_x (H*W)."""
+    texels = _f32(texels)
+    H, W, _ = texels.shape
+    cy, cx = np.empty(H, np.float32), np.empty(H * W, np.float32)
+    lib().ref_env_cdfs(_p(texels), _p(np.array([W, H], np.int32)), _p(np.asarray(addr, np.int32)), _p(cy), _p(cx))
+    C.CDLL(None).fflush(None)  # the border address mode prints a line per lookup (Texture.cpp:79)
+    return cy, cx
 
 
 def rgba8(rgba, srgb: bool) -> np.ndarray:

@@ -4,11 +4,12 @@ The reference's public header barney/include/barney.h and its
 barney/common/barneyConfig.h.in are CMake templates (#cmakedefine01,
 @VAR@).  This step does what the reference build's configure_file does for
 an embree-only (CPU backend), single-process build with NanoVDB (its
-headers are vendored in the reference, 3rdParty/nanovdb) and without MPI,
-denoisers or the multi-scatter build option, and writes the configured
-headers to oracle/_ref/gen/barney/ (build output, never committed).
+headers are vendored in the reference, 3rdParty/nanovdb) and without MPI
+or denoisers, and writes the configured headers to <out dir>/barney/ (build
+output, never committed): the default build, or with --multi-scatter the
+build with the BARNEY_USE_MULTI_SCATTERING option on (CMakeLists.txt:219-226).
 
-  python oracle/refpin/configure.py <reference root> <out dir>
+  python oracle/refpin/configure.py <reference root> <out dir> [--multi-scatter]
 """
 import re
 import sys
@@ -34,7 +35,8 @@ def configure(text: str) -> str:
     return text
 
 
-def main(ref: str, out: str) -> None:
+def main(ref: str, out: str, multi_scatter: bool = False) -> None:
+    VALUES["BARNEY_USE_MULTI_SCATTERING"] = "1" if multi_scatter else "0"
     ref_root, out_dir = Path(ref), Path(out) / "barney"
     out_dir.mkdir(parents=True, exist_ok=True)
     (out_dir / "barney.h").write_text(configure((ref_root / "barney/include/barney.h").read_text()))
@@ -42,4 +44,4 @@ def main(ref: str, out: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2])
+    main(sys.argv[1], sys.argv[2], "--multi-scatter" in sys.argv[3:])

@@ -25,6 +25,9 @@ template <typename T> struct vec_t<T, 3> {
   template <typename U> explicit vec_t(const vec_t<U, 3> &o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
   // the xyz of a 4-vector
   template <typename U> explicit vec_t(const vec_t<U, 4> &o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
+  // a plain struct of x, y, z (the backends' float3 records)
+  template <typename S, typename = decltype(S::x), typename = decltype(S::z)>
+  explicit vec_t(const S &o, ...) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
   T &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
   T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
 };

@@ -9,7 +9,10 @@ per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
 stream, DDA over the majorant grid, Woodcock tracking, hit record), the
 iso-surface intersection program MCIsoSurfaceAccel::isProg with an AnariMatte
 material (hit search, normal, opacity test, Ray::setHit), the material's
-Lambertian BSDF, and the frame buffer's 8-bit and sRGB packing.  Their outputs on fixed inputs are
+Lambertian BSDF, the shading step bounce() of the default and the
+multi-scatter build with the env map's importance tables
+(tests/golden/shade_pin.npz, make_shade_golden.py), and the frame buffer's
+8-bit and sRGB packing.  Their outputs on fixed inputs are
 stored in tests/golden/ref_pin.npz (tests/golden/make_ref_golden.py); the
 oracle must reproduce every one bit for bit.  Where the reference checkout
 is present the live library is also compared on fresh random inputs.
@@ -23,6 +26,7 @@ import oracle
 from oracle import refpin
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "ref_pin.npz"
+SHADE = GOLDEN.parent / "shade_pin.npz"
 
 
 @pytest.fixture(scope="module")
@@ -191,6 +195,63 @@ def test_lambertian_bsdf(pin):
     assert (o["lambertian"][:, 3] == 0).sum() > 500  # light below the surface: pdf 0
 
 
+def _shade_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_shade_golden", SHADE.parent / "make_shade_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="module")
+def shade():
+    z = np.load(SHADE)
+    c = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    o = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return c, o
+
+
+def test_env_importance_tables(shade):
+    """EnvMapLight::computeCDFs (EnvMap.cu:181-238): per-texel weights from
+    the 3x3 texture taps, row CDFs, the row weights and their CDF, for the
+    sky map and a random map under every address mode."""
+    c, o = shade
+    mod = _shade_module()
+    for t, tex in enumerate(mod.env_textures()):
+        for a, addr in enumerate(c["addrs"]):
+            cy, cx = oracle.env_cdfs(tex, tuple(int(v) for v in addr))
+            assert np.array_equal(bits(cy), bits(o[f"cdf_y_{t}_{a}"])), (t, addr)
+            assert np.array_equal(bits(cx), bits(o[f"cdf_x_{t}_{a}"])), (t, addr)
+
+
+def test_shading_step(shade):
+    """bounce() (shadeRays.cu:477-878) of the default and the multi-scatter
+    build: misses (background and env light), shadow rays, volume hits
+    (Phase) and matte-surface hits (Lambertian) at depths 0..10, on worlds
+    with directional lights, an env map and ambient light -- light
+    selection, env-map importance sampling, MIS weights, the phase and
+    Lambertian scatter, bounce limits and the path's random streams, all bit
+    for bit."""
+    c, o = shade
+    mod = _shade_module()
+    got = mod.run(c, oracle.bounce, (o["cdf_y_0_0"], o["cdf_x_0_0"]))
+    ref = o["bounce"]
+    assert np.array_equal(got, ref)
+    # what the cases cover
+    recs = (oracle.OrcShadePath * len(c["depth"])).from_buffer_copy(c["paths"].tobytes())
+    hits = np.array([p.hit for p in recs])
+    shadows = ref[:, 22] != 0
+    alive = ref[:, 6] != np.float32(-1).view(np.uint32)
+    for m in (0, 1):
+        for h in (0, 1, 2):
+            sel = (c["multi"] == m) & (hits == h)
+            assert sel.sum() > 100
+            if h:
+                assert shadows[sel].sum() > 20
+    assert alive[(c["multi"] == 1) & (hits == 1)].sum() > 20   # volume bounces of the multi-scatter build
+    assert alive[hits == 2].sum() > 20                          # diffuse surface bounces
+
+
 def test_frame_buffer_packing(pin):
     c, o = pin
     acc = c["rgba"].reshape(1, -1, 4)
@@ -220,6 +281,20 @@ def test_live_library_reproduces_the_fixtures(pin):
             assert same_or_both_nan(a, b), k
         else:
             assert np.array_equal(a, b), k
+
+
+@live
+def test_live_shading_reproduces_the_fixtures(shade):
+    c, o = shade
+    mod = _shade_module()
+    fresh = mod.cases()
+    for k, v in c.items():
+        assert np.array_equal(np.asarray(v), np.asarray(fresh[k])), k
+    out = mod.reference_outputs(c)
+    for k, v in o.items():
+        assert np.array_equal(np.asarray(v).view(np.uint32) if np.asarray(v).dtype == np.float32 else v,
+                              np.asarray(out[k]).view(np.uint32) if np.asarray(out[k]).dtype == np.float32
+                              else out[k]), k
 
 
 @live
