@@ -513,7 +513,9 @@ def run_ours(args):
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6800 GB/s",
                          "bytes_per_launch": bytes_launch, "kernel": "render_kernel"},
-            "gpu_launches": args.steps, "clocks": clk.summary()}
+            # per frame: the majorant-bitmask kernel, then the render kernel
+            # (profiles/launches_bench_512cube_1080p_64spp.md)
+            "gpu_launches": 2 * args.steps, "clocks": clk.summary()}
     if rank != 0:
         if world > 1:
             dist.barrier()

@@ -244,23 +244,29 @@ def test_multi_scatter_statistical(cuda):
 
 
 def test_rmse_falls_as_inverse_sqrt_spp(cuda):
+    """Multiple scattering (up to 4 bounces) with a directional light and
+    ambient light: the error against a 2048-spp image falls by 2x for every
+    4x the passes (MSE pooled over 4 independent runs per pass count).  The
+    env map's sun disk (radiance 50) makes the error of a few runs too
+    heavy-tailed to show the rate; that frame is checked bit for bit in the
+    bounded-math mode and per pixel within 3 sigma above."""
     import torch
-    s = _ms_scene(1, w=48, h=32, dims=32)
+    s = scenes.frame_scene(dims=32, width=48, height=32, spp=1, with_env=False)
     g = GpuScene(s)
     ref = g.new_accum()
-    g.render(spp=1024, accum=ref, accum_id_start=100000)
-    ref = ref.cpu().numpy()[..., :3] / 1024
+    g.render(spp=2048, accum=ref, accum_id_start=100000)
+    ref = ref.cpu().numpy()[..., :3] / 2048
     rmse = {}
     for spp in (4, 16, 64):
-        vals = []
-        for rep in range(3):
+        mse = []
+        for rep in range(4):
             acc = g.new_accum()
             g.render(spp=spp, accum=acc, accum_id_start=1 + rep * 1000)
-            vals.append(np.sqrt(np.mean((acc.cpu().numpy()[..., :3] / spp - ref) ** 2)))
-        rmse[spp] = float(np.mean(vals))
+            mse.append(np.mean((acc.cpu().numpy()[..., :3] / spp - ref) ** 2))
+        rmse[spp] = float(np.sqrt(np.mean(mse)))
     torch.cuda.synchronize()
     r1, r2 = rmse[4] / rmse[16], rmse[16] / rmse[64]
-    assert 1.5 < r1 < 2.7 and 1.5 < r2 < 2.7, rmse
+    assert 1.6 < r1 < 2.5 and 1.6 < r2 < 2.5, rmse
     # the oracle converges to the same image
     o = oracle.Oracle(s)
     ao = np.zeros((s.height, s.width, 4), np.float32)
