@@ -112,6 +112,8 @@ def lib() -> C.CDLL:
             "orc_lambertian": (None, [vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp]),
             "orc_bounce": (None, [C.POINTER(OrcShadeWorld), i, i, C.POINTER(OrcShadePath), C.POINTER(OrcShadePath),
                                   vp]),
+            "orc_camera_commit": (None, [vp, vp, vp, f, vp]),
+            "orc_generate": (i, [vp, vp, vp, f, i, i, i, vp, vp, vp]),
             "orc_render": (None, [sp, vp, i, i, i, i, i, i, C.POINTER(OrcStats)]),
             "orc_tonemap": (None, [vp, i, i, i, i, vp]),
             "orc_env_cdfs": (None, [vp, vp, vp, vp, vp]),
@@ -368,6 +370,26 @@ def bounce(world: OrcShadeWorld, multi: bool, depth: int, path: OrcShadePath):
     frag = np.zeros(3, np.float32)
     lib().orc_bounce(C.byref(world), 1 if multi else 0, depth, C.byref(io), C.byref(sh), _p(frag))
     return io, sh, frag
+
+
+def camera_commit(pos, direction, up, fovy) -> np.ndarray:
+    """PerspectiveCamera::commit (orc_camera_commit): dir_00, dir_du, dir_dv,
+    lens_00 as a (4, 3) array."""
+    out = np.zeros(12, np.float32)
+    f3 = lambda v: _p(np.ascontiguousarray(v, np.float32))
+    lib().orc_camera_commit(f3(pos), f3(direction), f3(up), fovy, _p(out))
+    return out.reshape(4, 3)
+
+
+def generate(pos, direction, up, fovy, W, H, accum_id, bg):
+    """_generateRays (orc_generate): (H, W, 11) float32 rays -- org, dir,
+    tMax, missColor -- (H, W) seed states, and the count of pixels with a
+    path state other than (throughput 1, misWeight 0)."""
+    out = np.zeros((H, W, 11), np.float32)
+    seeds = np.zeros((H, W), np.uint64)
+    f = lambda v: _p(np.ascontiguousarray(v, np.float32))
+    bad = lib().orc_generate(f(pos), f(direction), f(up), fovy, W, H, accum_id, f(bg), _p(out), _p(seeds))
+    return out, seeds, bad
 
 
 def env_cdfs(texels: np.ndarray, addr) -> tuple:

@@ -2247,6 +2247,46 @@ void orc_bounce(const orc_shade_world *w, int multi, int depth, orc_shade_path *
   }
 }
 
+// PerspectiveCamera::commit for these parameters: dir_00, dir_du, dir_dv,
+// lens_00 (12 floats), as ref_camera_commit exposes the reference's
+void orc_camera_commit(const float pos[3], const float dir[3], const float up[3], float fovy, float out[12]) {
+  const Camera c = commit_camera(pos, dir, up, fovy);
+  const V3<float> v[4] = {c.dir00, c.du, c.dv, c.lens00};
+  for (int i = 0; i < 4; i++)
+    for (int a = 0; a < 3; a++) out[3 * i + a] = v[i][a];
+}
+
+// _generateRays for pass accumID of a W x H frame, as ref_generate exposes
+// the reference's: per pixel (row-major) org[3], dir[3], tMax, missColor[4]
+// and the ray's seed state; returns the count of pixels whose path state is
+// not throughput 1, misWeight 0 (none)
+int orc_generate(const float pos[3], const float dir[3], const float up[3], float fovy, int W, int H, int accumID,
+                 const float bg[4], float *out, uint64_t *seeds) {
+  Scene S;
+  S.cam = commit_camera(pos, dir, up, fovy);
+  S.W = W;
+  S.H = H;
+  S.bg = {bg[0], bg[1], bg[2], bg[3]};
+  int bad = 0;
+  for (int iy = 0; iy < H; iy++)
+    for (int ix = 0; ix < W; ix++) {
+      Ray ray;
+      PathState st;
+      generate(S, ix, iy, accumID, ray, st);
+      float *o = out + 11 * ((size_t)iy * W + ix);
+      for (int a = 0; a < 3; a++) {
+        o[a] = ray.org[a];
+        o[3 + a] = ray.dir[a];
+      }
+      o[6] = ray.tMax;
+      o[7] = ray.missColor.x; o[8] = ray.missColor.y; o[9] = ray.missColor.z; o[10] = ray.missColor.w;
+      seeds[(size_t)iy * W + ix] = ray.rngSeed.state;
+      if (st.throughput.x != 0x3c00 || st.throughput.y != 0x3c00 || st.throughput.z != 0x3c00 || st.misWeight != 0.f)
+        bad++;
+    }
+  return bad;
+}
+
 void orc_render(const orc_scene *s, float *accum, int accum_id_start, int spp, int use_double, int nthreads,
                 int row0, int row1, orc_stats *stats) {
   Scene S;

@@ -196,6 +196,16 @@ typedef struct orc_shade_path {
 void  orc_bounce(const orc_shade_world *w, int multi, int depth, orc_shade_path *ray,
                  orc_shade_path *shadow, float fragment[3]);
 
+/* PerspectiveCamera::commit: dir_00, dir_du, dir_dv, lens_00 (12 floats) */
+void  orc_camera_commit(const float pos[3], const float dir[3], const float up[3], float fovy,
+                        float out[12]);
+/* _generateRays for pass accum_id of a W x H frame with background bg (w < 0:
+   the gradient): per pixel, row-major, org[3], dir[3], tMax, missColor[4]
+   and the ray's seed state; returns the count of pixels whose path state is
+   not (throughput 1, misWeight 0) */
+int   orc_generate(const float pos[3], const float dir[3], const float up[3], float fovy, int W, int H,
+                   int accum_id, const float bg[4], float *out, uint64_t *seeds);
+
 /* --- full render: bnRender's generate/trace/shade loop for `spp`
        consecutive accumulation passes starting at accum_id_start.
        accum: width*height RGBA, row-major, y=0 the bottom row.

@@ -72,6 +72,8 @@ def lib() -> C.CDLL:
             "ref_lambertian": (None, [vp, vp, vp, vp, u32, u32, vp]),
             "ref_env_cdfs": (None, [vp, vp, vp, vp, vp]),
             "ref_shade_multi_scatter": (i, []),
+            "ref_camera_commit": (None, [vp, vp, vp, f, vp]),
+            "ref_generate": (i, [vp, vp, vp, f, i, i, i, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -233,6 +235,24 @@ def bounce(world, multi: bool, depth: int, path):
     frag = np.zeros(3, np.float32)
     L.ref_bounce(C.byref(world), depth, C.byref(io), C.byref(sh), _p(frag))
     return io, sh, frag
+
+
+def camera_commit(pos, direction, up, fovy) -> np.ndarray:
+    """The reference's PerspectiveCamera::commit: dir_00, dir_du, dir_dv,
+    lens_00 as a (4, 3) array."""
+    out = np.zeros(12, np.float32)
+    lib().ref_camera_commit(_p(_f32(pos)), _p(_f32(direction)), _p(_f32(up)), fovy, _p(out))
+    return out.reshape(4, 3)
+
+
+def generate(pos, direction, up, fovy, W, H, accum_id, bg):
+    """The reference's _generateRays: (H, W, 11) rays, (H, W) seed states
+    and the count of pixels with a path state other than (1, 0)."""
+    out = np.zeros((H, W, 11), np.float32)
+    seeds = np.zeros((H, W), np.uint64)
+    bad = lib().ref_generate(_p(_f32(pos)), _p(_f32(direction)), _p(_f32(up)), fovy, W, H, accum_id,
+                             _p(_f32(bg)), _p(out), _p(seeds))
+    return out, seeds, bad
 
 
 def env_cdfs(texels, addr) -> tuple:

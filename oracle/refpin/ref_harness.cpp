@@ -32,6 +32,9 @@
 //   *objectToWorldXfm, v)); the trace set-up that rtcore/embree/Group.cpp:
 //   34-78 does before calling isProg (tmin 0, tmax = ray.tMax, the
 //   instance's index, geometry 0, primitive 0, identity instance transform).
+// ref_shade.cpp (the shading step and env-map tables, also built for the
+// multi-scatter configuration) and ref_gen.cpp (camera commit and ray
+// generation) are the pin's other two parts.
 // The owl math the reference calls (vec, box, frame, xfmVector ...) is the
 // shim's restatement: the owl submodule is absent, so what depends on it --
 // the Lambertian scatter direction through frame() -- is pinned only by

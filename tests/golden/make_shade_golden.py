@@ -1,5 +1,5 @@
-"""Generates tests/golden/shade_pin.npz: the reference's shading step on fixed
-inputs.
+"""Generates tests/golden/shade_pin.npz: the reference's per-pixel path steps
+on fixed inputs -- ray generation and the shading step.
 
 The outputs come from the reference renderer's code compiled unchanged
 (oracle/refpin/ref_shade.cpp, built by `make -C oracle ref` into
@@ -8,6 +8,8 @@ oracle/_ref/libbarney_ref_ms.so for the multi-scatter build):
 
 * EnvMapLight's importance tables (EnvMap.cu:181-238) of two env maps under
   every address mode;
+* PerspectiveCamera::commit (Camera.cu:83-97) and _generateRays
+  (generateRays.cu:44-243) for random cameras, frame sizes and passes;
 * bounce() (shadeRays.cu:477-878) of both builds on four worlds --
   directional light and ambient; env map and two directional lights; env
   map alone; ambient alone -- for random paths: misses, shadow rays, volume
@@ -127,7 +129,36 @@ def cases(seed: int = 2027) -> dict:
     c["depth"] = rng.integers(0, 11, size=n).astype(np.int32)
     c["world"] = np.repeat(np.arange(len(WORLDS), dtype=np.int32), 2 * PATHS_PER_WORLD)
     c["multi"] = np.tile(np.repeat(np.array([0, 1], np.int32), PATHS_PER_WORLD), len(WORLDS))
+    c.update(camera_cases(seed + 2))
     return c
+
+
+def camera_cases(seed: int, n: int = 12) -> dict:
+    """Random cameras (position, direction, up, fovy), frame sizes up to
+    24x20 (partial 32x32 tiles), passes (0, 1 and large accumIDs) and
+    background colours (a constant, or w < 0: the gradient)."""
+    rng = np.random.default_rng(seed)
+    cam = np.concatenate([rng.standard_normal((n, 9)) * np.array([3] * 3 + [1] * 6),
+                          20 + 80 * rng.random((n, 1))], axis=1).astype(np.float32)
+    frame = np.stack([rng.integers(1, 25, n), rng.integers(1, 21, n), rng.choice([0, 1, 7, 123456], n)],
+                     axis=1).astype(np.int32)
+    bg = np.where(rng.random((n, 1)) < .5, np.array([[0.1, 0.2, 0.3, 1.0]]), np.array([[0, 0, 0, -1.0]]))
+    return {"cam": cam, "frame": frame, "bg": bg.astype(np.float32)}
+
+
+def run_cameras(c: dict, commit, generate) -> dict:
+    """Camera commits and generated rays of every camera case with the
+    given implementation (oracle or refpin functions)."""
+    out = {"commit": [], "rays": [], "seeds": [], "bad": []}
+    for cm, fr, bg in zip(c["cam"], c["frame"], c["bg"]):
+        args = (cm[0:3], cm[3:6], cm[6:9], float(cm[9]))
+        out["commit"].append(commit(*args))
+        rays, seeds, bad = generate(*args, int(fr[0]), int(fr[1]), int(fr[2]), bg)
+        out["rays"].append(rays.reshape(-1))
+        out["seeds"].append(seeds.reshape(-1))
+        out["bad"].append(bad)
+    return {"commit": np.stack(out["commit"]), "rays": np.concatenate(out["rays"]),
+            "seeds": np.concatenate(out["seeds"]), "gen_bad": np.array(out["bad"], np.int32)}
 
 
 def summary(io, sh, frag) -> np.ndarray:
@@ -168,6 +199,7 @@ def reference_outputs(c: dict) -> dict:
     sky = (out["cdf_y_0_0"], out["cdf_x_0_0"])  # the sky map under (wrap, clamp), its address modes
     assert tuple(c["addrs"][0]) == env_frame()[2]
     out["bounce"] = run(c, R.bounce, sky)
+    out.update(run_cameras(c, R.camera_commit, R.generate))
     return out
 
 

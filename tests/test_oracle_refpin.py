@@ -9,10 +9,10 @@ per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
 stream, DDA over the majorant grid, Woodcock tracking, hit record), the
 iso-surface intersection program MCIsoSurfaceAccel::isProg with an AnariMatte
 material (hit search, normal, opacity test, Ray::setHit), the material's
-Lambertian BSDF, the shading step bounce() of the default and the
-multi-scatter build with the env map's importance tables
-(tests/golden/shade_pin.npz, make_shade_golden.py), and the frame buffer's
-8-bit and sRGB packing.  Their outputs on fixed inputs are
+Lambertian BSDF, the camera commit and ray generation, the shading step
+bounce() of the default and the multi-scatter build with the env map's
+importance tables (tests/golden/shade_pin.npz, make_shade_golden.py), and
+the frame buffer's 8-bit and sRGB packing.  Their outputs on fixed inputs are
 stored in tests/golden/ref_pin.npz (tests/golden/make_ref_golden.py); the
 oracle must reproduce every one bit for bit.  Where the reference checkout
 is present the live library is also compared on fresh random inputs.
@@ -250,6 +250,21 @@ def test_shading_step(shade):
                 assert shadows[sel].sum() > 20
     assert alive[(c["multi"] == 1) & (hits == 1)].sum() > 20   # volume bounces of the multi-scatter build
     assert alive[hits == 2].sum() > 20                          # diffuse surface bounces
+
+
+def test_camera_and_ray_generation(shade):
+    """PerspectiveCamera::commit and _generateRays: per pixel the origin,
+    direction, tMax, background colour and the ray's seed state, for frames
+    with partial 32x32 tiles, pass 0 (pixel centres) and jittered passes,
+    a constant background and the gradient; the path state starts at
+    throughput 1, MIS weight 0."""
+    c, o = shade
+    mod = _shade_module()
+    got = mod.run_cameras(c, oracle.camera_commit, oracle.generate)
+    assert np.array_equal(bits(got["commit"]), bits(o["commit"]))
+    assert np.array_equal(bits(got["rays"]), bits(o["rays"]))
+    assert np.array_equal(got["seeds"], o["seeds"])
+    assert not got["gen_bad"].any() and not o["gen_bad"].any()
 
 
 def test_frame_buffer_packing(pin):
