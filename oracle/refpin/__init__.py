@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
             "ref_env_cdfs": (None, [vp, vp, vp, vp, vp]),
             "ref_shade_multi_scatter": (i, []),
             "ref_camera_commit": (None, [vp, vp, vp, f, vp]),
+            "ref_mc_ranges": (None, [vp, vp, vp]),
             "ref_generate": (i, [vp, vp, vp, f, i, i, i, vp, vp, vp]),
         }
         for name, (res, args) in sigs.items():
@@ -235,6 +236,17 @@ def bounce(world, multi: bool, depth: int, path):
     frag = np.zeros(3, np.float32)
     L.ref_bounce(C.byref(world), depth, C.byref(io), C.byref(sh), _p(frag))
     return io, sh, frag
+
+
+def mc_ranges(scalars) -> np.ndarray:
+    """StructuredData::buildMCs' scalar ranges (8-cell macrocells), as an
+    (nmc, 2) array."""
+    scalars = _f32(scalars)
+    nz, ny, nx = scalars.shape
+    m = [(d - 1 + 7) // 8 for d in (nx, ny, nz)]
+    out = np.zeros((m[0] * m[1] * m[2], 2), np.float32)
+    lib().ref_mc_ranges(_p(scalars), _p(np.array([nx, ny, nz], np.int32)), _p(out))
+    return out
 
 
 def camera_commit(pos, direction, up, fovy) -> np.ndarray:

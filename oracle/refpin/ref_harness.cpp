@@ -16,7 +16,8 @@
 //                                   Volume::DD::sampleAndMap
 //   barney/volume/TransferFunction.h  TransferFunction::DD::map, majorant
 //   barney/volume/DDA.h             dda::dda3
-//   barney/volume/StructuredData.h  StructuredDataSampler::DD::sample
+//   barney/volume/StructuredData.{h,cu}  StructuredDataSampler::DD::sample,
+//                                   StructuredData_computeMCs
 //   barney/volume/MCAccelerator.h   MCVolumeAccel::isProg
 //   barney/render/Ray.h             boxTest, Ray::setVolumeHit
 //   barney/common/math.h            linear_to_srgb, make_8bit, make_rgba
@@ -43,7 +44,7 @@
 #include "barney/common/math.h"
 #include "barney/volume/DDA.h"
 #include "barney/volume/Volume.h"
-#include "barney/volume/StructuredData.h"
+#include "barney/volume/StructuredData.cu"
 #include "barney/geometry/IsoSurface.h"
 #include "barney/material/DeviceMaterial.h"
 #include "rtcore/embree/Texture.h"
@@ -406,6 +407,36 @@ void ref_lambertian(const float color[4], const float Ng[3], const float wo[3], 
   bsdf.scatter(s, dg, r);
   out[5] = s.dir.x; out[6] = s.dir.y; out[7] = s.dir.z; out[8] = s.pdf;
   out[9] = s.f_r.x; out[10] = s.f_r.y; out[11] = s.f_r.z;
+}
+
+// StructuredData::buildMCs (StructuredData.cu:29-61, 70-95): the macrocell
+// scalar ranges of a structured field, cellsPerMC = 8, read through the
+// field's NEAREST texture (StructuredData::setObject, :153-172: CLAMP on
+// every axis, unnormalised coordinates), StructuredData_computeMCs run for
+// every macrocell; ranges: 2 floats per macrocell, x fastest
+void ref_mc_ranges(const float *scalars, const int dims[3], float *ranges) {
+  rtc::embree::TextureData data(nullptr, vec3i(dims[0], dims[1], dims[2]), rtc::FLOAT, scalars);
+  rtc::TextureDesc desc;
+  desc.filterMode = rtc::FILTER_MODE_POINT;
+  desc.normalizedCoords = false;
+  for (int i = 0; i < 3; i++) desc.addressMode[i] = rtc::CLAMP;
+  rtc::embree::Texture *nn = data.createTexture(desc);
+  const vec3i numCells(dims[0] - 1, dims[1] - 1, dims[2] - 1);
+  const vec3i mcDims = divRoundUp(numCells, vec3i(cellsPerMC));
+  MCGrid::DD grid;
+  std::memset((void *)&grid, 0, sizeof(grid));
+  grid.dims = mcDims;
+  grid.scalarRanges = (range1f *)ranges;
+  rtc::embree::ComputeInterface ci;
+  std::memset((void *)&ci, 0, sizeof(ci));
+  ci.blockDim = vec3ui(1, 1, 1);
+  const int n = mcDims.x * mcDims.y * mcDims.z;
+  for (int t = 0; t < n; t++) {
+    ci.blockIdx = vec3ui(t, 0, 0);
+    StructuredData_computeMCs(ci, grid, vec3i(dims[0], dims[1], dims[2]), nn->getDD());
+  }
+  delete nn->sampler;
+  delete nn;
 }
 
 // linear_to_srgb and the 8-bit packing of the frame-buffer read

@@ -164,6 +164,7 @@ def reference_outputs(c: dict) -> dict:
     out["trace_majorants"] = maj
     out["rgba8"] = R.rgba8(c["rgba"], False)
     out["srgb8"] = R.rgba8(c["rgba"], True)
+    out["mc_ranges_8"] = R.mc_ranges(c["vol"])
     rg = iso_ranges(c)
     out["iso_ranges"] = rg
     hit, st, t, P, Nh, alb = [], [], [], [], [], []

@@ -4,8 +4,8 @@ The reference renderer's sources for the structured-volume path compile
 unchanged here (oracle/refpin, `make -C oracle ref`): its RNG and hash,
 fastLog, the float/half conversions of its CPU backend, the transfer
 function's map and majorant, the structured field's sampler with the CPU
-backend's trilinear texture, sampleAndMap, the macrocell DDA and the whole
-per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
+backend's trilinear texture, sampleAndMap, the macrocell range build, the
+macrocell DDA and the whole per-ray volume intersection program MCVolumeAccel::isProg (box test, RNG
 stream, DDA over the majorant grid, Woodcock tracking, hit record), the
 iso-surface intersection program MCIsoSurfaceAccel::isProg with an AnariMatte
 material (hit search, normal, opacity test, Ray::setHit), the material's
@@ -115,6 +115,15 @@ def test_field_sampler(pin):
     m = orc.tf_map(s)
     m[np.isnan(got)] = 0.0
     assert np.array_equal(bits(m), bits(o["sample_map"]))
+
+
+def test_macrocell_ranges(pin):
+    """StructuredData::buildMCs / StructuredData_computeMCs: the scalar range
+    of every 8-cell macrocell (9^3 voxels each, clipped at the field's edge)
+    through the field's nearest-neighbour texture."""
+    c, o = pin
+    got = _scene(c, c["tf_a"], (0.0, 1.0), 40.0, cells_per_mc=8).mc_ranges()
+    assert np.array_equal(bits(got), bits(o["mc_ranges_8"]))
 
 
 def test_volume_intersection_program(pin):
