@@ -5,6 +5,7 @@
  */
 #ifndef GBV_SCENE_GEN_H
 #define GBV_SCENE_GEN_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -19,6 +20,16 @@ extern "C" {
 int sg_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
                    float noise_amplitude, int fbm_octaves, float fbm_amplitude,
                    int nthreads, float *out);
+
+/* A NanoVDB float grid (format 32.7 memory layout) of a dense x-fastest
+   array placed at index `origin`, world = voxel_size * index + translation;
+   voxels equal to `background` are inactive.  *out receives a malloc'd
+   buffer of *bytes bytes (release with sg_free).  Returns 0, 1 for a bad
+   argument, 2 when no voxel is active, 3 when memory runs out. */
+int sg_nanovdb_from_dense(const float *values, const int dims[3], const int origin[3],
+                          float background, double voxel_size, const double translation[3],
+                          void **out, size_t *bytes);
+void sg_free(void *p);
 
 #ifdef __cplusplus
 }

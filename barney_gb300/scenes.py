@@ -127,6 +127,45 @@ def blob_volume(dims, num_blobs: int, seed: int, noise: float = 0.05, fbm_octave
     return out
 
 
+def nanovdb_grid(values: np.ndarray, origin=(0, 0, 0), voxel_size: float = 1.0, translation=(0.0, 0.0, 0.0),
+                 background: float = 0.0) -> bytes:
+    """A NanoVDB float grid (format 32.7 memory layout) of a dense
+    (nz, ny, nx) array placed at index `origin`, world = voxel_size * index +
+    translation; voxels equal to `background` are inactive."""
+    L = _scenegen()
+    if not hasattr(L, "_nvdb_ready"):
+        L.sg_nanovdb_from_dense.restype = C.c_int
+        L.sg_nanovdb_from_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_double, C.c_void_p,
+                                            C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+        L.sg_free.argtypes = [C.c_void_p]
+        L._nvdb_ready = True
+    v = np.ascontiguousarray(values, np.float32)
+    nz, ny, nx = v.shape
+    dims = np.array([nx, ny, nz], np.int32)
+    org = np.array(origin, np.int32)
+    tr = np.array(translation, np.float64)
+    buf, n = C.c_void_p(), C.c_size_t()
+    rc = L.sg_nanovdb_from_dense(v.ctypes.data, dims.ctypes.data, org.ctypes.data, background, voxel_size,
+                                 tr.ctypes.data, C.byref(buf), C.byref(n))
+    if rc != 0:
+        raise ValueError(f"sg_nanovdb_from_dense failed ({rc})")
+    try:
+        return C.string_at(buf, n.value)
+    finally:
+        L.sg_free(buf)
+
+
+def nanovdb_of_scene(scene: "Scene") -> bytes:
+    """The scene's volume as a NanoVDB grid whose voxel centres lie where the
+    structured field has its voxels (the NanoVDB sampler reads voxel i at
+    index i + 1/2; needs the same spacing on every axis)."""
+    origin, spacing = scene.geometry()
+    if not (spacing[0] == spacing[1] == spacing[2]):
+        raise ValueError("a NanoVDB grid has one voxel size")
+    vs = float(spacing[0])
+    return nanovdb_grid(scene.scalars, (0, 0, 0), vs, tuple(float(o) - 0.5 * vs for o in origin), background=-1.0)
+
+
 def tf_ramp(n: int = 128, max_opacity: float = 0.8) -> np.ndarray:
     """Opacity ramps linearly 0 -> max_opacity; colour ramps blue -> red."""
     t = np.linspace(0.0, 1.0, n, dtype=np.float64)

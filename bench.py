@@ -239,8 +239,8 @@ def ea_steps(scene, view, step):
 def _bias(d):
     """Mean signed error over the crop and its standard error from the
     per-row means (rows as independent batches): a storage format that
-    shifts the image shows a bias several sigma from zero, while path
-    divergence (a flipped decision changes the rest of a path) averages out."""
+    shifts the image shows a bias several sigma from zero, while paths that
+    part (a flipped decision changes the rest of a path) average out."""
     per_row = d.reshape(d.shape[0], -1).mean(axis=1)
     return {"bias_vs_fp64": float(d.mean()), "bias_sigma": float(per_row.std(ddof=1) / math.sqrt(per_row.size))}
 
@@ -257,13 +257,15 @@ def precision_study(scene, g32, rows=(523, 557), reps=2):
     delta_tracking: each format's full frame (samples/s, frame ms) and its
     error on a band of rows against the oracle's FP64 render from the FP32
     source voxels.  All formats and the oracle use the FP32 source's majorant
-    grid, so every pixel draws the same random numbers; still, a decision
-    that flips between precisions changes the rest of that path, so these
-    errors are dominated by path divergence: `oracle_fp32_vs_fp64` is that
-    floor for the FP32 arithmetic itself.  Two figures separate the storage
-    from that floor: `rmse_vs_f32` (the same store layout and streams, FP32
-    voxels against the format's) and `bias_vs_fp64` with `bias_sigma` (the
-    mean signed error over the crop and its standard error)."""
+    grid, so every pixel draws the same random numbers, and the shading
+    streams hash the hit distance truncated to an integer, so a small
+    difference in a distance keeps the path's streams; only a decision that
+    flips between precisions changes the rest of that path.
+    `oracle_fp32_vs_fp64` is the floor of the FP32 arithmetic itself;
+    `rmse_vs_f32` (the same store layout and streams, FP32 voxels against
+    the format's) isolates the storage, and `bias_vs_fp64` with `bias_sigma`
+    (the mean signed error over the crop and its standard error) tests for a
+    systematic shift."""
     import torch
     import oracle
     from barney_gb300 import _native as N
@@ -387,6 +389,72 @@ def wavefront_timing(g, scene, persistent_ms, reps=3):
     ms = min(ts)
     return {"frame_ms": ms, "persistent_frame_ms": persistent_ms, "vs_persistent": persistent_ms / ms,
             "frames_identical": identical}
+
+
+def iso_timing(g, scene, persistent_ms, reps=2):
+    """The frame with an iso-surface of the field (value 0.5, matte
+    material 0.8 grey): beside the volume in one group (the iso-surface's
+    instance first), and alone; frame times and rays per second (event
+    counts of one counted frame each)."""
+    import torch
+    from barney_gb300 import _native as N, scenes
+    out = {"iso_value": 0.5, "volume_only_frame_ms": persistent_ms}
+    saved = (scene.iso, scene.volume_instance, scene.no_volume)
+    try:
+        for name, (vi, nv) in {"iso_and_volume": (1, False), "iso_only": (0, True)}.items():
+            scene.iso = scenes.IsoSurface(0.5, (0.8, 0.8, 0.8, 1.0), 1.0, 0)
+            scene.volume_instance, scene.no_volume = vi, nv
+            acc = g.new_accum()
+            cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+            g.render(spp=scene.spp, accum=acc, counters=cnt)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ts = []
+            for _ in range(reps):
+                e0.record()
+                g.render(spp=scene.spp, accum=acc)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            c = [int(x) for x in cnt.cpu().tolist()]
+            ms = min(ts)
+            out[name] = {"frame_ms": ms, "rays": c[N.GBV_COUNTER_RAYS], "Mrays_s": c[N.GBV_COUNTER_RAYS] / ms / 1e3,
+                         "density_samples": c[N.GBV_COUNTER_SAMPLES], "loop_caps": c[N.GBV_COUNTER_CAPS]}
+    finally:
+        scene.iso, scene.volume_instance, scene.no_volume = saved
+    return out
+
+
+def nanovdb_timing(scene, persistent_ms, reps=2):
+    """The frame with its volume given as a NanoVDB float grid (voxel
+    centres where the structured field has its voxels; the grid made by the
+    input generator): grid bytes, frame time and density samples per second
+    against the FP32 brick store's frame."""
+    import torch
+    from barney_gb300 import _native as N, scenes
+    from barney_gb300.nanovdb import GpuNanoVDBScene
+    t0 = time.perf_counter()
+    grid = scenes.nanovdb_of_scene(scene)
+    make_s = time.perf_counter() - t0
+    g = GpuNanoVDBScene(scene, grid)
+    acc = g.new_accum()
+    cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    g.render(accum=acc, counters=cnt)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ts = []
+    for _ in range(reps):
+        e0.record()
+        g.render(accum=acc)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    c = [int(x) for x in cnt.cpu().tolist()]
+    ms = min(ts)
+    out = {"grid_bytes": len(grid), "grid_make_s": make_s, "frame_ms": ms, "density_samples": c[N.GBV_COUNTER_SAMPLES],
+           "Msamples_s": c[N.GBV_COUNTER_SAMPLES] / ms / 1e3, "brick_f32_frame_ms": persistent_ms,
+           "loop_caps": c[N.GBV_COUNTER_CAPS]}
+    del g, grid
+    torch.cuda.empty_cache()
+    return out
 
 
 def batch_timing(count=64, reps=3):
@@ -540,29 +608,44 @@ def run_ours(args):
             line["wavefront"] = wavefront_timing(g, scene, frame_ms)
         except Exception as e:
             line["wavefront"] = {"error": str(e)}
+        try:
+            line["iso_surface"] = iso_timing(g, scene, frame_ms)
+        except Exception as e:
+            line["iso_surface"] = {"error": str(e)}
+        try:
+            line["nanovdb"] = nanovdb_timing(scene, frame_ms)
+        except Exception as e:
+            line["nanovdb"] = {"error": str(e)}
     # ---- e2e through the bn* C-ABI with host buffers ----
     from barney_gb300 import bn
     host_vol = torch.from_numpy(np.ascontiguousarray(scene.scalars)).pin_memory()
     out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32).pin_memory()
-    e2e_times = []
+    e2e_times, phases = [], []
     with bn.BarneySession(local) as ses:
         for i in range(1 + args.e2e_steps):
             t0 = time.perf_counter()
             ses.build_scene(scene, host_vol.data_ptr(), voxel_format=fmt)
+            t1 = time.perf_counter()
             ses.render()
+            t2 = time.perf_counter()
             ses.read(out)
             dt = time.perf_counter() - t0
             ses.release_scene()
             if i > 0:
                 e2e_times.append(dt)
+                # the bn* calls return when their work is done (each upload
+                # and build synchronizes, bnRender waits for its frame)
+                phases.append((t1 - t0, t2 - t1, t0 + dt - t2))
     e2e_dt = sum(e2e_times) / len(e2e_times)
+    ph = [1e3 * sum(p[k] for p in phases) / len(phases) for k in range(3)]
     # the bn* frame is the device frame read out: same samples, same pixels
     same = bool(torch.equal(out.cuda(), g.tonemap(acc, scene.spp)))
     h2d = host_vol.numel() * 4 + scene.tf.nbytes + (scene.env.texels.nbytes if scene.env is not None else 0)
     line["e2e"] = {"value": world * samples / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(out.numel() * 4), "ms_per_step": 1e3 * e2e_dt,
                    "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers",
-                   "frame_identical_to_device_frame": same}
+                   "frame_identical_to_device_frame": same,
+                   "phases_ms": {"upload_and_build": ph[0], "render": ph[1], "read": ph[2]}}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
     line["extras_s"] = time.perf_counter() - extras_t0
