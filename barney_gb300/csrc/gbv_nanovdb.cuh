@@ -87,44 +87,6 @@ GBV_HD float nvdb_value(const NvdbGrid &g, int x, int y, int z) {
   return nvdb_ld<float>(lf + kNvdbLeafValues + 4 * (size_t)n);
 }
 
-// The leaf holding index coordinates (x, y, z), or null with the value of
-// the tile (or background) that covers its whole 8^3 region
-GBV_HD const unsigned char *nvdb_leaf(const NvdbGrid &g, int x, int y, int z, float &tile_value) {
-  const unsigned char *root = g.base + g.root;
-  const uint64_t key = (uint64_t)((uint32_t)z >> 12) | ((uint64_t)((uint32_t)y >> 12) << 21) |
-                       ((uint64_t)((uint32_t)x >> 12) << 42);
-  const unsigned char *tile = nullptr;
-  for (uint32_t i = 0; i < g.tiles; i++) {
-    const unsigned char *t = root + kNvdbRootTiles + (size_t)kNvdbRootTile * i;
-    if (nvdb_ld<uint64_t>(t) == key) {
-      tile = t;
-      break;
-    }
-  }
-  if (!tile) {
-    tile_value = g.background;
-    return nullptr;
-  }
-  const long long child = nvdb_ld<long long>(tile + kNvdbTileChild);
-  if (child == 0) {
-    tile_value = nvdb_ld<float>(tile + kNvdbTileValue);
-    return nullptr;
-  }
-  const unsigned char *up = root + child;
-  uint32_t n = (((uint32_t)x & 4095u) >> 7 << 10) | (((uint32_t)y & 4095u) >> 7 << 5) | (((uint32_t)z & 4095u) >> 7);
-  if (!((nvdb_ld<uint64_t>(up + kNvdbUpperChildMask + 8 * (n >> 6)) >> (n & 63)) & 1ull)) {
-    tile_value = nvdb_ld<float>(up + kNvdbUpperTable + 8 * (size_t)n);
-    return nullptr;
-  }
-  const unsigned char *lw = up + nvdb_ld<long long>(up + kNvdbUpperTable + 8 * (size_t)n);
-  n = (((uint32_t)x & 127u) >> 3 << 8) | (((uint32_t)y & 127u) >> 3 << 4) | (((uint32_t)z & 127u) >> 3);
-  if (!((nvdb_ld<uint64_t>(lw + kNvdbLowerChildMask + 8 * (n >> 6)) >> (n & 63)) & 1ull)) {
-    tile_value = nvdb_ld<float>(lw + kNvdbLowerTable + 8 * (size_t)n);
-    return nullptr;
-  }
-  return lw + nvdb_ld<long long>(lw + kNvdbLowerTable + 8 * (size_t)n);
-}
-
 // NanoVDBDataSampler::DD::sample (barney/volume/NanoVDB.h:100-129): world ->
 // index with the grid's single-precision inverse map (worldToIndexF: the
 // translation subtracted in double, the 3x3 product in float with fused
@@ -150,29 +112,13 @@ GBV_HD float nvdb_sample(const NvdbGrid &g, float px, float py, float pz) {
   iz = clampd(iz, (double)g.lo[2], (double)g.hi[2]);
   const int i = (int)floor(ix), j = (int)floor(iy), k = (int)floor(iz);
   const double u = ix - (double)i, v = iy - (double)j, w = iz - (double)k;
-  // the 8 corner values, as the accessor returns them: when all 8 lie in the
-  // 8^3 region of (i, j, k) -- the common case -- one walk reaches their
-  // leaf (or the tile covering the region), else one walk per corner
   float s[2][2][2];
-  if ((i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7) {
-    float tv;
-    const unsigned char *leaf = nvdb_leaf(g, i, j, k, tv);
-    const int n0 = ((i & 7) << 6) | ((j & 7) << 3) | (k & 7);
 #pragma unroll
-    for (int a = 0; a < 2; a++)
+  for (int a = 0; a < 2; a++)
 #pragma unroll
-      for (int b = 0; b < 2; b++)
+    for (int b = 0; b < 2; b++)
 #pragma unroll
-        for (int c = 0; c < 2; c++)
-          s[a][b][c] = leaf ? nvdb_ld<float>(leaf + kNvdbLeafValues + 4 * (size_t)(n0 + (a << 6) + (b << 3) + c)) : tv;
-  } else {
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-      for (int b = 0; b < 2; b++)
-#pragma unroll
-        for (int c = 0; c < 2; c++) s[a][b][c] = nvdb_value(g, i + a, j + b, k + c);
-  }
+      for (int c = 0; c < 2; c++) s[a][b][c] = nvdb_value(g, i + a, j + b, k + c);
   const float fu = (float)u, fv = (float)v, fw = (float)w;
   auto lerp = [](float p, float q, float t) { return p + t * (q - p); };
   return lerp(lerp(lerp(s[0][0][0], s[0][0][1], fw), lerp(s[0][1][0], s[0][1][1], fw), fv),

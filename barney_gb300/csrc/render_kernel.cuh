@@ -1011,10 +1011,15 @@ __device__ __forceinline__ int trace_sample(const FieldGeom &F, const Store &sto
 // value gives the hit t by linear interpolation.  The normal is the central
 // difference of the field at +-delta per axis, one-sided where a sample
 // falls outside the field, normalized.  Returns whether t < tmax.
+// `stop`: the search may end before a macrocell that begins beyond it (a
+// crossing found there would lie beyond `stop`: an interpolated t is never
+// more than a few ulps below its cell's start, far inside the 1e-5 margin);
+// +inf searches the whole ray.
 template <class Store>
 __device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &store, const MCGridDev &G,
                                            const float2 *__restrict__ ranges, float iso, float delta, Traversal &T,
-                                           float tmax, float &tOut, vec3 &N) {
+                                           float tmax, float &tOut, vec3 &N,
+                                           float stop = __int_as_float_hd(0x7f800000)) {
   const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
   const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
   float tHit = tmax;
@@ -1024,6 +1029,7 @@ __device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &stor
     const float tc = reduce_min(T.t_next);
     const float t0 = T.ray_t0 + T.ncb;
     const float t1 = T.ray_t0 + mn(tc, T.tMax);
+    if (t0 > stop + fabsf(stop) * 1e-5f) break;
     // the iso lambda (MCAccelerator.h:405-471)
     if (!(t0 >= mn(t1, tmax))) {
       const float2 vr = __ldg(ranges + (T.cx + G.M[0] * (T.cy + G.M[1] * T.cz)));
@@ -1083,6 +1089,54 @@ __device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &stor
 // rng() > opacity, MCAccelerator.h:533-539); and Ray::setHit's record (the
 // hit point and the normal in half precision).  Returns whether the surface
 // records a hit.
+// The iso-surface's box test and random stream alone -- what its
+// intersection program does to the ray's seed -- when it runs before the
+// volume's: the search itself waits until the volume's first collision is
+// known (iso_trace_after).  Returns whether the box test passed; the stream's
+// state goes to *rng.
+__device__ __forceinline__ bool iso_begin(const RenderParams &p, vec3 org, vec3 rayDir, float tmax, RNGSeed &seed,
+                                          uint64_t &rng) {
+  vec3 dir = rayDir;
+  if (dir.x == 0.f) dir.x = 1e-6f;
+  if (dir.y == 0.f) dir.y = 1e-6f;
+  if (dir.z == 0.f) dir.z = 1e-6f;
+  if (p.G.M[0] <= 0 || p.G.M[1] <= 0 || p.G.M[2] <= 0) return false;
+  float tLo = 0.f, tHi = tmax;
+  if (!box_test(org, dir, tLo, tHi, p.F.boundsLo, p.F.boundsHi)) return false;
+  rng = Random::derive(seed, p.isoHash).s.state;
+  return true;
+}
+
+// The rest of that program, after the volume traced without the surface's
+// bound and found its first collision at `stop` (+inf: none): the search on
+// the ray's own [0, tmax], as the program makes it, ends at `stop`; the
+// surface's hit counts when its t is at most `stop` (the volume's tracking,
+// bounded by the surface's hit, would have stopped there: the surface wins a
+// tie), after the material's opacity test on the stream iso_begin made.
+// The final hit, point, normal and every random stream equal those of
+// running the surface's program first.
+template <class Store>
+static __device__ __noinline__ bool iso_trace_after(const RenderParams &p, vec3 org, vec3 rayDir, float tmax,
+                                                    float stop, uint64_t rng, float &tOut, vec3 &P, vec3h &Nh) {
+  Traversal T;
+  Ctr<false> none;
+  RNGSeed scratch;  // the stream was derived by iso_begin
+  scratch.state = 0;
+  if (!trace_begin(p.F, p.G, p.rcpMc, org, rayDir, tmax, scratch, T, none, p.isoHash)) return false;
+  float t;
+  vec3 N;
+  if (!iso_search(p.F, make_store<Store>(p), p.G, p.isoRanges, p.isoValue, p.isoDelta, T, tmax, t, N, stop))
+    return false;
+  if (!(t <= stop)) return false;
+  Random r;
+  r.s.state = rng;
+  if (p.isoAlpha < 1.f && r() > p.isoAlpha) return false;
+  tOut = t;
+  P = T.org + t * T.dir;
+  Nh = to_half(N);
+  return true;
+}
+
 template <class Store>
 static __device__ __noinline__ bool iso_trace(const RenderParams &p, vec3 org, vec3 rayDir, float tmax, RNGSeed &seed,
                                               float &tOut, vec3 &P, vec3h &Nh) {
@@ -1204,11 +1258,14 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
   Traversal T;
   Hit h;
   h.hit = false;
-  // the iso-surface's hit of the current trace (Iso only)
+  // the iso-surface's hit of the current trace (Iso only); with the
+  // surface's instance first, whether its box test passed and its stream
   bool sHit = false;
   float sT = 0.f;
   vec3 sP;
   vec3h sN{0, 0, 0};
+  bool isoBox = false;
+  uint64_t isoRng = 0;
   unsigned long long cyc[3] = {0ull, 0ull, 0ull};
   // profile: traversal iterations and tracing lanes summed over them, shading
   // passes and shaded lanes summed over them (lane 0 of each warp counts)
@@ -1292,11 +1349,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         const vec3 org = shadowPending ? sray.org : ray.org, dir = shadowPending ? sray.dir : ray.dir;
         float tmax = shadowPending ? sray.tMax : ray.tMax;
         sHit = false;
+        isoBox = false;
         if (!p.hasVolume) GBV_COUNT(cnt, rays);
-        if (p.isoFirst) {
-          sHit = iso_trace<Store>(p, org, dir, tmax, seed, sT, sP, sN);
-          if (sHit) tmax = sT;
-        }
+        // the surface's instance first: its box test and stream now, its
+        // search once the volume's collision is known (iso_trace_after)
+        if (p.isoFirst) isoBox = iso_begin(p, org, dir, tmax, seed, isoRng);
         active = p.hasVolume && trace_begin(p.F, p.G, p.rcpMc, org, dir, tmax, seed, T, cnt, p.volHash);
       } else {
         active = trace_begin(p.F, p.G, p.rcpMc, shadowPending ? sray.org : ray.org, shadowPending ? sray.dir : ray.dir,
@@ -1342,6 +1399,13 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         simt[2]++;
         simt[3] += shading;
       }
+    }
+    if (Iso && tstate == DONE && p.isoFirst && isoBox) {
+      // the surface's search, up to the volume's first collision
+      PathRay &r = kind == K_SHADOW ? sray : ray;
+      sHit = iso_trace_after<Store>(p, r.org, r.dir, r.tMax, h.hit ? h.t : __int_as_float(0x7f800000), isoRng, sT,
+                                    sP, sN);
+      if (sHit) h.hit = false;
     }
     if (Iso && tstate == DONE && p.hasVolume && !p.isoFirst) {
       // the iso-surface after the volume, up to the volume's hit
