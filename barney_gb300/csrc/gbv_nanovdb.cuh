@@ -1,18 +1,24 @@
-// gbv_nanovdb.cuh -- NanoVDB float grids on the structured-volume path:
-// value lookup in a grid buffer, the reference's NanoVDB sampler and its
-// macrocell footprint.
+// gbv_nanovdb.cuh -- NanoVDB grids on the structured-volume path: value
+// lookup in a grid buffer, the reference's NanoVDB sampler and its macrocell
+// footprint.
 //
-// The grid buffer is one NanoVDB grid of value type Float in the NanoVDB
-// memory layout of format version 32 (the layout nanovdb::GridHandle holds
-// and nanovdb::io writes): a 672-byte grid header, a 64-byte tree header,
-// then the nodes -- a root of 32-byte tiles keyed by the coordinates of
-// their 4096^3 region, upper internal nodes of 32^3 entries, lower internal
-// nodes of 16^3 entries and 8^3-voxel leaves.  An internal entry whose
-// child-mask bit is set holds the signed byte offset of its child node,
-// otherwise a tile value; child offsets are relative to the parent node (to
-// the root node for the root's tiles).  The byte offsets below are those of
-// that layout for float values; the pin tests check them against the NanoVDB
-// headers the reference vendors (3rdParty/nanovdb, version 32.7).
+// The grid buffer is one NanoVDB grid in the NanoVDB memory layout of format
+// version 32 (the layout nanovdb::GridHandle holds and nanovdb::io writes),
+// of one of the value types the reference's NanoVDB field reads: Float, or
+// the quantized Fp4, Fp8, Fp16 and FpN.  A 672-byte grid header, a 64-byte
+// tree header, then the nodes -- a root of 32-byte tiles keyed by the
+// coordinates of their 4096^3 region, upper internal nodes of 32^3 entries,
+// lower internal nodes of 16^3 entries and 8^3-voxel leaves.  An internal
+// entry whose child-mask bit is set holds the signed byte offset of its
+// child node, otherwise a float tile value; child offsets are relative to the
+// parent node (to the root node for the root's tiles).  Root and internal
+// nodes are the same for every type; leaves differ: a Float leaf holds 512
+// floats, a quantized leaf a minimum m and a quantum q and 512 codes c of 4,
+// 8 or 16 bits (FpN: 1, 2, 4, 8 or 16 bits, the leaf's choice, in the top 3
+// bits of its flags byte), the value being float(c) * q + m.  The byte
+// offsets below are those of that layout; the pin tests check them against
+// the NanoVDB headers the reference vendors (3rdParty/nanovdb, version
+// 32.7).
 #pragma once
 #include <stdint.h>
 #include "gbv_math.cuh"
@@ -21,7 +27,9 @@ namespace gbv {
 
 constexpr uint64_t kNvdbMagic0 = 0x304244566f6e614eull;  // "NanoVDB0"
 constexpr uint64_t kNvdbMagic1 = 0x314244566f6e614eull;  // "NanoVDB1"
-constexpr uint32_t kNvdbGridTypeFloat = 1;
+// nanovdb::GridType of the types read
+constexpr uint32_t kNvdbGridTypeFloat = 1, kNvdbGridTypeFp4 = 13, kNvdbGridTypeFp8 = 14, kNvdbGridTypeFp16 = 15,
+                   kNvdbGridTypeFpN = 16;
 // grid header
 constexpr size_t kNvdbGridVersion = 16, kNvdbGridSize = 32, kNvdbGridInvMatF = 332, kNvdbGridVecF = 368;
 constexpr size_t kNvdbGridWorldBBox = 560, kNvdbGridVoxelSize = 608, kNvdbGridType = 636;
@@ -34,12 +42,17 @@ constexpr size_t kNvdbTileChild = 8, kNvdbTileValue = 20;
 // internal nodes: child mask and the table of values / child offsets
 constexpr size_t kNvdbUpperChildMask = 32 + 4096, kNvdbUpperTable = 8256;
 constexpr size_t kNvdbLowerChildMask = 32 + 512, kNvdbLowerTable = 1088;
-// leaves: the 512 values
-constexpr size_t kNvdbLeafValues = 96;
+// leaves: the 512 values (Float) or codes (quantized); a quantized leaf's
+// flags byte, minimum and quantum
+constexpr size_t kNvdbLeafValues = 96, kNvdbLeafFlags = 15, kNvdbLeafMinimum = 80, kNvdbLeafQuantum = 84;
+// leaf bytes: Float, Fp4, Fp8, Fp16; FpN: 96 + 64 x its bit width
+constexpr long long kNvdbLeafBytesFloat = 2144, kNvdbLeafBytesFp4 = 352, kNvdbLeafBytesFp8 = 608,
+                    kNvdbLeafBytesFp16 = 1120;
 
 // A parsed grid (host-side header fields, device pointer to the buffer).
 struct NvdbGrid {
   const unsigned char *base;  // the grid buffer (device memory for kernels)
+  uint32_t type;              // kNvdbGridType*
   long long root;             // byte offset of the root node from base
   uint32_t tiles;             // root table size
   float background;
@@ -55,6 +68,26 @@ template <typename T> GBV_HD T nvdb_ld(const unsigned char *p) {
   __builtin_memcpy(&v, p, sizeof(T));
   return v;
 #endif
+}
+
+// LeafData<BuildType>::getValue(n) (NanoVDB.h, LeafData<float>, LeafData<Fp4>,
+// <Fp8>, <Fp16>, <FpN>): the value of voxel n of the leaf at lf.
+GBV_HD float nvdb_leaf_value(uint32_t type, const unsigned char *lf, uint32_t n) {
+  if (type == kNvdbGridTypeFloat) return nvdb_ld<float>(lf + kNvdbLeafValues + 4 * (size_t)n);
+  uint32_t code;
+  if (type == kNvdbGridTypeFp8) {
+    code = nvdb_ld<uint8_t>(lf + kNvdbLeafValues + n);
+  } else if (type == kNvdbGridTypeFp16) {
+    code = nvdb_ld<uint16_t>(lf + kNvdbLeafValues + 2 * (size_t)n);
+  } else if (type == kNvdbGridTypeFp4) {
+    code = ((uint32_t)nvdb_ld<uint8_t>(lf + kNvdbLeafValues + (n >> 1)) >> ((n & 1u) << 2)) & 15u;
+  } else {  // FpN: b = log2 of the bit width (0..4, checked when the grid is parsed)
+    const uint32_t b = (uint32_t)nvdb_ld<uint8_t>(lf + kNvdbLeafFlags) >> 5;
+    code = nvdb_ld<uint32_t>(lf + kNvdbLeafValues + 4 * (size_t)(n >> (5u - b)));
+    code >>= (n & ((32u >> b) - 1u)) << b;
+    code &= (1u << (1u << b)) - 1u;
+  }
+  return (float)code * nvdb_ld<float>(lf + kNvdbLeafQuantum) + nvdb_ld<float>(lf + kNvdbLeafMinimum);
 }
 
 // ReadAccessor::getValue: the value at index coordinates (x, y, z) --
@@ -84,7 +117,7 @@ GBV_HD float nvdb_value(const NvdbGrid &g, int x, int y, int z) {
     return nvdb_ld<float>(lw + kNvdbLowerTable + 8 * (size_t)n);
   const unsigned char *lf = lw + nvdb_ld<long long>(lw + kNvdbLowerTable + 8 * (size_t)n);
   n = (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
-  return nvdb_ld<float>(lf + kNvdbLeafValues + 4 * (size_t)n);
+  return nvdb_leaf_value(g.type, lf, n);
 }
 
 // NanoVDBDataSampler::DD::sample (barney/volume/NanoVDB.h:100-129): world ->

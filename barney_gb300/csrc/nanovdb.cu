@@ -1,5 +1,5 @@
-// nanovdb.cu -- NanoVDB float grids: header parsing (host), the macrocell
-// range build and a sampling entry point (device).
+// nanovdb.cu -- NanoVDB grids (Float, Fp4, Fp8, Fp16, FpN): header parsing
+// (host), the macrocell range build and a sampling entry point (device).
 #include <cmath>
 #include <cstring>
 #include <cuda_runtime.h>
@@ -11,6 +11,7 @@ namespace gbv {
 NvdbGrid make_nvdb_grid(const void *d_grid, const gbv_nanovdb_info &info) {
   NvdbGrid g;
   g.base = reinterpret_cast<const unsigned char *>(d_grid);
+  g.type = (uint32_t)info.grid_type;
   g.root = info.root_offset;
   g.tiles = info.root_tiles;
   g.background = info.background;
@@ -53,8 +54,13 @@ __global__ void __launch_bounds__(128) nvdb_sample_kernel(NvdbGrid g, const floa
   out[i] = nvdb_sample(g, P[3 * i], P[3 * i + 1], P[3 * i + 2]);
 }
 
+static bool nvdb_type_read(uint32_t t) {
+  return t == kNvdbGridTypeFloat || t == kNvdbGridTypeFp4 || t == kNvdbGridTypeFp8 || t == kNvdbGridTypeFp16 ||
+         t == kNvdbGridTypeFpN;
+}
+
 static bool nvdb_info_ok(const gbv_nanovdb_info *info) {
-  if (!info) return false;
+  if (!info || !nvdb_type_read((uint32_t)info->grid_type)) return false;
   for (int i = 0; i < 3; i++)
     if (info->index_hi[i] < info->index_lo[i] || info->mc_dims[i] <= 0) return false;
   return info->root_offset > 0 && (unsigned long long)info->root_offset < info->bytes;
@@ -75,17 +81,21 @@ extern "C" gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_na
   const uint32_t version = nvdb_ld<uint32_t>(b + kNvdbGridVersion);
   if ((version >> 21) != 32)
     return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: NanoVDB format version other than 32");
-  if (nvdb_ld<uint32_t>(b + kNvdbGridType) != kNvdbGridTypeFloat)
-    return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: only grids of value type Float are supported");
+  // the types of BARNEY_NANOVDB_FLOAT_TYPES (barney/volume/NanoVDB.h:23-28)
+  const uint32_t type = nvdb_ld<uint32_t>(b + kNvdbGridType);
+  if (!nvdb_type_read(type))
+    return set_error(GBV_ERROR_UNSUPPORTED,
+                     "gbv_nanovdb_parse: grid value type other than Float, Fp4, Fp8, Fp16 or FpN");
   const uint64_t gridSize = nvdb_ld<uint64_t>(b + kNvdbGridSize);
   if (gridSize > bytes) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: buffer shorter than the grid");
   const long long rootRel = nvdb_ld<long long>(b + kNvdbGridHeader + kNvdbTreeRootOffset);
   const long long root = (long long)kNvdbGridHeader + rootRel;
-  if (rootRel <= 0 || (unsigned long long)root + kNvdbRootTiles > gridSize)
+  if (rootRel <= 0 || (root & 31) != 0 || (unsigned long long)root + kNvdbRootTiles > gridSize)
     return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: root node outside the grid");
   gbv_nanovdb_info r;
   std::memset(&r, 0, sizeof r);
   r.bytes = gridSize;
+  r.grid_type = (int)type;
   r.root_offset = root;
   r.root_tiles = nvdb_ld<uint32_t>(b + root + kNvdbRootTableSize);
   if ((unsigned long long)root + kNvdbRootTiles + (unsigned long long)kNvdbRootTile * r.root_tiles > gridSize)
@@ -107,13 +117,18 @@ extern "C" gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_na
     if (size > (1ll << 24)) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_nanovdb_parse: index bbox too large");
     r.mc_dims[i] = (int)((size + 15) / 16);
   }
-  // Every child offset must land a whole node inside the grid: the device
-  // follows them without checks.
+  // Every child offset must land a whole node inside the grid, on NanoVDB's
+  // 32-byte node alignment: the device follows them without checks and reads
+  // up to 8-byte words from the nodes.
   constexpr long long kUpperBytes = (long long)kNvdbUpperTable + 8ll * 32768;
   constexpr long long kLowerBytes = (long long)kNvdbLowerTable + 8ll * 4096;
-  constexpr long long kLeafBytes = (long long)kNvdbLeafValues + 4ll * 512;
+  const long long leafBytes = type == kNvdbGridTypeFloat  ? kNvdbLeafBytesFloat
+                            : type == kNvdbGridTypeFp4  ? kNvdbLeafBytesFp4
+                            : type == kNvdbGridTypeFp8  ? kNvdbLeafBytesFp8
+                            : type == kNvdbGridTypeFp16 ? kNvdbLeafBytesFp16
+                                                        : (long long)kNvdbLeafValues;  // FpN: its header first
   const long long end = (long long)gridSize;
-  auto inside = [&](long long off, long long size) { return off > 0 && off + size <= end; };
+  auto inside = [&](long long off, long long size) { return off > 0 && (off & 31) == 0 && off + size <= end; };
   for (uint32_t t = 0; t < r.root_tiles; t++) {
     const long long tile = root + (long long)kNvdbRootTiles + (long long)kNvdbRootTile * t;
     const long long c = nvdb_ld<long long>(b + tile + kNvdbTileChild);
@@ -128,7 +143,14 @@ extern "C" gbv_status gbv_nanovdb_parse(const void *h_grid, size_t bytes, gbv_na
       for (uint32_t k = 0; k < 4096; k++) {
         if (!((nvdb_ld<uint64_t>(b + lw + kNvdbLowerChildMask + 8 * (k >> 6)) >> (k & 63)) & 1ull)) continue;
         const long long lf = lw + nvdb_ld<long long>(b + lw + kNvdbLowerTable + 8ll * k);
-        if (!inside(lf, kLeafBytes)) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad leaf");
+        if (!inside(lf, leafBytes)) return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad leaf");
+        if (type == kNvdbGridTypeFpN) {  // codes of 1 << (flags >> 5) bits, 1 to 16
+          const uint32_t lb = (uint32_t)nvdb_ld<uint8_t>(b + lf + kNvdbLeafFlags) >> 5;
+          if (lb > 4)
+            return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: FpN leaf with a bit width above 16");
+          if (!inside(lf, (long long)kNvdbLeafValues + 64ll * (1ll << lb)))
+            return set_error(GBV_ERROR_INVALID_ARGUMENT, "gbv_nanovdb_parse: bad leaf");
+        }
       }
     }
   }

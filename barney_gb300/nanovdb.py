@@ -1,4 +1,5 @@
-"""NanoVDB float-grid fields (gbv_nanovdb_* in include/gbvol.h).
+"""NanoVDB grid fields of value type Float, Fp4, Fp8, Fp16 or FpN
+(gbv_nanovdb_* in include/gbvol.h).
 
 parse() checks a grid held in host memory; GpuNanoVDBScene renders a Scene
 whose field is such a grid (its transfer function, camera, lights and
@@ -18,7 +19,8 @@ class GbvNanovdbInfo(C.Structure):
     _fields_ = [("bytes", C.c_ulonglong), ("root_offset", C.c_longlong), ("root_tiles", C.c_uint),
                 ("background", C.c_float), ("inv_map", C.c_float * 9), ("map_offset", C.c_float * 3),
                 ("index_lo", C.c_int * 3), ("index_hi", C.c_int * 3), ("world_lo", C.c_float * 3),
-                ("world_hi", C.c_float * 3), ("voxel_size", C.c_double * 3), ("mc_dims", C.c_int * 3)]
+                ("world_hi", C.c_float * 3), ("voxel_size", C.c_double * 3), ("mc_dims", C.c_int * 3),
+                ("grid_type", C.c_int)]
 
 
 _ready = False
@@ -48,7 +50,7 @@ def parse(grid: bytes) -> GbvNanovdbInfo:
 
 
 class GpuNanoVDBScene(GpuScene):
-    """A Scene whose field is a NanoVDB float grid (bytes), on the device."""
+    """A Scene whose field is a NanoVDB grid (bytes), on the device."""
 
     def __init__(self, scene: Scene, grid: bytes):
         import torch

@@ -29,6 +29,13 @@ int sg_blob_volume(const int dims[3], int num_blobs, uint64_t seed,
 int sg_nanovdb_from_dense(const float *values, const int dims[3], const int origin[3],
                           float background, double voxel_size, const double translation[3],
                           void **out, size_t *bytes);
+/* The same grid with values of nanovdb::GridType grid_type: 1 Float, 13 Fp4,
+   14 Fp8, 15 Fp16 or 16 FpN, quantized as NanoVDB's builder does with
+   dithering off; tolerance: the absolute error an FpN leaf's bit width is
+   chosen for (negative: the builder's default for a fog volume, 0.01). */
+int sg_nanovdb_from_dense_typed(const float *values, const int dims[3], const int origin[3],
+                                float background, double voxel_size, const double translation[3],
+                                int grid_type, float tolerance, void **out, size_t *bytes);
 void sg_free(void *p);
 
 #ifdef __cplusplus

@@ -127,16 +127,24 @@ def blob_volume(dims, num_blobs: int, seed: int, noise: float = 0.05, fbm_octave
     return out
 
 
+# nanovdb::GridType of the value types the NanoVDB field reads
+NANOVDB_TYPES = {"float": 1, "fp4": 13, "fp8": 14, "fp16": 15, "fpn": 16}
+
+
 def nanovdb_grid(values: np.ndarray, origin=(0, 0, 0), voxel_size: float = 1.0, translation=(0.0, 0.0, 0.0),
-                 background: float = 0.0) -> bytes:
-    """A NanoVDB float grid (format 32.7 memory layout) of a dense
-    (nz, ny, nx) array placed at index `origin`, world = voxel_size * index +
-    translation; voxels equal to `background` are inactive."""
+                 background: float = 0.0, grid_type: str = "float", tolerance: float = -1.0) -> bytes:
+    """A NanoVDB grid (format 32.7 memory layout) of a dense (nz, ny, nx)
+    array placed at index `origin`, world = voxel_size * index +
+    translation; voxels equal to `background` are inactive.  grid_type: one
+    of NANOVDB_TYPES (quantized as NanoVDB's builder does, dithering off);
+    tolerance: the absolute error of an FpN leaf's bit width (negative: the
+    builder's default for a fog volume)."""
     L = _scenegen()
     if not hasattr(L, "_nvdb_ready"):
-        L.sg_nanovdb_from_dense.restype = C.c_int
-        L.sg_nanovdb_from_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_double, C.c_void_p,
-                                            C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+        L.sg_nanovdb_from_dense_typed.restype = C.c_int
+        L.sg_nanovdb_from_dense_typed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_double,
+                                                  C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_void_p),
+                                                  C.POINTER(C.c_size_t)]
         L.sg_free.argtypes = [C.c_void_p]
         L._nvdb_ready = True
     v = np.ascontiguousarray(values, np.float32)
@@ -145,25 +153,28 @@ def nanovdb_grid(values: np.ndarray, origin=(0, 0, 0), voxel_size: float = 1.0, 
     org = np.array(origin, np.int32)
     tr = np.array(translation, np.float64)
     buf, n = C.c_void_p(), C.c_size_t()
-    rc = L.sg_nanovdb_from_dense(v.ctypes.data, dims.ctypes.data, org.ctypes.data, background, voxel_size,
-                                 tr.ctypes.data, C.byref(buf), C.byref(n))
+    rc = L.sg_nanovdb_from_dense_typed(v.ctypes.data, dims.ctypes.data, org.ctypes.data, background, voxel_size,
+                                       tr.ctypes.data, NANOVDB_TYPES[grid_type], tolerance, C.byref(buf),
+                                       C.byref(n))
     if rc != 0:
-        raise ValueError(f"sg_nanovdb_from_dense failed ({rc})")
+        raise ValueError(f"sg_nanovdb_from_dense_typed failed ({rc})")
     try:
         return C.string_at(buf, n.value)
     finally:
         L.sg_free(buf)
 
 
-def nanovdb_of_scene(scene: "Scene") -> bytes:
+def nanovdb_of_scene(scene: "Scene", grid_type: str = "float", tolerance: float = -1.0) -> bytes:
     """The scene's volume as a NanoVDB grid whose voxel centres lie where the
     structured field has its voxels (the NanoVDB sampler reads voxel i at
-    index i + 1/2; needs the same spacing on every axis)."""
+    index i + 1/2; needs the same spacing on every axis), of the given value
+    type (see nanovdb_grid)."""
     origin, spacing = scene.geometry()
     if not (spacing[0] == spacing[1] == spacing[2]):
         raise ValueError("a NanoVDB grid has one voxel size")
     vs = float(spacing[0])
-    return nanovdb_grid(scene.scalars, (0, 0, 0), vs, tuple(float(o) - 0.5 * vs for o in origin), background=-1.0)
+    return nanovdb_grid(scene.scalars, (0, 0, 0), vs, tuple(float(o) - 0.5 * vs for o in origin), background=-1.0,
+                        grid_type=grid_type, tolerance=tolerance)
 
 
 def tf_ramp(n: int = 128, max_opacity: float = 0.8) -> np.ndarray:

@@ -424,36 +424,44 @@ def iso_timing(g, scene, persistent_ms, reps=2):
     return out
 
 
-def nanovdb_timing(scene, persistent_ms, reps=2):
-    """The frame with its volume given as a NanoVDB float grid (voxel
-    centres where the structured field has its voxels; the grid made by the
-    input generator): grid bytes, frame time and density samples per second
-    against the FP32 brick store's frame."""
+def nanovdb_timing(scene, persistent_ms, reps=2, types=("float", "fp16", "fp8", "fp4", "fpn")):
+    """The frame with its volume given as a NanoVDB grid (voxel centres where
+    the structured field has its voxels; the grid made by the input
+    generator), of each value type the NanoVDB field reads (FpN with the
+    builder's default tolerance for a fog volume, 0.01): grid bytes, frame
+    time and density samples per second against the FP32 brick store's
+    frame.  The Float grid's figures stay at the top level."""
     import torch
     from barney_gb300 import _native as N, scenes
     from barney_gb300.nanovdb import GpuNanoVDBScene
-    t0 = time.perf_counter()
-    grid = scenes.nanovdb_of_scene(scene)
-    make_s = time.perf_counter() - t0
-    g = GpuNanoVDBScene(scene, grid)
-    acc = g.new_accum()
-    cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
-    g.render(accum=acc, counters=cnt)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ts = []
-    for _ in range(reps):
-        e0.record()
-        g.render(accum=acc)
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
-    c = [int(x) for x in cnt.cpu().tolist()]
-    ms = min(ts)
-    out = {"grid_bytes": len(grid), "grid_make_s": make_s, "frame_ms": ms, "density_samples": c[N.GBV_COUNTER_SAMPLES],
-           "Msamples_s": c[N.GBV_COUNTER_SAMPLES] / ms / 1e3, "brick_f32_frame_ms": persistent_ms,
-           "loop_caps": c[N.GBV_COUNTER_CAPS]}
-    del g, grid
-    torch.cuda.empty_cache()
+    out = {"brick_f32_frame_ms": persistent_ms, "types": {}}
+    for t in types:
+        t0 = time.perf_counter()
+        grid = scenes.nanovdb_of_scene(scene, grid_type=t)
+        make_s = time.perf_counter() - t0
+        g = GpuNanoVDBScene(scene, grid)
+        acc = g.new_accum()
+        cnt = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+        g.render(accum=acc, counters=cnt)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            g.render(accum=acc)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        c = [int(x) for x in cnt.cpu().tolist()]
+        ms = min(ts)
+        r = {"grid_bytes": len(grid), "grid_make_s": make_s, "frame_ms": ms,
+             "density_samples": c[N.GBV_COUNTER_SAMPLES], "Msamples_s": c[N.GBV_COUNTER_SAMPLES] / ms / 1e3,
+             "loop_caps": c[N.GBV_COUNTER_CAPS]}
+        if t == "float":
+            out.update(r)
+        else:
+            out["types"][t] = r
+        del g, grid
+        torch.cuda.empty_cache()
     return out
 
 

@@ -153,11 +153,15 @@ typedef struct gbv_nanovdb_info {
   double voxel_size[3];
   /* macrocells: ceil(index bbox size / 16) per axis (NanoVDBData::buildMCs) */
   int mc_dims[3];
+  /* nanovdb::GridType of the values: 1 Float, 13 Fp4, 14 Fp8, 15 Fp16, 16 FpN */
+  int grid_type;
 } gbv_nanovdb_info;
 
-/* Parses and checks a NanoVDB float grid held in HOST memory (h_grid,
-   `bytes` long): magic number, format version 32, value type Float, the
-   size the header states, and every node of the tree inside the buffer (the
+/* Parses and checks a NanoVDB grid held in HOST memory (h_grid, `bytes`
+   long): magic number, format version 32, a value type the reference's
+   NanoVDB field reads (Float, Fp4, Fp8, Fp16, FpN; barney/volume/NanoVDB.h:
+   23-28), the size the header states, and every node of the tree inside the
+   buffer on 32-byte alignment, FpN leaves with bit widths of at most 16 (the
    device follows the child offsets unchecked, so a grid is parsed before it
    is used on the device).  Replaces
    NanoVDBData::commit (barney/volume/NanoVDB.cu:193-232). */

@@ -300,15 +300,19 @@ inline double fastLog(double f) {
 // Field and transfer function
 // ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
-// NanoVDB float grids (orc_scene.nanovdb): the reference's NanoVDB field
+// NanoVDB grids (orc_scene.nanovdb): the reference's NanoVDB field
 // (barney/volume/NanoVDB.{h,cu}) over the NanoVDB 32 buffer layout -- grid
-// header (672 B), tree header (64 B), root (64 B + 32-byte tiles keyed by
-// the 4096^3 region), upper nodes (32^3 entries, child mask at 4128, table
-// at 8256), lower nodes (16^3, 544, 1088), leaves (8^3 floats at 96); child
-// offsets are signed and relative to the parent (the root for root tiles).
+// header (672 B, value type at 636), tree header (64 B), root (64 B +
+// 32-byte tiles keyed by the 4096^3 region), upper nodes (32^3 entries,
+// child mask at 4128, table at 8256), lower nodes (16^3, 544, 1088), leaves
+// (8^3 values at 96: floats, or for the quantized types Fp4/Fp8/Fp16/FpN
+// codes c with value float(c) * quantum (at 84) + minimum (at 80), FpN's bit
+// width 1 << (flags (at 15) >> 5)); child offsets are signed and relative to
+// the parent (the root for root tiles).
 // ---------------------------------------------------------------------------
 struct Nvdb {
   const unsigned char *b = nullptr;
+  uint32_t type = 1;  // nanovdb::GridType: Float 1, Fp4 13, Fp8 14, Fp16 15, FpN 16
   int64_t root = 0;
   uint32_t tiles = 0;
   float background = 0.f;
@@ -325,6 +329,7 @@ template <typename T> inline T nv_get(const unsigned char *p) {
 inline Nvdb nv_parse(const unsigned char *b) {
   Nvdb g;
   g.b = b;
+  g.type = nv_get<uint32_t>(b + 636);
   g.root = 672 + nv_get<int64_t>(b + 672 + 24);
   g.tiles = nv_get<uint32_t>(b + g.root + 24);
   g.background = nv_get<float>(b + g.root + 28);
@@ -338,6 +343,29 @@ inline Nvdb nv_parse(const unsigned char *b) {
     g.M[i] = (g.hi[i] - g.lo[i] + 1 + 15) / 16;
   }
   return g;
+}
+// LeafData<BuildType>::getValue (NanoVDB.h: LeafData<float>, <Fp4>, <Fp8>,
+// <Fp16>, <FpN>) for voxel n of the leaf at lf
+inline float nv_leaf_value(uint32_t type, const unsigned char *lf, uint32_t n) {
+  const unsigned char *codes = lf + 96;
+  uint32_t c = 0;
+  switch (type) {
+  case 1: return nv_get<float>(codes + 4 * (size_t)n);
+  case 13: c = (codes[n / 2] >> (4 * (n % 2))) & 0xfu; break;
+  case 14: c = codes[n]; break;
+  case 15: c = nv_get<uint16_t>(codes + 2 * (size_t)n); break;
+  default: {  // FpN: the branched form of getValue
+    switch (lf[15] >> 5) {
+    case 0: c = (codes[n / 8] >> (n % 8)) & 1u; break;
+    case 1: c = (codes[n / 4] >> (2 * (n % 4))) & 3u; break;
+    case 2: c = (codes[n / 2] >> (4 * (n % 2))) & 15u; break;
+    case 3: c = codes[n]; break;
+    default: c = nv_get<uint16_t>(codes + 2 * (size_t)n); break;
+    }
+  }
+  }
+  const float q = nv_get<float>(lf + 84), m = nv_get<float>(lf + 80);
+  return float(c) * q + m;
 }
 // ReadAccessor::getValue
 inline float nv_value(const Nvdb &g, int x, int y, int z) {
@@ -361,7 +389,7 @@ inline float nv_value(const Nvdb &g, int x, int y, int z) {
       return nv_get<float>(lw + 1088 + 8 * (size_t)n1);
     const unsigned char *lf = lw + nv_get<int64_t>(lw + 1088 + 8 * (size_t)n1);
     const uint32_t n0 = (uint32_t(x) & 7u) * 64u + (uint32_t(y) & 7u) * 8u + (uint32_t(z) & 7u);
-    return nv_get<float>(lf + 96 + 4 * (size_t)n0);
+    return nv_leaf_value(g.type, lf, n0);
   }
   return g.background;
 }

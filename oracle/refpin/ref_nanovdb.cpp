@@ -26,6 +26,20 @@ nanovdb::GridHandle<nanovdb::HostBuffer> load(const unsigned char *bytes, size_t
   std::memcpy(buf.data(), bytes, n);
   return nanovdb::GridHandle<nanovdb::HostBuffer>(std::move(buf));
 }
+
+// The grid types the reference's NanoVDB field reads
+// (BARNEY_NANOVDB_FLOAT_TYPES, barney/volume/NanoVDB.h:23-28): f(BuildType)
+// for the grid's type; false for any other type.
+template <typename F> bool with_build_type(nanovdb::GridType t, F &&f) {
+  switch (t) {
+  case nanovdb::GridType::Float: f(float()); return true;
+  case nanovdb::GridType::Fp4: f(nanovdb::Fp4()); return true;
+  case nanovdb::GridType::Fp8: f(nanovdb::Fp8()); return true;
+  case nanovdb::GridType::Fp16: f(nanovdb::Fp16()); return true;
+  case nanovdb::GridType::FpN: f(nanovdb::FpN()); return true;
+  default: return false;
+  }
+}
 }  // namespace
 
 #pragma GCC visibility push(default)
@@ -76,13 +90,64 @@ int ref_nanovdb_layout(long long *out) {
   return n;
 }
 
-// A NanoVDB float grid from a dense x-fastest array: voxel (i,j,k) of the
-// array is index coordinate index_origin + (i,j,k); values equal to
-// `background` stay unset (inactive); map: uniform scale voxel_size and the
-// translation `translation`.  The grid's bytes go to a malloc'd buffer.
-int ref_nanovdb_from_dense(const float *values, const int dims[3], const int index_origin[3], float background,
-                           double voxel_size, const double translation[3], unsigned char **out, size_t *bytes) {
-  nanovdb::tools::build::Grid<float> grid(background, "pin");
+// Byte offsets and sizes of the quantized leaves (LeafData<Fp4|Fp8|Fp16|FpN>,
+// base LeafFnBase) and of the internal nodes above them:
+// [0] offsetof(mFlags), [1] offsetof(mMinimum), [2] offsetof(mQuantum),
+// [3] sizeof(LeafFnBase), [4..6] offsetof(mCode) of Fp4, Fp8, Fp16,
+// [7..9] sizeof leaf of Fp4, Fp8, Fp16, [10] sizeof(LeafData<FpN>),
+// [11] LeafData<FpN>::memUsage(8), [12..15] sizeof upper of Fp4, Fp8, Fp16,
+// FpN, [16..19] sizeof lower of the same, [20..23] GridType Float, Fp4, Fp8,
+// Fp16, [24] GridType FpN
+int ref_nanovdb_fp_layout(long long *out) {
+  using Base = nanovdb::LeafFnBase<nanovdb::Coord, nanovdb::Mask, 3>;
+  using L4 = nanovdb::NanoLeaf<nanovdb::Fp4>::DataType;
+  using L8 = nanovdb::NanoLeaf<nanovdb::Fp8>::DataType;
+  using L16 = nanovdb::NanoLeaf<nanovdb::Fp16>::DataType;
+  using LN = nanovdb::NanoLeaf<nanovdb::FpN>::DataType;
+  long long v[] = {(long long)offsetof(Base, mFlags),
+                   (long long)offsetof(Base, mMinimum),
+                   (long long)offsetof(Base, mQuantum),
+                   (long long)sizeof(Base),
+                   (long long)offsetof(L4, mCode),
+                   (long long)offsetof(L8, mCode),
+                   (long long)offsetof(L16, mCode),
+                   (long long)sizeof(L4),
+                   (long long)sizeof(L8),
+                   (long long)sizeof(L16),
+                   (long long)sizeof(LN),
+                   (long long)LN::memUsage(8u),
+                   (long long)sizeof(nanovdb::NanoUpper<nanovdb::Fp4>::DataType),
+                   (long long)sizeof(nanovdb::NanoUpper<nanovdb::Fp8>::DataType),
+                   (long long)sizeof(nanovdb::NanoUpper<nanovdb::Fp16>::DataType),
+                   (long long)sizeof(nanovdb::NanoUpper<nanovdb::FpN>::DataType),
+                   (long long)sizeof(nanovdb::NanoLower<nanovdb::Fp4>::DataType),
+                   (long long)sizeof(nanovdb::NanoLower<nanovdb::Fp8>::DataType),
+                   (long long)sizeof(nanovdb::NanoLower<nanovdb::Fp16>::DataType),
+                   (long long)sizeof(nanovdb::NanoLower<nanovdb::FpN>::DataType),
+                   (long long)nanovdb::GridType::Float,
+                   (long long)nanovdb::GridType::Fp4,
+                   (long long)nanovdb::GridType::Fp8,
+                   (long long)nanovdb::GridType::Fp16,
+                   (long long)nanovdb::GridType::FpN};
+  const int n = (int)(sizeof(v) / sizeof(v[0]));
+  for (int i = 0; i < n; i++) out[i] = v[i];
+  return n;
+}
+
+// A NanoVDB grid from a dense x-fastest array: voxel (i,j,k) of the array
+// is index coordinate index_origin + (i,j,k); values equal to `background`
+// stay unset (inactive); map: uniform scale voxel_size and the translation
+// `translation`.  grid_type: a nanovdb::GridType the reference reads (Float,
+// Fp4, Fp8, Fp16, FpN), made by the library's builder with dithering off;
+// for FpN, `tolerance` >= 0 is the absolute error the bit width of each leaf
+// is chosen for (tools::AbsDiff), else the builder's default for the grid
+// class.  `fog`: mark the grid a fog volume (else its class is unknown).
+// The grid's bytes go to a malloc'd buffer.
+int ref_nanovdb_from_dense_typed(const float *values, const int dims[3], const int index_origin[3], float background,
+                                 double voxel_size, const double translation[3], int grid_type, float tolerance,
+                                 int fog, unsigned char **out, size_t *bytes) {
+  nanovdb::tools::build::Grid<float> grid(background, "pin",
+                                          fog ? nanovdb::GridClass::FogVolume : nanovdb::GridClass::Unknown);
   grid.setTransform(voxel_size, nanovdb::Vec3d(translation[0], translation[1], translation[2]));
   auto acc = grid.getAccessor();
   for (int k = 0; k < dims[2]; k++)
@@ -92,7 +157,20 @@ int ref_nanovdb_from_dense(const float *values, const int dims[3], const int ind
         if (v != background)
           acc.setValue(nanovdb::Coord(index_origin[0] + i, index_origin[1] + j, index_origin[2] + k), v);
       }
-  auto handle = nanovdb::tools::createNanoGrid(grid);
+  using SrcT = nanovdb::tools::build::Grid<float>;
+  nanovdb::GridHandle<nanovdb::HostBuffer> handle;
+  switch ((nanovdb::GridType)grid_type) {
+  case nanovdb::GridType::Float: handle = nanovdb::tools::createNanoGrid(grid); break;
+  case nanovdb::GridType::Fp4: handle = nanovdb::tools::createNanoGrid<SrcT, nanovdb::Fp4>(grid); break;
+  case nanovdb::GridType::Fp8: handle = nanovdb::tools::createNanoGrid<SrcT, nanovdb::Fp8>(grid); break;
+  case nanovdb::GridType::Fp16: handle = nanovdb::tools::createNanoGrid<SrcT, nanovdb::Fp16>(grid); break;
+  case nanovdb::GridType::FpN:
+    handle = nanovdb::tools::createNanoGrid<SrcT, nanovdb::FpN>(
+        grid, nanovdb::tools::StatsMode::Default, nanovdb::CheckMode::Default, false, 0,
+        nanovdb::tools::AbsDiff(tolerance));
+    break;
+  default: return 2;
+  }
   *bytes = handle.size();
   *out = (unsigned char *)std::malloc(*bytes);
   if (!*out) return 1;
@@ -100,23 +178,36 @@ int ref_nanovdb_from_dense(const float *values, const int dims[3], const int ind
   return 0;
 }
 
+int ref_nanovdb_from_dense(const float *values, const int dims[3], const int index_origin[3], float background,
+                           double voxel_size, const double translation[3], unsigned char **out, size_t *bytes) {
+  return ref_nanovdb_from_dense_typed(values, dims, index_origin, background, voxel_size, translation,
+                                      (int)nanovdb::GridType::Float, -1.f, 0, out, bytes);
+}
+
 void ref_free(void *p) { std::free(p); }
 
-// NanoVDBDataSampler<float>::DD::sample at n points
+// NanoVDBDataSampler<BuildType>::DD::sample at n points, BuildType the
+// grid's type
 int ref_nanovdb_sample(const unsigned char *bytes, size_t n_bytes, const float *P, int n, float *out) {
   auto h = load(bytes, n_bytes);
-  auto *grid = h.grid<float>();
-  if (!grid) return 1;
-  NanoVDBDataSampler<float>::DD dd;
-  dd.nvdbGrid = grid;
-  (nanovdb::CoordBBox &)dd.indexBounds = grid->indexBBox();
-  for (int i = 0; i < n; i++) out[i] = dd.sample(vec3f(P[3 * i], P[3 * i + 1], P[3 * i + 2]));
-  return 0;
+  const nanovdb::GridMetaData *meta = h.gridMetaData();
+  int rc = 1;
+  with_build_type(meta->gridType(), [&](auto tag) {
+    using T = decltype(tag);
+    auto *grid = h.template grid<T>();
+    if (!grid) return;
+    typename NanoVDBDataSampler<T>::DD dd;
+    dd.nvdbGrid = grid;
+    (nanovdb::CoordBBox &)dd.indexBounds = grid->indexBBox();
+    for (int i = 0; i < n; i++) out[i] = dd.sample(vec3f(P[3 * i], P[3 * i + 1], P[3 * i + 2]));
+    rc = 0;
+  });
+  return rc;
 }
 
 // The field's macrocell grid as NanoVDBData::commit and ::buildMCs set it up
-// (NanoVDB.cu:70-92, 193-232), and NanoVDBData_computeMCs (NanoVDB.cu:28-60)
-// run for every macrocell.  mc_dims[3], world bounds (float, lower then
+// (NanoVDB.cu:70-92, 193-232), and NanoVDBData_computeMCs<BuildType>
+// (NanoVDB.cu:28-60, BuildType the grid's type) run for every macrocell.  mc_dims[3], world bounds (float, lower then
 // upper) and the ranges (2 floats per macrocell) are returned.
 int ref_nanovdb_mc_ranges(const unsigned char *bytes, size_t n_bytes, int mc_dims[3], float world[6],
                           float *ranges, long long max_mcs) {
@@ -147,10 +238,14 @@ int ref_nanovdb_mc_ranges(const unsigned char *bytes, size_t n_bytes, int mc_dim
   ci.threadIdx = vec3ui(0u);
   ci.blockDim = vec3ui(1u);
   ci.gridDim = vec3ui((uint32_t)nmc, 1u, 1u);
-  for (long long t = 0; t < nmc; t++) {
-    ci.blockIdx = vec3ui((uint32_t)t, 0u, 0u);
-    NanoVDBData_computeMCs<float>(ci, mc, dd);
-  }
+  const bool known = with_build_type(dd.gridType, [&](auto tag) {
+    using T = decltype(tag);
+    for (long long t = 0; t < nmc; t++) {
+      ci.blockIdx = vec3ui((uint32_t)t, 0u, 0u);
+      NanoVDBData_computeMCs<T>(ci, mc, dd);
+    }
+  });
+  if (!known) return 2;
   for (long long t = 0; t < nmc; t++) {
     ranges[2 * t] = r[(size_t)t].lower;
     ranges[2 * t + 1] = r[(size_t)t].upper;

@@ -85,3 +85,69 @@ def test_bn_nanovdb_field(cuda, pin):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(img), bits(ref))
     assert float(img[..., :3].sum()) > 0
+
+
+# ---- quantized grids (Fp4, Fp8, Fp16, FpN) ----------------------------------
+
+PIN_FP = Path(__file__).resolve().parent / "golden" / "nanovdb_fp_pin.npz"
+FP_NAMES = ["fp4", "fp8", "fp16", "fpn_fine", "fpn_coarse"]
+
+
+@pytest.fixture(scope="module")
+def pin_fp():
+    z = np.load(PIN_FP)
+    return {k: z[k] for k in z.files}
+
+
+@pytest.mark.parametrize("name", FP_NAMES)
+def test_quantized_sampler_and_macrocells_match_the_reference(cuda, pin_fp, name):
+    """The reference's NanoVDBDataSampler and NanoVDBData_computeMCs on
+    grids the vendored library quantized (FpN leaves of every bit width from
+    1 to 16 across the two FpN grids): samples and ranges bit for bit."""
+    import torch
+    g = GpuNanoVDBScene(_scene(), pin_fp[f"grid_{name}"].tobytes())
+    assert g.info.grid_type in (13, 14, 15, 16)
+    got = g.sample(torch.from_numpy(pin_fp["points"]).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(bits(got), bits(pin_fp[f"samples_{name}"]))
+    assert list(g.mc) == pin_fp[f"mc_dims_{name}"].tolist()
+    np.testing.assert_array_equal(bits(g.ranges.cpu().numpy().reshape(-1, 2)), bits(pin_fp[f"ranges_{name}"]))
+
+
+@pytest.mark.parametrize("name,multi", [("fp4", False), ("fp8", False), ("fp16", False), ("fpn_coarse", False),
+                                        ("fpn_fine", True)])
+def test_quantized_frames_match_the_oracle(cuda, pin_fp, name, multi):
+    """Frames of a quantized grid: bit-exact against the oracle (its
+    bounded-math mode with multiple scattering and the env map), event counts
+    equal."""
+    import torch
+    s = _scene(multi=multi)
+    grid = pin_fp[f"grid_{name}"].tobytes()
+    g = GpuNanoVDBScene(s, grid)
+    c = torch.zeros(N.GBV_NUM_COUNTERS, dtype=torch.int64, device="cuda")
+    acc = g.render(spp=4, accum_id_start=1, counters=c)
+    torch.cuda.synchronize()
+    o = oracle.Oracle(s, nanovdb=grid, bounded_math=multi)
+    ref = o.render(spp=4, accum_id_start=1)
+    np.testing.assert_array_equal(bits(acc.cpu().numpy()), bits(ref))
+    cc = c.cpu().tolist()
+    assert cc[0] == o.stats["density_samples"] and cc[1] == o.stats["mc_visits"] and cc[2] == o.stats["rays"]
+    assert cc[0] > 100
+
+
+def test_bn_quantized_nanovdb_field(cuda):
+    """A "NanoVDB" scalar field holding an Fp16 grid of the frame volume,
+    made by the input generator, renders through bn* the frame the gbv path
+    renders from the same grid."""
+    import torch
+    s = scenes.frame_scene(dims=40, width=48, height=32, spp=2)
+    grid = scenes.nanovdb_of_scene(s, grid_type="fp16")
+    with bn.BarneySession() as ses:
+        err = ses.build_scene(s, 0, nanovdb=grid)
+        assert err == "", err
+        ses.render()
+        img = ses.read()
+    g = GpuNanoVDBScene(s, grid)
+    ref = g.tonemap(g.render(), s.spp).cpu().numpy()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(img), bits(ref))
+    assert float(img[..., :3].sum()) > 0

@@ -423,3 +423,79 @@ def test_live_nanovdb_grids():
         mc, world, ranges = mod.reference_mc(grid)
         assert list(o.mc_grid()[0]) == mc.tolist()
         assert np.array_equal(o.mc_ranges().view(np.uint32), ranges.view(np.uint32))
+
+
+# ---- quantized NanoVDB grids (Fp4, Fp8, Fp16, FpN) ---------------------------
+
+NVDB_FP = Path(__file__).resolve().parent / "golden" / "nanovdb_fp_pin.npz"
+FP_NAMES = ["fp4", "fp8", "fp16", "fpn_fine", "fpn_coarse"]
+# LeafFnBase's flags, minimum and quantum offsets and size; the codes' offset
+# in Fp4/Fp8/Fp16 leaves and their sizes; LeafData<FpN>'s size and its
+# 8-bit memUsage; the upper and lower node sizes of the four types; the
+# GridType values of Float, Fp4, Fp8, Fp16, FpN
+NVDB_FP_LAYOUT = [15, 80, 84, 96, 96, 96, 96, 352, 608, 1120, 96, 608] + [270400] * 4 + [33856] * 4 + \
+    [1, 13, 14, 15, 16]
+
+
+@pytest.fixture(scope="module")
+def nvdb_fp():
+    z = np.load(NVDB_FP)
+    return {k: z[k] for k in z.files}
+
+
+def test_nanovdb_quantized_layout_is_the_vendored_library_layout(nvdb_fp):
+    assert nvdb_fp["fp_layout"].tolist() == NVDB_FP_LAYOUT
+
+
+def _fpn_widths(grid: bytes):
+    """Bit widths of an FpN grid's leaves, walked in storage order."""
+    import struct
+    leaf0 = 672 + struct.unpack_from("<Q", grid, 672)[0]
+    count = struct.unpack_from("<I", grid, 672 + 32)[0]
+    off, widths = leaf0, set()
+    for _ in range(count):
+        w = 1 << (grid[off + 15] >> 5)
+        widths.add(w)
+        off += 96 + 64 * w
+    return widths
+
+
+@pytest.mark.parametrize("name", FP_NAMES)
+def test_oracle_quantized_nanovdb_against_the_reference(nvdb_fp, name):
+    """The reference's NanoVDBDataSampler<Fp4|Fp8|Fp16|FpN> and
+    NanoVDBData_computeMCs<...> on grids the vendored library quantized,
+    against the oracle: samples and macrocell ranges bit for bit."""
+    grid = nvdb_fp[f"grid_{name}"].tobytes()
+    o = _nvdb_oracle(grid)
+    got = o.sample(nvdb_fp["points"])
+    assert same_or_both_nan(got, nvdb_fp[f"samples_{name}"])
+    assert (got > 0).sum() > 500
+    assert list(o.mc_grid()[0]) == nvdb_fp[f"mc_dims_{name}"].tolist()
+    assert np.array_equal(o.mc_ranges().view(np.uint32), nvdb_fp[f"ranges_{name}"].view(np.uint32))
+
+
+def test_fpn_fixtures_cover_every_bit_width(nvdb_fp):
+    widths = _fpn_widths(nvdb_fp["grid_fpn_fine"].tobytes()) | _fpn_widths(nvdb_fp["grid_fpn_coarse"].tobytes())
+    assert widths == {1, 2, 4, 8, 16}
+
+
+@live
+def test_live_quantized_nanovdb_grids():
+    """Fresh quantized grids of another volume and placement: the live
+    reference and the oracle agree for every type."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_nanovdb_golden", NVDB.parent / "make_nanovdb_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    from barney_gb300 import scenes
+    rng = np.random.default_rng(6)
+    vol = scenes.blob_volume((33, 25, 41), 5, seed=33, noise=0.02)
+    vol = np.where(vol < 0.03, np.float32(0.0), vol).astype(np.float32)
+    pts = (rng.random((2000, 3)) * 2.4 - 1.2).astype(np.float32)
+    for gtype, tol in ((13, -1.0), (14, -1.0), (15, -1.0), (16, 0.002), (16, 0.02), (16, -1.0)):
+        grid = mod.make_grid(vol, (-12, 40, 5), 0.027, (0.2, -0.4, 0.1), grid_type=gtype, tolerance=tol, fog=True)
+        o = _nvdb_oracle(grid)
+        assert same_or_both_nan(o.sample(pts), mod.reference_samples(grid, pts)), (gtype, tol)
+        mc, world, ranges = mod.reference_mc(grid)
+        assert list(o.mc_grid()[0]) == mc.tolist()
+        assert np.array_equal(o.mc_ranges().view(np.uint32), ranges.view(np.uint32)), (gtype, tol)
