@@ -151,3 +151,25 @@ def test_bn_quantized_nanovdb_field(cuda):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(img), bits(ref))
     assert float(img[..., :3].sum()) > 0
+
+
+@pytest.mark.parametrize("kind", ["iso-only", "iso-first", "volume-first"])
+def test_iso_world_on_a_nanovdb_field(cuda, pin, pin_fp, kind):
+    """An iso-surface of a NanoVDB field (MCIsoSurfaceAccel over
+    NanoVDBDataSampler, barney/volume/NanoVDB.cu), alone or beside the
+    field's volume in either instance order: bit-exact against the oracle in
+    its bounded-math mode, for a Float and an Fp8 grid."""
+    import torch
+    inst, vol_inst, no_vol = {"iso-only": (0, 0, True), "iso-first": (0, 1, False),
+                              "volume-first": (1, 0, False)}[kind]
+    for grid in (pin["grid"].tobytes(), pin_fp["grid_fp8"].tobytes()):
+        s = _scene(multi=True)
+        s.iso = scenes.IsoSurface(0.3, (0.9, 0.6, 0.3, 1.0), 1.0, inst)
+        s.volume_instance, s.no_volume = vol_inst, no_vol
+        g = GpuNanoVDBScene(s, grid)
+        acc = g.render(spp=4)
+        torch.cuda.synchronize()
+        o = oracle.Oracle(s, nanovdb=grid, bounded_math=True)
+        ref = o.render(spp=4)
+        np.testing.assert_array_equal(bits(acc.cpu().numpy()), bits(ref))
+        assert float(ref[..., :3].sum()) > 0
