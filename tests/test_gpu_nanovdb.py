@@ -173,3 +173,24 @@ def test_iso_world_on_a_nanovdb_field(cuda, pin, pin_fp, kind):
         ref = o.render(spp=4)
         np.testing.assert_array_equal(bits(acc.cpu().numpy()), bits(ref))
         assert float(ref[..., :3].sum()) > 0
+
+
+def test_bn_iso_surface_of_a_nanovdb_field(cuda, pin_fp):
+    """bn*: an "iso_surface" geometry whose "scalarField" is a "NanoVDB"
+    field (an FpN grid), beside the field's volume: the frame the gbv path
+    renders from the same grid."""
+    import torch
+    s = _scene(multi=True)
+    s.iso = scenes.IsoSurface(0.3, (0.9, 0.6, 0.3, 1.0), 1.0, 0)
+    s.volume_instance, s.no_volume = 1, False
+    grid = pin_fp["grid_fpn_coarse"].tobytes()
+    with bn.BarneySession() as ses:
+        err = ses.build_scene(s, 0, nanovdb=grid)
+        assert err == "", err
+        ses.render()
+        img = ses.read()
+    g = GpuNanoVDBScene(s, grid)
+    ref = g.tonemap(g.render(), s.spp).cpu().numpy()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(bits(img), bits(ref))
+    assert float(img[..., :3].sum()) > 0
