@@ -71,10 +71,11 @@ __device__ __forceinline__ bool ea_ray(const EAParams &p, const EAViewDev &v, in
 
 template <class Store> __device__ __forceinline__ Store ea_store(const EAParams &p);
 template <> __device__ __forceinline__ StoreLinearF32 ea_store<StoreLinearF32>(const EAParams &p) { return p.store; }
+// brick stores read through L1 (neighbouring rays and consecutive steps share cells)
 #define GBV_EA_BRICK_STORE(FMT)                                                                           \
-  template <> __device__ __forceinline__ StoreBrickCorners<FMT> ea_store<StoreBrickCorners<FMT>>(        \
+  template <> __device__ __forceinline__ StoreBrickCorners<FMT, true> ea_store<StoreBrickCorners<FMT, true>>( \
       const EAParams &p) {                                                                                \
-    return StoreBrickCorners<FMT>{p.vox, p.so, p.brick};                                                  \
+    return StoreBrickCorners<FMT, true>{p.vox, p.so, p.brick};                                            \
   }
 GBV_EA_BRICK_STORE(GBV_VOXEL_F32)
 GBV_EA_BRICK_STORE(GBV_VOXEL_F16)
@@ -500,11 +501,11 @@ gbv_status gbv_ea_render(const gbv_scene *s, const gbv_ea_view *views, int num_v
     float4 *out = reinterpret_cast<float4 *>(d_images);
     cudaStream_t cs = (cudaStream_t)stream;
     if (layout == GBV_LAYOUT_LINEAR) ea_forward_kernel<StoreLinearF32><<<grid, 128, 0, cs>>>(q, out);
-    else if (format == GBV_VOXEL_F32) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F32>><<<grid, 128, 0, cs>>>(q, out);
-    else if (format == GBV_VOXEL_F16) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F16>><<<grid, 128, 0, cs>>>(q, out);
+    else if (format == GBV_VOXEL_F32) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F32, true>><<<grid, 128, 0, cs>>>(q, out);
+    else if (format == GBV_VOXEL_F16) ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_F16, true>><<<grid, 128, 0, cs>>>(q, out);
     else if (format == GBV_VOXEL_BF16)
-      ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_BF16>><<<grid, 128, 0, cs>>>(q, out);
-    else ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_U8_SCALED>><<<grid, 128, 0, cs>>>(q, out);
+      ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_BF16, true>><<<grid, 128, 0, cs>>>(q, out);
+    else ea_forward_kernel<StoreBrickCorners<GBV_VOXEL_U8_SCALED, true>><<<grid, 128, 0, cs>>>(q, out);
     return check_launch("ea_forward_kernel");
   });
 }
