@@ -58,7 +58,34 @@ struct NvdbGrid {
   float background;
   float invMatF[9], vecF[3];  // world -> index map, single precision
   int lo[3], hi[3];           // index bbox of the active values
+  bool fixedMap;              // the bbox lies within +-2^21: nvdb_axis may work in fixed point
 };
+
+// One axis of the sampler's index position, as the reference computes it in
+// double: x = clamp((double)r - 0.5, lo, hi), i = floor(x), u = (float)(x - i).
+// For |r| in [2^-17, 2^22) (and a bbox within +-2^21) every one of those
+// double operations is exact, so they are done exactly in 64-bit fixed point
+// with 40 fraction bits instead (r * 2^40 is an integer there: r's last bit
+// is worth at least 2^-40), rounding u to float once as the double path's
+// conversion does.  Other r (tiny, huge, NaN) take the double path.
+// GB300's FP64 rate is low; this keeps the sampler off it for nearly every
+// sample.
+GBV_HD void nvdb_axis(float r, int lo, int hi, bool fixedMap, int &i, float &u) {
+  const float a = fabsf(r);
+  if (fixedMap && a >= 0x1p-17f && a < 0x1p22f) {
+    long long d = (long long)(r * 0x1p40f) - (1ll << 39);
+    const long long l = (long long)lo * (1ll << 40), h = (long long)hi * (1ll << 40);
+    d = d < l ? l : d > h ? h : d;
+    i = (int)(d >> 40);  // floor (arithmetic shift)
+    u = (float)(d & ((1ll << 40) - 1)) * 0x1p-40f;
+    return;
+  }
+  double x = (double)r - 0.5;
+  // nanovdb::math::Clamp(x, a, b) = fmax(fmin(x, b), a)
+  x = fmax(fmin(x, (double)hi), (double)lo);
+  i = (int)floor(x);
+  u = (float)(x - (double)i);
+}
 
 template <typename T> GBV_HD T nvdb_ld(const unsigned char *p) {
 #if defined(__CUDA_ARCH__)
@@ -128,23 +155,16 @@ GBV_HD float nvdb_value(const NvdbGrid &g, int x, int y, int z) {
 // at floor(x) + {0,1}^3 and lerp(a, b, w) = a + float(w) * (b - a) along z,
 // then y, then x.  Never NaN: points outside take the border values.
 GBV_HD float nvdb_sample(const NvdbGrid &g, float px, float py, float pz) {
-  const double dx = (double)px - (double)g.vecF[0], dy = (double)py - (double)g.vecF[1],
-               dz = (double)pz - (double)g.vecF[2];
-  const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+  // (float)((double)p - (double)v) is the float difference p - v: when the
+  // double difference is exact both round it once, else |v| < 2^-29 |p| (or
+  // the reverse) and both give p (v)
+  const float fx = px - g.vecF[0], fy = py - g.vecF[1], fz = pz - g.vecF[2];
   const float *m = g.invMatF;
-  double ix = (double)fmaf(fx, m[0], fmaf(fy, m[1], fz * m[2]));
-  double iy = (double)fmaf(fx, m[3], fmaf(fy, m[4], fz * m[5]));
-  double iz = (double)fmaf(fx, m[6], fmaf(fy, m[7], fz * m[8]));
-  ix -= 0.5;
-  iy -= 0.5;
-  iz -= 0.5;
-  // nanovdb::math::Clamp(x, a, b) = fmax(fmin(x, b), a)
-  auto clampd = [](double x, double a, double b) { return fmax(fmin(x, b), a); };
-  ix = clampd(ix, (double)g.lo[0], (double)g.hi[0]);
-  iy = clampd(iy, (double)g.lo[1], (double)g.hi[1]);
-  iz = clampd(iz, (double)g.lo[2], (double)g.hi[2]);
-  const int i = (int)floor(ix), j = (int)floor(iy), k = (int)floor(iz);
-  const double u = ix - (double)i, v = iy - (double)j, w = iz - (double)k;
+  int i, j, k;
+  float fu, fv, fw;
+  nvdb_axis(fmaf(fx, m[0], fmaf(fy, m[1], fz * m[2])), g.lo[0], g.hi[0], g.fixedMap, i, fu);
+  nvdb_axis(fmaf(fx, m[3], fmaf(fy, m[4], fz * m[5])), g.lo[1], g.hi[1], g.fixedMap, j, fv);
+  nvdb_axis(fmaf(fx, m[6], fmaf(fy, m[7], fz * m[8])), g.lo[2], g.hi[2], g.fixedMap, k, fw);
   float s[2][2][2];
 #pragma unroll
   for (int a = 0; a < 2; a++)
@@ -152,7 +172,6 @@ GBV_HD float nvdb_sample(const NvdbGrid &g, float px, float py, float pz) {
     for (int b = 0; b < 2; b++)
 #pragma unroll
       for (int c = 0; c < 2; c++) s[a][b][c] = nvdb_value(g, i + a, j + b, k + c);
-  const float fu = (float)u, fv = (float)v, fw = (float)w;
   auto lerp = [](float p, float q, float t) { return p + t * (q - p); };
   return lerp(lerp(lerp(s[0][0][0], s[0][0][1], fw), lerp(s[0][1][0], s[0][1][1], fw), fv),
               lerp(lerp(s[1][0][0], s[1][0][1], fw), lerp(s[1][1][0], s[1][1][1], fw), fv), fu);

@@ -16,10 +16,12 @@ NvdbGrid make_nvdb_grid(const void *d_grid, const gbv_nanovdb_info &info) {
   g.tiles = info.root_tiles;
   g.background = info.background;
   for (int i = 0; i < 9; i++) g.invMatF[i] = info.inv_map[i];
+  g.fixedMap = true;
   for (int i = 0; i < 3; i++) {
     g.vecF[i] = info.map_offset[i];
     g.lo[i] = info.index_lo[i];
     g.hi[i] = info.index_hi[i];
+    if (g.lo[i] < -(1 << 21) || g.hi[i] > (1 << 21)) g.fixedMap = false;
   }
   return g;
 }

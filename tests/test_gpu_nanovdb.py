@@ -194,3 +194,32 @@ def test_bn_iso_surface_of_a_nanovdb_field(cuda, pin_fp):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(bits(img), bits(ref))
     assert float(img[..., :3].sum()) > 0
+
+
+@pytest.mark.parametrize("origin", [(-5, 3, 7), (-1, 0, -2), (3_000_000, -2_500_000, 40)])
+def test_sampler_index_arithmetic_edge_cases(cuda, origin):
+    """The sampler's index position (the reference computes it in double;
+    the device in exact fixed point where that is exact, else in double):
+    points whose index coordinates fall on and one float step either side of
+    voxel centres, within 2^-17 of index 0 (the double path), outside the
+    grid (clamped), and a grid placed beyond +-2^21 (the double path
+    throughout) sample bit-identically to the oracle."""
+    import torch
+    vol = scenes.blob_volume((24, 20, 18), 4, seed=7, noise=0.02)
+    vs, tr = 0.03, (-0.4, -0.55, -0.35)
+    grid = scenes.nanovdb_grid(vol, origin, vs, tr, background=-1.0)
+    g = GpuNanoVDBScene(_scene(), grid)
+    o = oracle.Oracle(_scene(), nanovdb=grid)
+    rng = np.random.default_rng(11)
+    n = 20000
+    lo = np.array(origin, np.float64)
+    hi = lo + np.array([24, 20, 18]) - 1
+    idx = lo - 3 + rng.random((n, 3)) * (hi - lo + 6)      # inside and around the grid
+    idx[: n // 4] = np.round(idx[: n // 4]) + 0.5          # voxel centres (u = 0)
+    idx[n // 4: n // 2] = np.round(idx[n // 4: n // 2])    # voxel corners
+    tiny = rng.standard_normal((n // 8, 3)) * 1e-6          # around index 0 on one axis
+    idx[n // 2: n // 2 + n // 8, 0] = tiny[:, 0]
+    P = (idx * vs + np.array(tr)).astype(np.float32)
+    P[: n // 2] = np.nextafter(P[: n // 2], np.float32(rng.choice([-np.inf, np.inf])))  # one float step off
+    got = g.sample(torch.from_numpy(P).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(bits(got), bits(o.sample(P)))
