@@ -10,7 +10,8 @@ host buffers (volume upload, macrocell and brick build, render, frame read).
 
   python bench.py [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun each rank renders its own replica of the frame (replicas only:
-the frame is one GPU's work; there is no data-path collective).
+the frame is one GPU's work; there is no data-path collective); `value` and
+`e2e` take the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -592,6 +593,19 @@ def run_ours(args):
             # per frame: the majorant-bitmask kernel, then the render kernel
             # (profiles/launches_bench_512cube_1080p_64spp.md)
             "gpu_launches": 2 * args.steps, "clocks": clk.summary()}
+    # ---- e2e through the bn* C-ABI with host buffers, on every rank; the
+    # slowest rank's step time counts ----
+    if world > 1:
+        dist.barrier()
+    e2e = e2e_timing(args, scene, g, acc, fmt, local)
+    if world > 1:
+        t = torch.tensor([e2e["dt"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e["dt"] = float(t.item())
+    line["e2e"] = {"value": world * samples / e2e["dt"] / 1e6, "unit": UNIT, "h2d_bytes_per_step": e2e["h2d"],
+                   "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": 1e3 * e2e["dt"],
+                   "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers",
+                   "frame_identical_to_device_frame": e2e["same"], "phases_ms": e2e["phases_ms"]}
     if rank != 0:
         if world > 1:
             dist.barrier()
@@ -624,7 +638,22 @@ def run_ours(args):
             line["nanovdb"] = nanovdb_timing(scene, frame_ms)
         except Exception as e:
             line["nanovdb"] = {"error": str(e)}
-    # ---- e2e through the bn* C-ABI with host buffers ----
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
+    line["extras_s"] = time.perf_counter() - extras_t0
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+
+
+def e2e_timing(args, scene, g, acc, fmt, local):
+    """Steps through the public bn* API with host buffers: each uploads the
+    volume from pinned host memory (bnTextureData3DCreate), builds the
+    scene, renders the frame (bnRender) and reads it into pinned host memory
+    (bnFrameBufferRead); one untimed step first.  Returns the mean step
+    time, its three phases, the bytes copied each way, and whether the frame
+    read equals the device-timed frame `acc`."""
+    import torch
     from barney_gb300 import bn
     host_vol = torch.from_numpy(np.ascontiguousarray(scene.scalars)).pin_memory()
     out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32).pin_memory()
@@ -644,22 +673,12 @@ def run_ours(args):
                 # the bn* calls return when their work is done (each upload
                 # and build synchronizes, bnRender waits for its frame)
                 phases.append((t1 - t0, t2 - t1, t0 + dt - t2))
-    e2e_dt = sum(e2e_times) / len(e2e_times)
     ph = [1e3 * sum(p[k] for p in phases) / len(phases) for k in range(3)]
     # the bn* frame is the device frame read out: same samples, same pixels
     same = bool(torch.equal(out.cuda(), g.tonemap(acc, scene.spp)))
     h2d = host_vol.numel() * 4 + scene.tf.nbytes + (scene.env.texels.nbytes if scene.env is not None else 0)
-    line["e2e"] = {"value": world * samples / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                   "d2h_bytes_per_step": int(out.numel() * 4), "ms_per_step": 1e3 * e2e_dt,
-                   "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers",
-                   "frame_identical_to_device_frame": same,
-                   "phases_ms": {"upload_and_build": ph[0], "render": ph[1], "read": ph[2]}}
-    if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
-    line["extras_s"] = time.perf_counter() - extras_t0
-    print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.barrier()
+    return {"dt": sum(e2e_times) / len(e2e_times), "h2d": int(h2d), "d2h": int(out.numel() * 4), "same": same,
+            "phases_ms": {"upload_and_build": ph[0], "render": ph[1], "read": ph[2]}}
 
 
 def profile_render_case(args):
