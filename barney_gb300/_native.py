@@ -27,7 +27,7 @@ _i3 = C.c_int * 3
 class GbvIsoSurface(C.Structure):
     """gbv_iso_surface: an iso-surface of the field with a matte material."""
     _fields_ = [("iso_value", C.c_float), ("d_ranges", C.c_void_p), ("color", C.c_float * 4),
-                ("opacity", C.c_float), ("instance", C.c_int)]
+                ("opacity", C.c_float), ("instance", C.c_int), ("user_id", C.c_int)]
 
 
 class GbvScene(C.Structure):
@@ -48,7 +48,8 @@ class GbvScene(C.Structure):
         ("multi_scatter", C.c_int), ("volume_multi_scatter", C.c_int), ("max_volume_bounces", C.c_int),
         ("brick_log2", _i3),
         ("nanovdb", C.c_void_p),
-        ("iso", C.c_void_p), ("volume_instance", C.c_int),
+        ("iso", C.c_void_p), ("volume_instance", C.c_int), ("volume_user_id", C.c_int),
+        ("d_depth", C.c_void_p), ("d_prim_id", C.c_void_p), ("d_inst_id", C.c_void_p), ("d_obj_id", C.c_void_p),
     ]
 
 

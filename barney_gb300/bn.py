@@ -25,6 +25,8 @@ BN_UFIXED8_RGBA = 301
 BN_UFIXED8_RGBA_SRGB = 302
 BN_UFIXED16 = 303
 BN_FB_COLOR = 1
+BN_FB_DEPTH, BN_FB_PRIMID, BN_FB_INSTID, BN_FB_OBJID = 2, 4, 8, 16
+BN_INT32, BN_FLOAT = 140, 180
 BN_TEXTURE_NEAREST, BN_TEXTURE_LINEAR = 0, 1
 
 BN_SYMBOLS = [
@@ -137,7 +139,7 @@ class BarneySession:
     def build_scene(self, scene: Scene, scalars_ptr: int, voxel_format: int = N.GBV_VOXEL_F32,
                     layout: int = N.GBV_LAYOUT_BRICK_CORNERS, color_format: int = BN_FLOAT4, brick=None,
                     texel_format: int = BN_FLOAT32, frame_stats: bool = False, anari: Optional[str] = None,
-                    nanovdb: Optional[bytes] = None):
+                    nanovdb: Optional[bytes] = None, channels: int = BN_FB_COLOR):
         """anari: None (bn* calls as an app makes them), "vec4" or
         "vec3+opacity": the field and the transfer function made through the
         ANARI parameter translation (include/gbv_anari.h) from the
@@ -191,6 +193,7 @@ class BarneySession:
             geom = _ok(L.bnGeometryCreate(ctx, 0, b"iso_surface"), "bnGeometryCreate")
             L.bnSetObject(geom, b"scalarField", sf)
             L.bnSet1f(geom, b"isoValue", float(s.iso.value))
+            L.bnSet1i(geom, b"userID", int(s.iso.user_id))
             L.bnSetObject(geom, b"material", mat)
             L.bnCommit(geom)
         vol = _ok(L.bnVolumeCreate(ctx, 0, sf), "bnVolumeCreate")
@@ -212,6 +215,8 @@ class BarneySession:
                     "gbv_anari_transfer_function_1d")
         L.bnSet1f(vol, b"anisotropy", s.anisotropy)
         L.bnSet1f(vol, b"scatteringAlbedo", s.scattering_albedo)
+        if anari is None:
+            L.bnSet1i(vol, b"userID", int(getattr(s, "volume_user_id", 0)))
         L.bnCommit(vol)
         lights = []
         for d, c, rad in s.dir_lights:
@@ -279,7 +284,7 @@ class BarneySession:
         L.bnSet1i(r, b"maxVolumeBounces", s.max_volume_bounces)
         L.bnCommit(r)
         fb = _ok(L.bnFrameBufferCreate(ctx, 0), "bnFrameBufferCreate")
-        L.bnFrameBufferResize(fb, color_format, s.width, s.height, BN_FB_COLOR)
+        L.bnFrameBufferResize(fb, color_format, s.width, s.height, BN_FB_COLOR | channels)
         self.handles = dict(td=td, sf=sf, vol=vol, grp=grp, grp2=grp2, geom=geom, mat=mat, model=model, cam=cam,
                             renderer=r, fb=fb)
         self.handles = {k: v for k, v in self.handles.items() if v is not None}
@@ -298,6 +303,16 @@ class BarneySession:
                    else np.empty((s.height, s.width), np.uint32))
         ptr = out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()
         self.L.bnFrameBufferRead(self.handles["fb"], BN_FB_COLOR, C.c_void_p(ptr), self.color_format)
+        return out
+
+    def read_channel(self, channel: int) -> np.ndarray:
+        """An aux channel the frame buffer was resized with: BN_FB_DEPTH as
+        float32, BN_FB_PRIMID/INSTID/OBJID as int32, (H, W)."""
+        s = self.scene
+        depth = channel == BN_FB_DEPTH
+        out = np.empty((s.height, s.width), np.float32 if depth else np.int32)
+        self.L.bnFrameBufferRead(self.handles["fb"], channel, C.c_void_p(out.ctypes.data),
+                                 BN_FLOAT if depth else BN_INT32)
         return out
 
     def stats(self):

@@ -328,7 +328,7 @@ struct Volume : Object {  // volume/Volume.{h,cpp}, TransferFunction
   bool tfDirty = true;
   DevBuf<float> tf;
   DevBuf<float> majorants;
-  int userID = 0;  // Volume::set1i("userID"); used by hit-ID channels, which this path has none of
+  int userID = 0;  // Volume::set1i("userID"): the object ID of its hits (BN_FB_OBJID)
   bool set1f(const std::string &m, float v) override {
     if (m == "anisotropy") { anisotropy = v; return true; }
     if (m == "scatteringAlbedo") { scatteringAlbedo = v; return true; }
@@ -459,7 +459,7 @@ struct IsoSurfaceGeom : Object {
   std::shared_ptr<Field> sf;
   std::shared_ptr<Material> material;
   float isoValue = NAN;  // IsoSurface.h:79
-  int userID = 0;        // used by hit-ID channels, which this path has none of
+  int userID = 0;        // the object ID of its hits (BN_FB_OBJID)
   bool set1f(const std::string &m, float v) override {
     if (m == "isoValue") { isoValue = v; return true; }
     return false;
@@ -574,8 +574,13 @@ struct FrameBuffer : Object {  // fb/FrameBuffer, LocalFB
   int W = 0, H = 0;
   int colorFormat = BN_FLOAT4;
   int accumID = 0;
+  uint32_t channels = BN_FB_COLOR;  // the resize's requiredChannels
   DevBuf<float> accum;
   DevBuf<unsigned char> color;
+  // the aux channels (TiledFB's auxTiles, fb/TiledFB.cu:276-290), allocated
+  // when the resize asks for them
+  DevBuf<float> depth;
+  DevBuf<int> primId, instId, objId;
   DevBuf<unsigned long long> counters;
   unsigned long long lastStats[4] = {0, 0, 0, 0};
 };
@@ -963,7 +968,7 @@ void bnAccumReset(BNFrameBuffer fb) {
   if (f) f->accumID = 0;
 }
 
-void bnFrameBufferResize(BNFrameBuffer fb, BNDataType colorFormat, int sx, int sy, uint32_t) {
+void bnFrameBufferResize(BNFrameBuffer fb, BNDataType colorFormat, int sx, int sy, uint32_t requiredChannels) {
   auto f = as<FrameBuffer>(lookup(fb));
   if (!f) return fail("bnFrameBufferResize: unknown frame buffer");
   if (fbFormat(colorFormat) < 0) return fail("bnFrameBufferResize: unsupported color format");
@@ -972,9 +977,15 @@ void bnFrameBufferResize(BNFrameBuffer fb, BNDataType colorFormat, int sx, int s
   f->H = sy;
   f->colorFormat = colorFormat;
   f->accumID = 0;
+  f->channels = requiredChannels | BN_FB_COLOR;
   cudaSetDevice(f->ctx->device);
-  if (!f->accum.alloc((size_t)4 * sx * sy, f->ctx->mem)) return;
-  f->color.alloc((size_t)16 * sx * sy, f->ctx->mem);
+  const size_t n = (size_t)sx * sy;
+  if (!f->accum.alloc(4 * n, f->ctx->mem)) return;
+  if (!f->color.alloc(16 * n, f->ctx->mem)) return;
+  if ((f->channels & BN_FB_DEPTH) && !f->depth.alloc(n, f->ctx->mem)) return;
+  if ((f->channels & BN_FB_PRIMID) && !f->primId.alloc(n, f->ctx->mem)) return;
+  if ((f->channels & BN_FB_INSTID) && !f->instId.alloc(n, f->ctx->mem)) return;
+  if ((f->channels & BN_FB_OBJID) && !f->objId.alloc(n, f->ctx->mem)) return;
 }
 
 void bnFrameBufferGetSize(BNFrameBuffer fb, int *sx, int *sy) {
@@ -1048,6 +1059,7 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
     for (int a = 0; a < 4; a++) isoRec.color[a] = iso->material->live.color[a];
     isoRec.opacity = iso->material->live.opacity;
     isoRec.instance = isoInst;
+    isoRec.user_id = iso->userID;
   }
   if (env && !env->buildEnv(c->stream)) return;
   if (dirs.size() > 4) return fail("at most 4 directional lights are supported");
@@ -1061,6 +1073,12 @@ void bnRender(BNRenderer renderer, BNModel model, BNCamera camera, BNFrameBuffer
   }
   if (iso) s.iso = &isoRec;
   s.volume_instance = vol ? volInst : 0;
+  s.volume_user_id = vol ? vol->userID : 0;
+  // the aux channels the frame buffer holds
+  if (f->channels & BN_FB_DEPTH) s.d_depth = f->depth.p;
+  if (f->channels & BN_FB_PRIMID) s.d_prim_id = f->primId.p;
+  if (f->channels & BN_FB_INSTID) s.d_inst_id = f->instId.p;
+  if (f->channels & BN_FB_OBJID) s.d_obj_id = f->objId.p;
   if (vol) {
     s.d_majorants = vol->majorants.p;
     s.d_tf = vol->tf.p;
@@ -1129,12 +1147,33 @@ void bnFrameBufferRead(BNFrameBuffer fb, BNFrameBufferChannel channel, void *dst
   Context *c = nullptr;
   auto f = as<FrameBuffer>(lookup(fb, &c));
   if (!f) return fail("bnFrameBufferRead: unknown frame buffer");
-  if (channel != BN_FB_COLOR) return fail("bnFrameBufferRead: only the color channel is supported");
-  if (requiredFormat != f->colorFormat) return fail("bnFrameBufferRead: format differs from the resize format");
   if (f->accumID == 0) return fail("bnFrameBufferRead: nothing rendered since the last reset");
-  size_t bytes = (size_t)f->W * f->H * (f->colorFormat == BN_FLOAT4 ? 16 : 4);
+  const size_t n = (size_t)f->W * f->H;
+  const void *src = nullptr;
+  size_t bytes = 0;
+  if (channel == BN_FB_COLOR) {
+    if (requiredFormat != f->colorFormat) return fail("bnFrameBufferRead: format differs from the resize format");
+    src = f->color.p;
+    bytes = n * (f->colorFormat == BN_FLOAT4 ? 16 : 4);
+  } else if (channel == BN_FB_DEPTH || channel == BN_FB_PRIMID || channel == BN_FB_INSTID ||
+             channel == BN_FB_OBJID) {
+    // FrameBuffer::read (fb/FrameBuffer.cu:310-360): depth as BN_FLOAT, the
+    // IDs as 32-bit integers
+    if (!(f->channels & channel)) return fail("bnFrameBufferRead: channel not requested at the resize");
+    const bool isDepth = channel == BN_FB_DEPTH;
+    if (isDepth ? requiredFormat != BN_FLOAT
+                : (requiredFormat != BN_INT32 && requiredFormat != BN_UINT32))
+      return fail("bnFrameBufferRead: depth reads as BN_FLOAT, IDs as BN_INT32 or BN_UINT32");
+    src = isDepth ? (const void *)f->depth.p
+          : channel == BN_FB_PRIMID ? (const void *)f->primId.p
+          : channel == BN_FB_INSTID ? (const void *)f->instId.p
+                                    : (const void *)f->objId.p;
+    bytes = n * 4;
+  } else {
+    return fail("bnFrameBufferRead: the normal channel is not supported");
+  }
   cudaSetDevice(c->device);
-  if (cudaMemcpyAsync(dst, f->color.p, bytes, cudaMemcpyDefault, c->stream) != cudaSuccess ||
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)
     fail("bnFrameBufferRead: copy failed");
 }

@@ -134,6 +134,13 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
   p.isoRanges = nullptr;
   p.isoAlbedo = vec3(0.f);
   p.isoHash = 0;
+  p.depth = s->d_depth;
+  p.primId = s->d_prim_id;
+  p.instId = s->d_inst_id;
+  p.objId = s->d_obj_id;
+  p.volInst = s->volume_instance;
+  p.volUser = s->volume_user_id;
+  p.isoInst = p.isoUser = -1;
   if (p.isoOn) {
     const gbv_iso_surface &iso = *s->iso;
     if (!iso.d_ranges) return set_error(GBV_ERROR_INVALID_ARGUMENT, "iso-surface without macrocell ranges");
@@ -142,6 +149,8 @@ static gbv_status fill_params(const gbv_scene *s, RenderParams &p) {
                        "iso-surface instance must be >= 0 and differ from the volume's");
     p.isoFirst = !p.hasVolume || iso.instance < s->volume_instance;
     p.isoHash = fnv_hash3((uint32_t)iso.instance, 0, 0);
+    p.isoInst = iso.instance;
+    p.isoUser = iso.user_id;
     p.isoValue = iso.iso_value;
     p.isoRanges = reinterpret_cast<const float2 *>(iso.d_ranges);
     // MCAccelerator.h:476-479: delta = |bounds size| * .1 / (Mx + My + Mz)
@@ -235,6 +244,10 @@ static gbv_status render_frame(const char *fn, const gbv_scene *s, float *d_accu
   }
   if (s->iso && lc.mode == GBV_RENDER_WAVEFRONT) {
     snprintf(msg, sizeof msg, "%s: the wavefront mode renders volume-only worlds", fn);
+    return set_error(GBV_ERROR_UNSUPPORTED, msg);
+  }
+  if ((s->d_depth || s->d_prim_id || s->d_inst_id || s->d_obj_id) && lc.mode == GBV_RENDER_WAVEFRONT) {
+    snprintf(msg, sizeof msg, "%s: the wavefront mode writes no auxiliary channels", fn);
     return set_error(GBV_ERROR_UNSUPPORTED, msg);
   }
   if (spp == 0) return GBV_OK;
@@ -425,6 +438,8 @@ extern "C" gbv_status gbv_batch_create(const gbv_scene *scenes, float *const *d_
     if (s->format != scenes[0].format || s->layout != scenes[0].layout)
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: items must share voxel format and layout");
     if (s->iso) return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: batches render volume-only worlds");
+    if (s->d_depth || s->d_prim_id || s->d_inst_id || s->d_obj_id)
+      return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: batches write no auxiliary channels");
     if (s->layout == GBV_LAYOUT_LINEAR && s->format != GBV_VOXEL_F32)
       return set_error(GBV_ERROR_UNSUPPORTED, "gbv_batch_create: the linear layout holds FP32 voxels only");
     if (s->format == GBV_VOXEL_U8_SCALED && !s->d_scale_offset)

@@ -81,6 +81,11 @@ struct RenderParams {
   const float2 *isoRanges;
   vec3 isoAlbedo;
   uint64_t isoHash;
+  // auxiliary channels (gbv_scene.d_depth, ...; null: not written) and the
+  // hit IDs they take
+  float *depth;
+  int *primId, *instId, *objId;
+  int volInst, isoInst, volUser, isoUser;
 };
 
 // The reference frame buffer's tiles (TiledFB tileSize) and their
@@ -1154,6 +1159,22 @@ static __device__ __noinline__ bool iso_trace(const RenderParams &p, vec3 org, v
   return true;
 }
 
+// The auxiliary channels of pixel px from its primary ray (shadeRays.cu:
+// 1003-1023): pass 0 writes the depth (the ray's tMax: the closest hit's t,
+// or the generated 1e30 on a miss) and the closest hit's IDs (primitive 0 of
+// the user geometry, its instance index and userID; -1 on a miss); later
+// passes keep the smaller depth.  The lane owns the pixel: no atomics.
+static __device__ __noinline__ void write_aux(const RenderParams &p, size_t px, int accumID, float z, int hitKind) {
+  if (accumID == 0) {
+    if (p.depth) p.depth[px] = z;
+    if (p.primId) p.primId[px] = hitKind ? 0 : -1;
+    if (p.instId) p.instId[px] = hitKind == 1 ? p.volInst : hitKind == 2 ? p.isoInst : -1;
+    if (p.objId) p.objId[px] = hitKind == 1 ? p.volUser : hitKind == 2 ? p.isoUser : -1;
+  } else if (p.depth && z < p.depth[px]) {
+    p.depth[px] = z;
+  }
+}
+
 // -------------------------------------------------------------------------
 // The persistent frame kernel.  Each lane owns one pixel for all of the
 // launch's passes, so fragments accumulate in the reference's order
@@ -1448,6 +1469,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks)
         if (!anyHit) accum_add(acc, vmin(sray.misWeight * from_half(sray.tp), vec3(clampMax)));
         shadowPending = false;
       } else {
+        if (!Batch && gen == 0 && (p.depth || p.primId || p.instId || p.objId))
+          write_aux(p, (size_t)iy * p.W + ix, accumID, !anyHit ? ray.tMax : h.hit ? h.t : sT,
+                    !anyHit ? 0 : h.hit ? 1 : 2);
         vec3 frag(0.f);
         float alpha = 0.f;
         if (!anyHit) {

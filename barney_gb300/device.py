@@ -156,6 +156,7 @@ class GpuScene:
         r.volume_multi_scatter = s.volume_multi_scatter
         r.max_volume_bounces = s.max_volume_bounces
         r.volume_instance = s.volume_instance
+        r.volume_user_id = getattr(s, "volume_user_id", 0)
         if s.iso is not None:
             iso = N.GbvIsoSurface()
             iso.iso_value = s.iso.value
@@ -163,6 +164,7 @@ class GpuScene:
             iso.color[:] = [float(c) for c in s.iso.color]
             iso.opacity = s.iso.opacity
             iso.instance = s.iso.instance
+            iso.user_id = s.iso.user_id
             self._iso_record = iso  # kept alive with the scene record's pointer to it
             r.iso = C.addressof(iso)
             if s.no_volume:
@@ -176,14 +178,22 @@ class GpuScene:
                            device="cuda")
 
     def render(self, spp: Optional[int] = None, accum=None, accum_id_start: int = 0, counters=None,
-               width: Optional[int] = None, height: Optional[int] = None, config: Optional[dict] = None):
+               width: Optional[int] = None, height: Optional[int] = None, config: Optional[dict] = None,
+               aux: Optional[dict] = None):
         """Accumulates `spp` passes into accum (H, W, 4); returns accum.
         config: launch settings of gbv_render_ex (blocks_per_sm,
-        threshold_pct, skip_cells, stage, profile); None = defaults."""
+        threshold_pct, skip_cells, stage, profile); None = defaults.
+        aux: auxiliary channels to write, CUDA tensors of (H, W) entries
+        under "depth" (float32), "prim_id", "inst_id", "obj_id" (int32)."""
         w, h = width or self.s.width, height or self.s.height
         if accum is None:
             accum = self.new_accum(w, h)
         rec = self.record()
+        if aux:
+            for f, k in (("d_depth", "depth"), ("d_prim_id", "prim_id"), ("d_inst_id", "inst_id"),
+                         ("d_obj_id", "obj_id")):
+                t = aux.get(k)
+                setattr(rec, f, t.data_ptr() if t is not None else None)
         n = self.s.spp if spp is None else spp
         if config is None:
             N.check(N.lib().gbv_render(C.byref(rec), _ptr(accum), w, h, accum_id_start, n, _ptr(counters),

@@ -48,6 +48,7 @@ class IsoSurface:
     color: tuple = (0.8, 0.8, 0.8, 1.0)  # AnariMatte default color (AnariMatte.h:43), alpha 1
     opacity: float = 1.0
     instance: int = 0
+    user_id: int = 0  # the geometry's "userID": the object ID of its hits
 
 
 @dataclass
@@ -80,6 +81,7 @@ class Scene:
     # the iso-surface only
     iso: Optional[IsoSurface] = None
     volume_instance: int = 0
+    volume_user_id: int = 0  # the volume's "userID": the object ID of its hits
     no_volume: bool = False
 
     @property

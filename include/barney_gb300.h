@@ -100,12 +100,15 @@ typedef enum {
   BN_TEXTURE_3D,
   BN_UINT8 = 110,
   BN_UINT16 = 130,
+  BN_INT32 = 140,
+  BN_UINT32 = 150,
   BN_FLOAT32 = 180,
   BN_FLOAT32_VEC2,
   BN_FLOAT32_VEC3,
   BN_FLOAT32_VEC4,
   BN_FLOAT = BN_FLOAT32,
   BN_FLOAT4 = BN_FLOAT32_VEC4,
+  BN_INT = BN_INT32,
   BN_UFIXED8 = 300,
   BN_UFIXED8_RGBA,
   BN_UFIXED8_RGBA_SRGB,

@@ -206,6 +206,7 @@ typedef struct gbv_iso_surface {
   float color[4];         /* AnariMatte color, RGBA (a color set as 3 floats has alpha 1) */
   float opacity;          /* AnariMatte opacity */
   int instance;           /* RTC instance index of the geometry's group */
+  int user_id;            /* the geometry's "userID": objID of its hits */
 } gbv_iso_surface;
 
 typedef struct gbv_scene {
@@ -259,6 +260,19 @@ typedef struct gbv_scene {
      used either). */
   const gbv_iso_surface *iso;
   int volume_instance;   /* RTC instance index of the volume's group (0 without an iso-surface) */
+  int volume_user_id;    /* the volume's "userID": objID of its hits */
+  /* Auxiliary frame channels (device memory, width*height entries each, row
+     by row; 0 = not wanted), written from each pixel's primary ray as the
+     reference's shading step writes its aux tiles (barney/kernels/
+     shadeRays.cu:1003-1023, the hit IDs of MCAccelerator.h:552-565,
+     685-700): on pass 0 depth = the primary ray's tMax (its hit distance,
+     or 1e30 on a miss) and the closest hit's primitive (0), instance (its
+     RTC instance index) and object IDs (its userID), -1 on a miss; on
+     later passes depth = min(depth, tMax) and the IDs stay.  Persistent
+     mode only (gbv_render, gbv_render_ex, gbv_render_tiles,
+     gbv_render_noalloc). */
+  float *d_depth;
+  int *d_prim_id, *d_inst_id, *d_obj_id;
 } gbv_scene;
 
 /* Counters written by gbv_render when d_counters != 0 (uint64 each):

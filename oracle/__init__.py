@@ -38,7 +38,9 @@ class OrcScene(C.Structure):
         ("nanovdb", C.c_void_p), ("nanovdb_bytes", C.c_ulonglong),
         ("iso_enabled", C.c_int), ("iso_value", C.c_float), ("iso_color", C.c_float * 4),
         ("iso_opacity", C.c_float), ("iso_instance", C.c_int), ("volume_instance", C.c_int),
-        ("no_volume", C.c_int),
+        ("no_volume", C.c_int), ("volume_user_id", C.c_int), ("iso_user_id", C.c_int),
+        ("aux_depth", C.c_void_p), ("aux_prim_id", C.c_void_p), ("aux_inst_id", C.c_void_p),
+        ("aux_obj_id", C.c_void_p),
     ]
 
 
@@ -220,8 +222,10 @@ class Oracle:
             r.iso_color[:] = [float(c) for c in iso.color]
             r.iso_opacity = iso.opacity
             r.iso_instance = iso.instance
+            r.iso_user_id = getattr(iso, "user_id", 0)
             r.no_volume = 1 if scene.no_volume else 0
         r.volume_instance = getattr(scene, "volume_instance", 0)
+        r.volume_user_id = getattr(scene, "volume_user_id", 0)
         self.rec = r
 
     # -- macrocells --
@@ -295,7 +299,9 @@ class Oracle:
         return out
 
     # -- render --
-    def render(self, spp=None, accum=None, accum_id_start=0, use_double=False, nthreads=0, rows=None):
+    def render(self, spp=None, accum=None, accum_id_start=0, use_double=False, nthreads=0, rows=None, aux=None):
+        """aux: auxiliary channels to write, numpy arrays of (H, W) entries
+        under "depth" (float32), "prim_id", "inst_id", "obj_id" (int32)."""
         W, H = self.s.width, self.s.height
         if use_double and self.u8:
             raise ValueError("the U8 storage form is sampled in float only")
@@ -303,8 +309,17 @@ class Oracle:
             accum = np.zeros((H, W, 4), dtype=np.float32)
         st = OrcStats()
         r0, r1 = rows if rows is not None else (0, 0)
+        aux = aux or {}
+        for f, k, dt in (("aux_depth", "depth", np.float32), ("aux_prim_id", "prim_id", np.int32),
+                         ("aux_inst_id", "inst_id", np.int32), ("aux_obj_id", "obj_id", np.int32)):
+            a = aux.get(k)
+            if a is not None:
+                assert a.dtype == dt and a.flags.c_contiguous and a.size == W * H, k
+            setattr(self.rec, f, a.ctypes.data if a is not None else None)
         lib().orc_render(C.byref(self.rec), _p(accum), accum_id_start, self.s.spp if spp is None else spp,
                          1 if use_double else 0, nthreads, r0, r1, C.byref(st))
+        for f in ("aux_depth", "aux_prim_id", "aux_inst_id", "aux_obj_id"):
+            setattr(self.rec, f, None)
         self.stats = dict(density_samples=st.density_samples, mc_visits=st.mc_visits, rays=st.rays)
         return accum
 

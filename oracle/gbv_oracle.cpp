@@ -897,6 +897,11 @@ struct Scene {
   // RTC instance hashes of the volume and the iso-surface (hash(instance,
   // 0, 0), MCAccelerator.h:389-392 and :614-615)
   uint64_t volHash = 0, isoHash = 0;
+  // hit IDs (instance index and userID of the volume and the iso-surface)
+  // and the auxiliary channels to write (orc_scene.aux_*)
+  int volInst = 0, isoInst = -1, volUser = 0, isoUser = -1;
+  float *auxDepth = nullptr;
+  int *auxPrim = nullptr, *auxInst = nullptr, *auxObj = nullptr;
   // iso-surface geometry with its AnariMatte material
   bool iso = false, noVolume = false, isoFirst = false;
   float isoValue = 0.f, isoAlpha = 1.f, isoDelta = 0.f;
@@ -940,7 +945,15 @@ inline void build_scene(const orc_scene *s, Scene &S) {
     S.maj = S.majorants_own.data();
   }
   S.volHash = fnv_hash3((uint32_t)s->volume_instance, 0, 0);
+  S.volInst = s->volume_instance;
+  S.volUser = s->volume_user_id;
+  S.auxDepth = s->aux_depth;
+  S.auxPrim = s->aux_prim_id;
+  S.auxInst = s->aux_inst_id;
+  S.auxObj = s->aux_obj_id;
   if (s->iso_enabled) {
+    S.isoInst = s->iso_instance;
+    S.isoUser = s->iso_user_id;
     S.iso = true;
     S.noVolume = s->no_volume != 0;
     S.isoFirst = S.noVolume || s->iso_instance < s->volume_instance;
@@ -1908,6 +1921,20 @@ template <typename R> inline void render_pixel(const Scene &S, int ix, int iy, i
     if (rayAlive) {
       trace_and_record<R>(S, ray, cnt);
       float alpha = (gen == 0) ? (ray.hit ? 1.f : ray.missColor.w) : 0.f;
+      if (gen == 0) {
+        // the aux tiles (shadeRays.cu:923, 1003-1023): incomingZ = ray.tMax;
+        // the closest hit's IDs, primID 0 of the one-primitive user geometry
+        const size_t px = (size_t)iy * S.W + ix;
+        const float z = ray.tMax;
+        if (accumID == 0) {
+          if (S.auxDepth) S.auxDepth[px] = z;
+          if (S.auxPrim) S.auxPrim[px] = ray.hit ? 0 : -1;
+          if (S.auxInst) S.auxInst[px] = !ray.hit ? -1 : ray.surf ? S.isoInst : S.volInst;
+          if (S.auxObj) S.auxObj[px] = !ray.hit ? -1 : ray.surf ? S.isoUser : S.volUser;
+        } else if (S.auxDepth && z < S.auxDepth[px]) {
+          S.auxDepth[px] = z;
+        }
+      }
       V3<float> frag = bounce(S, ray, state, nsray, nsstate, nsValid, gen);
       frag = vmin(frag, V3<float>(clampMax));
       if (accumID == 0 && gen == 0) {

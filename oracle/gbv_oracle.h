@@ -96,6 +96,14 @@ typedef struct orc_scene {
   int   iso_instance;
   int   volume_instance;
   int   no_volume;           /* 1: the world holds the iso-surface only */
+  /* the geometries' "userID" (the object ID of their hits) and auxiliary
+     frame channels (host memory, width*height each, or 0): the reference's
+     aux tiles written at a pixel's primary-ray shading (shadeRays.cu:
+     1003-1023) from its closest hit's IDs (MCAccelerator.h:552-565,
+     685-700) */
+  int   volume_user_id, iso_user_id;
+  float *aux_depth;
+  int   *aux_prim_id, *aux_inst_id, *aux_obj_id;
 } orc_scene;
 
 typedef struct orc_stats {
