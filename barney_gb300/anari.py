@@ -14,6 +14,9 @@ import numpy as np
 from . import _native as N
 
 GBV_ANARI_FLOAT32, GBV_ANARI_UFIXED8, GBV_ANARI_UINT8 = 0, 1, 2
+# frame channel element types
+(GBV_ANARI_UNKNOWN, GBV_ANARI_UFIXED8_VEC4, GBV_ANARI_UFIXED8_RGBA_SRGB, GBV_ANARI_FLOAT32_VEC3,
+ GBV_ANARI_FLOAT32_VEC4, GBV_ANARI_UINT32) = -1, 10, 11, 12, 13, 14
 
 _ready = False
 
@@ -29,6 +32,9 @@ def lib() -> C.CDLL:
             "gbv_anari_tf1d_rgba_map": (i, [vp, i, ll, vp, ll, vp, f, vp, C.POINTER(ll)]),
             "gbv_anari_density_scale": (f, [f]),
             "gbv_anari_transfer_function_1d": (i, [vp, vp, i, ll, vp, ll, vp, f, vp, f, i]),
+            "gbv_anari_frame_color_format": (i, [i]),
+            "gbv_anari_frame_channels": (C.c_uint32, [i, i, i, i, i]),
+            "gbv_anari_frame_resize": (i, [vp, i, i, i, i, i, i, i, i]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -72,3 +78,15 @@ def structured_regular_bounds(dims, origin=None, spacing=None):
     N.check(lib().gbv_anari_structured_regular_bounds(_p(np.asarray(dims, np.int32)), _p(o), _p(s), _p(lo),
                                                       _p(hi)), "gbv_anari_structured_regular_bounds")
     return lo, hi
+
+
+def frame_color_format(color_type: int) -> int:
+    """The bn color format of an ANARI "channel.color" type (toBarney)."""
+    return int(lib().gbv_anari_frame_color_format(color_type))
+
+
+def frame_channels(depth=GBV_ANARI_UNKNOWN, primitive_id=GBV_ANARI_UNKNOWN, object_id=GBV_ANARI_UNKNOWN,
+                   instance_id=GBV_ANARI_UNKNOWN, normal=GBV_ANARI_UNKNOWN) -> int:
+    """Frame::finalize's requiredChannels for the frame's channel types."""
+    return int(lib().gbv_anari_frame_channels(depth, primitive_id, object_id, instance_id, normal))
+

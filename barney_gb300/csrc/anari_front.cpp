@@ -128,4 +128,42 @@ gbv_status gbv_anari_transfer_function_1d(BNVolume volume, const float *color, i
   return GBV_OK;
 }
 
+BNDataType gbv_anari_frame_color_format(int color_type) {
+  switch (color_type) {
+    case GBV_ANARI_UFIXED8_VEC4: return BN_UFIXED8_RGBA;
+    case GBV_ANARI_UFIXED8_RGBA_SRGB: return BN_UFIXED8_RGBA_SRGB;
+    case GBV_ANARI_FLOAT32: return BN_FLOAT;
+    case GBV_ANARI_FLOAT32_VEC3: return BN_FLOAT32_VEC3;
+    case GBV_ANARI_FLOAT32_VEC4: return BN_FLOAT4;
+  }
+  return BN_DATA_UNDEFINED;
+}
+
+uint32_t gbv_anari_frame_channels(int depth_type, int primitive_id_type, int object_id_type, int instance_id_type,
+                                  int normal_type) {
+  uint32_t c = BN_FB_COLOR;
+  if (depth_type == GBV_ANARI_FLOAT32) c |= BN_FB_DEPTH;
+  if (primitive_id_type == GBV_ANARI_UINT32) c |= BN_FB_PRIMID;
+  if (object_id_type == GBV_ANARI_UINT32) c |= BN_FB_OBJID;
+  if (instance_id_type == GBV_ANARI_UINT32) c |= BN_FB_INSTID;
+  if (normal_type == GBV_ANARI_FLOAT32_VEC3) c |= BN_FB_NORMAL;
+  return c;
+}
+
+gbv_status gbv_anari_frame_resize(BNFrameBuffer fb, int color_type, int depth_type, int primitive_id_type,
+                                  int object_id_type, int instance_id_type, int normal_type, int width,
+                                  int height) {
+  if (!fb) return set_error(GBV_ERROR_INVALID_ARGUMENT, "anari frame: null frame buffer");
+  if (width <= 0 || height <= 0) return set_error(GBV_ERROR_INVALID_ARGUMENT, "anari frame: empty size");
+  const BNDataType fmt = gbv_anari_frame_color_format(color_type);
+  if (fmt != BN_FLOAT4 && fmt != BN_UFIXED8_RGBA && fmt != BN_UFIXED8_RGBA_SRGB)
+    return set_error(GBV_ERROR_UNSUPPORTED, "anari frame: color channel type other than UFIXED8_VEC4, "
+                                            "UFIXED8_RGBA_SRGB or FLOAT32_VEC4");
+  const uint32_t channels =
+      gbv_anari_frame_channels(depth_type, primitive_id_type, object_id_type, instance_id_type, normal_type);
+  if (channels & BN_FB_NORMAL) return set_error(GBV_ERROR_UNSUPPORTED, "anari frame: no normal channel on this path");
+  bnFrameBufferResize(fb, fmt, width, height, channels);
+  return GBV_OK;
+}
+
 }  // extern "C"

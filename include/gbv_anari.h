@@ -67,6 +67,42 @@ gbv_status gbv_anari_transfer_function_1d(BNVolume volume, const float *color, i
                                           const float uniform_color[4], float opacity_param,
                                           const float value_range[2], float unit_distance, int user_id);
 
+/* Element types of an ANARI frame's channels ("channel.color",
+   "channel.depth", "channel.primitiveId", "channel.objectId",
+   "channel.instanceId", "channel.normal"); GBV_ANARI_UNKNOWN: the channel
+   is not set. */
+enum {
+  GBV_ANARI_UNKNOWN = -1,
+  GBV_ANARI_UFIXED8_VEC4 = 10,
+  GBV_ANARI_UFIXED8_RGBA_SRGB = 11,
+  GBV_ANARI_FLOAT32_VEC3 = 12,
+  GBV_ANARI_FLOAT32_VEC4 = 13,
+  GBV_ANARI_UINT32 = 14
+};
+
+/* toBarney (anari/Frame.cpp:20-35): the bn color format of a "channel.color"
+   type -- UFIXED8_VEC4 -> BN_UFIXED8_RGBA, UFIXED8_RGBA_SRGB ->
+   BN_UFIXED8_RGBA_SRGB, FLOAT32 -> BN_FLOAT, FLOAT32_VEC3 -> BN_FLOAT3,
+   FLOAT32_VEC4 -> BN_FLOAT4, anything else BN_DATA_UNDEFINED. */
+BNDataType gbv_anari_frame_color_format(int color_type);
+
+/* Frame::finalize's requiredChannels (anari/Frame.cpp:108-120): BN_FB_COLOR,
+   plus BN_FB_DEPTH for a FLOAT32 depth channel, BN_FB_PRIMID, BN_FB_OBJID,
+   BN_FB_INSTID for UINT32 ID channels, BN_FB_NORMAL for a FLOAT32_VEC3
+   normal channel. */
+uint32_t gbv_anari_frame_channels(int depth_type, int primitive_id_type, int object_id_type, int instance_id_type,
+                                  int normal_type);
+
+/* Frame::finalize (anari/Frame.cpp:86-140) on the frame buffer: resize to
+   width x height with the color format and channels above.  The frame's
+   channels are then read as the reference's Frame::map reads them
+   (anari/Frame.cpp:232-300): bnFrameBufferRead(fb, BN_FB_COLOR, ..., the
+   color format), BN_FB_DEPTH as BN_FLOAT, the IDs as BN_INT32.  This path
+   renders no normal channel: a FLOAT32_VEC3 normal channel is refused. */
+gbv_status gbv_anari_frame_resize(BNFrameBuffer fb, int color_type, int depth_type, int primitive_id_type,
+                                  int object_id_type, int instance_id_type, int normal_type, int width,
+                                  int height);
+
 #ifdef __cplusplus
 }
 #endif

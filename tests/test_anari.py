@@ -99,3 +99,31 @@ def test_rejected_inputs():
     assert L.gbv_anari_structured_regular(C.c_void_p(16), 0, 0, None, N.ivec(4, 4, 4), None, None,
                                           C.byref(h)) == N.GBV_ERROR_INVALID_ARGUMENT
     assert "missing required parameter 'data'" in N.lib().gbv_last_error().decode()
+
+
+# ---- the frame (anari/Frame.cpp) ---------------------------------------------
+
+def test_frame_color_format_is_to_barney():
+    from barney_gb300 import anari as A
+    from barney_gb300 import bn
+    assert A.frame_color_format(A.GBV_ANARI_UFIXED8_VEC4) == bn.BN_UFIXED8_RGBA
+    assert A.frame_color_format(A.GBV_ANARI_UFIXED8_RGBA_SRGB) == bn.BN_UFIXED8_RGBA_SRGB
+    assert A.frame_color_format(A.GBV_ANARI_FLOAT32) == bn.BN_FLOAT32
+    assert A.frame_color_format(A.GBV_ANARI_FLOAT32_VEC3) == bn.BN_FLOAT32 + 2
+    assert A.frame_color_format(A.GBV_ANARI_FLOAT32_VEC4) == bn.BN_FLOAT4
+    assert A.frame_color_format(A.GBV_ANARI_UINT32) == 0 and A.frame_color_format(A.GBV_ANARI_UNKNOWN) == 0
+
+
+def test_frame_required_channels():
+    """Frame::finalize: color always; depth for a FLOAT32 depth channel, the
+    IDs for UINT32 ones, the normal for FLOAT32_VEC3; other types add
+    nothing."""
+    from barney_gb300 import anari as A
+    from barney_gb300 import bn
+    assert A.frame_channels() == bn.BN_FB_COLOR
+    assert A.frame_channels(depth=A.GBV_ANARI_FLOAT32) == bn.BN_FB_COLOR | bn.BN_FB_DEPTH
+    assert A.frame_channels(depth=A.GBV_ANARI_UINT32, primitive_id=A.GBV_ANARI_FLOAT32) == bn.BN_FB_COLOR
+    all_ids = A.frame_channels(primitive_id=A.GBV_ANARI_UINT32, object_id=A.GBV_ANARI_UINT32,
+                               instance_id=A.GBV_ANARI_UINT32)
+    assert all_ids == bn.BN_FB_COLOR | bn.BN_FB_PRIMID | bn.BN_FB_OBJID | bn.BN_FB_INSTID
+    assert A.frame_channels(normal=A.GBV_ANARI_FLOAT32_VEC3) == bn.BN_FB_COLOR | 32

@@ -112,3 +112,38 @@ def test_bn_frame_buffer_channels():
     for k in got:
         np.testing.assert_array_equal(bits(got[k]), bits(ag[k].cpu().numpy()), err_msg=k)
     assert set(np.unique(got["obj_id"])) <= {-1, 21, 34} and (got["obj_id"] == 21).any()
+
+
+def test_anari_frame_resize_and_map():
+    """The ANARI frame's channel set-up (gbv_anari_frame_resize: sRGB color,
+    FLOAT32 depth, UINT32 object IDs) on a bn* frame buffer, then the
+    frame's maps: the color and the two channels asked for read back, the
+    instance-ID channel (not asked for) is refused, and a normal channel is
+    refused at the resize."""
+    from barney_gb300 import anari as A
+    from barney_gb300 import bn
+    s = scenes.small_scene(dims=32, spp=2, width=40, height=32)
+    s.volume_user_id = 9
+    vol = np.ascontiguousarray(s.scalars)
+    L = A.lib()
+    with bn.BarneySession() as ses:
+        assert ses.build_scene(s, vol.ctypes.data, color_format=bn.BN_UFIXED8_RGBA_SRGB) == ""
+        fb = ses.handles["fb"]
+        st = L.gbv_anari_frame_resize(fb, A.GBV_ANARI_UFIXED8_RGBA_SRGB, A.GBV_ANARI_FLOAT32, A.GBV_ANARI_UNKNOWN,
+                                      A.GBV_ANARI_UINT32, A.GBV_ANARI_UNKNOWN, A.GBV_ANARI_UNKNOWN, 40, 32)
+        assert st == 0
+        ses.render()
+        img = ses.read()
+        depth = ses.read_channel(bn.BN_FB_DEPTH)
+        obj = ses.read_channel(bn.BN_FB_OBJID)
+        assert bn.last_error() == ""
+        ses.read_channel(bn.BN_FB_INSTID)
+        assert "not requested" in bn.last_error()
+        st = L.gbv_anari_frame_resize(fb, A.GBV_ANARI_FLOAT32_VEC4, A.GBV_ANARI_UNKNOWN, A.GBV_ANARI_UNKNOWN,
+                                      A.GBV_ANARI_UNKNOWN, A.GBV_ANARI_UNKNOWN, A.GBV_ANARI_FLOAT32_VEC3, 40, 32)
+        assert st != 0
+    assert img.shape == (32, 40) and depth.shape == (32, 40)
+    hit = obj == 9
+    assert hit.any() and (obj[~hit] == -1).all() and (depth[hit] < 1e3).all()
+    # a pixel whose first pass missed keeps IDs -1; its depth is 1e30 unless a later pass hit
+    assert ((depth[~hit] == np.float32(1e30)) | (depth[~hit] < 1e3)).all()
