@@ -37,7 +37,8 @@ BN_SYMBOLS = [
     "bnSet1i", "bnSet2i", "bnSet3i", "bnSet4i", "bnSet1f", "bnSet2f", "bnSet3f", "bnSet4f", "bnSet4x3fv",
     "bnSetInstances", "bnBuild", "bnAccumReset", "bnFrameBufferResize", "bnFrameBufferRead",
     "bnFrameBufferGetSize", "bnRender", "bnGetLastError", "bnFrameBufferGetStats", "bnGeometryCreate",
-    "bnMaterialCreate",
+    "bnMaterialCreate", "bnDataSet", "bnTextureData2DCreate", "bnTexture3DCreate", "bnSamplerCreate",
+    "bnSet4x4fv", "bnUpdateInstanceTransforms", "bnSetInstanceAttributes",
 ]
 
 
@@ -91,6 +92,13 @@ def lib() -> C.CDLL:
             "bnGeometryCreate": (vp, [vp, i, cp]),
             "bnMaterialCreate": (vp, [vp, i, cp]),
             "bnSetString": (None, [vp, cp, cp]),
+            "bnDataSet": (None, [vp, C.c_size_t, vp]),
+            "bnTextureData2DCreate": (vp, [vp, i, i, i, i, vp]),
+            "bnTexture3DCreate": (vp, [vp, i, i, C.c_uint32, C.c_uint32, C.c_uint32, vp, i, i]),
+            "bnSamplerCreate": (vp, [vp, i, cp]),
+            "bnSet4x4fv": (None, [vp, cp, vp]),
+            "bnUpdateInstanceTransforms": (None, [vp, i, vp, i]),
+            "bnSetInstanceAttributes": (None, [vp, i, cp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -141,9 +141,15 @@ template <typename T> static T *track(Context *ctx, std::shared_ptr<T> obj, cons
 // ---------------------------------------------------------------- objects --
 
 struct Data : Object {  // bnDataCreate: ObjectRefsData (BN_OBJECT) or PODData (BN_UINT8)
+  int type = BN_OBJECT;
   std::vector<SP> objects;
   std::vector<unsigned char> bytes;
 };
+
+// Objects this path makes but does not render with: image texture data, 3D
+// textures and samplers for material parameters (which the materials here
+// refuse), kept so that callers holding them work unchanged.
+struct Inert : Object {};
 
 struct TextureData3D : Object {  // common/Texture.cpp, cudaCommon/TextureData.cu
   int dims[3] = {0, 0, 0};
@@ -504,6 +510,7 @@ struct Group : Object {
 struct Model : Object {
   std::vector<std::shared_ptr<Group>> groups;
   std::vector<BNTransform> xfms;
+  std::map<std::string, SP> instanceAttributes;  // bnSetInstanceAttributes; not read by this path
 };
 
 struct Camera : Object {  // Camera.cu PerspectiveCamera
@@ -695,32 +702,62 @@ BNRenderer bnRendererCreate(BNContext ctx, const char *) {
   return (BNRenderer)track((Context *)ctx, std::make_shared<Renderer>(), "renderer");
 }
 
-BNData bnDataCreate(BNContext context, int, BNDataType dataType, size_t numItems, const void *items) {
-  Context *c = (Context *)context;
-  if (dataType == BN_UINT8) {  // a byte array (PODData), e.g. a NanoVDB grid
-    auto d = std::make_shared<Data>();
+// the contents of a data array of d->type from numItems items
+static bool fill_data(Context *c, Data *d, size_t numItems, const void *items) {
+  if (d->type == BN_UINT8) {
     if (numItems && !items) {
       fail("bnDataCreate: null data");
-      return nullptr;
+      return false;
     }
     const unsigned char *b = (const unsigned char *)items;
     d->bytes.assign(b, b + numItems);
-    return (BNData)track(c, d, "data");
+    return true;
   }
-  if (dataType != BN_OBJECT) {
+  std::vector<SP> objs;
+  const BNObject *handles = (const BNObject *)items;
+  for (size_t i = 0; i < numItems; i++) {
+    SP o = c->find(handles[i]);
+    if (!o) {
+      fail("data array references an unknown object");
+      return false;
+    }
+    objs.push_back(o);
+  }
+  d->objects = std::move(objs);
+  return true;
+}
+
+void bnDataSet(BNData data, size_t numItems, const void *items) {
+  Context *c = nullptr;
+  auto d = as<Data>(lookup(data, &c));
+  if (!d) return fail("bnDataSet: unknown data array");
+  fill_data(c, d.get(), numItems, items);
+}
+
+BNTextureData bnTextureData2DCreate(BNContext context, int, BNDataType, int, int, const void *) {
+  return (BNTextureData)track((Context *)context, std::make_shared<Inert>(), "textureData2D");
+}
+
+BNTexture3D bnTexture3DCreate(BNContext context, int, BNDataType, uint32_t, uint32_t, uint32_t, const void *,
+                              BNTextureFilterMode, BNTextureAddressMode) {
+  return (BNTexture3D)track((Context *)context, std::make_shared<Inert>(), "texture3D");
+}
+
+BNSampler bnSamplerCreate(BNContext context, int, const char *) {
+  return (BNSampler)track((Context *)context, std::make_shared<Inert>(), "sampler");
+}
+
+BNData bnDataCreate(BNContext context, int, BNDataType dataType, size_t numItems, const void *items) {
+  Context *c = (Context *)context;
+  // BN_UINT8: a byte array (PODData), e.g. a NanoVDB grid; BN_OBJECT: object
+  // references (ObjectRefsData)
+  if (dataType != BN_UINT8 && dataType != BN_OBJECT) {
     fail("only BN_OBJECT and BN_UINT8 data arrays are used by this path");
     return nullptr;
   }
   auto d = std::make_shared<Data>();
-  const BNObject *objs = (const BNObject *)items;
-  for (size_t i = 0; i < numItems; i++) {
-    SP o = c->find(objs[i]);
-    if (!o) {
-      fail("data array references an unknown object");
-      return nullptr;
-    }
-    d->objects.push_back(o);
-  }
+  d->type = dataType;
+  if (!fill_data(c, d.get(), numItems, items)) return nullptr;
   return (BNData)track(c, d, "data");
 }
 
@@ -931,6 +968,11 @@ void bnSet4x3fv(BNObject target, const char *paramName, const BNTransform *) {
   SP o = lookup(target, &c);
   if (o) c->warnOnce(o->kind + " ignores transform parameter '" + paramName + "'");
 }
+void bnSet4x4fv(BNObject target, const char *paramName, const bn_float4 *) {
+  Context *c = nullptr;
+  SP o = lookup(target, &c);
+  if (o) c->warnOnce(o->kind + " ignores 4x4 matrix parameter '" + paramName + "'");
+}
 
 void bnSetInstances(BNModel model, int, BNGroup *groups, BNTransform *xfms, int n) {
   Context *c = nullptr;
@@ -947,6 +989,21 @@ void bnSetInstances(BNModel model, int, BNGroup *groups, BNTransform *xfms, int 
     else { x.l.vx.x = 1; x.l.vy.y = 1; x.l.vz.z = 1; }
     m->xfms.push_back(x);
   }
+}
+
+void bnUpdateInstanceTransforms(BNModel model, int, BNTransform *xfms, int n) {
+  auto m = as<Model>(lookup(model));
+  if (!m) return fail("bnUpdateInstanceTransforms: unknown model");
+  if (n != (int)m->xfms.size() || (n > 0 && !xfms))
+    return fail("bnUpdateInstanceTransforms: the count differs from the instances bnSetInstances set");
+  for (int i = 0; i < n; i++) m->xfms[i] = xfms[i];
+}
+
+void bnSetInstanceAttributes(BNModel model, int, const char *attributeName, BNData data) {
+  Context *c = nullptr;
+  auto m = as<Model>(lookup(model, &c));
+  if (!m) return fail("bnSetInstanceAttributes: unknown model");
+  m->instanceAttributes[attributeName ? attributeName : ""] = data ? c->find(data) : SP();
 }
 
 void bnBuild(BNModel model, int) {

@@ -137,6 +137,19 @@ BARNEY_API BNData bnDataCreate(BNContext context, int whichSlot, BNDataType data
                                const void *items);
 BARNEY_API BNTextureData bnTextureData3DCreate(BNContext context, int whichSlot, BNDataType texelFormat,
                                                int width, int height, int depth, const void *items);
+/* barney.h:428: new contents for a data array (same element type) */
+BARNEY_API void bnDataSet(BNData data, size_t numItems, const void *items);
+/* barney.h:436, 476-488, 518: image textures and samplers for material
+   parameters.  This path renders constant material parameters only: the
+   objects are made (an ANARI device creates them for its samplers) and a
+   material that is given one refuses it with a recorded message. */
+BARNEY_API BNTextureData bnTextureData2DCreate(BNContext context, int whichSlot, BNDataType texelFormat,
+                                               int width, int height, const void *items);
+BARNEY_API BNTexture3D bnTexture3DCreate(BNContext context, int whichSlot, BNDataType texelFormat,
+                                         uint32_t size_x, uint32_t size_y, uint32_t size_z, const void *texels,
+                                         BNTextureFilterMode filterMode BN_IF_CPP(= BN_TEXTURE_LINEAR),
+                                         BNTextureAddressMode addressMode BN_IF_CPP(= BN_TEXTURE_CLAMP));
+BARNEY_API BNSampler bnSamplerCreate(BNContext context, int whichSlot, const char *type);
 BARNEY_API BNTexture2D bnTexture2DCreate(BNContext context, int whichSlot, BNDataType texelFormat,
                                          uint32_t size_x, uint32_t size_y, const void *texels,
                                          BNTextureFilterMode filterMode BN_IF_CPP(= BN_TEXTURE_LINEAR),
@@ -174,10 +187,18 @@ BARNEY_API void bnSet2f(BNObject target, const char *paramName, float x, float y
 BARNEY_API void bnSet3f(BNObject target, const char *paramName, float x, float y, float z);
 BARNEY_API void bnSet4f(BNObject target, const char *paramName, float x, float y, float z, float w);
 BARNEY_API void bnSet4x3fv(BNObject target, const char *paramName, const BNTransform *affineMatrix);
+BARNEY_API void bnSet4x4fv(BNObject target, const char *paramName, const bn_float4 *xfm);
 
 /* model and render (barney.h:351-390) */
 BARNEY_API void bnSetInstances(BNModel model, int whichSlot, BNGroup *groupsToInstantiate,
                                BNTransform *instanceTransforms, int numInstances);
+/* barney.h:397: new transforms for the instances bnSetInstances set */
+BARNEY_API void bnUpdateInstanceTransforms(BNModel model, int whichSlot, BNTransform *instanceTransforms,
+                                           int numInstances);
+/* barney.h:405: per-instance attribute arrays ("instID", "attribute0".."4",
+   "color"); kept with the model -- the reference's device code reads none
+   of them on this path (its instance-ID map stays unset) */
+BARNEY_API void bnSetInstanceAttributes(BNModel model, int whichSlot, const char *attributeName, BNData data);
 BARNEY_API void bnBuild(BNModel model, int whichDataSlot);
 BARNEY_API void bnAccumReset(BNFrameBuffer fb);
 BARNEY_API void bnFrameBufferResize(BNFrameBuffer fb, BNDataType colorFormat, int sizeX, int sizeY,
@@ -194,5 +215,15 @@ BARNEY_API const char *bnGetLastError(void);
 /* Statistics of the last bnRender on this frame buffer: density samples,
    macrocells entered, rays traced, loop-cap events. */
 BARNEY_API void bnFrameBufferGetStats(BNFrameBuffer fb, unsigned long long stats[4]);
+
+#ifdef __cplusplus
+/* barney.h:537-551: the C++ overloads over the typed setters */
+inline void bnSet(BNObject o, const char *n, bn_float2 v) { bnSet2f(o, n, v.x, v.y); }
+inline void bnSet(BNObject o, const char *n, bn_float3 v) { bnSet3f(o, n, v.x, v.y, v.z); }
+inline void bnSet(BNObject o, const char *n, bn_float4 v) { bnSet4f(o, n, v.x, v.y, v.z, v.w); }
+inline void bnSet(BNObject o, const char *n, bn_int2 v) { bnSet2i(o, n, v.x, v.y); }
+inline void bnSet(BNObject o, const char *n, bn_int3 v) { bnSet3i(o, n, v.x, v.y, v.z); }
+inline void bnSet(BNObject o, const char *n, bn_int4 v) { bnSet4i(o, n, v.x, v.y, v.z, v.w); }
+#endif
 
 #endif /* BARNEY_GB300_H */

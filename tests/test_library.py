@@ -19,6 +19,7 @@ def declared_functions():
     for h in (ROOT / "include").glob("*.h"):
         text = h.read_text()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"(?m)^inline .*$", "", text)  # header-only C++ overloads (bnSet)
         for m in re.finditer(r"\b((?:gbv|bn)[A-Za-z0-9_]*)\s*\(", text):
             name = m.group(1)
             if name.startswith("gbv_") or re.match(r"bn[A-Z]", name):
@@ -288,3 +289,27 @@ def test_nanovdb_parse():
     bad = bytearray(grid)
     bad[root + 64 + 8:root + 64 + 16] = (len(grid)).to_bytes(8, "little", signed=True)
     assert parse(bytes(bad)) == N.GBV_ERROR_INVALID_ARGUMENT
+
+
+# every function barney/include/barney.h declares (its C++-only inline bnSet
+# overloads aside, which this library's header defines the same way)
+BARNEY_H_FUNCTIONS = [
+    "bnAccumReset", "bnAddReference", "bnBuild", "bnCameraCreate", "bnCommit", "bnContextCreate",
+    "bnContextDestroy", "bnDataCreate", "bnDataSet", "bnFrameBufferCreate", "bnFrameBufferGetSize",
+    "bnFrameBufferRead", "bnFrameBufferResize", "bnGeometryCreate", "bnGroupBuild", "bnGroupCreate",
+    "bnLightCreate", "bnMaterialCreate", "bnModelCreate", "bnRelease", "bnRender", "bnRendererCreate",
+    "bnSamplerCreate", "bnScalarFieldCreate", "bnSet1f", "bnSet1i", "bnSet2f", "bnSet2i", "bnSet3f", "bnSet3i",
+    "bnSet4f", "bnSet4i", "bnSet4x3fv", "bnSet4x4fv", "bnSetData", "bnSetInstanceAttributes", "bnSetInstances",
+    "bnSetLight", "bnSetObject", "bnSetString", "bnTexture2DCreate", "bnTexture3DCreate", "bnTextureData2DCreate",
+    "bnTextureData3DCreate", "bnUpdateInstanceTransforms", "bnVolumeCreate", "bnVolumeSetXF"]
+
+
+def test_every_barney_h_function_is_declared_and_exported():
+    """An application or ANARI device written against barney.h links
+    against this library: every one of its functions is declared in
+    include/barney_gb300.h and exported (those outside the volume path make
+    inert objects or record a message)."""
+    L = N.lib()
+    names = declared_functions()
+    assert not [n for n in BARNEY_H_FUNCTIONS if n not in names]
+    assert not [n for n in BARNEY_H_FUNCTIONS if not hasattr(L, n)]
