@@ -466,6 +466,54 @@ def nanovdb_timing(scene, persistent_ms, reps=2, types=("float", "fp16", "fp8", 
     return out
 
 
+def tiles_timing(g, scene, persistent_ms, worlds=(2, 4, 8)):
+    """The frame partition of a multi-GPU frame measured on one GPU: for N
+    ranks, each rank's share of the frame (the 32x32 tiles it owns,
+    gbv_render_tiles) timed alone -- the slowest share is the frame time N
+    GPUs would take, the sum the partition's overhead against the whole
+    frame -- and the compressed tile codec of the gather (gbv_compress_tiles
+    / gbv_unpack_tiles, 6144 bytes per tile) over the whole 1080p frame."""
+    import torch
+    from barney_gb300 import _native as N, tiles as T
+    out = {"full_frame_ms": persistent_ms, "ranks": {}}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    acc = g.new_accum()
+    for world in worlds:
+        ms = []
+        for rank in range(world):
+            g.render_tiles(rank, world, accum=acc)  # warm
+            e0.record()
+            g.render_tiles(rank, world, accum=acc)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out["ranks"][str(world)] = {"max_rank_ms": max(ms), "sum_ms": sum(ms),
+                                    "speedup_vs_full": persistent_ms / max(ms)}
+    g.render(accum=acc)
+    torch.cuda.synchronize()
+    tiles = T.compress_tiles(acc, scene.spp, 0, 1)
+    frame = torch.zeros_like(acc)
+    for _ in range(2):
+        T.compress_tiles(acc, scene.spp, 0, 1)
+        T.unpack_tiles_into(frame, tiles, 0, 1)
+    torch.cuda.synchronize()
+    e0.record()
+    tiles = T.compress_tiles(acc, scene.spp, 0, 1)
+    e1.record()
+    torch.cuda.synchronize()
+    enc = e0.elapsed_time(e1)
+    e0.record()
+    T.unpack_tiles_into(frame, tiles, 0, 1)
+    e1.record()
+    torch.cuda.synchronize()
+    dec = e0.elapsed_time(e1)
+    nb = tiles.numel()
+    out["codec"] = {"tiles": int(tiles.shape[0]), "compressed_bytes": int(nb), "accum_bytes": int(acc.numel() * 4),
+                    "encode_ms": enc, "decode_ms": dec,
+                    "encode_GBps": (acc.numel() * 4 + nb) / enc / 1e6, "decode_GBps": (nb + acc.numel() * 4) / dec / 1e6}
+    return out
+
+
 def batch_timing(count=64, reps=3):
     """The batched uneven workload: `count` volumes (sides log-uniform in
     [32, 256] per axis), each with its own TF, camera and image size from
@@ -638,6 +686,10 @@ def run_ours(args):
             line["nanovdb"] = nanovdb_timing(scene, frame_ms)
         except Exception as e:
             line["nanovdb"] = {"error": str(e)}
+        try:
+            line["tiles"] = tiles_timing(g, scene, frame_ms)
+        except Exception as e:
+            line["tiles"] = {"error": str(e)}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, g.majorants.cpu().numpy())
     line["extras_s"] = time.perf_counter() - extras_t0
