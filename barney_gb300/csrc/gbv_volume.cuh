@@ -141,6 +141,15 @@ template <int FMT, bool kViaL1 = false> struct StoreBrickCorners {
   }
 };
 
+// The same store reading through L1, for samples that follow each other
+// closely along a ray (the iso-surface search's sub-steps), where L1 pays;
+// other stores are returned as they are.
+template <class S> __device__ __forceinline__ const S &via_l1(const S &s) { return s; }
+template <int FMT>
+__device__ __forceinline__ StoreBrickCorners<FMT, true> via_l1(const StoreBrickCorners<FMT, false> &s) {
+  return StoreBrickCorners<FMT, true>{s.v, s.so, s.g};
+}
+
 // StructuredDataSampler::DD::sample (StructuredData.h:104-115) with the CPU
 // backend's trilinear filter (rtcore/embree/Texture.cpp:339-411).  NaN
 // outside [0, numCells).

@@ -1021,10 +1021,12 @@ __device__ __forceinline__ int trace_sample(const FieldGeom &F, const Store &sto
 // more than a few ulps below its cell's start, far inside the 1e-5 margin);
 // +inf searches the whole ray.
 template <class Store>
-__device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &store, const MCGridDev &G,
+__device__ __forceinline__ bool iso_search(const FieldGeom &F, const Store &renderStore, const MCGridDev &G,
                                            const float2 *__restrict__ ranges, float iso, float delta, Traversal &T,
                                            float tmax, float &tOut, vec3 &N,
                                            float stop = __int_as_float_hd(0x7f800000)) {
+  // the sub-steps' samples lie close together along the ray: read through L1
+  const auto &store = via_l1(renderStore);
   const bool sx = T.stopx >= 0, sy = T.stopy >= 0, sz = T.stopz >= 0;
   const int maxCells = G.M[0] + G.M[1] + G.M[2] + 8;
   float tHit = tmax;
