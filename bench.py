@@ -653,7 +653,8 @@ def run_ours(args):
     line["e2e"] = {"value": world * samples / e2e["dt"] / 1e6, "unit": UNIT, "h2d_bytes_per_step": e2e["h2d"],
                    "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": 1e3 * e2e["dt"],
                    "path": "bnTextureData3DCreate(host) .. bnRender .. bnFrameBufferRead(host), pinned buffers",
-                   "frame_identical_to_device_frame": e2e["same"], "phases_ms": e2e["phases_ms"]}
+                   "frame_identical_to_device_frame": e2e["same"], "phases_ms": e2e["phases_ms"],
+                   "host_cpus": e2e["host_cpus"]}
     if rank != 0:
         if world > 1:
             dist.barrier()
@@ -698,6 +699,28 @@ def run_ours(args):
         dist.barrier()
 
 
+def bind_to_gpu_numa_node(local: int) -> str:
+    """Runs this process on the CPUs attached to GPU `local` (its PCI
+    device's local_cpulist in sysfs), as numactl --cpunodebind would, so that
+    host buffers pinned afterwards are first touched in the GPU's own host
+    memory; returns the CPU list, or why it was left as it was."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(local)
+        dev = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        text = Path("/sys/bus/pci/devices/%s/local_cpulist" % dev).read_text().strip()
+        cpus = set()
+        for part in text.split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        if not cpus or cpus == set(range(os.cpu_count() or 0)):
+            return "all CPUs are local"
+        os.sched_setaffinity(0, cpus)
+        return text
+    except Exception as e:  # no sysfs entry, no permission: leave the process where it is
+        return "not bound: %s" % e
+
+
 def e2e_timing(args, scene, g, acc, fmt, local):
     """Steps through the public bn* API with host buffers: each uploads the
     volume from pinned host memory (bnTextureData3DCreate), builds the
@@ -707,6 +730,8 @@ def e2e_timing(args, scene, g, acc, fmt, local):
     read equals the device-timed frame `acc`."""
     import torch
     from barney_gb300 import bn
+    before = os.sched_getaffinity(0)
+    cpus = bind_to_gpu_numa_node(local)
     host_vol = torch.from_numpy(np.ascontiguousarray(scene.scalars)).pin_memory()
     out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32).pin_memory()
     e2e_times, phases = [], []
@@ -725,12 +750,13 @@ def e2e_timing(args, scene, g, acc, fmt, local):
                 # the bn* calls return when their work is done (each upload
                 # and build synchronizes, bnRender waits for its frame)
                 phases.append((t1 - t0, t2 - t1, t0 + dt - t2))
+    os.sched_setaffinity(0, before)  # the CPU baseline afterwards uses every core
     ph = [1e3 * sum(p[k] for p in phases) / len(phases) for k in range(3)]
     # the bn* frame is the device frame read out: same samples, same pixels
     same = bool(torch.equal(out.cuda(), g.tonemap(acc, scene.spp)))
     h2d = host_vol.numel() * 4 + scene.tf.nbytes + (scene.env.texels.nbytes if scene.env is not None else 0)
     return {"dt": sum(e2e_times) / len(e2e_times), "h2d": int(h2d), "d2h": int(out.numel() * 4), "same": same,
-            "phases_ms": {"upload_and_build": ph[0], "render": ph[1], "read": ph[2]}}
+            "phases_ms": {"upload_and_build": ph[0], "render": ph[1], "read": ph[2]}, "host_cpus": cpus}
 
 
 def profile_render_case(args):
