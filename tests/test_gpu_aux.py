@@ -147,3 +147,30 @@ def test_anari_frame_resize_and_map():
     assert hit.any() and (obj[~hit] == -1).all() and (depth[hit] < 1e3).all()
     # a pixel whose first pass missed keeps IDs -1; its depth is 1e30 unless a later pass hit
     assert ((depth[~hit] == np.float32(1e30)) | (depth[~hit] < 1e3)).all()
+
+
+def test_noalloc_entry_writes_the_same_channels():
+    """gbv_render_noalloc with the aux channels in its scene record writes
+    the channels gbv_render writes (it allocates nothing for them: the
+    caller's buffers are written in place)."""
+    import ctypes as C
+    import torch
+    from barney_gb300 import _native as N
+    from barney_gb300.device import _ptr, _stream
+    s = scenes.small_scene(dims=32, spp=3, width=40, height=32)
+    s.volume_user_id = 6
+    g = GpuScene(s)
+    want = _aux_gpu(s.width, s.height)
+    acc_w = g.render(spp=3, aux=want)
+    got = _aux_gpu(s.width, s.height)
+    acc = g.new_accum()
+    rec = g.record()
+    for f, k in (("d_depth", "depth"), ("d_prim_id", "prim_id"), ("d_inst_id", "inst_id"), ("d_obj_id", "obj_id")):
+        setattr(rec, f, got[k].data_ptr())
+    st = N.lib().gbv_render_noalloc(C.byref(rec), _ptr(acc), s.width, s.height, 0, 3, None, _stream())
+    assert st == N.GBV_OK, N.lib().gbv_last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(acc, acc_w)
+    for k in want:
+        assert torch.equal(got[k], want[k]), k
+    assert (got["obj_id"] == 6).any()
