@@ -770,11 +770,16 @@ def profile_render_case(args):
       ncu --clock-control none -k regex:render_kernel -s <warmup> -c <launches> ...
     With --mode wavefront a frame is a sequence of wf_trace_kernel and
     wf_shade_kernel launches (one of each per step).  Count=0 in the trace
-    kernel's template arguments marks the uncounted frames."""
+    kernel's template arguments marks the uncounted frames.  --iso V adds the
+    iso-surface of value V (matte, its instance first); --iso-only renders
+    the surface alone (the kernel's last template argument is then 1)."""
     import torch
     from barney_gb300 import _native as N, scenes
     from barney_gb300.device import GpuScene
     s = scenes.frame_scene(dims=args.dims, width=args.width, height=args.height, spp=args.spp)
+    if args.iso is not None:
+        s.iso = scenes.IsoSurface(args.iso, (0.8, 0.8, 0.8, 1.0), 1.0, 0)
+        s.volume_instance, s.no_volume = (0, True) if args.iso_only else (1, False)
     fmt = {"f32": 0, "f16": 1, "bf16": 2, "u8": 3}[args.format]
     layout = N.GBV_LAYOUT_BRICK_CORNERS if args.layout == "brick" else N.GBV_LAYOUT_LINEAR
     g = GpuScene(s, layout=layout, fmt=fmt)
@@ -787,8 +792,8 @@ def profile_render_case(args):
     torch.cuda.synchronize()
     c = [int(x) for x in cnt.cpu().tolist()]
     rec = dict(dims=args.dims, width=args.width, height=args.height, spp=args.spp, format=args.format,
-               layout=args.layout, mode=args.mode, samples_per_launch=c[0], mc_visits_per_launch=c[1],
-               rays_per_launch=c[2])
+               layout=args.layout, mode=args.mode, iso=args.iso, iso_only=bool(args.iso_only),
+               samples_per_launch=c[0], mc_visits_per_launch=c[1], rays_per_launch=c[2])
     if args.out:
         Path(args.out).parent.mkdir(parents=True, exist_ok=True)
         Path(args.out).write_text(json.dumps(rec, indent=1))
@@ -842,6 +847,8 @@ def main():
     ap.add_argument("--views", type=int, default=32, help="--profile-case ea: views")
     ap.add_argument("--size", type=int, default=256, help="--profile-case ea: view edge in pixels")
     ap.add_argument("--out", default="", help="--profile-case render: counters JSON")
+    ap.add_argument("--iso", type=float, default=None, help="--profile-case render: an iso-surface of this value")
+    ap.add_argument("--iso-only", action="store_true", help="--profile-case render: the iso-surface alone")
     args = ap.parse_args()
     if args.dims is None:
         args.dims = 128 if args.profile_case == "ea" else 512
